@@ -1,0 +1,12 @@
+"""GB300 (sm_103a) stochastic progressive photon mapping: a drop-in for glslppm's GPU path.
+
+The compute path is the native library ``_lib/libsppm.so`` (hand-written CUDA kernels behind the C
+ABI of ``include/sppm.h``); this package is its host-side mirror.  Importing the package fails with
+``NativeLibraryMissing`` when the library has not been built.
+"""
+from .native import NativeLibraryMissing, SppmError, device_count  # noqa: F401
+from .renderer import Mesh, Renderer, default_config, look_at, scene_from_arrays  # noqa: F401
+from . import native, scenes  # noqa: F401
+
+__all__ = ["Mesh", "Renderer", "default_config", "look_at", "scene_from_arrays", "SppmError",
+           "NativeLibraryMissing", "device_count", "native", "scenes"]

@@ -1,0 +1,206 @@
+// Device-side data layout and exact single-precision helpers of the SPPM path.
+//
+// Layout in HBM (one render job = one scene + camera + progressive state; a batch launch covers
+// many jobs through a job table and prefix sums of their work items):
+//   scene   NodeX   [6 orderings][num_nodes]  32 B, in the traversal order of each ordering, so the
+//                   "hit" successor of node i is i+1 and only the miss link is stored
+//           TriIsect[num_tris]  48 B  v0, e0 = v1-v0, e1 = v2-v0 (the intersection test's operands)
+//           TriShade[num_tris]  96 B  geometric normal + material, v0..v2, decoded shading normals
+//           DevMaterial[num_mats] 32 B, light CDF + triangle table
+//   pixels  float4 SoA: position, reflectance, normal, rng, (emission, N), (tau, R); int tri; float t
+//   photons float4 SoA: position(+nrm.x), flux(+nrm.y), direction(+nrm.z), rng; int2 (tri, depth)
+//   hash    uint32 winner[slots], uint32 count[slots]
+// float4 SoA keeps every per-item access a single coalesced 16-byte load or store.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sppm.h"
+#include "sppm_fpmath.h"
+
+namespace sppm_dev {
+
+constexpr int32_t kEmitterBit = 1 << 30;  // leaf triangle belongs to a light (skipped by photons)
+constexpr int32_t kTriMask = kEmitterBit - 1;
+constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
+
+constexpr uint32_t kErrWatchdogTraverse = 1u;
+constexpr uint32_t kErrWatchdogLight = 2u;
+
+struct __align__(16) NodeX {
+    float bmin[3];
+    int32_t miss;  // position in the same ordering, -1 = end
+    float bmax[3];
+    int32_t tri;   // -1 internal; leaf: triangle id, | kEmitterBit for lights
+};
+static_assert(sizeof(NodeX) == 32, "NodeX is one 32-byte sector");
+
+struct __align__(16) DevMaterial {
+    float color[3];
+    float eta;
+    int32_t brdf;
+    float g;
+    float pad[2];
+};
+
+struct DevScene {
+    const NodeX* nodes;       // [6][num_nodes]
+    const float4* tri_isect;  // [num_tris][3]
+    const float4* tri_shade;  // [num_tris][6]
+    const DevMaterial* mats;
+    const float* light_cdf;
+    const int32_t* light_tri;
+    uint32_t num_nodes, num_tris, num_lights, num_mats;
+    float light_area, light_stride;
+    float bsphere[4];
+};
+
+struct DevPixels {
+    float4 *pos, *refl, *nrm, *rng, *emi_n, *flux_r;
+    int32_t* tri;
+    float* t;
+    double *stat_n, *stat_r2, *stat_tau;  // mixed precision statistics (tau: 3 per pixel)
+};
+
+struct DevPhotons {
+    float4 *pos, *flux, *dir, *rng;
+    int2* hit;  // (triangle or -1, path depth)
+};
+
+// mutable per-job frame state (written by single threads between stages)
+struct JobState {
+    uint32_t frame;           // index of the frame in progress
+    uint32_t frames_started;
+    uint32_t eye_samples;
+    uint32_t is_eye_frame;
+    uint32_t xs[4];           // xorshift128 stream of the anti-aliasing offsets
+    float aa[2];
+    uint32_t bbmax_key[3], bbmin_key[3];  // order-preserving encodings for atomicMax/atomicMin
+    float bbmin[3], bbmax[3];             // expanded grid bbox (BBMin/BBMax)
+    float initial_radius, grid_scale, hash_scale1, r0;
+    uint32_t emitted_frame;
+    uint32_t segments_frame;
+    float num_photons_f32;
+    uint32_t err;
+    unsigned long long num_photons, photon_segments, eye_segments;
+};
+
+struct JobDesc {
+    DevScene scene;
+    DevPixels px;
+    DevPhotons ph;
+    uint32_t* winner;
+    uint32_t* count;
+    JobState* state;
+    float* image;  // W*H*3 resolve target
+    float cam_pos[3], cam_u[3], cam_v[3], cam_w[3];
+    float cam_cx, cam_cy, cam_dist;
+    uint32_t W, H, PW, PH, hash_num;
+    uint32_t max_path, eye_interval, radius_rule, flags, precision;
+    float alpha, footprint, focal, aperture, fixed_radius;
+};
+
+// the work of one launch: items [prefix[k], prefix[k+1]) belong to jobs[job_ids[k]]
+struct LaunchSet {
+    const JobDesc* jobs;
+    const uint32_t* job_ids;
+    const uint32_t* prefix;
+    uint32_t njobs;
+    uint32_t total;
+};
+
+__device__ __forceinline__ int find_job(const LaunchSet& ls, uint32_t g) {
+    int lo = 0, hi = (int)ls.njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&ls.prefix[mid]) <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---- exact single-precision vector helpers (pinned evaluation order, never fused) ----------
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 xyz(float4 a) { return f3{a.x, a.y, a.z}; }
+__device__ __forceinline__ float4 f4(f3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+__device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float xdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ f3 add(f3 a, f3 b) { return mk(xadd(a.x, b.x), xadd(a.y, b.y), xadd(a.z, b.z)); }
+__device__ __forceinline__ f3 sub(f3 a, f3 b) { return mk(xsub(a.x, b.x), xsub(a.y, b.y), xsub(a.z, b.z)); }
+__device__ __forceinline__ f3 mul(f3 a, f3 b) { return mk(xmul(a.x, b.x), xmul(a.y, b.y), xmul(a.z, b.z)); }
+__device__ __forceinline__ f3 scl(f3 a, float s) { return mk(xmul(a.x, s), xmul(a.y, s), xmul(a.z, s)); }
+__device__ __forceinline__ f3 neg(f3 a) { return mk(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return xadd(xadd(xmul(a.x, b.x), xmul(a.y, b.y)), xmul(a.z, b.z)); }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+    return mk(xsub(xmul(a.y, b.z), xmul(b.y, a.z)), xsub(xmul(a.z, b.x), xmul(b.z, a.x)),
+              xsub(xmul(a.x, b.y), xmul(b.x, a.y)));
+}
+__device__ __forceinline__ float length(f3 a) { return xsqrt(dot(a, a)); }
+__device__ __forceinline__ f3 normalize(f3 a) { return scl(a, xdiv(1.0f, xsqrt(dot(a, a)))); }
+__device__ __forceinline__ f3 reflect(f3 i, f3 n) {
+    const float d = xmul(2.0f, dot(n, i));
+    return sub(i, scl(n, d));
+}
+__device__ __forceinline__ f3 refract(f3 i, f3 n, float eta) {
+    const float d = dot(n, i);
+    const float k = xsub(1.0f, xmul(xmul(eta, eta), xsub(1.0f, xmul(d, d))));
+    if (k < 0.0f) return mk(0.0f, 0.0f, 0.0f);
+    return sub(scl(i, eta), scl(n, xadd(xmul(eta, d), xsqrt(k))));
+}
+__device__ __forceinline__ float signf(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+__device__ __forceinline__ float fractf(float x) { return xsub(x, floorf(x)); }
+
+// ---- GPURnd (eyeraytrace.fs:326-347) and the cell hash (hash.fs:21-48) ---------------------
+// lane constants q, r, a, m and the single-precision 1/m, 1/q, m/2 the shaders derive from them
+#define SPPM_RND_LANE(i, q, r, a, m, qinv, minv)                                                \
+    {                                                                                            \
+        const float beta = floorf(xmul(s[i], qinv));                                             \
+        const float p = xsub(xmul(a, xsub(s[i], xmul(beta, q))), xmul(beta, r));                 \
+        const float beta2 = xadd(xmul(signf(-p), 0.5f * (m)), 0.5f * (m));                       \
+        s[i] = xadd(p, beta2);                                                                   \
+        v[i] = xmul(s[i], minv);                                                                 \
+    }
+
+__device__ __forceinline__ void schrage4(float s[4], float v[4]) {
+    SPPM_RND_LANE(0, 1225.0f, 1112.0f, 3423.0f, 4194287.0f, 8.163265302e-04f, 2.384195454e-07f)
+    SPPM_RND_LANE(1, 1585.0f, 367.0f, 2646.0f, 4194277.0f, 6.309148157e-04f, 2.384201139e-07f)
+    SPPM_RND_LANE(2, 2457.0f, 92.0f, 1707.0f, 4194191.0f, 4.070004215e-04f, 2.384250024e-07f)
+    SPPM_RND_LANE(3, 2098.0f, 265.0f, 1999.0f, 4194167.0f, 4.766444326e-04f, 2.384263666e-07f)
+}
+
+__device__ __forceinline__ float gpu_rnd(float4& n) {
+    float s[4] = {n.x, n.y, n.z, n.w}, v[4];
+    schrage4(s, v);
+    n = make_float4(s[0], s[1], s[2], s[3]);
+    return fractf(xsub(xadd(xsub(v[0], v[1]), v[2]), v[3]));
+}
+
+__device__ __forceinline__ uint32_t hash_cell(f3 cell, float grid_scale, float hash_scale1, float hash_num) {
+    float s[4] = {xmul(cell.x, hash_scale1), xmul(cell.y, hash_scale1), xmul(cell.z, hash_scale1),
+                  xmul(xmul(grid_scale, 0.5f), hash_scale1)};
+    float v[4];
+    schrage4(s, v);
+    float h = floorf(xmul(fractf(xsub(xadd(xsub(v[0], v[1]), v[2]), v[3])), hash_num));
+    if (!(h >= 0.0f)) h = 0.0f;
+    const float hmax = xsub(hash_num, 1.0f);
+    if (h > hmax) h = hmax;
+    return (uint32_t)h;
+}
+
+// order-preserving float <-> uint32 encoding (for atomicMin/atomicMax on floats)
+__device__ __forceinline__ uint32_t float_key(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+}  // namespace sppm_dev

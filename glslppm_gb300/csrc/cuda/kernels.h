@@ -1,0 +1,22 @@
+// Launchers of the SPPM kernels (host side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+
+namespace sppm_dev {
+
+// plain FP32 path (kernels_fp32.cu)
+void launch_frame_begin(const LaunchSet& ls, cudaStream_t s);
+void launch_eye_fp32(const LaunchSet& ls, cudaStream_t s);
+void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s);
+void launch_photon_fp32(const LaunchSet& ls, cudaStream_t s);
+void launch_gather_fp32(const LaunchSet& ls, cudaStream_t s);
+void launch_resolve_fp32(const LaunchSet& ls, uint32_t display, cudaStream_t s);
+void launch_hash_build(const float4* pos, const float4* flux, uint32_t pw, uint32_t ph, uint32_t hash_num,
+                       const float bbmin[3], float grid_scale, uint32_t flags, uint32_t* winner, uint32_t* count,
+                       cudaStream_t s);
+void launch_fpmath(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t s);
+
+}  // namespace sppm_dev

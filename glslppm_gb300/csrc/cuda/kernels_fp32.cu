@@ -1,0 +1,793 @@
+// Plain-FP32 SPPM kernels for sm_103a: every operation of the reference shaders in IEEE single
+// precision, in the order the shaders write it (see device_common.cuh for the pinned helpers),
+// so each per-pixel and per-photon value is bit-identical to the CPU restatement.  This
+// translation unit is also compiled with -fmad=false.
+//
+// One SPPM frame (m_display, glslppm.cpp:214-536) is four to six launches over all jobs of a
+// batch:
+//   k_frame_begin   hash-slot clear + per-job frame bookkeeping (AA offset of the eye pass)
+//   k_eye           eyeraytrace.fs, fused with the max/min reductions (warp shuffles + one
+//                   atomic per warp) that replace ReduceTexture's 2x2 passes and 18 readbacks
+//   k_grid          InitialRadius / grid (glslppm.cpp:294-311), on the device: no host round trip
+//   k_photon        photontrace.fs, fused with the sum reduction of emitted photons and with the
+//                   hashed-grid build of hash.fs + scatter.vs (depth test = atomicMin of the photon
+//                   index) + correction.vs (additive blend = atomicAdd), warp-aggregated per slot
+//   k_gather        progressive.fs
+//   k_resolve       re.fs (on demand)
+#include <cstdint>
+
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace sppm_dev {
+
+// ----------------------------------------------------------------------------------------------
+// traversal: the threaded BVH walk of raytrace() (eyeraytrace.fs:67-290, photontrace.fs:123-255)
+// ----------------------------------------------------------------------------------------------
+struct Hit {
+    float t;
+    int32_t tri;
+    int32_t mat;
+    float bu, bv, bw;  // Barycentric = (v, w, u)
+};
+
+__device__ __forceinline__ int cube_face(f3 d) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    if (ax >= ay && ax >= az) return d.x < 0.0f ? 1 : 0;
+    if (ay >= az) return d.y < 0.0f ? 3 : 2;
+    return d.z < 0.0f ? 5 : 4;
+}
+
+template <bool PHOTON>
+__device__ __forceinline__ Hit trace_exact(const DevScene& s, f3 org, f3 dir, bool cull, uint32_t& err) {
+    Hit h;
+    h.t = PHOTON ? 1.0e30f : 1.0e20f;
+    h.tri = -1;
+    h.mat = -1;
+    h.bu = h.bv = h.bw = 0.0f;
+    const NodeX* nodes = s.nodes + (size_t)cube_face(dir) * s.num_nodes;
+    const f3 rcp = mk(xdiv(1.0f, dir.x), xdiv(1.0f, dir.y), xdiv(1.0f, dir.z));
+    const f3 t0 = mul(neg(rcp), org);
+    const int32_t nn = (int32_t)s.num_nodes;
+    int32_t i = 0;
+    for (int32_t steps = 0;; steps++) {
+        if (steps > nn) {
+            err |= kErrWatchdogTraverse;
+            break;
+        }
+        const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + i));
+        const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + i) + 1);
+        const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
+        const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
+        const float tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
+        const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
+        const bool hit = (tmin <= tmax) && (tmin <= h.t) && (tmax >= 0.0f);
+        const int32_t tri = __float_as_int(B.w);
+        if (hit && tri >= 0 && (!PHOTON || !(tri & kEmitterBit))) {
+            const int32_t t = tri & kTriMask;
+            const float4 a = __ldg(&s.tri_isect[(size_t)t * 3 + 0]);
+            const float4 b = __ldg(&s.tri_isect[(size_t)t * 3 + 1]);
+            const float4 c = __ldg(&s.tri_isect[(size_t)t * 3 + 2]);
+            const f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
+            const f3 pv = cross(dir, e1);
+            const float det = dot(e0, pv);
+            if (PHOTON || !cull || det > 1e-10f) {
+                const f3 tv = sub(org, v0);
+                const f3 qv = cross(tv, e0);
+                const float u = xdiv(dot(tv, pv), det);
+                const float v = xdiv(dot(dir, qv), det);
+                const float tt = xdiv(dot(e1, qv), det);
+                const float w = xsub(xsub(1.0f, u), v);
+                if (u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt < h.t) {
+                    h.t = tt;
+                    h.tri = t;
+                    h.mat = __float_as_int(c.y);
+                    h.bu = v;
+                    h.bv = w;
+                    h.bw = u;
+                }
+            }
+        }
+        const int32_t next = hit ? i + 1 : __float_as_int(A.w);
+        if (next < 0 || next >= nn) break;
+        i = next;
+    }
+    return h;
+}
+
+struct Shade {
+    f3 pos, nrm, gnrm, col;
+    int brdf;
+    float eta, g;
+};
+
+// Result of raytrace() for a hit (eyeraytrace.fs:256-287)
+__device__ __forceinline__ Shade shade_hit(const DevScene& s, const Hit& h) {
+    const float4* ts = s.tri_shade + (size_t)h.tri * 6;
+    const float4 r0 = __ldg(ts + 0), r1 = __ldg(ts + 1), r2 = __ldg(ts + 2);
+    const float4 r3 = __ldg(ts + 3), r4 = __ldg(ts + 4), r5 = __ldg(ts + 5);
+    const f3 V0 = mk(r1.x, r1.y, r1.z), V1 = mk(r1.w, r2.x, r2.y), V2 = mk(r2.z, r2.w, r3.x);
+    const f3 N0 = mk(r3.y, r3.z, r3.w), N1 = mk(r4.x, r4.y, r4.z), N2 = mk(r4.w, r5.x, r5.y);
+    Shade o;
+    o.pos = add(add(scl(V2, h.bu), scl(V0, h.bv)), scl(V1, h.bw));
+    o.nrm = normalize(add(add(scl(N2, h.bu), scl(N0, h.bv)), scl(N1, h.bw)));
+    o.gnrm = mk(r0.x, r0.y, r0.z);
+    const DevMaterial& m = s.mats[h.mat];
+    o.col = mk(m.color[0], m.color[1], m.color[2]);
+    o.brdf = m.brdf;
+    o.eta = m.eta;
+    o.g = m.g;
+    return o;
+}
+
+// ----------------------------------------------------------------------------------------------
+// BRDF helpers (eyeraytrace.fs:293-392, photontrace.fs:60-89, 258-280, 443-461)
+// ----------------------------------------------------------------------------------------------
+__device__ __forceinline__ f3 onb(f3 x, f3 n) {
+    if (n.z < -0.9999999f) return sub(scl(n, x.y), mk(x.z, x.x, 0.0f));
+    const float a = xdiv(1.0f, xadd(1.0f, n.z));
+    const float b = xmul(xmul(-n.x, n.y), a);
+    const f3 u = mk(xsub(1.0f, xmul(xmul(n.x, n.x), a)), b, -n.x);
+    const f3 w = mk(b, xsub(1.0f, xmul(xmul(n.y, n.y), a)), -n.y);
+    return add(add(scl(u, x.x), scl(n, x.y)), scl(w, x.z));
+}
+
+__device__ __forceinline__ float fresnel(f3 incom, f3 normal, float ii, float ie) {
+    const float eta = xdiv(ii, ie);
+    const float c1 = dot(incom, normal);
+    float c2 = xsub(1.0f, xmul(xmul(eta, eta), xsub(1.0f, xmul(c1, c1))));
+    if (c2 < 0.0f) return 1.0f;
+    c2 = xsqrt(c2);
+    const float rs = xdiv(xsub(xmul(ii, c1), xmul(ie, c2)), xadd(xmul(ii, c1), xmul(ie, c2)));
+    const float rp = xdiv(xsub(xmul(ii, c2), xmul(ie, c1)), xadd(xmul(ii, c2), xmul(ie, c1)));
+    return xmul(xadd(xmul(rs, rs), xmul(rp, rp)), 0.5f);
+}
+
+__device__ __forceinline__ f3 glossy_reflect(f3 d, f3 n, float g, float4& rndv) {
+    const f3 r = normalize(add(scl(reflect(d, n), xsub(xsub(1.0f, g), g)), scl(n, xadd(g, g))));
+    const float rnd1 = gpu_rnd(rndv);
+    const float rnd2 = gpu_rnd(rndv);
+    const float temp1 = xmul(6.283184f, rnd1);
+    const float temp2_ = sppm_fpow(rnd2, g);
+    const float temp2 = xsqrt(xsub(1.0f, xmul(temp2_, temp2_)));
+    const f3 v = mk(xmul(sppm_fsin(temp1), temp2), temp2_, xmul(sppm_fcos(temp1), temp2));
+    f3 result = normalize(onb(v, r));
+    if (dot(result, n) < 0.0f) result = reflect(result, n);
+    return result;
+}
+
+__device__ __forceinline__ uint32_t grid_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+// ----------------------------------------------------------------------------------------------
+// k_frame_begin: clear the hashed grid of every job; per-job bookkeeping by the job's slot 0
+// ----------------------------------------------------------------------------------------------
+__device__ __forceinline__ float xorshift_frand(uint32_t* s) {
+    const uint32_t t = s[0] ^ (s[0] << 11);
+    s[0] = s[1];
+    s[1] = s[2];
+    s[2] = s[3];
+    s[3] = (s[3] ^ (s[3] >> 19)) ^ (t ^ (t >> 8));
+    return xmul(__uint2float_rn(s[3]), 1.0f / 4294967295.0f);
+}
+
+__global__ void k_frame_begin(LaunchSet ls) {
+    const uint32_t g = grid_tid();
+    if (g >= ls.total) return;
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    const uint32_t local = g - ls.prefix[k];
+    J.winner[local] = kEmptySlot;
+    J.count[local] = 0;
+    if (local == 0) {
+        JobState* st = J.state;
+        const uint32_t f = st->frames_started;
+        st->frame = f;
+        st->frames_started = f + 1;
+        st->emitted_frame = 0;
+        st->segments_frame = 0;
+        const uint32_t interval = J.eye_interval ? J.eye_interval : 1u;
+        st->is_eye_frame = (f % interval) == 0;
+        if (st->is_eye_frame) {
+            // AAOffset (glslppm.cpp:276-277)
+            st->aa[0] = xmul(xsub(xorshift_frand(st->xs), 0.5f), 1.25f);
+            st->aa[1] = xmul(xsub(xorshift_frand(st->xs), 0.5f), 1.25f);
+            st->eye_samples += 1;
+            for (int c = 0; c < 3; c++) {
+                st->bbmax_key[c] = 0u;           // below every float
+                st->bbmin_key[c] = 0xFFFFFFFFu;  // above every float
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------------------------
+// k_eye: eyeraytrace.fs main (:396-554) + max/min reduction of the hit positions
+// ----------------------------------------------------------------------------------------------
+__device__ __forceinline__ void warp_bbox_atomics(JobState* st, f3 p, int job_k) {
+    // lanes of the same job combine with warp reductions; the leader issues one atomic per
+    // component; a NaN component is ignored, as fminf/fmaxf ignore it
+    const unsigned mask = __match_any_sync(__activemask(), job_k);
+    const float v[3] = {p.x, p.y, p.z};
+    for (int c = 0; c < 3; c++) {
+        const bool ok = v[c] == v[c];
+        uint32_t kmx = ok ? float_key(v[c]) : 0u;
+        uint32_t kmn = ok ? float_key(v[c]) : 0xFFFFFFFFu;
+        kmx = __reduce_max_sync(mask, kmx);
+        kmn = __reduce_min_sync(mask, kmn);
+        if ((threadIdx.x & 31) == (__ffs(mask) - 1)) {
+            atomicMax(&st->bbmax_key[c], kmx);
+            atomicMin(&st->bbmin_key[c], kmn);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_eye(LaunchSet ls) {
+    const uint32_t g = grid_tid();
+    if (g >= ls.total) return;
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    JobState* st = J.state;
+    const uint32_t p = g - ls.prefix[k];
+    const uint32_t px = p % J.W, py = p / J.W;
+    const DevScene& S = J.scene;
+    uint32_t err = 0;
+    float4 rndv = J.px.rng[p];
+    const float eps = 1e-5f;
+    const f3 U = mk(J.cam_u[0], J.cam_u[1], J.cam_u[2]);
+    const f3 V = mk(J.cam_v[0], J.cam_v[1], J.cam_v[2]);
+    const f3 Wd = mk(J.cam_w[0], J.cam_w[1], J.cam_w[2]);
+    const f3 CP = mk(J.cam_pos[0], J.cam_pos[1], J.cam_pos[2]);
+    const float aax = st->aa[0], aay = st->aa[1];
+    const float ppx = xsub(xadd(xadd((float)px, 0.5f), aax), J.cam_cx);
+    const float ppy = xsub(xadd(xadd((float)py, 0.5f), aay), J.cam_cy);
+    f3 rdir = normalize(add(add(scl(U, ppx), scl(V, ppy)), scl(Wd, J.cam_dist)));
+    f3 rorg;
+    const float filter = xmul(xsub(1.0f, xdiv(fabsf(aax), 1.5f)), xsub(1.0f, xdiv(fabsf(aay), 1.5f)));
+    {
+        const f3 fp = add(CP, scl(rdir, J.focal));
+        const float radius = xmul(xsqrt(gpu_rnd(rndv)), J.aperture);
+        const float theta = xmul(6.283184f, gpu_rnd(rndv));
+        const f3 lens = add(CP, scl(add(scl(U, sppm_fcos(theta)), scl(V, sppm_fsin(theta))), radius));
+        rdir = normalize(sub(fp, lens));
+        rorg = lens;
+    }
+    f3 col = mk(filter, filter, filter);
+    f3 nrm = mk(0, 0, 0), pos = mk(0, 0, 0), emi = mk(0, 0, 0);
+    Hit last;
+    last.tri = -1;
+    last.t = 1.0e20f;
+    uint32_t segs = 0;
+    for (uint32_t j = 0; j < J.max_path; j++) {
+        const Hit h = trace_exact<false>(S, rorg, rdir, j == 0, err);
+        last = h;
+        segs++;
+        if (h.tri < 0) {
+            nrm = mk(0, 0, 0);
+            if (S.light_area == 0.0f) emi = mul(mk(0.7f, 0.7f, 1.0f), col);
+            break;
+        }
+        const Shade i = shade_hit(S, h);
+        pos = i.pos;
+        nrm = i.nrm;
+        if (i.brdf == -1) {
+            nrm = mk(0, 0, 0);
+            emi = mul(col, i.col);
+            break;
+        } else if (i.brdf == 0) {
+            col = mul(col, i.col);
+            break;
+        } else if (i.brdf == 1 || i.brdf == 4) {
+            rorg = add(pos, scl(i.gnrm, eps));
+            if (i.brdf == 4) nrm = glossy_reflect(nrm, nrm, i.g, rndv);
+            rdir = reflect(rdir, nrm);
+            if (dot(rdir, i.gnrm) < 0.0f) rdir = neg(rdir);
+            col = mul(col, i.col);
+        } else if (i.brdf == 2 || i.brdf == 5) {
+            if (i.brdf == 5) nrm = glossy_reflect(nrm, nrm, i.g, rndv);
+            const float ln = dot(nrm, rdir);
+            if (ln < 0.0f) {
+                const float re = fresnel(neg(rdir), nrm, 1.0f, i.eta);
+                if (gpu_rnd(rndv) < re) {
+                    rorg = add(pos, scl(i.gnrm, eps));
+                    rdir = reflect(rdir, nrm);
+                    if (dot(rdir, i.gnrm) < 0.0f) rdir = neg(rdir);
+                } else {
+                    col = mul(col, i.col);
+                    rorg = sub(pos, scl(i.gnrm, eps));
+                    rdir = refract(rdir, nrm, xdiv(1.0f, i.eta));
+                    if (dot(rdir, i.gnrm) > 0.0f) rdir = neg(rdir);
+                }
+            } else {
+                const float re = fresnel(neg(rdir), neg(nrm), i.eta, 1.0f);
+                col = mul(col, i.col);
+                if (gpu_rnd(rndv) < re) {
+                    rorg = sub(pos, scl(i.gnrm, eps));
+                    rdir = reflect(rdir, neg(nrm));
+                    if (dot(rdir, neg(i.gnrm)) < 0.0f) rdir = neg(rdir);
+                } else {
+                    rorg = add(pos, scl(i.gnrm, eps));
+                    rdir = refract(rdir, neg(nrm), i.eta);
+                    if (dot(rdir, neg(i.gnrm)) > 0.0f) rdir = neg(rdir);
+                }
+            }
+        } else if (i.brdf == 3 || i.brdf == 6) {
+            if (i.brdf == 6) nrm = glossy_reflect(nrm, nrm, i.g, rndv);
+            const float re = fresnel(neg(rdir), nrm, 1.0f, i.eta);
+            if (gpu_rnd(rndv) < re) {
+                rorg = add(pos, scl(i.gnrm, eps));
+                rdir = reflect(rdir, nrm);
+                if (dot(rdir, i.gnrm) < 0.0f) rdir = neg(rdir);
+            } else {
+                col = mul(col, i.col);
+                break;
+            }
+        }
+    }
+    float4 qe = J.px.emi_n[p];
+    const float a = xdiv(1.0f, (float)st->eye_samples);
+    const float oma = xsub(1.0f, a);
+    qe.x = xadd(xmul(qe.x, oma), xmul(emi.x, a));
+    qe.y = xadd(xmul(qe.y, oma), xmul(emi.y, a));
+    qe.z = xadd(xmul(qe.z, oma), xmul(emi.z, a));
+    J.px.pos[p] = f4(pos, rdir.x);
+    J.px.refl[p] = f4(col, rdir.y);
+    J.px.nrm[p] = f4(nrm, rdir.z);
+    J.px.rng[p] = rndv;
+    J.px.tri[p] = last.tri;
+    J.px.t[p] = last.t;
+    J.px.emi_n[p] = qe;
+    warp_bbox_atomics(st, pos, k);
+    // segment count and errors: one atomic per warp and job
+    const unsigned mask = __match_any_sync(__activemask(), k);
+    const uint32_t wsegs = __reduce_add_sync(mask, segs);
+    const uint32_t werr = __reduce_or_sync(mask, err);
+    if ((threadIdx.x & 31) == (__ffs(mask) - 1)) {
+        atomicAdd(&st->eye_segments, (unsigned long long)wsegs);
+        if (werr) atomicOr(&st->err, werr);
+    }
+}
+
+// ----------------------------------------------------------------------------------------------
+// k_grid: glslppm.cpp:292-311 for every job in an eye frame (one thread per job)
+// ----------------------------------------------------------------------------------------------
+__global__ void k_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs) {
+    const uint32_t k = grid_tid();
+    if (k >= njobs) return;
+    const JobDesc& J = jobs[job_ids[k]];
+    JobState* st = J.state;
+    float mx[3], mn[3];
+    for (int c = 0; c < 3; c++) {
+        mx[c] = key_float(st->bbmax_key[c]);
+        mn[c] = key_float(st->bbmin_key[c]);
+    }
+    float r0;
+    if (J.radius_rule == SPPM_RADIUS_DIAGONAL) {
+        r0 = J.fixed_radius;
+    } else {
+        float bbsize = 0.0f;
+        for (int c = 0; c < 3; c++) bbsize = xadd(bbsize, xsub(mx[c], mn[c]));
+        r0 = xmul(xdiv(xdiv(bbsize, 3.0f), (float)J.W), J.footprint);
+    }
+    st->initial_radius = r0;
+    for (int c = 0; c < 3; c++) {
+        st->bbmin[c] = xsub(mn[c], r0);
+        st->bbmax[c] = xadd(mx[c], r0);
+    }
+    st->grid_scale = xdiv(0.5f, r0);
+    st->hash_scale1 = xdiv(4194304.0f, st->grid_scale);
+    if (st->frame == 0) st->r0 = r0;
+}
+
+// ----------------------------------------------------------------------------------------------
+// k_photon: photontrace.fs main (:464-720), sum.fs, hash.fs + scatter.vs + correction.vs
+// ----------------------------------------------------------------------------------------------
+__device__ __forceinline__ void light_sample(const JobDesc& J, float4& rndv, f3& flux, f3& dir, f3& org, uint32_t& err) {
+    const DevScene& S = J.scene;
+    const float rnd = gpu_rnd(rndv);
+    int low = 0;
+    int high = (int)xadd(xdiv(1.0f, S.light_stride), 0.5f);
+    const int nl = (int)S.num_lights;
+    // texel of search step `mid` at texcoord (mid - 0.5)*stride: index mid-1, clamped
+    int guard = 0;
+    while (low < high) {
+        if (++guard > 64) {
+            err |= kErrWatchdogLight;
+            break;
+        }
+        const int mid = low + ((high - low) / 2);
+        const int kk = min(max(mid - 1, 0), nl - 1);
+        if (__ldg(&S.light_cdf[kk]) < rnd) low = mid + 1;
+        else high = mid;
+    }
+    const int32_t lt = __ldg(&S.light_tri[min(max(high - 1, 0), nl - 1)]);
+    const float rndv2 = gpu_rnd(rndv);
+    const float t = xsqrt(xsub(1.0f, rndv2));
+    const float sv = gpu_rnd(rndv);
+    const float a = xsub(1.0f, t);
+    const float c = xmul(sv, t);
+    const float b = xsub(t, c);
+    const float4* ts = S.tri_shade + (size_t)lt * 6;
+    const float4 r0 = __ldg(ts + 0), r1 = __ldg(ts + 1), r2 = __ldg(ts + 2);
+    const float4 r3 = __ldg(ts + 3), r4 = __ldg(ts + 4), r5 = __ldg(ts + 5);
+    const f3 V0 = mk(r1.x, r1.y, r1.z), V1 = mk(r1.w, r2.x, r2.y), V2 = mk(r2.z, r2.w, r3.x);
+    const f3 N0 = mk(r3.y, r3.z, r3.w), N1 = mk(r4.x, r4.y, r4.z), N2 = mk(r4.w, r5.x, r5.y);
+    const DevMaterial& m = S.mats[__float_as_int(r0.w)];
+    flux = scl(mk(m.color[0], m.color[1], m.color[2]), xmul(S.light_area, 3.141592f));
+    f3 o = add(add(scl(V0, a), scl(V1, b)), scl(V2, c));
+    const f3 nrm = normalize(add(add(scl(N0, a), scl(N1, b)), scl(N2, c)));
+    const f3 gnrm = mk(r0.x, r0.y, r0.z);
+    o = add(o, scl(gnrm, 1.0e-5f));
+    float rx = gpu_rnd(rndv);
+    float ry = gpu_rnd(rndv);
+    rx = xmul(6.283184f, rx);
+    ry = xsqrt(ry);
+    dir = onb(mk(xmul(sppm_fsin(rx), ry), xsqrt(xsub(1.0f, xmul(ry, ry))), xmul(sppm_fcos(rx), ry)), nrm);
+    org = o;
+}
+
+__device__ __forceinline__ void ibl_sample(const JobDesc& J, float4& rndv, f3& flux, f3& dir, f3& org) {
+    const float* bs = J.scene.bsphere;
+    const float area = xmul(xmul(12.566368f, bs[3]), bs[3]);
+    const float temp2 = xmul(6.283184f, gpu_rnd(rndv));
+    const float aaa = xsqrt(xsub(1.0f, gpu_rnd(rndv)));
+    const float sinA = sppm_fsin(aaa);
+    const float sinTemp1 = xmul(xadd(sinA, sinA), sppm_fcos(aaa));
+    f3 d = mk(xmul(sinTemp1, sppm_fcos(temp2)), xsub(1.0f, xmul(xadd(sinA, sinA), sinA)), xmul(sinTemp1, sppm_fsin(temp2)));
+    if (gpu_rnd(rndv) > 0.5f) {
+        d = mk(1.0f, 1.0f, 1.0f);
+        d.y = xadd(d.y, d.y);
+        d.z = -d.z;
+        d = normalize(d);
+        flux = scl(mk(1.0f, 1.0f, 0.7f), area);
+    } else {
+        flux = scl(mk(0.7f, 0.7f, 1.0f), area);
+    }
+    const float radius = xsqrt(gpu_rnd(rndv));
+    const float theta = xmul(6.283184f, gpu_rnd(rndv));
+    const f3 temp = mk(xmul(radius, sppm_fcos(theta)), 0.0f, xmul(radius, sppm_fsin(theta)));
+    org = add(add(onb(scl(temp, bs[3]), d), scl(d, bs[3])), mk(bs[0], bs[1], bs[2]));
+    dir = neg(d);
+}
+
+__device__ __forceinline__ void matte_bounce(float4& rndv, f3 ipos, f3 gnrm, f3 inrm, float eps, f3& rorg, f3& rdir) {
+    const float r0 = xmul(6.283184f, gpu_rnd(rndv));
+    const float r1 = xsqrt(gpu_rnd(rndv));
+    const f3 v = mk(xmul(sppm_fsin(r0), r1), xsqrt(xsub(1.0f, xmul(r1, r1))), xmul(sppm_fcos(r0), r1));
+    rorg = add(ipos, scl(gnrm, eps));
+    rdir = onb(v, inrm);
+    if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
+}
+
+__global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
+    const uint32_t g = grid_tid();
+    if (g >= ls.total) return;
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    JobState* st = J.state;
+    const DevScene& S = J.scene;
+    const uint32_t sidx = g - ls.prefix[k];
+    const float eps = 1e-6f;
+    uint32_t err = 0;
+    const uint32_t frame = st->frame;
+    float4 rndv = J.ph.rng[sidx];
+    const int2 hitin = frame == 0 ? make_int2(-1, 0) : J.ph.hit[sidx];
+    f3 flux, rorg = mk(0, 0, 0), rdir = mk(0, 0, 0);
+    bool cont;
+    uint32_t emitted;
+    float depth = xadd((float)hitin.y, 1.0f);
+    if (hitin.x < 0 || depth >= (float)J.max_path) {
+        if (S.light_area != 0.0f) light_sample(J, rndv, flux, rdir, rorg, err);
+        else ibl_sample(J, rndv, flux, rdir, rorg);
+        emitted = 1;
+        depth = 0.0f;
+        cont = true;
+    } else {
+        const float4 PP = J.ph.pos[sidx], PF = J.ph.flux[sidx], PD = J.ph.dir[sidx];
+        flux = mk(fabsf(PF.x), fabsf(PF.y), fabsf(PF.z));
+        const f3 ipos = xyz(PP);
+        f3 inrm = mk(PP.w, PF.w, PD.w);
+        const f3 pd = xyz(PD);
+        const float4 r0 = __ldg(S.tri_shade + (size_t)hitin.x * 6);
+        const f3 gnrm = mk(r0.x, r0.y, r0.z);
+        const DevMaterial& m = S.mats[__float_as_int(r0.w)];
+        f3 icol = mk(m.color[0], m.color[1], m.color[2]);
+        const int brdf = m.brdf;
+        if (brdf == 0) {
+            matte_bounce(rndv, ipos, gnrm, inrm, eps, rorg, rdir);
+        } else if (brdf == 1 || brdf == 4) {
+            rorg = add(ipos, scl(gnrm, eps));
+            if (brdf == 4) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
+            rdir = reflect(pd, inrm);
+            if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
+        } else if (brdf == 2 || brdf == 5) {
+            if (brdf == 5) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
+            const float ln = dot(inrm, pd);
+            if (ln < 0.0f) {
+                const float re = fresnel(neg(pd), inrm, 1.0f, m.eta);
+                if (gpu_rnd(rndv) < re) {
+                    rorg = add(ipos, scl(gnrm, eps));
+                    rdir = reflect(pd, inrm);
+                    icol = mk(1.0f, 1.0f, 1.0f);
+                    if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
+                } else {
+                    rorg = sub(ipos, scl(gnrm, eps));
+                    rdir = refract(pd, inrm, xdiv(1.0f, m.eta));
+                    if (dot(rdir, gnrm) > 0.0f) rdir = neg(rdir);
+                }
+            } else {
+                const float re = fresnel(neg(pd), neg(inrm), m.eta, 1.0f);
+                if (gpu_rnd(rndv) < re) {
+                    rorg = sub(ipos, scl(gnrm, eps));
+                    rdir = reflect(pd, neg(inrm));
+                    if (dot(rdir, neg(gnrm)) < 0.0f) rdir = neg(rdir);
+                } else {
+                    rorg = add(ipos, scl(gnrm, eps));
+                    rdir = refract(pd, neg(inrm), m.eta);
+                    if (dot(rdir, neg(gnrm)) > 0.0f) rdir = neg(rdir);
+                }
+            }
+        } else if (brdf == 3 || brdf == 6) {
+            if (brdf == 6) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
+            const float re = fresnel(neg(pd), inrm, 1.0f, m.eta);
+            if (gpu_rnd(rndv) < re) {
+                rorg = add(ipos, scl(gnrm, eps));
+                rdir = reflect(pd, inrm);
+                icol = mk(1.0f, 1.0f, 1.0f);
+                if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
+            } else {
+                matte_bounce(rndv, ipos, gnrm, inrm, eps, rorg, rdir);
+            }
+        }
+        // Russian roulette (:671-685)
+        const float pmax = fmaxf(fmaxf(icol.x, icol.y), icol.z);
+        if (pmax < gpu_rnd(rndv)) {
+            cont = false;
+        } else {
+            cont = true;
+            icol = mk(xdiv(icol.x, pmax), xdiv(icol.y, pmax), xdiv(icol.z, pmax));
+            flux = mul(flux, icol);
+        }
+        emitted = 0;
+    }
+    bool store = false;
+    f3 ppos = mk(0, 0, 0);
+    if (cont) {
+        const Hit h = trace_exact<true>(S, rorg, rdir, false, err);
+        f3 pnrm = mk(0, 0, 0), pg = mk(0, 0, 0);
+        int brdf = 0;
+        if (h.tri >= 0) {
+            const Shade i = shade_hit(S, h);
+            ppos = i.pos;
+            pnrm = i.nrm;
+            pg = i.gnrm;
+            brdf = i.brdf;
+        }
+        if (h.tri < 0 || (brdf != 0 && brdf != 6 && brdf != 3)) flux = neg(flux);
+        const float gf = fminf(fabsf(xdiv(dot(rdir, pnrm), dot(rdir, pg))), 2.236068010e+00f);
+        flux = scl(flux, gf);
+        J.ph.pos[sidx] = f4(ppos, pnrm.x);
+        J.ph.flux[sidx] = f4(flux, pnrm.y);
+        J.ph.dir[sidx] = f4(rdir, pnrm.z);
+        J.ph.hit[sidx] = make_int2(h.tri, (int)depth);
+        store = !(flux.x < 0.0f);
+    } else {
+        J.ph.pos[sidx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        J.ph.flux[sidx] = make_float4(-1.0f, -1.0f, -1.0f, 0.0f);
+        J.ph.dir[sidx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        J.ph.hit[sidx] = make_int2(-1, 0);
+    }
+    J.ph.rng[sidx] = rndv;
+
+    // ---- hashed grid build (hash.fs main :51-68, scatter.vs :11-23, correction.vs :8-13) ----
+    uint32_t slot = 0xFFFFFFFFu;
+    if (store) {
+        const f3 cell = mk(floorf(xmul(xsub(ppos.x, st->bbmin[0]), st->grid_scale)),
+                           floorf(xmul(xsub(ppos.y, st->bbmin[1]), st->grid_scale)),
+                           floorf(xmul(xsub(ppos.z, st->bbmin[2]), st->grid_scale)));
+        slot = hash_cell(cell, st->grid_scale, st->hash_scale1, (float)J.hash_num);
+    }
+    // photon index order = depth order; photons of the last row with i >= w/2 have z >= 1 and
+    // are clipped by the scatter draw (counted by the correction draw all the same)
+    const bool clipped = (J.flags & SPPM_FLAG_GL_DEPTH_CLIP) && sidx >= (J.PH - 1) * J.PW + (J.PW + 1) / 2;
+    const unsigned active = __activemask();
+    // slot keys are unique per job: combine job index and slot in 64 bits
+    const unsigned long long key = store ? ((unsigned long long)k << 32) | slot : ~0ull;
+    const unsigned peers = __match_any_sync(active, key);
+    if (store) {
+        const uint32_t n = __popc(peers);
+        const uint32_t wmin = __reduce_min_sync(peers, clipped ? 0xFFFFFFFFu : sidx);
+        if ((threadIdx.x & 31) == (__ffs(peers) - 1)) {
+            atomicAdd(&J.count[slot], n);
+            if (wmin != 0xFFFFFFFFu) atomicMin(&J.winner[slot], wmin);
+        }
+    }
+    // ---- sum.fs: emitted photons; traced segments; errors (one atomic per warp and job) ----
+    const unsigned jm = __match_any_sync(active, k);
+    const uint32_t we = __reduce_add_sync(jm, emitted);
+    const uint32_t ws = __reduce_add_sync(jm, cont ? 1u : 0u);
+    const uint32_t wr = __reduce_or_sync(jm, err);
+    if ((threadIdx.x & 31) == (__ffs(jm) - 1)) {
+        if (we) atomicAdd(&st->emitted_frame, we);
+        if (ws) atomicAdd(&st->segments_frame, ws);
+        if (wr) atomicOr(&st->err, wr);
+    }
+}
+
+// ----------------------------------------------------------------------------------------------
+// k_gather: progressive.fs (:98-142, AccumulatePhotons :65-95)
+// ----------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_gather(LaunchSet ls) {
+    const uint32_t g = grid_tid();
+    if (g >= ls.total) return;
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    JobState* st = J.state;
+    const uint32_t p = g - ls.prefix[k];
+    const uint32_t frame = st->frame;
+    if (p == 0) {
+        // NumPhotons += int(sum) (glslppm.cpp:397) once the photon pass of this frame is done
+        const uint32_t e = st->emitted_frame;
+        st->num_photons_f32 = xadd(st->num_photons_f32, (float)(int)e);
+        st->num_photons += e;
+        st->photon_segments += st->segments_frame;
+    }
+    float4 qfr = frame == 0 ? make_float4(0.0f, 0.0f, 0.0f, st->r0) : J.px.flux_r[p];
+    float4 qe = J.px.emi_n[p];
+    if (J.px.tri[p] >= 0) {
+        const float G = st->grid_scale;
+        const float hs1 = st->hash_scale1;
+        const float hn = (float)J.hash_num;
+        const float alpha = J.alpha;
+        const f3 bbmin = mk(st->bbmin[0], st->bbmin[1], st->bbmin[2]);
+        const f3 qp = xyz(J.px.pos[p]), qn = xyz(J.px.nrm[p]), qr = xyz(J.px.refl[p]);
+        float N = qe.w, R = qfr.w;
+        f3 tau = xyz(qfr);
+        const f3 ii = mk(floorf(xsub(xmul(fabsf(xsub(qp.x, bbmin.x)), G), 0.5f)),
+                         floorf(xsub(xmul(fabsf(xsub(qp.y, bbmin.y)), G), 0.5f)),
+                         floorf(xsub(xmul(fabsf(xsub(qp.z, bbmin.z)), G), 0.5f)));
+        f3 flux = mk(0, 0, 0);
+        float M = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const f3 cell = mk(xadd(ii.x, (float)(c & 1)), xadd(ii.y, (float)((c >> 1) & 1)), xadd(ii.z, (float)(c >> 2)));
+            const uint32_t slot = hash_cell(cell, G, hs1, hn);
+            const uint32_t w = J.winner[slot];
+            if (w == kEmptySlot) continue;  // the cleared texel: photon 0 weighted by count 0
+            const float4 pp = J.ph.pos[w];
+            const f3 rmin = mk(xadd(xdiv(cell.x, G), bbmin.x), xadd(xdiv(cell.y, G), bbmin.y), xadd(xdiv(cell.z, G), bbmin.z));
+            const f3 rmax = mk(xadd(xdiv(xadd(cell.x, 1.0f), G), bbmin.x), xadd(xdiv(xadd(cell.y, 1.0f), G), bbmin.y),
+                               xadd(xdiv(xadd(cell.z, 1.0f), G), bbmin.z));
+            if (pp.x > rmin.x && pp.y > rmin.y && pp.z > rmin.z && pp.x < rmax.x && pp.y < rmax.y && pp.z < rmax.z) {
+                const f3 diff = sub(xyz(pp), qp);
+                const float4 pd = J.ph.dir[w];
+                if (length(diff) < R && dot(qn, neg(xyz(pd))) > 0.0f) {
+                    const float4 pf = J.ph.flux[w];
+                    const float cnt = (float)J.count[slot];
+                    flux = add(flux, scl(xyz(pf), cnt));
+                    M = xadd(M, cnt);
+                }
+            }
+        }
+        flux = mul(flux, scl(qr, 3.183099627e-01f));
+        const float gg = fminf(xdiv(xadd(N, xmul(alpha, M)), xadd(N, M)), 1.0f);
+        R = xmul(R, xsqrt(gg));
+        N = xadd(N, xmul(M, alpha));
+        tau = scl(add(tau, flux), gg);
+        qfr = f4(tau, R);
+        qe.w = N;
+        J.px.emi_n[p] = qe;
+    }
+    J.px.flux_r[p] = qfr;
+}
+
+// ----------------------------------------------------------------------------------------------
+// k_resolve: re.fs
+// ----------------------------------------------------------------------------------------------
+__global__ void k_resolve(LaunchSet ls, uint32_t display) {
+    const uint32_t g = grid_tid();
+    if (g >= ls.total) return;
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    const uint32_t p = g - ls.prefix[k];
+    const float4 fr = J.px.flux_r[p];
+    const float4 qe = J.px.emi_n[p];
+    const float total = J.state->num_photons_f32;
+    const float den = xmul(xmul(xmul(fr.w, fr.w), 3.141592f), total);
+    float L[3] = {xadd(xdiv(fr.x, den), qe.x), xadd(xdiv(fr.y, den), qe.y), xadd(xdiv(fr.z, den), qe.z)};
+    for (int c = 0; c < 3; c++) {
+        float v = L[c];
+        if (display) {
+            v = xsub(1.0f, sppm_fexp(xmul(-v, 60000.0f)));
+            if (v < 0.0031308f) v = xmul(12.92f, v);
+            else v = xsub(xmul(xadd(1.0f, 0.055f), sppm_fpow(v, 0.416666666667f)), 0.055f);
+        }
+        J.image[(size_t)p * 3 + c] = v;
+    }
+}
+
+// ----------------------------------------------------------------------------------------------
+// stage-level hash build on caller arrays (sppm_hash_build)
+// ----------------------------------------------------------------------------------------------
+__global__ void k_hash_clear(uint32_t* winner, uint32_t* count, uint32_t n) {
+    const uint32_t g = grid_tid();
+    if (g < n) {
+        winner[g] = kEmptySlot;
+        count[g] = 0;
+    }
+}
+
+__global__ void k_hash_build(const float4* pos, const float4* flux, uint32_t pw, uint32_t ph, uint32_t hash_num,
+                             float bx, float by, float bz, float G, uint32_t flags, uint32_t* winner, uint32_t* count) {
+    const uint32_t id = grid_tid();
+    if (id >= pw * ph) return;
+    const float hs1 = xdiv(4194304.0f, G);
+    const float4 f = flux[id];
+    const bool store = !(f.x < 0.0f);
+    uint32_t slot = 0;
+    if (store) {
+        const float4 pp = pos[id];
+        const f3 cell = mk(floorf(xmul(xsub(pp.x, bx), G)), floorf(xmul(xsub(pp.y, by), G)), floorf(xmul(xsub(pp.z, bz), G)));
+        slot = hash_cell(cell, G, hs1, (float)hash_num);
+    }
+    const bool clipped = (flags & SPPM_FLAG_GL_DEPTH_CLIP) && id >= (ph - 1) * pw + (pw + 1) / 2;
+    const unsigned peers = __match_any_sync(__activemask(), store ? slot : 0xFFFFFFFFu);
+    if (store) {
+        const uint32_t n = __popc(peers);
+        const uint32_t wmin = __reduce_min_sync(peers, clipped ? 0xFFFFFFFFu : id);
+        if ((threadIdx.x & 31) == (__ffs(peers) - 1)) {
+            atomicAdd(&count[slot], n);
+            if (wmin != 0xFFFFFFFFu) atomicMin(&winner[slot], wmin);
+        }
+    }
+}
+
+// pinned math on the device, for the accuracy / determinism tests
+__global__ void k_fpmath(int fn, const float* x, const float* y, float* out, uint32_t n) {
+    const uint32_t i = grid_tid();
+    if (i >= n) return;
+    float r;
+    switch (fn) {
+        case 0: r = sppm_fsin(x[i]); break;
+        case 1: r = sppm_fcos(x[i]); break;
+        case 2: r = sppm_fpow(x[i], y[i]); break;
+        case 3: r = sppm_fexp(x[i]); break;
+        case 4: r = sppm_flog2(x[i]); break;
+        default: r = sppm_fexp2(x[i]); break;
+    }
+    out[i] = r;
+}
+
+// ----------------------------------------------------------------------------------------------
+// launchers
+// ----------------------------------------------------------------------------------------------
+static inline uint32_t blocks_for(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
+
+void launch_frame_begin(const LaunchSet& ls, cudaStream_t s) {
+    if (ls.total) k_frame_begin<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls);
+}
+void launch_eye_fp32(const LaunchSet& ls, cudaStream_t s) {
+    if (ls.total) k_eye<<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
+}
+void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s) {
+    if (njobs) k_grid<<<blocks_for(njobs, 64), 64, 0, s>>>(jobs, job_ids, njobs);
+}
+void launch_photon_fp32(const LaunchSet& ls, cudaStream_t s) {
+    if (ls.total) k_photon<<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
+}
+void launch_gather_fp32(const LaunchSet& ls, cudaStream_t s) {
+    if (ls.total) k_gather<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls);
+}
+void launch_resolve_fp32(const LaunchSet& ls, uint32_t display, cudaStream_t s) {
+    if (ls.total) k_resolve<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls, display);
+}
+void launch_hash_build(const float4* pos, const float4* flux, uint32_t pw, uint32_t ph, uint32_t hash_num,
+                       const float bbmin[3], float G, uint32_t flags, uint32_t* winner, uint32_t* count, cudaStream_t s) {
+    k_hash_clear<<<blocks_for(hash_num, 256), 256, 0, s>>>(winner, count, hash_num);
+    const uint32_t n = pw * ph;
+    if (n) k_hash_build<<<blocks_for(n, 256), 256, 0, s>>>(pos, flux, pw, ph, hash_num, bbmin[0], bbmin[1], bbmin[2], G, flags, winner, count);
+}
+void launch_fpmath(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t s) {
+    if (n) k_fpmath<<<blocks_for(n, 256), 256, 0, s>>>(fn, x, y, out, n);
+}
+
+}  // namespace sppm_dev

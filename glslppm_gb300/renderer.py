@@ -1,0 +1,299 @@
+"""Host-side mirror of the reference's interface for the SPPM path.
+
+``Mesh`` plays the part of ``TMesh`` + ``TBVH`` (mesh.cpp, bvh.cpp): OBJ/MTL loading or flat
+arrays, and the six threaded BVH orderings.  ``Renderer`` plays the part of ``CGPURT``
+(gpurt.h:29-67) together with the frame driver ``m_display`` (glslppm.cpp:214-536): upload the
+scene (``precalculate_mesh_data``), set the camera, run SPPM frames (``display``), read the image
+(``re.fs``) and any state texture.  Every call goes through the C ABI of ``libsppm.so``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import native as N
+
+
+def _fptr(a: np.ndarray, ctype=C.c_float):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def default_config(resolution: int = 512, **overrides) -> N.Config:
+    """The reference's constants (glslppm.cpp:28-40, 488) for a square image; keyword overrides."""
+    cfg = N.Config()
+    N.lib.sppm_config_defaults(C.byref(cfg), resolution)
+    for k, v in overrides.items():
+        if not hasattr(cfg, k):
+            raise AttributeError(f"sppm_config has no field {k!r}")
+        setattr(cfg, k, v)
+    return cfg
+
+
+def look_at(origin, lookat, width: int, height: int, fov_degrees: float = 45.0) -> N.Camera:
+    """TCamera::Set (camera.cpp:4-18)."""
+    cam = N.Camera()
+    o = (C.c_float * 3)(*origin)
+    l = (C.c_float * 3)(*lookat)
+    N.lib.sppm_camera_look_at(C.byref(cam), o, l, width, height, C.c_float(fov_degrees))
+    return cam
+
+
+@dataclass
+class SceneArrays:
+    """Copies of the arrays an sppm_scene points to (for tests and fixtures)."""
+
+    positions: np.ndarray
+    normals: np.ndarray
+    texcoords: np.ndarray
+    material_ids: np.ndarray
+    materials: np.ndarray  # structured: color[3], eta, brdf, glossiness
+    light_triangles: np.ndarray
+    light_cdf: np.ndarray
+    light_area: float
+    bbox_min: np.ndarray
+    bbox_max: np.ndarray
+    node_bounds: np.ndarray
+    node_triangle: np.ndarray
+    order_base: np.ndarray
+    order_miss: np.ndarray
+
+
+MATERIAL_DTYPE = np.dtype([("color", "<f4", 3), ("eta", "<f4"), ("brdf", "<i4"), ("glossiness", "<f4")])
+
+
+class Mesh:
+    """An sppm_mesh: triangles, materials, light table and (after build_bvh) the BVH."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def load_obj(cls, path: str, offset=(0.0, 0.0, 0.0), scale: float = 1.0) -> "Mesh":
+        out = C.c_void_p()
+        off = (C.c_float * 3)(*offset)
+        N.check(N.lib.sppm_mesh_load_obj(str(path).encode(), off, C.c_float(scale), C.byref(out)))
+        return cls(out.value)
+
+    @classmethod
+    def from_arrays(cls, positions, material_ids, materials, normals=None) -> "Mesh":
+        pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)
+        mid = np.ascontiguousarray(material_ids, dtype=np.int32).reshape(-1)
+        mats = np.ascontiguousarray(materials, dtype=MATERIAL_DTYPE)
+        nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 9)
+        if len(mid) != len(pos):
+            raise ValueError("one material id per triangle")
+        out = C.c_void_p()
+        N.check(N.lib.sppm_mesh_from_arrays(len(pos), pos.ctypes.data, None if nrm is None else nrm.ctypes.data,
+                                            mid.ctypes.data, len(mats), mats.ctypes.data, C.byref(out)))
+        return cls(out.value)
+
+    def build_bvh(self) -> "Mesh":
+        N.check(N.lib.sppm_mesh_build_bvh(self._h))
+        return self
+
+    def scene(self) -> N.Scene:
+        s = N.Scene()
+        N.check(N.lib.sppm_mesh_get_scene(self._h, C.byref(s)))
+        s._owner = self  # keep the mesh alive while the struct is in use
+        return s
+
+    def arrays(self) -> SceneArrays:
+        s = self.scene()
+        n, nn, nm, nl = s.num_triangles, s.num_nodes, s.num_materials, s.num_lights
+
+        def grab(ptr, count, dtype):
+            if count == 0 or not ptr:
+                return np.zeros(0, dtype=dtype)
+            return np.ctypeslib.as_array(ptr, shape=(count,)).astype(dtype).copy()
+
+        mats = np.zeros(nm, dtype=MATERIAL_DTYPE)
+        C.memmove(mats.ctypes.data, s.materials, nm * MATERIAL_DTYPE.itemsize)
+        return SceneArrays(
+            positions=grab(s.positions, n * 9, np.float32).reshape(n, 3, 3),
+            normals=grab(s.normals, n * 9, np.float32).reshape(n, 3, 3),
+            texcoords=grab(s.texcoords, n * 6, np.float32).reshape(n, 3, 2),
+            material_ids=grab(s.material_ids, n, np.int32),
+            materials=mats,
+            light_triangles=grab(s.light_triangles, nl, np.int32),
+            light_cdf=grab(s.light_cdf, nl, np.float32),
+            light_area=float(s.light_area),
+            bbox_min=np.array(list(s.bbox_min), dtype=np.float32),
+            bbox_max=np.array(list(s.bbox_max), dtype=np.float32),
+            node_bounds=grab(s.node_bounds, nn * 6, np.float32).reshape(nn, 6),
+            node_triangle=grab(s.node_triangle, nn, np.int32),
+            order_base=grab(s.order_base, nn * 6, np.int32).reshape(6, nn),
+            order_miss=grab(s.order_miss, nn * 6, np.int32).reshape(6, nn),
+        )
+
+    @property
+    def num_triangles(self) -> int:
+        return int(self.scene().num_triangles)
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            N.lib.sppm_mesh_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def scene_from_arrays(a: SceneArrays) -> N.Scene:
+    """An sppm_scene pointing at numpy arrays (kept alive by the returned struct)."""
+    keep = {}
+
+    def arr(x, dtype):
+        x = np.ascontiguousarray(x, dtype=dtype)
+        keep[id(x)] = x
+        return x
+
+    s = N.Scene()
+    pos = arr(a.positions, np.float32)
+    s.num_triangles = pos.shape[0]
+    s.positions = _fptr(pos)
+    s.normals = _fptr(arr(a.normals, np.float32))
+    s.texcoords = _fptr(arr(a.texcoords, np.float32))
+    s.material_ids = _fptr(arr(a.material_ids, np.int32), C.c_int32)
+    mats = arr(a.materials, MATERIAL_DTYPE)
+    s.num_materials = len(mats)
+    s.materials = C.cast(mats.ctypes.data, C.POINTER(N.Material))
+    lt = arr(a.light_triangles, np.int32)
+    s.num_lights = len(lt)
+    s.light_triangles = _fptr(lt, C.c_int32)
+    s.light_cdf = _fptr(arr(a.light_cdf, np.float32))
+    s.light_area = float(a.light_area)
+    for k in range(3):
+        s.bbox_min[k] = float(a.bbox_min[k])
+        s.bbox_max[k] = float(a.bbox_max[k])
+    nb = arr(a.node_bounds, np.float32)
+    s.num_nodes = nb.shape[0]
+    s.node_bounds = _fptr(nb)
+    s.node_triangle = _fptr(arr(a.node_triangle, np.int32), C.c_int32)
+    s.order_base = _fptr(arr(a.order_base, np.int32), C.c_int32)
+    s.order_miss = _fptr(arr(a.order_miss, np.int32), C.c_int32)
+    s._keep = keep
+    return s
+
+
+class Renderer:
+    """One SPPM render job on one GPU (CGPURT + m_display)."""
+
+    def __init__(self, config: N.Config, device: int = 0):
+        self.config = config
+        out = C.c_void_p()
+        N.check(N.lib.sppm_create(C.byref(config), device, C.byref(out)))
+        self._h = out
+        self.width, self.height = config.width, config.height
+
+    # CGPURT::PrecalculateMeshData + CreateTextures
+    def upload_scene(self, scene) -> None:
+        if isinstance(scene, Mesh):
+            scene = scene.scene()
+        elif isinstance(scene, SceneArrays):
+            scene = scene_from_arrays(scene)
+        N.check(N.lib.sppm_upload_scene(self._h, C.byref(scene)))
+
+    precalculate_mesh_data = upload_scene
+
+    def set_camera(self, cam: N.Camera) -> None:
+        N.check(N.lib.sppm_set_camera(self._h, C.byref(cam)))
+
+    def reset(self) -> None:
+        N.check(N.lib.sppm_reset(self._h))
+
+    def run_passes(self, n: int = 1) -> None:
+        N.check(N.lib.sppm_run_passes(self._h, n))
+
+    def display(self) -> None:
+        """One SPPM frame (m_display)."""
+        self.run_passes(1)
+
+    def synchronize(self) -> None:
+        N.check(N.lib.sppm_synchronize(self._h))
+
+    def read_image(self, kind: int = N.IMAGE_RADIANCE, out: np.ndarray | None = None) -> np.ndarray:
+        n = self.width * self.height * 3
+        if out is None:
+            out = np.empty((self.height, self.width, 3), dtype=np.float32)
+        N.check(N.lib.sppm_read_image(self._h, kind, out.ctypes.data, n))
+        return out
+
+    def state_bytes(self, kind: str) -> int:
+        return int(N.lib.sppm_state_bytes(self._h, N.STATE[kind]))
+
+    def read_state(self, kind: str) -> np.ndarray:
+        k = N.STATE[kind]
+        nbytes = self.state_bytes(kind)
+        if nbytes == 0:
+            raise N.SppmError(N.ERR_ARG, f"state {kind} is not kept by this context")
+        if kind in ("hit_triangle",):
+            out = np.empty(nbytes // 4, dtype=np.int32)
+        elif kind in ("slot_winner", "slot_count"):
+            out = np.empty(nbytes // 4, dtype=np.uint32)
+        elif kind == "photon_hit":
+            out = np.empty((nbytes // 8, 2), dtype=np.int32)
+        elif kind == "hit_t":
+            out = np.empty(nbytes // 4, dtype=np.float32)
+        elif kind.startswith("stats_"):
+            out = np.empty(nbytes // 8, dtype=np.float64)
+        else:
+            out = np.empty((nbytes // 16, 4), dtype=np.float32)
+        N.check(N.lib.sppm_read_state(self._h, k, out.ctypes.data, nbytes))
+        return out
+
+    def frame_info(self) -> N.FrameInfo:
+        fi = N.FrameInfo()
+        N.check(N.lib.sppm_get_frame_info(self._h, C.byref(fi)))
+        return fi
+
+    def enable_stage_timing(self, enable: bool = True) -> None:
+        N.check(N.lib.sppm_enable_stage_timing(self._h, 1 if enable else 0))
+
+    def read_stage_times(self) -> dict:
+        ms = (C.c_float * len(N.STAGES))()
+        n = (C.c_uint32 * len(N.STAGES))()
+        N.check(N.lib.sppm_read_stage_times(self._h, ms, n))
+        return {name: (float(ms[i]), int(n[i])) for i, name in enumerate(N.STAGES)}
+
+    def time_passes(self, n: int) -> float:
+        ms = C.c_float()
+        N.check(N.lib.sppm_time_passes(self._h, n, C.byref(ms)))
+        return float(ms.value)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            N.lib.sppm_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def hash_build(d_pos: int, d_flux: int, photon_width: int, photon_height: int, hash_slots: int, bbox_min,
+               grid_scale: float, flags: int, d_winner: int, d_count: int, stream: int = 0) -> None:
+    """Stage-level hashed-grid build on device pointers (sppm_hash_build)."""
+    bb = (C.c_float * 3)(*bbox_min)
+    N.check(N.lib.sppm_hash_build(d_pos, d_flux, photon_width, photon_height, hash_slots, bb, C.c_float(grid_scale),
+                                  flags, d_winner, d_count, stream))
+
+
+def debug_fpmath(fn: int, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    yy = None if y is None else np.ascontiguousarray(y, dtype=np.float32)
+    out = np.empty_like(x)
+    N.check(N.lib.sppm_debug_fpmath(fn, x.ctypes.data, None if yy is None else yy.ctypes.data, out.ctypes.data, x.size))
+    return out

@@ -1,0 +1,268 @@
+/*
+ * sppm.h -- C ABI of the GB300 (sm_103a) stochastic progressive photon mapping path.
+ *
+ * This library replaces the OpenGL shader path of glslppm (T. Hachisuka, Tokyo Demo Fest 2015,
+ * modified by tigrazone).  In the reference, the host class CGPURT (gpurt.h:29-67) packs the
+ * scene built by TMesh (mesh.cpp) and TBVH (bvh.cpp) into RGBA32F textures, and m_display()
+ * (glslppm.cpp:214-536) drives one SPPM frame as a chain of fragment/vertex-shader draws:
+ *
+ *   eyeraytrace.fs -> ReduceTexture(max/min) -> photontrace.fs -> ReduceTexture(sum)
+ *   -> hash.fs -> scatter.vs/.fs (depth test) -> correction.vs/.fs (blend) -> progressive.fs
+ *   -> re.fs
+ *
+ * Every entry point below takes plain pointers and sizes; no GL, torch or C++ type crosses the
+ * boundary.  All entry points return an sppm_status (0 = success); the message of the last
+ * failure on the calling thread is available from sppm_last_error().  No entry point calls
+ * exit() or lets a C++ exception escape.
+ *
+ * Threading: a context is used by one host thread at a time.  Work is queued on the context's
+ * CUDA stream; sppm_synchronize() waits for it and reports device-side errors (for example a
+ * BVH traversal that exceeded its step bound because the scene's links are corrupt).
+ */
+#ifndef SPPM_H
+#define SPPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPPM_ABI_VERSION 1
+
+/* ---- status codes ----------------------------------------------------------------------------- */
+typedef enum sppm_status {
+    SPPM_OK = 0,
+    SPPM_ERR_ARG = 1,         /* invalid argument (null pointer, size mismatch, bad enum)          */
+    SPPM_ERR_OOM = 2,         /* device or host allocation failed, or admission limit exceeded     */
+    SPPM_ERR_CUDA = 3,        /* a CUDA runtime call failed                                         */
+    SPPM_ERR_WATCHDOG = 4,    /* a bounded device loop gave up (corrupt BVH links, bad light table) */
+    SPPM_ERR_STATE = 5,       /* call out of order (e.g. run before a scene is uploaded)            */
+    SPPM_ERR_IO = 6,          /* file could not be opened or parsed                                 */
+    SPPM_ERR_UNSUPPORTED = 7, /* feature not available in this build                                */
+    SPPM_ERR_NO_DEVICE = 8    /* no CUDA device                                                     */
+} sppm_status;
+
+/* ---- configuration ---------------------------------------------------------------------------- */
+typedef enum sppm_precision {
+    /* Plain FP32: every operation of the reference shaders in IEEE single precision, in the order
+       the shaders write it, transcendentals from sppm_fpmath.h.  Bit-identical to the CPU
+       restatement of the shaders. */
+    SPPM_PRECISION_FP32 = 0,
+    /* Mixed: FMA-contracted traversal over outward-rounded quantised child boxes, photon flux
+       and direction stored in FP16, flux gathered in FP32, per-pixel N, R^2 and tau in FP64. */
+    SPPM_PRECISION_MIXED = 1
+} sppm_precision;
+
+typedef enum sppm_radius_rule {
+    /* InitialRadius = (mean extent of the hit-point bounding box) / width * footprint,
+       recomputed after every eye pass (glslppm.cpp:294-311). */
+    SPPM_RADIUS_FOOTPRINT = 0,
+    /* InitialRadius = radius_fraction * |scene bbox diagonal| (a fixed radius). */
+    SPPM_RADIUS_DIAGONAL = 1
+} sppm_radius_rule;
+
+typedef enum sppm_seed_mode {
+    /* Xorshift128 fills the eye, then the photon random-state tables at start, row-major, and
+       draws the anti-aliasing offset of each eye pass (glslppm.cpp:77-140, 276-278).  With
+       seed = 0 the stream starts from the reference's constants. */
+    SPPM_SEED_XORSHIFT = 0,
+    /* Per-pixel and per-photon state from an integer hash of (seed, index): no host fill. */
+    SPPM_SEED_HASH = 1
+} sppm_seed_mode;
+
+/* Flags */
+#define SPPM_FLAG_GL_DEPTH_CLIP 0x1u /* scatter.vs: photons whose depth z >= 1 (last row, i >= w/2)
+                                        are counted but never become a slot's stored photon */
+
+typedef struct sppm_config {
+    uint32_t width, height;               /* image (ImageResolution x ImageResolution in the ref)  */
+    uint32_t photon_width, photon_height; /* photon slots, P = w*h per pass (PhotonBufferSize^2)  */
+    uint32_t hash_slots;                  /* HashNum; 0 means P (HashResolution^2 in the ref)      */
+    uint32_t max_path_length;             /* MaxNumberOfBounces = 10 (glslppm.cpp:36)              */
+    uint32_t eye_pass_interval;           /* eye pass every N frames; 10 in the ref (:238)         */
+    float alpha;                          /* 0.7 (glslppm.cpp:488)                                 */
+    float initial_footprint;              /* 2.5 (glslppm.cpp:40)                                  */
+    uint32_t radius_rule;                 /* sppm_radius_rule                                      */
+    float radius_fraction;                /* for SPPM_RADIUS_DIAGONAL                              */
+    uint32_t precision;                   /* sppm_precision                                        */
+    uint32_t seed_mode;                   /* sppm_seed_mode                                        */
+    uint32_t seed;                        /* 0 = the reference's xorshift constants                */
+    uint32_t flags;                       /* SPPM_FLAG_*                                           */
+    float focal_length;                   /* 13 (glslppm.cpp:31)                                   */
+    float aperture;                       /* 0  (glslppm.cpp:32)                                   */
+} sppm_config;
+
+/* Fills *cfg with the reference's constants for a square image of side `resolution`. */
+void sppm_config_defaults(sppm_config* cfg, uint32_t resolution);
+
+/* ---- scene -------------------------------------------------------------------------------------
+ * Mirrors TMesh (mesh.h:49-67) and TBVH (bvh.h:24-33) after TMesh::LoadOBJ and TBVH::Build.
+ * Material fields are the ones CGPURT::CreateTextures packs (gpurt.cpp:109-132).               */
+typedef struct sppm_material {
+    float color[3];   /* TMaterial::color (diffuse already x0.9 for brdf 0/3, mesh.cpp:591-594) */
+    float eta;        /* TMaterial::eta                                                         */
+    int32_t brdf;     /* -1 light, 0 matte, 1 mirror, 2 glass, 3 plastic, 4/5/6 glossy, 7 sss   */
+    float glossiness; /* 1/((2/(1-specularity))^2.71828 + 1), the packed g (gpurt.cpp:126)      */
+} sppm_material;
+
+typedef struct sppm_scene {
+    uint32_t num_triangles;
+    const float* positions;       /* [n][3 vertices][xyz]  TTriangle::positions                  */
+    const float* normals;         /* [n][3][xyz]           TTriangle::normals                    */
+    const float* texcoords;       /* [n][3][uv] or NULL    TTriangle::texcoords (1e30 = none)    */
+    const int32_t* material_ids;  /* [n]                   TTriangle::idMaterial                 */
+    uint32_t num_materials;
+    const sppm_material* materials;
+    uint32_t num_lights;
+    const int32_t* light_triangles; /* TMesh::lightsIndices                                      */
+    const float* light_cdf;         /* TMesh::lightsCDF (normalised, ascending)                  */
+    float light_area;               /* TMesh::lightsArea; 0 means image-based light (IBL)        */
+    float bbox_min[3], bbox_max[3]; /* TMesh::bbox                                               */
+    /* TBVH after Build(): 2n-1 nodes; node arrays of the canonical ordering (face 0) ... */
+    uint32_t num_nodes;
+    const float* node_bounds;      /* [num_nodes][6] = min xyz, max xyz of nodes[0][i].bbox      */
+    const int32_t* node_triangle;  /* [num_nodes] nodes[0][i].idTriangle for leaves, -1 else     */
+    /* ... and for each of the 6 orderings o (+x,-x,+y,-y,+z,-z), the traversal sequence:      */
+    const int32_t* order_base;     /* [6][num_nodes] nodes[o][i].idBase (canonical id)           */
+    const int32_t* order_miss;     /* [6][num_nodes] nodes[o][i].idMiss (index in ordering o)    */
+} sppm_scene;
+
+/* Camera as the eye pass consumes it (glslppm.cpp:259-273): TCamera after TCamera::Set. */
+typedef struct sppm_camera {
+    float origin[3];
+    float u[3], v[3], w[3];
+    float distance;
+    uint32_t width, height;
+} sppm_camera;
+
+/* TCamera::Set (camera.cpp:4-18): look-at basis and distance = H / (2 tan(fov/2)). */
+void sppm_camera_look_at(sppm_camera* cam, const float origin[3], const float lookat[3],
+                         uint32_t width, uint32_t height, float fov_degrees);
+
+/* ---- host-side scene construction (what mesh.cpp and bvh.cpp do in the reference) ------------- */
+typedef struct sppm_mesh sppm_mesh; /* owns the arrays an sppm_scene points into */
+
+/* TMesh::LoadOBJ (mesh.cpp:491-693): OBJ + MTL, triangles only, positions*scale+offset. */
+int sppm_mesh_load_obj(const char* path, const float offset[3], float scale, sppm_mesh** out);
+/* Builds a mesh from flat arrays (positions [n][3][3], normals may be NULL -> face normals);
+   materials as in sppm_material; light table derived like TMesh::PrepareLightSources. */
+int sppm_mesh_from_arrays(uint32_t num_triangles, const float* positions, const float* normals,
+                          const int32_t* material_ids, uint32_t num_materials,
+                          const sppm_material* materials, sppm_mesh** out);
+/* TBVH::Build (bvh.cpp:244-317): exact-SAH binary BVH, one triangle per leaf, 6 threaded
+   orderings.  Stores the node arrays in the mesh. */
+int sppm_mesh_build_bvh(sppm_mesh* mesh);
+/* Fills *scene with pointers into the mesh (valid until sppm_mesh_destroy). */
+int sppm_mesh_get_scene(const sppm_mesh* mesh, sppm_scene* scene);
+void sppm_mesh_destroy(sppm_mesh* mesh);
+
+/* ---- render context: one scene, one camera, one progressive state ------------------------------ */
+typedef struct sppm_ctx sppm_ctx;
+
+/* Allocates the per-pixel and per-photon state on `device` (CGPURT() + the texture and FBO set-up
+   of main(), glslppm.cpp:691-795). */
+int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out);
+/* Copies the scene to the device in the traversal layout (CGPURT::PrecalculateMeshData +
+   CreateTextures, gpurt.cpp:8-16, 47-552). The caller's arrays are not retained. */
+int sppm_upload_scene(sppm_ctx* ctx, const sppm_scene* scene);
+int sppm_set_camera(sppm_ctx* ctx, const sppm_camera* cam);
+/* Back to frame 0: re-seeds the random state (RandomizeTextures, glslppm.cpp:113-140). */
+int sppm_reset(sppm_ctx* ctx);
+/* Queues n SPPM frames (m_display, glslppm.cpp:214-536) on the context's stream. */
+int sppm_run_passes(sppm_ctx* ctx, uint32_t n);
+/* Waits for queued work; returns SPPM_ERR_WATCHDOG if a device loop bound was hit. */
+int sppm_synchronize(sppm_ctx* ctx);
+
+typedef enum sppm_image_kind {
+    SPPM_IMAGE_RADIANCE = 0, /* linear L = tau / (R^2 pi Nemitted) + emission (re.fs:35-38)      */
+    SPPM_IMAGE_DISPLAY = 1   /* 1 - exp(-60000 L), then sRGB (re.fs:41-47)                        */
+} sppm_image_kind;
+/* Resolves the image and copies width*height*3 floats (row 0 = bottom row, as GL) to rgb. */
+int sppm_read_image(sppm_ctx* ctx, uint32_t kind, float* rgb, size_t num_floats);
+
+/* Per-pixel / per-photon / per-slot state, for parity checks and checkpointing. */
+typedef enum sppm_state_kind {
+    SPPM_STATE_HIT_POSITION = 0,    /* float4/pixel  QueryPositionTexture (pos.xyz, dir.x)      */
+    SPPM_STATE_HIT_REFLECTANCE = 1, /* float4/pixel  QueryReflectanceTexture (col, dir.y)       */
+    SPPM_STATE_HIT_NORMAL = 2,      /* float4/pixel  QueryNormalTexture (nrm, dir.z)            */
+    SPPM_STATE_EYE_RNG = 3,         /* float4/pixel  RandomEyeRayTexture                        */
+    SPPM_STATE_HIT_TRIANGLE = 4,    /* int32/pixel   triangle of QueryIntersectionTexture, -1   */
+    SPPM_STATE_EMISSION_N = 5,      /* float4/pixel  QueryEmissionPhotonCountTexture (emi, N)   */
+    SPPM_STATE_FLUX_RADIUS = 6,     /* float4/pixel  QueryFluxRadiusTexture (tau, R)            */
+    SPPM_STATE_PHOTON_POSITION = 7, /* float4/photon PhotonPositionTexture (pos, nrm.x)         */
+    SPPM_STATE_PHOTON_FLUX = 8,     /* float4/photon PhotonFluxTexture (flux, nrm.y)            */
+    SPPM_STATE_PHOTON_DIRECTION = 9,/* float4/photon PhotonDirectionTexture (dir, nrm.z)        */
+    SPPM_STATE_PHOTON_RNG = 10,     /* float4/photon RandomPhotonTexture                        */
+    SPPM_STATE_PHOTON_HIT = 11,     /* int32x2/photon (triangle or -1, path depth)              */
+    SPPM_STATE_SLOT_WINNER = 12,    /* uint32/slot   photon id stored in the slot, 0xFFFFFFFF   */
+    SPPM_STATE_SLOT_COUNT = 13,     /* uint32/slot   photons hashed to the slot                 */
+    SPPM_STATE_HIT_T = 14,          /* float/pixel   t of QueryIntersectionTexture (.w)         */
+    SPPM_STATE_STATS_N = 15,        /* double/pixel  N (mixed precision statistics)             */
+    SPPM_STATE_STATS_R2 = 16,       /* double/pixel  R^2                                        */
+    SPPM_STATE_STATS_TAU = 17       /* double3/pixel tau                                        */
+} sppm_state_kind;
+/* Copies one state array to host memory; `bytes` must equal the array's size. */
+int sppm_read_state(sppm_ctx* ctx, uint32_t kind, void* dst, size_t bytes);
+/* Size in bytes of a state array (0 if the kind is not kept by this precision). */
+size_t sppm_state_bytes(const sppm_ctx* ctx, uint32_t kind);
+
+typedef struct sppm_frame_info {
+    uint32_t frames;              /* FrameCount                                               */
+    uint32_t eye_samples;         /* NumEyeSamples                                            */
+    uint64_t photons_emitted;     /* NumPhotons, kept as an exact integer                     */
+    float num_photons_f32;        /* NumPhotons as the reference accumulates it (float)        */
+    float initial_radius;         /* InitialRadius of the last eye pass                        */
+    float grid_scale;             /* GridScale                                                 */
+    float bbox_min[3], bbox_max[3]; /* expanded hit-point bbox (BBMin/BBMax)                   */
+    float aa_offset[2];           /* AAOffset of the last eye pass                             */
+    uint64_t photon_segments;     /* photon ray segments traced so far                         */
+    uint64_t eye_segments;        /* eye ray segments traced so far                            */
+} sppm_frame_info;
+int sppm_get_frame_info(sppm_ctx* ctx, sppm_frame_info* info);
+
+/* Per-stage device time (ms) accumulated since the last call, measured with CUDA events on the
+   context's stream around each stage launch; enable before the passes to be timed. */
+typedef enum sppm_stage {
+    SPPM_STAGE_FRAME_BEGIN = 0, /* hash clear + per-frame scalars                          */
+    SPPM_STAGE_EYE = 1,         /* eyeraytrace.fs + max/min reductions                      */
+    SPPM_STAGE_GRID = 2,        /* InitialRadius / GridScale (glslppm.cpp:294-311)          */
+    SPPM_STAGE_PHOTON = 3,      /* photontrace.fs + sum reduction + hash.fs/scatter/correction */
+    SPPM_STAGE_GATHER = 4,      /* progressive.fs                                          */
+    SPPM_STAGE_RESOLVE = 5,     /* re.fs                                                   */
+    SPPM_STAGE_COUNT = 6
+} sppm_stage;
+int sppm_enable_stage_timing(sppm_ctx* ctx, int enable);
+int sppm_read_stage_times(sppm_ctx* ctx, float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]);
+
+/* Device time (ms) of `n` frames measured with CUDA events on the context's stream. */
+int sppm_time_passes(sppm_ctx* ctx, uint32_t n, float* ms);
+
+void sppm_destroy(sppm_ctx* ctx);
+
+/* ---- stage-level entry points (device pointers) --------------------------------------------- */
+/* The hash build of hash.fs + scatter.vs + correction.vs on caller-owned device arrays:
+   for photon i (row-major in a photon_width-wide buffer) with flux[i].x >= 0, slot = hash of
+   the grid cell floor((pos[i]-bbox_min)*grid_scale); count[slot] += 1; winner[slot] =
+   min i unless the GL depth clip removes photon i.  pos/flux are float4 arrays (xyz used).
+   winner/count (hash_slots entries each) are overwritten. Runs on `stream` (cudaStream_t). */
+int sppm_hash_build(const float* d_pos, const float* d_flux, uint32_t photon_width,
+                    uint32_t photon_height, uint32_t hash_slots, const float bbox_min[3],
+                    float grid_scale, uint32_t flags, uint32_t* d_winner, uint32_t* d_count,
+                    void* stream);
+
+/* ---- diagnostics ------------------------------------------------------------------------------ */
+/* Message of the last failed call on this thread; returns the full message length. */
+size_t sppm_last_error(char* buf, size_t buf_size);
+/* Runs the pinned FP32 functions of sppm_fpmath.h on the GPU: fn 0 sin, 1 cos, 2 pow(x,y),
+   3 exp, 4 log2, 5 exp2.  x, y, out are host arrays of n floats. */
+int sppm_debug_fpmath(int fn, const float* x, const float* y, float* out, size_t n);
+/* Number of CUDA devices (0 when none); never fails. */
+int sppm_device_count(void);
+uint32_t sppm_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPPM_H */

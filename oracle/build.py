@@ -1,0 +1,110 @@
+"""Build recipes of the checker (test infrastructure, not the product).
+
+* ``build_oracle()`` compiles the C restatement of the shader path (``sppm_oracle.c``) twice --
+  single precision and double precision -- into ``oracle/_build/``.
+* ``build_ref()`` compiles the reference's own sources from the reference checkout into
+  ``oracle/_ref/`` when that checkout is present (``SPPM_REFERENCE_DIR``, default the directory the
+  reference is mounted at on the development machine):
+    - ``ref_host_dump``: the reference's ``mesh.cpp``, ``bvh.cpp``, ``bbox.cpp`` and ``camera.cpp``,
+      unmodified, linked with ``ref_host_dump.cpp``;
+    - ``libref_shaders.so``: the reference's GLSL shaders compiled as C++ through
+      ``glsl_compat.hpp`` (see ``ref_shaders.cpp``).
+  The sources are read where they lie; nothing of the reference is copied into the repository.
+  ``oracle/_ref/`` is git-ignored.
+
+All host code is compiled with ``-ffp-contract=off`` and without fast-math so that every
+single-precision operation rounds exactly as written, on x86-64 and on aarch64 alike.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+ORACLE_DIR = Path(__file__).resolve().parent
+REPO = ORACLE_DIR.parent
+BUILD_DIR = ORACLE_DIR / "_build"
+REF_DIR = ORACLE_DIR / "_ref"
+INCLUDE = REPO / "include"
+REFERENCE = Path(os.environ.get("SPPM_REFERENCE_DIR", "/root/reference"))
+
+STRICT_FP = ["-ffp-contract=off", "-fno-fast-math"]
+
+
+def _run(cmd: list[str]) -> None:
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(f"command failed ({proc.returncode}): {' '.join(cmd)}\n{proc.stdout}\n{proc.stderr}")
+
+
+def _stale(target: Path, sources: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(s.stat().st_mtime > t for s in sources)
+
+
+def build_oracle(force: bool = False) -> dict[str, Path]:
+    """Compile the FP32 and FP64 oracles; returns {"f32": path, "f64": path}."""
+    BUILD_DIR.mkdir(parents=True, exist_ok=True)
+    src = ORACLE_DIR / "sppm_oracle.c"
+    deps = [src, INCLUDE / "sppm.h", INCLUDE / "sppm_fpmath.h"]
+    out = {}
+    for tag, extra in (("f32", []), ("f64", ["-DORACLE_FP64"])):
+        lib = BUILD_DIR / f"liboracle_{tag}.so"
+        if force or _stale(lib, deps):
+            tmp = lib.with_suffix(f".so.tmp{os.getpid()}")
+            _run(["gcc", "-std=gnu11", "-O2", "-fopenmp", *STRICT_FP, "-fPIC", "-shared",
+                  "-fvisibility=hidden", *extra, f"-I{INCLUDE}", str(src), "-o", str(tmp), "-lm"])
+            os.replace(tmp, lib)
+        out[tag] = lib
+    return out
+
+
+def reference_available() -> bool:
+    return (REFERENCE / "bvh.cpp").is_file() and (REFERENCE / "photontrace.fs").is_file()
+
+
+def build_ref(force: bool = False) -> dict[str, Path]:
+    """Compile the reference's host code and shaders into oracle/_ref (needs the reference)."""
+    if not reference_available():
+        return {}
+    REF_DIR.mkdir(parents=True, exist_ok=True)
+    out = {}
+    host_srcs = [REFERENCE / f for f in ("mesh.cpp", "bvh.cpp", "bbox.cpp", "camera.cpp")]
+    dump = REF_DIR / "ref_host_dump"
+    dump_src = ORACLE_DIR / "ref_host_dump.cpp"
+    if force or _stale(dump, host_srcs + [dump_src]):
+        _run(["g++", "-std=c++14", "-O2", *STRICT_FP, "-w", f"-I{REFERENCE}", str(dump_src),
+              *map(str, host_srcs), "-o", str(dump)])
+    out["host_dump"] = dump
+    shader_src = ORACLE_DIR / "ref_shaders.cpp"
+    if shader_src.exists():
+        compat = ORACLE_DIR / "glsl_compat.hpp"
+        lib = REF_DIR / "libref_shaders.so"
+        shaders = [REFERENCE / f for f in ("eyeraytrace.fs", "photontrace.fs", "hash.fs", "progressive.fs",
+                                           "scatter.vs", "correction.vs", "re.fs", "min.fs", "max.fs", "sum.fs")]
+        if force or _stale(lib, shaders + [shader_src, compat, INCLUDE / "sppm_fpmath.h"]):
+            # each shader body (the source without its '#version' line) is placed in its own
+            # namespace by ref_shaders.cpp; the bodies are produced into oracle/_ref only
+            for sh in shaders:
+                body = REF_DIR / (sh.name.replace(".", "_") + ".inc")
+                lines = sh.read_text(encoding="latin-1").splitlines(keepends=True)
+                body.write_text("".join(l if not l.lstrip().startswith("#version") else "\n" for l in lines),
+                                encoding="latin-1")
+            _run(["g++", "-std=c++17", "-O2", *STRICT_FP, "-fPIC", "-shared", "-fvisibility=hidden", "-w",
+                  f"-I{INCLUDE}", f"-I{ORACLE_DIR}", f"-I{REF_DIR}", str(shader_src), "-o", str(lib)])
+        out["shaders"] = lib
+    return out
+
+
+def clean() -> None:
+    for d in (BUILD_DIR, REF_DIR):
+        if d.exists():
+            shutil.rmtree(d)
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_ref(force=True))
