@@ -88,6 +88,7 @@ struct sppm_ctx {
     float fixed_radius = 0.0f;
     // stage timing
     bool timing = false;
+    bool count_traversal = false;
     std::vector<StageEvent> pending;
     std::vector<cudaEvent_t> event_pool;
     float stage_ms[SPPM_STAGE_COUNT] = {0};
@@ -564,7 +565,7 @@ int sppm_run_passes(sppm_ctx* c, uint32_t n) {
             timed(c, SPPM_STAGE_GRID, false);
         }
         timed(c, SPPM_STAGE_PHOTON, true);
-        launch_photon_fp32(pho, c->stream);
+        launch_photon_fp32(pho, c->count_traversal, c->stream);
         timed(c, SPPM_STAGE_PHOTON, false);
         timed(c, SPPM_STAGE_GATHER, true);
         launch_gather_fp32(pix, c->stream);
@@ -662,6 +663,15 @@ int sppm_get_frame_info(sppm_ctx* c, sppm_frame_info* fi) {
     fi->aa_offset[1] = st.aa[1];
     fi->photon_segments = st.photon_segments;
     fi->eye_segments = st.eye_segments;
+    fi->counted_segments = st.count_segments;
+    fi->counted_nodes = st.count_nodes;
+    fi->counted_triangles = st.count_tris;
+    return SPPM_OK;
+}
+
+int sppm_enable_traversal_counters(sppm_ctx* c, int enable) {
+    if (!c) return fail(SPPM_ERR_ARG, "null context");
+    c->count_traversal = enable != 0;
     return SPPM_OK;
 }
 

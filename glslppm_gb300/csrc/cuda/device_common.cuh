@@ -84,6 +84,7 @@ struct JobState {
     float num_photons_f32;
     uint32_t err;
     unsigned long long num_photons, photon_segments, eye_segments;
+    unsigned long long count_nodes, count_tris, count_segments;  // traversal counters (when enabled)
 };
 
 struct JobDesc {

@@ -38,8 +38,13 @@ __device__ __forceinline__ int cube_face(f3 d) {
     return d.z < 0.0f ? 5 : 4;
 }
 
-template <bool PHOTON>
-__device__ __forceinline__ Hit trace_exact(const DevScene& s, f3 org, f3 dir, bool cull, uint32_t& err) {
+struct TraversalCount {
+    uint32_t nodes = 0, tris = 0;
+};
+
+template <bool PHOTON, bool COUNT = false>
+__device__ __forceinline__ Hit trace_exact(const DevScene& s, f3 org, f3 dir, bool cull, uint32_t& err,
+                                           TraversalCount* cnt = nullptr) {
     Hit h;
     h.t = PHOTON ? 1.0e30f : 1.0e20f;
     h.tri = -1;
@@ -57,6 +62,7 @@ __device__ __forceinline__ Hit trace_exact(const DevScene& s, f3 org, f3 dir, bo
         }
         const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + i));
         const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + i) + 1);
+        if (COUNT) cnt->nodes++;
         const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
         const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
         const float tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
@@ -65,6 +71,7 @@ __device__ __forceinline__ Hit trace_exact(const DevScene& s, f3 org, f3 dir, bo
         const int32_t tri = __float_as_int(B.w);
         if (hit && tri >= 0 && (!PHOTON || !(tri & kEmitterBit))) {
             const int32_t t = tri & kTriMask;
+            if (COUNT) cnt->tris++;
             const float4 a = __ldg(&s.tri_isect[(size_t)t * 3 + 0]);
             const float4 b = __ldg(&s.tri_isect[(size_t)t * 3 + 1]);
             const float4 c = __ldg(&s.tri_isect[(size_t)t * 3 + 2]);
@@ -458,6 +465,7 @@ __device__ __forceinline__ void matte_bounce(float4& rndv, f3 ipos, f3 gnrm, f3 
     if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
 }
 
+template <bool COUNT>
 __global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
     const uint32_t g = grid_tid();
     if (g >= ls.total) return;
@@ -551,8 +559,9 @@ __global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
     }
     bool store = false;
     f3 ppos = mk(0, 0, 0);
+    TraversalCount tc;
     if (cont) {
-        const Hit h = trace_exact<true>(S, rorg, rdir, false, err);
+        const Hit h = trace_exact<true, COUNT>(S, rorg, rdir, false, err, &tc);
         f3 pnrm = mk(0, 0, 0), pg = mk(0, 0, 0);
         int brdf = 0;
         if (h.tri >= 0) {
@@ -610,6 +619,15 @@ __global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
         if (we) atomicAdd(&st->emitted_frame, we);
         if (ws) atomicAdd(&st->segments_frame, ws);
         if (wr) atomicOr(&st->err, wr);
+    }
+    if (COUNT) {
+        const uint32_t wn = __reduce_add_sync(jm, tc.nodes);
+        const uint32_t wt = __reduce_add_sync(jm, tc.tris);
+        if ((threadIdx.x & 31) == (__ffs(jm) - 1)) {
+            atomicAdd(&st->count_nodes, (unsigned long long)wn);
+            atomicAdd(&st->count_tris, (unsigned long long)wt);
+            atomicAdd(&st->count_segments, (unsigned long long)ws);
+        }
     }
 }
 
@@ -771,8 +789,10 @@ void launch_eye_fp32(const LaunchSet& ls, cudaStream_t s) {
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s) {
     if (njobs) k_grid<<<blocks_for(njobs, 64), 64, 0, s>>>(jobs, job_ids, njobs);
 }
-void launch_photon_fp32(const LaunchSet& ls, cudaStream_t s) {
-    if (ls.total) k_photon<<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
+void launch_photon_fp32(const LaunchSet& ls, bool count, cudaStream_t s) {
+    if (!ls.total) return;
+    if (count) k_photon<true><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
+    else k_photon<false><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
 }
 void launch_gather_fp32(const LaunchSet& ls, cudaStream_t s) {
     if (ls.total) k_gather<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls);

@@ -84,6 +84,7 @@ class FrameInfo(C.Structure):
         ("num_photons_f32", C.c_float), ("initial_radius", C.c_float), ("grid_scale", C.c_float),
         ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3), ("aa_offset", C.c_float * 2),
         ("photon_segments", C.c_uint64), ("eye_segments", C.c_uint64),
+        ("counted_segments", C.c_uint64), ("counted_nodes", C.c_uint64), ("counted_triangles", C.c_uint64),
     ]
 
 
@@ -109,6 +110,7 @@ SIGNATURES = {
     "sppm_state_bytes": (C.c_size_t, [P, C.c_uint32]),
     "sppm_get_frame_info": (C.c_int, [P, C.POINTER(FrameInfo)]),
     "sppm_enable_stage_timing": (C.c_int, [P, C.c_int]),
+    "sppm_enable_traversal_counters": (C.c_int, [P, C.c_int]),
     "sppm_read_stage_times": (C.c_int, [P, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     "sppm_time_passes": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_float)]),
     "sppm_destroy": (None, [P]),

@@ -260,6 +260,22 @@ class Renderer:
         N.check(N.lib.sppm_read_stage_times(self._h, ms, n))
         return {name: (float(ms[i]), int(n[i])) for i, name in enumerate(N.STAGES)}
 
+    def traversal_counters(self, passes: int = 10) -> dict:
+        """Runs `passes` more frames with the counting photon kernel; returns the mean BVH nodes
+        visited and triangles tested per photon segment."""
+        f0 = self.frame_info()
+        N.check(N.lib.sppm_enable_traversal_counters(self._h, 1))
+        try:
+            self.run_passes(passes)
+            self.synchronize()
+        finally:
+            N.check(N.lib.sppm_enable_traversal_counters(self._h, 0))
+        f1 = self.frame_info()
+        segs = f1.counted_segments - f0.counted_segments
+        return {"passes": passes, "photon_segments": segs,
+                "nodes_per_segment": (f1.counted_nodes - f0.counted_nodes) / max(segs, 1),
+                "tris_per_segment": (f1.counted_triangles - f0.counted_triangles) / max(segs, 1)}
+
     def time_passes(self, n: int) -> float:
         ms = C.c_float()
         N.check(N.lib.sppm_time_passes(self._h, n, C.byref(ms)))

@@ -219,8 +219,14 @@ typedef struct sppm_frame_info {
     float aa_offset[2];           /* AAOffset of the last eye pass                             */
     uint64_t photon_segments;     /* photon ray segments traced so far                         */
     uint64_t eye_segments;        /* eye ray segments traced so far                            */
+    uint64_t counted_segments;    /* photon segments traced while traversal counters were on   */
+    uint64_t counted_nodes;       /* BVH nodes those segments visited                          */
+    uint64_t counted_triangles;   /* triangles those segments tested                           */
 } sppm_frame_info;
 int sppm_get_frame_info(sppm_ctx* ctx, sppm_frame_info* info);
+/* While enabled, the photon pass also counts BVH nodes visited and triangles tested (a separate
+   kernel instantiation; results are unchanged).  Used for the algorithmic-byte roofline. */
+int sppm_enable_traversal_counters(sppm_ctx* ctx, int enable);
 
 /* Per-stage device time (ms) accumulated since the last call, measured with CUDA events on the
    context's stream around each stage launch; enable before the passes to be timed. */

@@ -1193,6 +1193,21 @@ EXPORT uint32_t ORACLE_API(hash_of_cell)(float cx, float cy, float cz, float gri
     return hash_cell(v3(cx, cy, cz), grid_scale, hs1, (real)hash_num);
 }
 
+/* the pinned single-precision functions of sppm_fpmath.h evaluated on the host:
+   fn 0 sin, 1 cos, 2 pow(x,y), 3 exp, 4 log2, 5 exp2 */
+EXPORT void ORACLE_API(fpmath)(int fn, const float* x, const float* y, float* out, size_t n) {
+    for (size_t i = 0; i < n; i++) {
+        switch (fn) {
+            case 0: out[i] = sppm_fsin(x[i]); break;
+            case 1: out[i] = sppm_fcos(x[i]); break;
+            case 2: out[i] = sppm_fpow(x[i], y[i]); break;
+            case 3: out[i] = sppm_fexp(x[i]); break;
+            case 4: out[i] = sppm_flog2(x[i]); break;
+            default: out[i] = sppm_fexp2(x[i]); break;
+        }
+    }
+}
+
 EXPORT void ORACLE_API(destroy)(oracle_ctx* c) {
     if (!c) return;
     oscene* s = &c->sc;

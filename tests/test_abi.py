@@ -1,0 +1,102 @@
+"""The C-ABI library loads and exports every function include/*.h declares (no GPU needed)."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+REPO = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    names = set()
+    for h in (REPO / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        # extern "C" declarations: <type> sppm_name(   (the static inline helpers of sppm_fpmath.h,
+        # defined with SPPM_FP_FN, are header-only and not part of the exported ABI)
+        for m in re.finditer(r"^(?!static|SPPM_FP_FN)[A-Za-z_][\w \t\*]*?\b(sppm_\w+)[ \t]*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for required in ("sppm_create", "sppm_upload_scene", "sppm_set_camera", "sppm_run_passes", "sppm_read_image",
+                     "sppm_read_state", "sppm_last_error", "sppm_destroy", "sppm_hash_build"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    lib = native_lib.lib
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"declared but not exported: {missing}"
+    assert lib.sppm_abi_version() == 1
+
+
+def test_python_binding_covers_every_symbol(native_lib):
+    assert set(declared_functions()) <= set(native_lib.SIGNATURES), \
+        set(declared_functions()) - set(native_lib.SIGNATURES)
+
+
+def test_struct_sizes_match_the_header(native_lib):
+    import ctypes as C
+    N = native_lib
+    # sizes of the C structs as the C compiler lays them out
+    assert C.sizeof(N.Config) == 17 * 4
+    assert C.sizeof(N.Material) == 24
+    assert C.sizeof(N.Camera) == 15 * 4
+    assert C.sizeof(N.FrameInfo) == 4 + 4 + 8 + 4 * 3 + 4 * 6 + 4 * 2 + 8 * 5
+
+
+def test_config_defaults_are_the_reference_constants(native_lib):
+    import glslppm_gb300 as g
+    c = g.default_config(512)
+    assert (c.width, c.height, c.photon_width, c.photon_height) == (512, 512, 512, 512)
+    assert c.max_path_length == 10 and c.eye_pass_interval == 10
+    assert c.alpha == pytest.approx(0.7) and c.initial_footprint == 2.5
+    assert c.focal_length == 13.0 and c.aperture == 0.0
+    assert c.flags & native_lib.FLAG_GL_DEPTH_CLIP
+
+
+def test_errors_are_reported_not_raised_across_the_abi(native_lib, tmp_path):
+    import glslppm_gb300 as g
+    N = native_lib
+    with pytest.raises(N.SppmError) as e:
+        g.Mesh.load_obj(str(tmp_path / "missing.obj"))
+    assert e.value.status == N.ERR_IO and "cannot open" in str(e.value)
+    bad = tmp_path / "bad.obj"
+    bad.write_text("v 0 0 0\nv 1 0 0\nf 1 2\n")
+    with pytest.raises(N.SppmError) as e:
+        g.Mesh.load_obj(str(bad))
+    assert e.value.status == N.ERR_IO
+    oob = tmp_path / "oob.obj"
+    oob.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 9\n")
+    with pytest.raises(N.SppmError) as e:
+        g.Mesh.load_obj(str(oob))
+    assert e.value.status == N.ERR_IO
+    # stage entry point validates its arguments before touching the device
+    import ctypes
+    st = N.lib.sppm_hash_build(None, None, 4, 4, 16, (ctypes.c_float * 3)(0, 0, 0), 1.0, 0, None, None, None)
+    assert st == N.ERR_ARG
+    assert "null" in N.last_error()
+
+
+def test_create_without_a_device_fails_cleanly(native_lib):
+    import glslppm_gb300 as g
+    N = native_lib
+    if N.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(N.SppmError) as e:
+        g.Renderer(g.default_config(16))
+    assert e.value.status == N.ERR_NO_DEVICE
+
+
+def test_invalid_configs_are_rejected(native_lib):
+    import glslppm_gb300 as g
+    N = native_lib
+    for bad in (dict(width=0), dict(alpha=0.0), dict(max_path_length=0), dict(precision=9), dict(seed_mode=5)):
+        with pytest.raises(N.SppmError) as e:
+            g.Renderer(g.default_config(16, **bad))
+        assert e.value.status in (N.ERR_ARG, N.ERR_UNSUPPORTED)

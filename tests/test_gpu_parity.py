@@ -1,0 +1,142 @@
+"""Parity of the CUDA FP32 path with the CPU oracle (bit-exact state after K frames).
+
+Every per-pixel and per-photon array of the progressive state -- hit points, hit triangle ids,
+(emission, N), (tau, R), photon records, the hashed grid's winner and count per slot -- is compared
+word for word after several frames, including eye passes (every 10th frame) and the frame-0
+initialisation.  The radiance image (re.fs) is compared exactly as well.
+"""
+import numpy as np
+import pytest
+
+import glslppm_gb300 as g
+from glslppm_gb300 import native as N
+from oracle.binding import Oracle, fpmath
+from tests.golden.fixtures import camera_from, load_npz
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["hit_position", "hit_reflectance", "hit_normal", "eye_rng", "hit_triangle", "hit_t", "emission_n",
+         "flux_radius", "photon_position", "photon_flux", "photon_direction", "photon_rng", "photon_hit",
+         "slot_winner", "slot_count"]
+
+
+def bits(a: np.ndarray) -> np.ndarray:
+    a = np.ascontiguousarray(a)
+    return a.view(np.uint32) if a.dtype.itemsize == 4 else a.view(np.uint8)
+
+
+def assert_same(kind, gpu, cpu):
+    gb, cb = bits(gpu), bits(cpu)
+    assert gb.shape == cb.shape, f"{kind}: shape {gb.shape} vs {cb.shape}"
+    bad = np.nonzero(gb.reshape(len(gb), -1) != cb.reshape(len(cb), -1))[0]
+    assert bad.size == 0, (f"{kind}: {np.unique(bad).size} of {len(gb)} elements differ; first {bad[:5]}: "
+                           f"gpu {gpu[bad[:3]]} cpu {cpu[bad[:3]]}")
+
+
+def run_pair(cfg, scene, cam, checkpoints):
+    r = g.Renderer(cfg)
+    r.upload_scene(scene)
+    r.set_camera(cam)
+    o = Oracle(cfg, scene, cam)
+    done = 0
+    for k in checkpoints:
+        r.run_passes(k - done)
+        o.run_frames(k - done)
+        done = k
+        r.synchronize()
+        for kind in KINDS:
+            assert_same(f"{kind} after {k} frames", r.read_state(kind), o.read_state(kind))
+        fg, fo = r.frame_info(), o.frame_info()
+        assert fg.frames == fo.frames == k
+        assert fg.photons_emitted == fo.photons_emitted
+        assert fg.num_photons_f32 == fo.num_photons_f32
+        assert fg.eye_samples == fo.eye_samples
+        assert fg.grid_scale == fo.grid_scale and fg.initial_radius == fo.initial_radius
+        assert list(fg.bbox_min) == list(fo.bbox_min) and list(fg.bbox_max) == list(fo.bbox_max)
+        assert fg.photon_segments == fo.photon_segments and fg.eye_segments == fo.eye_segments
+        img = r.read_image(N.IMAGE_RADIANCE)
+        ref = o.read_image(0).astype(np.float32)
+        assert_same(f"radiance after {k} frames", img.reshape(-1, 3), ref.reshape(-1, 3))
+    return r, o
+
+
+def test_state_bit_exact_cornell_metal(cornell_metal):
+    arrays, d = cornell_metal
+    scene = g.scene_from_arrays(arrays)
+    cfg = g.default_config(32)
+    cam = camera_from(d, 32, 32)
+    cam.distance = float(load_npz("kat_frames_cm32.npz")["cam_distance_32"])
+    run_pair(cfg, scene, cam, [1, 10, 11, 23])
+
+
+def test_state_bit_exact_cornell_box_diagonal_radius(cornell_c1_mesh):
+    sc, mesh = cornell_c1_mesh
+    cfg = g.default_config(48, photon_width=64, photon_height=32, radius_rule=N.RADIUS_DIAGONAL,
+                           radius_fraction=0.005)
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 48, 48, sc.fov)
+    run_pair(cfg, mesh.scene(), cam, [1, 12, 30])
+
+
+def test_state_bit_exact_non_square_and_hash_seed(cornell_c1_mesh):
+    sc, mesh = cornell_c1_mesh
+    cfg = g.default_config(40, height=24, photon_width=48, photon_height=20, hash_slots=1500,
+                           seed_mode=N.SEED_HASH, seed=7, flags=0, eye_pass_interval=4)
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 40, 24, sc.fov)
+    run_pair(cfg, mesh.scene(), cam, [1, 5, 9])
+
+
+def test_matches_committed_golden_frames(cornell_metal):
+    """The GPU state equals the oracle outputs committed in tests/golden (generated on another
+    machine): a check that neither side drifted."""
+    arrays, d = cornell_metal
+    gold = load_npz("kat_frames_cm32.npz")
+    cfg = g.default_config(32)
+    cam = camera_from(d, 32, 32)
+    cam.distance = float(gold["cam_distance_32"])
+    r = g.Renderer(cfg)
+    r.upload_scene(arrays)
+    r.set_camera(cam)
+    done = 0
+    for k in (1, 10, 23):
+        r.run_passes(k - done)
+        done = k
+        for kind in ("hit_triangle", "hit_position", "flux_radius", "emission_n", "photon_position", "photon_flux",
+                     "photon_hit", "slot_winner", "slot_count"):
+            assert_same(f"{kind}_{k}", r.read_state(kind), gold[f"{kind}_{k}"])
+        assert r.frame_info().photons_emitted == int(gold[f"photons_{k}"])
+
+
+def test_fpmath_device_equals_host():
+    rng = np.random.default_rng(5)
+    x = np.concatenate([np.linspace(-10, 10, 20001, dtype=np.float32), rng.random(20000, dtype=np.float32) * 6.3])
+    for fn in (0, 1, 3, 5):
+        assert np.array_equal(bits(g.renderer.debug_fpmath(fn, x)), bits(fpmath(fn, x))), fn
+    xp = rng.random(40000, dtype=np.float32)
+    yp = (rng.random(40000, dtype=np.float32) * 3).astype(np.float32)
+    assert np.array_equal(bits(g.renderer.debug_fpmath(2, xp, yp)), bits(fpmath(2, xp, yp)))
+    assert np.array_equal(bits(g.renderer.debug_fpmath(4, xp + 1e-3)), bits(fpmath(4, xp + 1e-3)))
+
+
+def test_watchdog_on_cyclic_bvh_links(cornell_metal):
+    """Corrupt miss links that form a cycle: every traversal hits its step bound, the kernel
+    records the error and returns, and the context stays usable (no hang, no fault)."""
+    arrays, d = cornell_metal
+    bad = g.renderer.SceneArrays(**{k: (v.copy() if isinstance(v, np.ndarray) else v)
+                                    for k, v in arrays.__dict__.items()})
+    internal = bad.node_triangle[bad.order_base] < 0  # [6, nn] positions holding internal nodes
+    bad.order_miss[internal] = 0  # back to the root
+    cfg = g.default_config(16)
+    cam = camera_from(d, 16, 16)
+    r = g.Renderer(cfg)
+    r.upload_scene(bad)
+    r.set_camera(cam)
+    r.run_passes(2)
+    with pytest.raises(N.SppmError) as e:
+        r.synchronize()
+    assert e.value.status == N.ERR_WATCHDOG
+    # the device is still healthy: a clean scene renders on a new context
+    ok = g.Renderer(cfg)
+    ok.upload_scene(arrays)
+    ok.set_camera(cam)
+    ok.run_passes(2)
+    ok.synchronize()
