@@ -40,14 +40,28 @@ def test_python_binding_covers_every_symbol(native_lib):
         set(declared_functions()) - set(native_lib.SIGNATURES)
 
 
-def test_struct_sizes_match_the_header(native_lib):
+def test_struct_layouts_match_the_header(native_lib, tmp_path):
+    """ctypes mirrors of the C structs have the size and field offsets the C compiler gives them."""
     import ctypes as C
+    import subprocess
     N = native_lib
-    # sizes of the C structs as the C compiler lays them out
-    assert C.sizeof(N.Config) == 17 * 4
-    assert C.sizeof(N.Material) == 24
-    assert C.sizeof(N.Camera) == 15 * 4
-    assert C.sizeof(N.FrameInfo) == 4 + 4 + 8 + 4 * 3 + 4 * 6 + 4 * 2 + 8 * 5
+    structs = {"sppm_config": N.Config, "sppm_material": N.Material, "sppm_scene": N.Scene,
+               "sppm_camera": N.Camera, "sppm_frame_info": N.FrameInfo}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sppm.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", f"-I{REPO / 'include'}", str(src), "-o", str(exe)], check=True)
+    out = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines())
+    for cname, cls in structs.items():
+        assert int(out[cname]) == C.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert int(out[f"{cname}.{fname}"]) == getattr(cls, fname).offset, f"{cname}.{fname}"
 
 
 def test_config_defaults_are_the_reference_constants(native_lib):
