@@ -158,8 +158,10 @@ void seed_streams(const sppm_config& cfg, uint32_t npix, uint32_t P, std::vector
     eye.resize((size_t)npix * 4);
     ph.resize((size_t)P * 4);
     if (cfg.seed_mode == SPPM_SEED_XORSHIFT) {
-        for (size_t i = 0; i < eye.size(); i++) eye[i] = (float)((double)xorshift_frand(xs) * 4194304.0);
-        for (size_t i = 0; i < ph.size(); i++) ph[i] = (float)((double)xorshift_frand(xs) * 4194304.0);
+        for (size_t i = 0; i < eye.size(); i += 4)
+            for (int k = 3; k >= 0; k--) eye[i + k] = (float)((double)xorshift_frand(xs) * 4194304.0);
+        for (size_t i = 0; i < ph.size(); i += 4)
+            for (int k = 3; k >= 0; k--) ph[i + k] = (float)((double)xorshift_frand(xs) * 4194304.0);
     } else {
         static const uint32_t mlane[4] = {4194287u, 4194277u, 4194191u, 4194167u};
         for (size_t e = 0; e < (size_t)npix + P; e++) {

@@ -31,6 +31,10 @@ REFERENCE = Path(os.environ.get("SPPM_REFERENCE_DIR", "/root/reference"))
 
 STRICT_FP = ["-ffp-contract=off", "-fno-fast-math"]
 
+# a GLSL floating literal (single precision): digits with a point and/or an exponent
+_FLOAT_LITERAL = __import__("re").compile(
+    r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
+
 
 def _run(cmd: list[str]) -> None:
     proc = subprocess.run(cmd, capture_output=True, text=True)
@@ -91,8 +95,8 @@ def build_ref(force: bool = False) -> dict[str, Path]:
             for sh in shaders:
                 body = REF_DIR / (sh.name.replace(".", "_") + ".inc")
                 lines = sh.read_text(encoding="latin-1").splitlines(keepends=True)
-                body.write_text("".join(l if not l.lstrip().startswith("#version") else "\n" for l in lines),
-                                encoding="latin-1")
+                text = "".join(l if not l.lstrip().startswith("#version") else "\n" for l in lines)
+                body.write_text(_FLOAT_LITERAL.sub(lambda m: m.group(1) + "f", text), encoding="latin-1")
             _run(["g++", "-std=c++17", "-O2", *STRICT_FP, "-fPIC", "-shared", "-fvisibility=hidden", "-w",
                   f"-I{INCLUDE}", f"-I{ORACLE_DIR}", f"-I{REF_DIR}", str(shader_src), "-o", str(lib)])
         out["shaders"] = lib

@@ -68,3 +68,78 @@ def run_ref_host_dump(obj: str | Path, scale: float = 1.0, camera=None) -> dict:
             args += [repr(float(x)) for x in o] + [repr(float(x)) for x in l] + [str(int(w)), str(int(h)), repr(float(fov))]
         subprocess.run(args, cwd=str(obj.parent), check=True, capture_output=True)
         return read_dump(out)
+
+
+class RefShaders:
+    """The reference's GLSL shaders compiled as C++ (oracle/_ref/libref_shaders.so), driven like
+    m_display; states are returned in the layout of the oracle's read_state."""
+
+    def __init__(self, scene, camera, resolution: int):
+        import ctypes as C
+        lib_path = REF_DIR / "libref_shaders.so"
+        if not lib_path.exists():
+            raise FileNotFoundError(f"{lib_path} not built (the reference sources are needed)")
+        self.lib = C.CDLL(str(lib_path))
+        P = C.c_void_p
+        for name, res, args in (("ref_gl_create", P, [P, P, C.c_int]), ("ref_gl_run_frames", C.c_int, [P, C.c_uint]),
+                                ("ref_gl_read", C.c_int, [P, C.c_int, P]), ("ref_gl_scalars", None, [P, P]),
+                                ("ref_gl_display", None, [P, P]), ("ref_gl_destroy", None, [P])):
+            fn = getattr(self.lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        self._scene = scene
+        self.R = resolution
+        self._h = self.lib.ref_gl_create(C.addressof(scene), C.addressof(camera), resolution)
+
+    def run_frames(self, n: int) -> int:
+        return self.lib.ref_gl_run_frames(self._h, n)  # texture3D calls (0 for untextured scenes)
+
+    def texture(self, which: int) -> np.ndarray:
+        out = np.empty((self.R * self.R, 4), np.float32)
+        self.lib.ref_gl_read(self._h, which, out.ctypes.data)
+        return out
+
+    def scalars(self) -> np.ndarray:
+        out = np.zeros(16, np.float32)
+        self.lib.ref_gl_scalars(self._h, out.ctypes.data)
+        return out
+
+    def display(self) -> np.ndarray:
+        out = np.empty((self.R, self.R, 3), np.float32)
+        self.lib.ref_gl_display(self._h, out.ctypes.data)
+        return out
+
+    def _tri(self, tc: np.ndarray) -> np.ndarray:
+        X = np.float32(self.scalars()[11])
+        i = np.floor(tc[:, 0].astype(np.float32) * X).astype(np.int64)
+        j = np.floor(tc[:, 1].astype(np.float32) * X).astype(np.int64)
+        tri = (j * int(X) + i) // 6
+        return np.where(tc[:, 0] < 0, -1, tri).astype(np.int32)
+
+    def read_state(self, kind: str) -> np.ndarray:
+        T = {"hit_position": 0, "hit_reflectance": 1, "hit_normal": 2, "eye_rng": 3, "emission_n": 5,
+             "flux_radius": 6, "photon_position": 7, "photon_flux": 8, "photon_direction": 9, "photon_rng": 10}
+        if kind in T:
+            return self.texture(T[kind])
+        if kind == "hit_triangle":
+            return self._tri(self.texture(4))
+        if kind == "hit_t":
+            return self.texture(4)[:, 3].copy()
+        if kind == "photon_hit":
+            t = self.texture(11)
+            return np.stack([self._tri(t), t[:, 2].astype(np.int32)], axis=1)
+        if kind == "slot_winner":
+            h = self.texture(12)
+            R = np.float32(self.R)
+            i = np.floor(h[:, 0] * R).astype(np.int64)
+            j = np.floor(h[:, 1] * R).astype(np.int64)
+            empty = (h[:, 0] == 0) & (h[:, 1] == 0)
+            return np.where(empty, 0xFFFFFFFF, j * self.R + i).astype(np.uint32)
+        if kind == "slot_count":
+            return self.texture(13)[:, 0].astype(np.uint32)
+        raise KeyError(kind)
+
+    def close(self):
+        if self._h:
+            self.lib.ref_gl_destroy(self._h)
+            self._h = None

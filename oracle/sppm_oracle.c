@@ -793,7 +793,7 @@ static void seed_state(oracle_ctx* c) {
     if (c->cfg.seed_mode == SPPM_SEED_XORSHIFT) {
         for (size_t p = 0; p < npix; p++) {
             float v[4];
-            for (int k = 0; k < 4; k++) v[k] = (float)((double)xorshift_frand(c->xs) * 4194304.0);
+            for (int k = 3; k >= 0; k--) v[k] = (float)((double)xorshift_frand(c->xs) * 4194304.0);
             c->q_rng[p].x = v[0];
             c->q_rng[p].y = v[1];
             c->q_rng[p].z = v[2];
@@ -801,7 +801,7 @@ static void seed_state(oracle_ctx* c) {
         }
         for (size_t p = 0; p < c->P; p++) {
             float v[4];
-            for (int k = 0; k < 4; k++) v[k] = (float)((double)xorshift_frand(c->xs) * 4194304.0);
+            for (int k = 3; k >= 0; k--) v[k] = (float)((double)xorshift_frand(c->xs) * 4194304.0);
             c->p_rng[p].x = v[0];
             c->p_rng[p].y = v[1];
             c->p_rng[p].z = v[2];

@@ -1,0 +1,69 @@
+"""The CPU oracle (oracle/sppm_oracle.c) equals the reference's own GLSL shaders, compiled as C++
+through oracle/glsl_compat.hpp and driven like m_display (oracle/ref_shaders.cpp): the complete
+per-pixel and per-photon state after every frame, word for word.
+
+Needs the reference sources (built into oracle/_ref); skipped where they are absent (the GPU machine),
+where the committed fixtures of tests/golden carry the pinned outputs instead.
+"""
+import numpy as np
+import pytest
+
+import glslppm_gb300 as g
+from glslppm_gb300 import native as N
+from tests.golden.fixtures import camera_from
+
+pytestmark = pytest.mark.reference
+
+KINDS = ["hit_position", "hit_reflectance", "hit_normal", "eye_rng", "hit_triangle", "hit_t", "emission_n",
+         "flux_radius", "photon_position", "photon_flux", "photon_direction", "photon_rng", "photon_hit",
+         "slot_winner", "slot_count"]
+
+
+def bits(a):
+    a = np.ascontiguousarray(a)
+    return a.view(np.uint32) if a.dtype.itemsize == 4 else a
+
+
+def compare(o, r, label):
+    bad = []
+    for kind in KINDS:
+        a, b = bits(o.read_state(kind)), bits(r.read_state(kind))
+        if a.shape != b.shape or not np.array_equal(a, b):
+            bad.append((kind, int((a != b).reshape(len(a), -1).any(axis=1).sum()) if a.shape == b.shape else -1))
+    assert not bad, f"{label}: oracle differs from the reference shaders: {bad}"
+
+
+def run(scene, cam, R, checkpoints):
+    from oracle.binding import Oracle
+    from oracle.build import build_ref
+    from oracle.refdump import RefShaders
+    build_ref()
+    cfg = g.default_config(R)
+    o = Oracle(cfg, scene, cam)
+    r = RefShaders(scene, cam, R)
+    done = 0
+    for k in checkpoints:
+        o.run_frames(k - done)
+        assert r.run_frames(k - done) == 0  # no texture lookups on untextured scenes
+        done = k
+        compare(o, r, f"after {k} frames")
+        s, fi = r.scalars(), o.frame_info()
+        assert np.float32(s[2]) == np.float32(fi.num_photons_f32)
+        assert np.float32(s[3]) == np.float32(fi.initial_radius) and np.float32(s[4]) == np.float32(fi.grid_scale)
+        assert np.array_equal(s[5:8], np.array(list(fi.bbox_min), np.float32))
+        assert np.array_equal(s[8:11], np.array(list(fi.bbox_max), np.float32))
+    disp = o.read_image(N.IMAGE_DISPLAY).astype(np.float32)
+    assert np.array_equal(bits(disp), bits(r.display()))
+
+
+def test_oracle_equals_reference_shaders_cornell_metal(cornell_metal):
+    arrays, d = cornell_metal
+    scene = g.scene_from_arrays(arrays)
+    cam = camera_from(d, 16, 16)
+    run(scene, cam, 16, [1, 2, 10, 11, 21])
+
+
+def test_oracle_equals_reference_shaders_cornell_box(cornell_c1_mesh):
+    sc, mesh = cornell_c1_mesh
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 32, 32, sc.fov)
+    run(mesh.scene(), cam, 32, [1, 3, 12])
