@@ -83,6 +83,16 @@ def build_ref(force: bool = False) -> dict[str, Path]:
         _run(["g++", "-std=c++14", "-O2", *STRICT_FP, "-w", f"-I{REFERENCE}", str(dump_src),
               *map(str, host_srcs), "-o", str(dump)])
     out["host_dump"] = dump
+    # the drop-in header include/sppm_gpurt.hpp compiled into the reference's own host code
+    shim = REF_DIR / "ref_gpurt_shim_test"
+    shim_src = ORACLE_DIR / "ref_gpurt_shim_test.cpp"
+    native_lib = REPO / "glslppm_gb300" / "_lib" / "libsppm.so"
+    if native_lib.exists() and (force or _stale(shim, host_srcs + [shim_src, INCLUDE / "sppm_gpurt.hpp", native_lib])):
+        _run(["g++", "-std=c++14", "-O2", *STRICT_FP, "-w", f"-I{REFERENCE}", f"-I{INCLUDE}", str(shim_src),
+              *map(str, host_srcs), f"-L{native_lib.parent}", "-lsppm", f"-Wl,-rpath,{native_lib.parent}",
+              "-o", str(shim)])
+    if shim.exists():
+        out["gpurt_shim"] = shim
     shader_src = ORACLE_DIR / "ref_shaders.cpp"
     if shader_src.exists():
         compat = ORACLE_DIR / "glsl_compat.hpp"

@@ -102,3 +102,27 @@ def test_loader_quirks_equal_reference(tmp_path):
     ref = run_ref_host_dump(tmp_path / "q.obj", 2.0)
     mine = g.Mesh.load_obj(str(tmp_path / "q.obj"), (0, 0, 0), 2.0).build_bvh().arrays()
     assert_scene_equal(ref, mine)
+
+
+@pytest.mark.reference
+def test_drop_in_gpurt_header_with_reference_host_code(tmp_path):
+    """include/sppm_gpurt.hpp compiled into the reference's own mesh.cpp/bvh.cpp/camera.cpp flattens
+    the TMesh + TBVH into exactly the arrays the reference builds; without a GPU it reports
+    SPPM_ERR_NO_DEVICE through its status instead of crashing."""
+    import subprocess
+    from oracle.build import REFERENCE, build_ref
+    from oracle.refdump import read_dump, run_ref_host_dump
+    from glslppm_gb300 import native as N
+    exe = build_ref().get("gpurt_shim")
+    assert exe is not None
+    out = tmp_path / "shim.bin"
+    frames = 3 if N.device_count() else 2
+    proc = subprocess.run([str(exe), "cornell_metal.obj", "0.01", str(out), str(frames)], cwd=str(REFERENCE),
+                          capture_output=True, text=True)
+    if N.device_count():
+        assert proc.returncode == 0 and "rendered 3 frames" in proc.stdout
+    else:
+        assert proc.returncode == N.ERR_NO_DEVICE and "no CUDA device" in proc.stdout
+    a, b = read_dump(out), run_ref_host_dump(REFERENCE / "cornell_metal.obj", 0.01)
+    for k in FIELDS:
+        assert np.array_equal(np.asarray(a[k]).view(np.uint8), np.asarray(b[k]).view(np.uint8)), k
