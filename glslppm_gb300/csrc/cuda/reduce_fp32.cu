@@ -1,0 +1,83 @@
+// ReduceTexture (glslppm.cpp:170-209) as a stage-level entry point.
+//
+// The reference reduces an R x R RGBA32F texture to one texel by drawing quads of R/2, R/4, ... 1
+// pixels into a ping-pong texture; each output texel applies min.fs / max.fs / sum.fs to the four
+// texels (i,j), (i+n,j), (i,j+n), (i+n,j+n) of the previous level, and the host reads texel (0,0).
+// One kernel launch per level restates it; the levels after the first run in place on a
+// (R/2) x (R/2) float4 scratch buffer (a thread reads its own output texel and three texels outside
+// the level's output square, so no thread reads what another writes).  The sums are evaluated as
+// ((v0 + v1) + v2) + v3 with non-fused adds, so all three results are bit-identical to the
+// reference's fold.
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "../host/scene_internal.h"
+#include "device_common.cuh"
+
+namespace sppm_dev {
+
+__global__ void k_reduce_level(const float4* src, uint32_t src_stride, float4* dst, uint32_t dst_stride,
+                               uint32_t n, uint32_t op) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * n) return;
+    const uint32_t i = t % n, j = t / n;
+    const float4 v0 = src[(size_t)j * src_stride + i];
+    const float4 v1 = src[(size_t)j * src_stride + i + n];
+    const float4 v2 = src[(size_t)(j + n) * src_stride + i];
+    const float4 v3 = src[(size_t)(j + n) * src_stride + i + n];
+    float4 r;
+    if (op == SPPM_REDUCE_MIN) {
+        r = make_float4(fminf(fminf(v0.x, v1.x), fminf(v2.x, v3.x)), fminf(fminf(v0.y, v1.y), fminf(v2.y, v3.y)),
+                        fminf(fminf(v0.z, v1.z), fminf(v2.z, v3.z)), fminf(fminf(v0.w, v1.w), fminf(v2.w, v3.w)));
+    } else if (op == SPPM_REDUCE_MAX) {
+        r = make_float4(fmaxf(fmaxf(v0.x, v1.x), fmaxf(v2.x, v3.x)), fmaxf(fmaxf(v0.y, v1.y), fmaxf(v2.y, v3.y)),
+                        fmaxf(fmaxf(v0.z, v1.z), fmaxf(v2.z, v3.z)), fmaxf(fmaxf(v0.w, v1.w), fmaxf(v2.w, v3.w)));
+    } else {
+        r = make_float4(__fadd_rn(__fadd_rn(__fadd_rn(v0.x, v1.x), v2.x), v3.x),
+                        __fadd_rn(__fadd_rn(__fadd_rn(v0.y, v1.y), v2.y), v3.y),
+                        __fadd_rn(__fadd_rn(__fadd_rn(v0.z, v1.z), v2.z), v3.z),
+                        __fadd_rn(__fadd_rn(__fadd_rn(v0.w, v1.w), v2.w), v3.w));
+    }
+    dst[(size_t)j * dst_stride + i] = r;
+}
+
+// all levels of one reduction; the result is scratch[0] when the last launch completes
+void launch_reduce_texture(const float4* tex, uint32_t resolution, uint32_t op, float4* scratch, cudaStream_t s) {
+    const uint32_t n1 = resolution / 2;
+    const float4* src = tex;
+    uint32_t stride = resolution;
+    for (uint32_t n = n1; n >= 1; n /= 2) {
+        const uint32_t items = n * n;
+        k_reduce_level<<<(items + 255) / 256, 256, 0, s>>>(src, stride, scratch, n1, n, op);
+        src = scratch;
+        stride = n1;
+        if (n == 1) break;
+    }
+}
+
+}  // namespace sppm_dev
+
+using sppm::fail;
+
+extern "C" int sppm_reduce_texture(const float* d_texture, uint32_t resolution, uint32_t op, float out[4],
+                                   void* stream) {
+    if (!d_texture || !out) return fail(SPPM_ERR_ARG, "sppm_reduce_texture: null argument");
+    if (resolution < 2 || (resolution & (resolution - 1)) || resolution > 16384)
+        return fail(SPPM_ERR_ARG, "sppm_reduce_texture: resolution %u must be a power of two in [2, 16384]", resolution);
+    if (op > SPPM_REDUCE_SUM) return fail(SPPM_ERR_ARG, "sppm_reduce_texture: unknown op %u", op);
+    if (reinterpret_cast<uintptr_t>(d_texture) & 15) return fail(SPPM_ERR_ARG, "texture must be 16-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t n1 = resolution / 2;
+    float4* scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, n1 * n1 * sizeof(float4), s);
+    if (e != cudaSuccess) return fail(SPPM_ERR_OOM, "sppm_reduce_texture: scratch allocation failed: %s", cudaGetErrorString(e));
+    sppm_dev::launch_reduce_texture(reinterpret_cast<const float4*>(d_texture), resolution, op, scratch, s);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, scratch, sizeof(float4), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(scratch, s);
+    const cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e != cudaSuccess || e2 != cudaSuccess)
+        return fail(SPPM_ERR_CUDA, "sppm_reduce_texture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    return SPPM_OK;
+}

@@ -307,6 +307,16 @@ def hash_build(d_pos: int, d_flux: int, photon_width: int, photon_height: int, h
                                   flags, d_winner, d_count, stream))
 
 
+REDUCE_MIN, REDUCE_MAX, REDUCE_SUM = 0, 1, 2
+
+
+def reduce_texture(d_texture: int, resolution: int, op: int, stream: int = 0) -> np.ndarray:
+    """ReduceTexture on a device float4 texture (sppm_reduce_texture); returns the 1x1 texel."""
+    out = (C.c_float * 4)()
+    N.check(N.lib.sppm_reduce_texture(d_texture, resolution, op, out, stream))
+    return np.array(list(out), dtype=np.float32)
+
+
 def debug_fpmath(fn: int, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
     x = np.ascontiguousarray(x, dtype=np.float32)
     yy = None if y is None else np.ascontiguousarray(y, dtype=np.float32)

@@ -258,6 +258,16 @@ int sppm_hash_build(const float* d_pos, const float* d_flux, uint32_t photon_wid
                     float grid_scale, uint32_t flags, uint32_t* d_winner, uint32_t* d_count,
                     void* stream);
 
+typedef enum sppm_reduce_op { SPPM_REDUCE_MIN = 0, SPPM_REDUCE_MAX = 1, SPPM_REDUCE_SUM = 2 } sppm_reduce_op;
+/* ReduceTexture (glslppm.cpp:170-209) with min.fs / max.fs / sum.fs on a caller's device texture:
+   d_texture holds resolution x resolution float4 texels, row 0 first (16-byte aligned), resolution
+   a power of two in [2, 16384].  The texture is folded 2x2 level by level in the order of the
+   reference's ping-pong draws, so min, max and sums are bit-identical to it; the 1x1 result is in
+   out[4] (host memory) when the call returns.  Scratch: a (resolution/2)^2 float4 ping-pong buffer,
+   allocated stream-ordered on `stream` (cudaStream_t, 0 = default stream) and freed before the call
+   returns; the call synchronizes `stream`. */
+int sppm_reduce_texture(const float* d_texture, uint32_t resolution, uint32_t op, float out[4], void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------------------------ */
 /* Message of the last failed call on this thread; returns the full message length. */
 size_t sppm_last_error(char* buf, size_t buf_size);

@@ -146,3 +146,18 @@ def fpmath(fn: int, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
     out = np.empty_like(x)
     lib.fpmath(fn, x.ctypes.data, yy.ctypes.data, out.ctypes.data, x.size)
     return out
+
+
+def reduce_texture(tex: np.ndarray, resolution: int, op: int) -> np.ndarray:
+    """ReduceTexture restated by the oracle (op 0 min.fs, 1 max.fs, 2 sum.fs)."""
+    lib = load(False)
+    if not hasattr(lib, "reduce_texture"):
+        fn = lib.oracle32_reduce_texture
+        fn.restype = C.c_int
+        fn.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
+        lib.reduce_texture = fn
+    t = np.ascontiguousarray(tex, dtype=np.float32)
+    out = np.zeros(4, np.float32)
+    if lib.reduce_texture(t.ctypes.data, resolution, op, out.ctypes.data):
+        raise ValueError("bad resolution or op")
+    return out

@@ -587,3 +587,13 @@ EXPORT void ref_gl_display(void* h, float* rgb) {
 }
 
 EXPORT void ref_gl_destroy(void* h) { delete (RefGL*)h; }
+
+// ReduceTexture with min.fs (op 0), max.fs (op 1) or sum.fs (op 2) on an R x R float4 texture
+EXPORT void ref_gl_reduce(const float* texels, int R, int op, float* out) {
+    Tex src, work;
+    src.init(R, R);
+    work.init(R, R);
+    for (size_t i = 0; i < src.t.size(); i++) src.t[i] = vec4(texels[i * 4], texels[i * 4 + 1], texels[i * 4 + 2], texels[i * 4 + 3]);
+    const vec4 r = reduce_texture(work, src, op == 0 ? RED_MIN : (op == 1 ? RED_MAX : RED_SUM));
+    for (int c = 0; c < 4; c++) out[c] = r[c];
+}

@@ -1193,6 +1193,41 @@ EXPORT uint32_t ORACLE_API(hash_of_cell)(float cx, float cy, float cz, float gri
     return hash_cell(v3(cx, cy, cz), grid_scale, hs1, (real)hash_num);
 }
 
+/* ReduceTexture (glslppm.cpp:170-209) with min.fs / max.fs / sum.fs (op 0 / 1 / 2): an R x R
+   float4 texture (row 0 first), R a power of two >= 2, folded level by level: the n x n output of a
+   level takes texels (i,j), (i+n,j), (i,j+n), (i+n,j+n) of its input, min(min(v0,v1),min(v2,v3)),
+   max likewise, or ((v0+v1)+v2)+v3; the result is texel (0,0) after the 1 x 1 level. */
+EXPORT int ORACLE_API(reduce_texture)(const float* tex, uint32_t R, uint32_t op, float out[4]) {
+    if (R < 2 || (R & (R - 1)) || op > 2) return SPPM_ERR_ARG;
+    const uint32_t n1 = R / 2;
+    float* w = (float*)malloc(sizeof(float) * 4 * n1 * n1);
+    const float* src = tex;
+    uint32_t stride = R;
+    for (uint32_t n = n1; n >= 1; n /= 2) {
+        for (uint32_t j = 0; j < n; j++) {
+            for (uint32_t i = 0; i < n; i++) {
+                const float* v0 = &src[((size_t)j * stride + i) * 4];
+                const float* v1 = &src[((size_t)j * stride + i + n) * 4];
+                const float* v2 = &src[((size_t)(j + n) * stride + i) * 4];
+                const float* v3 = &src[((size_t)(j + n) * stride + i + n) * 4];
+                float r[4];
+                for (int c = 0; c < 4; c++) {
+                    if (op == 0) r[c] = fminf(fminf(v0[c], v1[c]), fminf(v2[c], v3[c]));
+                    else if (op == 1) r[c] = fmaxf(fmaxf(v0[c], v1[c]), fmaxf(v2[c], v3[c]));
+                    else r[c] = ((v0[c] + v1[c]) + v2[c]) + v3[c];
+                }
+                memcpy(&w[((size_t)j * n1 + i) * 4], r, sizeof(r));
+            }
+        }
+        src = w;
+        stride = n1;
+        if (n == 1) break;
+    }
+    memcpy(out, w, 4 * sizeof(float));
+    free(w);
+    return 0;
+}
+
 /* the pinned single-precision functions of sppm_fpmath.h evaluated on the host:
    fn 0 sin, 1 cos, 2 pow(x,y), 3 exp, 4 log2, 5 exp2 */
 EXPORT void ORACLE_API(fpmath)(int fn, const float* x, const float* y, float* out, size_t n) {

@@ -140,3 +140,27 @@ def test_watchdog_on_cyclic_bvh_links(cornell_metal):
     ok.set_camera(cam)
     ok.run_passes(2)
     ok.synchronize()
+
+
+def test_hash_build_stage_entry_point_matches_oracle_and_golden():
+    """sppm_hash_build (hash.fs + scatter.vs depth test + correction.vs blend) on caller device
+    arrays: winners and counts bit-equal the oracle and the committed golden grid."""
+    torch = pytest.importorskip("torch")
+    from oracle.binding import hash_build as oracle_hash_build
+    k = load_npz("kat_hash.npz")
+    pw, ph = int(k["photon_width"]), int(k["photon_height"])
+    pos = torch.from_numpy(k["pos"]).cuda()
+    flux = torch.from_numpy(k["flux"]).cuda()
+    stream = torch.cuda.current_stream()
+    for hs in (4096, 1000):
+        for flags in (0, 1):
+            w = torch.empty(hs, dtype=torch.int32, device="cuda")
+            c = torch.empty(hs, dtype=torch.int32, device="cuda")
+            g.renderer.hash_build(pos.data_ptr(), flux.data_ptr(), pw, ph, hs, k["bbox_min"], float(k["grid_scale"]),
+                                  flags, w.data_ptr(), c.data_ptr(), stream.cuda_stream)
+            stream.synchronize()
+            wg = w.cpu().numpy().view(np.uint32)
+            cg = c.cpu().numpy().view(np.uint32)
+            assert np.array_equal(wg, k[f"winner_{hs}_{flags}"]) and np.array_equal(cg, k[f"count_{hs}_{flags}"])
+            wo, co = oracle_hash_build(k["pos"], k["flux"], pw, ph, hs, k["bbox_min"], float(k["grid_scale"]), flags)
+            assert np.array_equal(wg, wo) and np.array_equal(cg, co)
