@@ -61,22 +61,31 @@ class ClockSampler:
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,timestamp")
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
         self.out = None
+        self.window = None
 
     def __enter__(self):
         try:
             self.out = tempfile.TemporaryFile(mode="w+")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.out, stderr=subprocess.DEVNULL)
+            # wait (bounded) for the first sample so that the timed region is covered
+            t0 = time.time()
+            while time.time() - t0 < 5.0 and self.out.tell() == 0:
+                time.sleep(0.05)
         except Exception:
             self.proc = None
         return self
+
+    def mark(self, start: float, end: float):
+        """Wall-clock window of the timed region; samples outside it are ignored."""
+        self.window = (start, end)
 
     def __exit__(self, *exc):
         if self.proc:
@@ -93,6 +102,17 @@ class ClockSampler:
         rows = [r.split(", ") for r in self.out.read().strip().splitlines() if r.strip()]
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        import datetime
+        inside = []
+        for r in rows:
+            try:
+                ts = datetime.datetime.strptime(r[9].strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except (ValueError, IndexError):
+                ts = None
+            if self.window is None or ts is None or (self.window[0] - 0.06 <= ts <= self.window[1] + 0.06):
+                inside.append(r)
+        if len(inside) >= 2:
+            rows = inside
         for r in rows:
             try:
                 sm.append(float(r[1]))
@@ -218,6 +238,7 @@ def run_gpu(args, rank, world, local):
     K, W = args.steps, args.warmup
     P = cfg.photon_width * cfg.photon_height
     npix = cfg.width * cfg.height
+    clocks = ClockSampler(dev).__enter__()
     # warm-up passes (include at least one eye pass), then align to an eye-pass boundary so the
     # timed region holds exactly one eye pass per 10 passes
     r.run_passes(W)
@@ -231,8 +252,10 @@ def run_gpu(args, rank, world, local):
     r.enable_stage_timing(True)
     r.read_stage_times()
     barrier(world)
-    with ClockSampler(dev) as clocks:
-        ms = r.time_passes(K)
+    t_wall = time.time()
+    ms = r.time_passes(K)
+    clocks.mark(t_wall, time.time())
+    clocks.__exit__(None, None, None)
     stages = r.read_stage_times()
     r.enable_stage_timing(False)
     fi1 = r.frame_info()
