@@ -9,6 +9,7 @@
 // ((v0 + v1) + v2) + v3 with non-fused adds, so all three results are bit-identical to the
 // reference's fold.
 #include <cstdint>
+#include <mutex>
 
 #include <cuda_runtime.h>
 
@@ -59,6 +60,62 @@ void launch_reduce_texture(const float4* tex, uint32_t resolution, uint32_t op, 
 }  // namespace sppm_dev
 
 using sppm::fail;
+
+// ---- variant without device allocation ---------------------------------------------------------
+// Its scratch is this file-scope device array: 512 x 512 float4 = 4 MiB, held by every GPU that
+// loads the library until the process exits.  Host code must not pass `g_reduce_scratch` itself to a
+// kernel (on the host it names a host-side shadow, not device memory): the device address is looked
+// up with cudaGetSymbolAddress once per device, with that device current, and cached.
+static __device__ __align__(256) float4 g_reduce_scratch[(SPPM_REDUCE_NOALLOC_MAX_RESOLUTION / 2) *
+                                                         (SPPM_REDUCE_NOALLOC_MAX_RESOLUTION / 2)];
+
+namespace {
+std::mutex g_scratch_mutex;
+float4* g_scratch_ptr[64] = {nullptr};  // device address of g_reduce_scratch, per device ordinal
+
+int scratch_address(float4** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(SPPM_ERR_CUDA, "cudaGetDevice failed: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= 64) return fail(SPPM_ERR_ARG, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_reduce_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(SPPM_ERR_CUDA, "cudaGetSymbolAddress(g_reduce_scratch) failed: %s", cudaGetErrorString(e));
+        g_scratch_ptr[dev] = static_cast<float4*>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return SPPM_OK;
+}
+}  // namespace
+
+extern "C" int sppm_reduce_texture_noalloc(const float* d_texture, uint32_t resolution, uint32_t op, float out[4],
+                                           void* stream) {
+    if (!d_texture || !out) return fail(SPPM_ERR_ARG, "sppm_reduce_texture_noalloc: null argument");
+    if (resolution < 2 || (resolution & (resolution - 1)))
+        return fail(SPPM_ERR_ARG, "sppm_reduce_texture_noalloc: resolution %u must be a power of two >= 2", resolution);
+    if (resolution > SPPM_REDUCE_NOALLOC_MAX_RESOLUTION)
+        return fail(SPPM_ERR_ARG,
+                    "sppm_reduce_texture_noalloc: resolution %u exceeds the maximum %u of its fixed scratch "
+                    "(use sppm_reduce_texture)", resolution, (unsigned)SPPM_REDUCE_NOALLOC_MAX_RESOLUTION);
+    if (op > SPPM_REDUCE_SUM) return fail(SPPM_ERR_ARG, "sppm_reduce_texture_noalloc: unknown op %u", op);
+    if (reinterpret_cast<uintptr_t>(d_texture) & 15) return fail(SPPM_ERR_ARG, "texture must be 16-byte aligned");
+    float4* scratch = nullptr;
+    int st = scratch_address(&scratch);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    // no clearing needed: every level writes each scratch texel it later reads
+    sppm_dev::launch_reduce_texture(reinterpret_cast<const float4*>(d_texture), resolution, op, scratch, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, scratch, sizeof(float4), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e2 = cudaStreamSynchronize(s);
+    if (e != cudaSuccess || e2 != cudaSuccess)
+        return fail(SPPM_ERR_CUDA, "sppm_reduce_texture_noalloc failed: %s",
+                    cudaGetErrorString(e != cudaSuccess ? e : e2));
+    return SPPM_OK;
+}
 
 extern "C" int sppm_reduce_texture(const float* d_texture, uint32_t resolution, uint32_t op, float out[4],
                                    void* stream) {

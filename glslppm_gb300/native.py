@@ -117,6 +117,7 @@ SIGNATURES = {
     "sppm_hash_build": (C.c_int, [P, P, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), C.c_float,
                                   C.c_uint32, P, P, P]),
     "sppm_reduce_texture": (C.c_int, [P, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), P]),
+    "sppm_reduce_texture_noalloc": (C.c_int, [P, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), P]),
     "sppm_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "sppm_debug_fpmath": (C.c_int, [C.c_int, P, P, P, C.c_size_t]),
     "sppm_device_count": (C.c_int, []),

@@ -268,6 +268,21 @@ typedef enum sppm_reduce_op { SPPM_REDUCE_MIN = 0, SPPM_REDUCE_MAX = 1, SPPM_RED
    returns; the call synchronizes `stream`. */
 int sppm_reduce_texture(const float* d_texture, uint32_t resolution, uint32_t op, float out[4], void* stream);
 
+/* sppm_reduce_texture for callers that must not allocate device memory -- an engine that reserved
+   the GPU's memory for its own allocator before loading this library, a render loop that forbids
+   allocation (and the implicit synchronization cudaMalloc may bring) once it is running.  It has
+   no counterpart in the reference, whose ReduceTexture draws into a texture created at start-up.
+   Its scratch is a fixed 4 MiB array in the library's device memory, which every GPU that loads the
+   library keeps until the process exits; resolutions above SPPM_REDUCE_NOALLOC_MAX_RESOLUTION are
+   rejected with SPPM_ERR_ARG.  The first call on a device looks up the array's device address
+   (cudaGetSymbolAddress, which may load the library's device code): make that first call before
+   any stream capture.  All calls share the array: calls that overlap on the GPU (on different
+   streams, or from several threads) race on it and must be serialised by the caller.  Nothing in
+   the array needs to start at zero.  Results equal sppm_reduce_texture's bit for bit. */
+#define SPPM_REDUCE_NOALLOC_MAX_RESOLUTION 1024u
+int sppm_reduce_texture_noalloc(const float* d_texture, uint32_t resolution, uint32_t op, float out[4],
+                                void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------------------------ */
 /* Message of the last failed call on this thread; returns the full message length. */
 size_t sppm_last_error(char* buf, size_t buf_size);
