@@ -126,9 +126,9 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def profile_traffic():
-    """Per-launch DRAM traffic of the photon kernel on this workload, from the committed ncu summary."""
-    p = REPO / "profiles" / "k_photon_cornell1024.md"
+def profile_traffic(kernel: str):
+    """Per-launch DRAM traffic of `kernel` on this workload, from its committed ncu summary."""
+    p = REPO / "profiles" / f"{kernel}_cornell1024.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -288,16 +288,17 @@ def run_gpu(args, rank, world, local):
     # roofline of the photon kernel: algorithmic bytes per photon segment = 64 + 32 V + 36 T
     # (ray state in/out, 32-byte nodes, 36-byte triangles), V/T from the traversal counters
     peak, peak_kind = measured_peaks()
-    ph_ms, ph_n = stages["photon"]
+    kernel = "k_trace_photons" if stages["photon_trace"][1] else "k_photon"
+    ph_ms, ph_n = stages["photon_trace"] if stages["photon_trace"][1] else stages["photon"]
     roof = None
     cnt = traversal_counters(r)
     if ph_n and cnt:
         seg_per_launch = cnt["photon_segments"] / cnt["passes"]
         bytes_per_launch = seg_per_launch * (64 + 32 * cnt["nodes_per_segment"] + 36 * cnt["tris_per_segment"])
         achieved = bytes_per_launch / (ph_ms / ph_n / 1000.0) / 1e9
-        traffic = profile_traffic()
+        traffic = profile_traffic(kernel)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": "k_photon",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": kernel,
                 "peak_kind": peak_kind, "nodes_per_segment": round(cnt["nodes_per_segment"], 2),
                 "tris_per_segment": round(cnt["tris_per_segment"], 2),
                 "algorithmic_bytes_per_launch": round(bytes_per_launch)}

@@ -82,6 +82,8 @@ struct sppm_ctx {
     JobDesc* d_job = nullptr;
     JobState* d_state = nullptr;
     uint32_t* d_tables = nullptr;  // job_ids[1], prefix_pix[2], prefix_ph[2], prefix_hash[2]
+    RayQueue queue{};
+    uint32_t trace_blocks = 0;
     float* d_image = nullptr;
     bool have_scene = false, have_camera = false;
     uint32_t frames = 0;  // host mirror of frames queued since reset
@@ -411,6 +413,7 @@ int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out) {
     bytes += 6 * Arena::align(np * 16) + 2 * Arena::align(np * 4) + Arena::align(np * 12);
     bytes += 4 * Arena::align(P * 16) + Arena::align(P * 8);
     bytes += 2 * Arena::align(hn * 4);
+    bytes += 3 * Arena::align(P * 16) + Arena::align(64);  // ray queue of the wavefront photon pass
     if ((st = c->state_mem.reserve(bytes))) return st;
     Arena& a = c->state_mem;
     c->d_job = a.take<JobDesc>(1);
@@ -434,6 +437,16 @@ int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out) {
     J.ph.hit = a.take<int2>(P);
     J.winner = a.take<uint32_t>(hn);
     J.count = a.take<uint32_t>(hn);
+    c->queue.org = a.take<float4>(P);
+    c->queue.dir = a.take<float4>(P);
+    c->queue.hit = a.take<float4>(P);
+    c->queue.counters = a.take<uint32_t>(16);
+    c->queue.capacity = c->P;
+    {
+        int sms = 0;
+        SPPM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        c->trace_blocks = (uint32_t)sms * trace_photons_blocks_per_sm();
+    }
     if (!J.count) return fail(SPPM_ERR_OOM, "state arena sizing error");
     J.state = c->d_state;
     J.image = c->d_image;
@@ -556,7 +569,7 @@ int sppm_run_passes(sppm_ctx* c, uint32_t n) {
     for (uint32_t k = 0; k < n; k++) {
         const bool eye = (c->frames % interval) == 0;
         timed(c, SPPM_STAGE_FRAME_BEGIN, true);
-        launch_frame_begin(hsh, c->stream);
+        launch_frame_begin(hsh, c->queue, c->stream);
         timed(c, SPPM_STAGE_FRAME_BEGIN, false);
         if (eye) {
             timed(c, SPPM_STAGE_EYE, true);
@@ -566,9 +579,21 @@ int sppm_run_passes(sppm_ctx* c, uint32_t n) {
             launch_grid(c->d_job, c->d_tables, 1, c->stream);
             timed(c, SPPM_STAGE_GRID, false);
         }
-        timed(c, SPPM_STAGE_PHOTON, true);
-        launch_photon_fp32(pho, c->count_traversal, c->stream);
-        timed(c, SPPM_STAGE_PHOTON, false);
+        if (c->cfg.flags & SPPM_FLAG_FUSED_PHOTON) {
+            timed(c, SPPM_STAGE_PHOTON, true);
+            launch_photon_fp32(pho, c->count_traversal, c->stream);
+            timed(c, SPPM_STAGE_PHOTON, false);
+        } else {
+            timed(c, SPPM_STAGE_PHOTON, true);
+            launch_photon_gen_fp32(pho, c->queue, c->stream);
+            timed(c, SPPM_STAGE_PHOTON, false);
+            timed(c, SPPM_STAGE_PHOTON_TRACE, true);
+            launch_trace_photons_fp32(pho, c->queue, c->count_traversal, c->trace_blocks, c->stream);
+            timed(c, SPPM_STAGE_PHOTON_TRACE, false);
+            timed(c, SPPM_STAGE_PHOTON_STORE, true);
+            launch_photon_store_fp32(pho, c->queue, c->stream);
+            timed(c, SPPM_STAGE_PHOTON_STORE, false);
+        }
         timed(c, SPPM_STAGE_GATHER, true);
         launch_gather_fp32(pix, c->stream);
         timed(c, SPPM_STAGE_GATHER, false);

@@ -102,6 +102,15 @@ struct JobDesc {
     float alpha, footprint, focal, aperture, fixed_radius;
 };
 
+// ray queue of the wavefront photon pass: org.w holds the photon's global item index
+struct RayQueue {
+    float4* org;
+    float4* dir;
+    float4* hit;          // (triangle or -1 as int bits, barycentrics v, w, u)
+    uint32_t* counters;   // [0] rays queued, [1] fetch head of the trace kernel
+    uint32_t capacity;
+};
+
 // the work of one launch: items [prefix[k], prefix[k+1]) belong to jobs[job_ids[k]]
 struct LaunchSet {
     const JobDesc* jobs;

@@ -8,10 +8,15 @@
 namespace sppm_dev {
 
 // plain FP32 path (kernels_fp32.cu)
-void launch_frame_begin(const LaunchSet& ls, cudaStream_t s);
+void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
 void launch_eye_fp32(const LaunchSet& ls, cudaStream_t s);
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s);
 void launch_photon_fp32(const LaunchSet& ls, bool count_traversal, cudaStream_t s);
+void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
+void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool count_traversal,
+                               uint32_t persistent_blocks, cudaStream_t s);
+void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
+uint32_t trace_photons_blocks_per_sm();
 void launch_gather_fp32(const LaunchSet& ls, cudaStream_t s);
 void launch_resolve_fp32(const LaunchSet& ls, uint32_t display, cudaStream_t s);
 void launch_hash_build(const float4* pos, const float4* flux, uint32_t pw, uint32_t ph, uint32_t hash_num,

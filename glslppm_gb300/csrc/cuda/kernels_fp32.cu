@@ -177,8 +177,12 @@ __device__ __forceinline__ float xorshift_frand(uint32_t* s) {
     return xmul(__uint2float_rn(s[3]), 1.0f / 4294967295.0f);
 }
 
-__global__ void k_frame_begin(LaunchSet ls) {
+__global__ void k_frame_begin(LaunchSet ls, RayQueue q) {
     const uint32_t g = grid_tid();
+    if (g == 0 && q.counters) {
+        q.counters[0] = 0;
+        q.counters[1] = 0;
+    }
     if (g >= ls.total) return;
     const int k = find_job(ls, g);
     const JobDesc& J = ls.jobs[ls.job_ids[k]];
@@ -465,77 +469,53 @@ __device__ __forceinline__ void matte_bounce(float4& rndv, f3 ipos, f3 gnrm, f3 
     if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
-    const uint32_t g = grid_tid();
-    if (g >= ls.total) return;
-    const int k = find_job(ls, g);
-    const JobDesc& J = ls.jobs[ls.job_ids[k]];
-    JobState* st = J.state;
-    const DevScene& S = J.scene;
-    const uint32_t sidx = g - ls.prefix[k];
-    const float eps = 1e-6f;
-    uint32_t err = 0;
-    const uint32_t frame = st->frame;
-    float4 rndv = J.ph.rng[sidx];
-    const int2 hitin = frame == 0 ? make_int2(-1, 0) : J.ph.hit[sidx];
-    f3 flux, rorg = mk(0, 0, 0), rdir = mk(0, 0, 0);
+// emit a photon or bounce the stored one (photontrace.fs main :464-686): the ray of this pass
+struct PhotonRay {
+    f3 org, dir, flux;
+    float depth;
     bool cont;
     uint32_t emitted;
-    float depth = xadd((float)hitin.y, 1.0f);
-    if (hitin.x < 0 || depth >= (float)J.max_path) {
-        if (S.light_area != 0.0f) light_sample(J, rndv, flux, rdir, rorg, err);
-        else ibl_sample(J, rndv, flux, rdir, rorg);
-        emitted = 1;
-        depth = 0.0f;
-        cont = true;
-    } else {
-        const float4 PP = J.ph.pos[sidx], PF = J.ph.flux[sidx], PD = J.ph.dir[sidx];
-        flux = mk(fabsf(PF.x), fabsf(PF.y), fabsf(PF.z));
-        const f3 ipos = xyz(PP);
-        f3 inrm = mk(PP.w, PF.w, PD.w);
-        const f3 pd = xyz(PD);
-        const float4 r0 = __ldg(S.tri_shade + (size_t)hitin.x * 6);
-        const f3 gnrm = mk(r0.x, r0.y, r0.z);
-        const DevMaterial& m = S.mats[__float_as_int(r0.w)];
-        f3 icol = mk(m.color[0], m.color[1], m.color[2]);
-        const int brdf = m.brdf;
-        if (brdf == 0) {
-            matte_bounce(rndv, ipos, gnrm, inrm, eps, rorg, rdir);
-        } else if (brdf == 1 || brdf == 4) {
-            rorg = add(ipos, scl(gnrm, eps));
-            if (brdf == 4) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
-            rdir = reflect(pd, inrm);
-            if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
-        } else if (brdf == 2 || brdf == 5) {
-            if (brdf == 5) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
-            const float ln = dot(inrm, pd);
-            if (ln < 0.0f) {
-                const float re = fresnel(neg(pd), inrm, 1.0f, m.eta);
-                if (gpu_rnd(rndv) < re) {
-                    rorg = add(ipos, scl(gnrm, eps));
-                    rdir = reflect(pd, inrm);
-                    icol = mk(1.0f, 1.0f, 1.0f);
-                    if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
-                } else {
-                    rorg = sub(ipos, scl(gnrm, eps));
-                    rdir = refract(pd, inrm, xdiv(1.0f, m.eta));
-                    if (dot(rdir, gnrm) > 0.0f) rdir = neg(rdir);
-                }
-            } else {
-                const float re = fresnel(neg(pd), neg(inrm), m.eta, 1.0f);
-                if (gpu_rnd(rndv) < re) {
-                    rorg = sub(ipos, scl(gnrm, eps));
-                    rdir = reflect(pd, neg(inrm));
-                    if (dot(rdir, neg(gnrm)) < 0.0f) rdir = neg(rdir);
-                } else {
-                    rorg = add(ipos, scl(gnrm, eps));
-                    rdir = refract(pd, neg(inrm), m.eta);
-                    if (dot(rdir, neg(gnrm)) > 0.0f) rdir = neg(rdir);
-                }
-            }
-        } else if (brdf == 3 || brdf == 6) {
-            if (brdf == 6) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
+};
+
+__device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t sidx, uint32_t frame, float4& rndv,
+                                                     uint32_t& err) {
+    const DevScene& S = J.scene;
+    const float eps = 1e-6f;
+    PhotonRay R;
+    R.org = mk(0, 0, 0);
+    R.dir = mk(0, 0, 0);
+    const int2 hitin = frame == 0 ? make_int2(-1, 0) : J.ph.hit[sidx];
+    R.depth = xadd((float)hitin.y, 1.0f);
+    if (hitin.x < 0 || R.depth >= (float)J.max_path) {
+        if (S.light_area != 0.0f) light_sample(J, rndv, R.flux, R.dir, R.org, err);
+        else ibl_sample(J, rndv, R.flux, R.dir, R.org);
+        R.emitted = 1;
+        R.depth = 0.0f;
+        R.cont = true;
+        return R;
+    }
+    const float4 PP = J.ph.pos[sidx], PF = J.ph.flux[sidx], PD = J.ph.dir[sidx];
+    f3 flux = mk(fabsf(PF.x), fabsf(PF.y), fabsf(PF.z));
+    const f3 ipos = xyz(PP);
+    f3 inrm = mk(PP.w, PF.w, PD.w);
+    const f3 pd = xyz(PD);
+    const float4 r0 = __ldg(S.tri_shade + (size_t)hitin.x * 6);
+    const f3 gnrm = mk(r0.x, r0.y, r0.z);
+    const DevMaterial& m = S.mats[__float_as_int(r0.w)];
+    f3 icol = mk(m.color[0], m.color[1], m.color[2]);
+    const int brdf = m.brdf;
+    f3 rorg = mk(0, 0, 0), rdir = mk(0, 0, 0);
+    if (brdf == 0) {
+        matte_bounce(rndv, ipos, gnrm, inrm, eps, rorg, rdir);
+    } else if (brdf == 1 || brdf == 4) {
+        rorg = add(ipos, scl(gnrm, eps));
+        if (brdf == 4) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
+        rdir = reflect(pd, inrm);
+        if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
+    } else if (brdf == 2 || brdf == 5) {
+        if (brdf == 5) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
+        const float ln = dot(inrm, pd);
+        if (ln < 0.0f) {
             const float re = fresnel(neg(pd), inrm, 1.0f, m.eta);
             if (gpu_rnd(rndv) < re) {
                 rorg = add(ipos, scl(gnrm, eps));
@@ -543,63 +523,91 @@ __global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
                 icol = mk(1.0f, 1.0f, 1.0f);
                 if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
             } else {
-                matte_bounce(rndv, ipos, gnrm, inrm, eps, rorg, rdir);
+                rorg = sub(ipos, scl(gnrm, eps));
+                rdir = refract(pd, inrm, xdiv(1.0f, m.eta));
+                if (dot(rdir, gnrm) > 0.0f) rdir = neg(rdir);
+            }
+        } else {
+            const float re = fresnel(neg(pd), neg(inrm), m.eta, 1.0f);
+            if (gpu_rnd(rndv) < re) {
+                rorg = sub(ipos, scl(gnrm, eps));
+                rdir = reflect(pd, neg(inrm));
+                if (dot(rdir, neg(gnrm)) < 0.0f) rdir = neg(rdir);
+            } else {
+                rorg = add(ipos, scl(gnrm, eps));
+                rdir = refract(pd, neg(inrm), m.eta);
+                if (dot(rdir, neg(gnrm)) > 0.0f) rdir = neg(rdir);
             }
         }
-        // Russian roulette (:671-685)
-        const float pmax = fmaxf(fmaxf(icol.x, icol.y), icol.z);
-        if (pmax < gpu_rnd(rndv)) {
-            cont = false;
+    } else if (brdf == 3 || brdf == 6) {
+        if (brdf == 6) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
+        const float re = fresnel(neg(pd), inrm, 1.0f, m.eta);
+        if (gpu_rnd(rndv) < re) {
+            rorg = add(ipos, scl(gnrm, eps));
+            rdir = reflect(pd, inrm);
+            icol = mk(1.0f, 1.0f, 1.0f);
+            if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
         } else {
-            cont = true;
-            icol = mk(xdiv(icol.x, pmax), xdiv(icol.y, pmax), xdiv(icol.z, pmax));
-            flux = mul(flux, icol);
+            matte_bounce(rndv, ipos, gnrm, inrm, eps, rorg, rdir);
         }
-        emitted = 0;
     }
-    bool store = false;
-    f3 ppos = mk(0, 0, 0);
-    TraversalCount tc;
-    if (cont) {
-        const Hit h = trace_exact<true, COUNT>(S, rorg, rdir, false, err, &tc);
-        f3 pnrm = mk(0, 0, 0), pg = mk(0, 0, 0);
-        int brdf = 0;
-        if (h.tri >= 0) {
-            const Shade i = shade_hit(S, h);
-            ppos = i.pos;
-            pnrm = i.nrm;
-            pg = i.gnrm;
-            brdf = i.brdf;
-        }
-        if (h.tri < 0 || (brdf != 0 && brdf != 6 && brdf != 3)) flux = neg(flux);
-        const float gf = fminf(fabsf(xdiv(dot(rdir, pnrm), dot(rdir, pg))), 2.236068010e+00f);
-        flux = scl(flux, gf);
-        J.ph.pos[sidx] = f4(ppos, pnrm.x);
-        J.ph.flux[sidx] = f4(flux, pnrm.y);
-        J.ph.dir[sidx] = f4(rdir, pnrm.z);
-        J.ph.hit[sidx] = make_int2(h.tri, (int)depth);
-        store = !(flux.x < 0.0f);
+    // Russian roulette (:671-685)
+    const float pmax = fmaxf(fmaxf(icol.x, icol.y), icol.z);
+    if (pmax < gpu_rnd(rndv)) {
+        R.cont = false;
     } else {
-        J.ph.pos[sidx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        J.ph.flux[sidx] = make_float4(-1.0f, -1.0f, -1.0f, 0.0f);
-        J.ph.dir[sidx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        J.ph.hit[sidx] = make_int2(-1, 0);
+        R.cont = true;
+        icol = mk(xdiv(icol.x, pmax), xdiv(icol.y, pmax), xdiv(icol.z, pmax));
+        flux = mul(flux, icol);
     }
-    J.ph.rng[sidx] = rndv;
+    R.emitted = 0;
+    R.org = rorg;
+    R.dir = rdir;
+    R.flux = flux;
+    return R;
+}
 
-    // ---- hashed grid build (hash.fs main :51-68, scatter.vs :11-23, correction.vs :8-13) ----
-    uint32_t slot = 0xFFFFFFFFu;
-    if (store) {
-        const f3 cell = mk(floorf(xmul(xsub(ppos.x, st->bbmin[0]), st->grid_scale)),
-                           floorf(xmul(xsub(ppos.y, st->bbmin[1]), st->grid_scale)),
-                           floorf(xmul(xsub(ppos.z, st->bbmin[2]), st->grid_scale)));
-        slot = hash_cell(cell, st->grid_scale, st->hash_scale1, (float)J.hash_num);
+__device__ __forceinline__ void photon_terminate(const JobDesc& J, uint32_t sidx) {
+    J.ph.pos[sidx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    J.ph.flux[sidx] = make_float4(-1.0f, -1.0f, -1.0f, 0.0f);
+    J.ph.dir[sidx] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    J.ph.hit[sidx] = make_int2(-1, 0);
+}
+
+// store the traced photon (photontrace.fs :692-709); returns the hash slot or 0xFFFFFFFF
+__device__ __forceinline__ uint32_t photon_store(const JobDesc& J, const JobState* st, uint32_t sidx, const Hit& h,
+                                                 f3 rdir, f3 flux, float depth) {
+    const DevScene& S = J.scene;
+    f3 ppos = mk(0, 0, 0), pnrm = mk(0, 0, 0), pg = mk(0, 0, 0);
+    int brdf = 0;
+    if (h.tri >= 0) {
+        const Shade i = shade_hit(S, h);
+        ppos = i.pos;
+        pnrm = i.nrm;
+        pg = i.gnrm;
+        brdf = i.brdf;
     }
-    // photon index order = depth order; photons of the last row with i >= w/2 have z >= 1 and
-    // are clipped by the scatter draw (counted by the correction draw all the same)
+    if (h.tri < 0 || (brdf != 0 && brdf != 6 && brdf != 3)) flux = neg(flux);
+    const float gf = fminf(fabsf(xdiv(dot(rdir, pnrm), dot(rdir, pg))), 2.236068010e+00f);
+    flux = scl(flux, gf);
+    J.ph.pos[sidx] = f4(ppos, pnrm.x);
+    J.ph.flux[sidx] = f4(flux, pnrm.y);
+    J.ph.dir[sidx] = f4(rdir, pnrm.z);
+    J.ph.hit[sidx] = make_int2(h.tri, (int)depth);
+    if (flux.x < 0.0f) return 0xFFFFFFFFu;
+    // hash.fs main (:51-68): cell = floor((p - BBoxMin) * GridScale), slot = hash(cell)
+    const f3 cell = mk(floorf(xmul(xsub(ppos.x, st->bbmin[0]), st->grid_scale)),
+                       floorf(xmul(xsub(ppos.y, st->bbmin[1]), st->grid_scale)),
+                       floorf(xmul(xsub(ppos.z, st->bbmin[2]), st->grid_scale)));
+    return hash_cell(cell, st->grid_scale, st->hash_scale1, (float)J.hash_num);
+}
+
+// scatter.vs + depth test and correction.vs + blend, one atomic pair per warp and slot
+__device__ __forceinline__ void hash_insert(const JobDesc& J, int k, uint32_t sidx, uint32_t slot, unsigned active) {
+    const bool store = slot != 0xFFFFFFFFu;
+    // photon index order = depth order; photons of the last row with i >= w/2 have z >= 1 and are
+    // clipped by the scatter draw (counted by the correction draw all the same)
     const bool clipped = (J.flags & SPPM_FLAG_GL_DEPTH_CLIP) && sidx >= (J.PH - 1) * J.PW + (J.PW + 1) / 2;
-    const unsigned active = __activemask();
-    // slot keys are unique per job: combine job index and slot in 64 bits
     const unsigned long long key = store ? ((unsigned long long)k << 32) | slot : ~0ull;
     const unsigned peers = __match_any_sync(active, key);
     if (store) {
@@ -610,25 +618,229 @@ __global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
             if (wmin != 0xFFFFFFFFu) atomicMin(&J.winner[slot], wmin);
         }
     }
-    // ---- sum.fs: emitted photons; traced segments; errors (one atomic per warp and job) ----
+}
+
+// sum.fs (emitted photons), traced segments and errors: one atomic per warp and job
+__device__ __forceinline__ void photon_counters(JobState* st, int k, unsigned active, uint32_t emitted, uint32_t segs,
+                                                uint32_t err) {
     const unsigned jm = __match_any_sync(active, k);
     const uint32_t we = __reduce_add_sync(jm, emitted);
-    const uint32_t ws = __reduce_add_sync(jm, cont ? 1u : 0u);
+    const uint32_t ws = __reduce_add_sync(jm, segs);
     const uint32_t wr = __reduce_or_sync(jm, err);
     if ((threadIdx.x & 31) == (__ffs(jm) - 1)) {
         if (we) atomicAdd(&st->emitted_frame, we);
         if (ws) atomicAdd(&st->segments_frame, ws);
         if (wr) atomicOr(&st->err, wr);
     }
+}
+
+// fused photon pass: one thread per photon slot, generate + trace + store + hash insert
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
+    const uint32_t g = grid_tid();
+    if (g >= ls.total) return;
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    JobState* st = J.state;
+    const uint32_t sidx = g - ls.prefix[k];
+    uint32_t err = 0;
+    float4 rndv = J.ph.rng[sidx];
+    const PhotonRay R = photon_generate(J, sidx, st->frame, rndv, err);
+    uint32_t slot = 0xFFFFFFFFu;
+    TraversalCount tc;
+    if (R.cont) {
+        const Hit h = trace_exact<true, COUNT>(J.scene, R.org, R.dir, false, err, &tc);
+        slot = photon_store(J, st, sidx, h, R.dir, R.flux, R.depth);
+    } else {
+        photon_terminate(J, sidx);
+    }
+    J.ph.rng[sidx] = rndv;
+    const unsigned active = __activemask();
+    hash_insert(J, k, sidx, slot, active);
+    photon_counters(st, k, active, R.emitted, R.cont ? 1u : 0u, err);
     if (COUNT) {
+        const unsigned jm = __match_any_sync(active, k);
         const uint32_t wn = __reduce_add_sync(jm, tc.nodes);
         const uint32_t wt = __reduce_add_sync(jm, tc.tris);
+        const uint32_t ws = __reduce_add_sync(jm, R.cont ? 1u : 0u);
         if ((threadIdx.x & 31) == (__ffs(jm) - 1)) {
             atomicAdd(&st->count_nodes, (unsigned long long)wn);
             atomicAdd(&st->count_tris, (unsigned long long)wt);
             atomicAdd(&st->count_segments, (unsigned long long)ws);
         }
     }
+}
+
+// ----------------------------------------------------------------------------------------------
+// wavefront photon pass: generate -> trace (persistent, dynamic ray fetch) -> store
+// ----------------------------------------------------------------------------------------------
+// generate: emit/bounce every slot; RR-terminated photons are finished here, the others append
+// their ray to the queue (warp-aggregated append)
+__global__ void __launch_bounds__(128) k_photon_gen(LaunchSet ls, RayQueue q) {
+    const uint32_t g = grid_tid();
+    if (g >= ls.total) return;
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    JobState* st = J.state;
+    const uint32_t sidx = g - ls.prefix[k];
+    uint32_t err = 0;
+    float4 rndv = J.ph.rng[sidx];
+    const PhotonRay R = photon_generate(J, sidx, st->frame, rndv, err);
+    J.ph.rng[sidx] = rndv;
+    if (R.cont) {
+        J.ph.flux[sidx] = f4(R.flux, 0.0f);  // flux before the segment, read back by k_photon_store
+        J.ph.hit[sidx] = make_int2(-1, (int)R.depth);
+    } else {
+        photon_terminate(J, sidx);
+    }
+    const unsigned active = __activemask();
+    const unsigned live = __ballot_sync(active, R.cont);
+    uint32_t base = 0;
+    const int leader = __ffs(active) - 1;
+    if ((int)(threadIdx.x & 31) == leader && live) base = atomicAdd(&q.counters[0], __popc(live));
+    base = __shfl_sync(active, base, leader);
+    if (R.cont) {
+        const uint32_t qi = base + __popc(live & ((1u << (threadIdx.x & 31)) - 1));
+        q.org[qi] = make_float4(R.org.x, R.org.y, R.org.z, __uint_as_float(g));
+        q.dir[qi] = make_float4(R.dir.x, R.dir.y, R.dir.z, 0.0f);
+    }
+    photon_counters(st, k, active, R.emitted, R.cont ? 1u : 0u, err);
+}
+
+// trace: persistent warps; a lane whose ray finished fetches the next one from the queue, so
+// lanes stay busy while their neighbours walk longer paths (dynamic fetch)
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q) {
+    const uint32_t total = q.counters[0];
+    const unsigned lane = threadIdx.x & 31;
+    const uint32_t kNeed = 0xFFFFFFFFu, kDone = 0xFFFFFFFEu;
+    uint32_t idx = kNeed;
+    const NodeX* nodes = nullptr;
+    const float4* tri_isect = nullptr;
+    int32_t nn = 0;
+    f3 org = mk(0, 0, 0), dir = mk(0, 0, 0), rcp = mk(0, 0, 0), t0 = mk(0, 0, 0);
+    Hit h;
+    int32_t node = 0, steps = 0;
+    uint32_t err = 0;
+    int job_k = 0;
+    TraversalCount tc;
+    for (;;) {
+        const bool need = idx == kNeed;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(&q.counters[1], __popc(m));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (need) {
+                idx = base + __popc(m & ((1u << lane) - 1));
+                if (idx >= total) {
+                    idx = kDone;
+                } else {
+                    const float4 o = q.org[idx], d = q.dir[idx];
+                    const uint32_t g = __float_as_uint(o.w);
+                    job_k = find_job(ls, g);
+                    const DevScene& S = ls.jobs[ls.job_ids[job_k]].scene;
+                    org = mk(o.x, o.y, o.z);
+                    dir = mk(d.x, d.y, d.z);
+                    nn = (int32_t)S.num_nodes;
+                    nodes = S.nodes + (size_t)cube_face(dir) * nn;
+                    tri_isect = S.tri_isect;
+                    rcp = mk(xdiv(1.0f, dir.x), xdiv(1.0f, dir.y), xdiv(1.0f, dir.z));
+                    t0 = mul(neg(rcp), org);
+                    h.t = 1.0e30f;
+                    h.tri = -1;
+                    h.mat = -1;
+                    h.bu = h.bv = h.bw = 0.0f;
+                    node = 0;
+                    steps = 0;
+                }
+            }
+        }
+        if (__all_sync(0xFFFFFFFFu, idx == kDone)) break;
+        if (idx == kDone) continue;
+        bool finished = false;
+#pragma unroll 1
+        for (int it = 0; it < 32; it++) {
+            if (steps++ > nn) {
+                err |= kErrWatchdogTraverse;
+                finished = true;
+                break;
+            }
+            const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + node));
+            const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + node) + 1);
+            if (COUNT) tc.nodes++;
+            const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
+            const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
+            const float tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
+            const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
+            const bool hit = (tmin <= tmax) && (tmin <= h.t) && (tmax >= 0.0f);
+            const int32_t tri = __float_as_int(B.w);
+            if (hit && tri >= 0 && !(tri & kEmitterBit)) {
+                if (COUNT) tc.tris++;
+                const float4 a = __ldg(&tri_isect[(size_t)tri * 3 + 0]);
+                const float4 b = __ldg(&tri_isect[(size_t)tri * 3 + 1]);
+                const float4 c = __ldg(&tri_isect[(size_t)tri * 3 + 2]);
+                const f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
+                const f3 pv = cross(dir, e1);
+                const float det = dot(e0, pv);
+                const f3 tv = sub(org, v0);
+                const f3 qv = cross(tv, e0);
+                const float u = xdiv(dot(tv, pv), det);
+                const float v = xdiv(dot(dir, qv), det);
+                const float tt = xdiv(dot(e1, qv), det);
+                const float w = xsub(xsub(1.0f, u), v);
+                if (u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt < h.t) {
+                    h.t = tt;
+                    h.tri = tri;
+                    h.mat = __float_as_int(c.y);
+                    h.bu = v;
+                    h.bv = w;
+                    h.bw = u;
+                }
+            }
+            const int32_t next = hit ? node + 1 : __float_as_int(A.w);
+            if (next < 0 || next >= nn) {
+                finished = true;
+                break;
+            }
+            node = next;
+        }
+        if (finished) {
+            q.hit[idx] = make_float4(__int_as_float(h.tri), h.bu, h.bv, h.bw);
+            if (COUNT) {
+                JobState* st = ls.jobs[ls.job_ids[job_k]].state;
+                atomicAdd(&st->count_nodes, (unsigned long long)tc.nodes);
+                atomicAdd(&st->count_tris, (unsigned long long)tc.tris);
+                atomicAdd(&st->count_segments, 1ull);
+                tc.nodes = tc.tris = 0;
+            }
+            idx = kNeed;
+        }
+    }
+    if (err) atomicOr(&ls.jobs[ls.job_ids[job_k]].state->err, err);
+}
+
+// store: shade the hit of each queued ray, write the photon record, insert it into the grid
+__global__ void __launch_bounds__(128) k_photon_store(LaunchSet ls, RayQueue q) {
+    const uint32_t qi = grid_tid();
+    if (qi >= q.counters[0]) return;
+    const float4 o = q.org[qi], d = q.dir[qi], hr = q.hit[qi];
+    const uint32_t g = __float_as_uint(o.w);
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    const JobState* st = J.state;
+    const uint32_t sidx = g - ls.prefix[k];
+    Hit h;
+    h.tri = __float_as_int(hr.x);
+    h.bu = hr.y;
+    h.bv = hr.z;
+    h.bw = hr.w;
+    h.mat = h.tri >= 0 ? __float_as_int(__ldg(&J.scene.tri_isect[(size_t)h.tri * 3 + 2]).y) : -1;
+    const float4 f = J.ph.flux[sidx];
+    const int depth = J.ph.hit[sidx].y;
+    const uint32_t slot = photon_store(J, st, sidx, h, mk(d.x, d.y, d.z), mk(f.x, f.y, f.z), (float)depth);
+    hash_insert(J, k, sidx, slot, __activemask());
 }
 
 // ----------------------------------------------------------------------------------------------
@@ -780,8 +992,8 @@ __global__ void k_fpmath(int fn, const float* x, const float* y, float* out, uin
 // ----------------------------------------------------------------------------------------------
 static inline uint32_t blocks_for(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
 
-void launch_frame_begin(const LaunchSet& ls, cudaStream_t s) {
-    if (ls.total) k_frame_begin<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls);
+void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
+    if (ls.total) k_frame_begin<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls, q);
 }
 void launch_eye_fp32(const LaunchSet& ls, cudaStream_t s) {
     if (ls.total) k_eye<<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
@@ -793,6 +1005,27 @@ void launch_photon_fp32(const LaunchSet& ls, bool count, cudaStream_t s) {
     if (!ls.total) return;
     if (count) k_photon<true><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
     else k_photon<false><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
+}
+
+void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
+    if (ls.total) k_photon_gen<<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q);
+}
+
+void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool count, uint32_t persistent_blocks,
+                               cudaStream_t s) {
+    if (!ls.total) return;
+    if (count) k_trace_photons<true><<<persistent_blocks, 128, 0, s>>>(ls, q);
+    else k_trace_photons<false><<<persistent_blocks, 128, 0, s>>>(ls, q);
+}
+
+void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
+    if (ls.total) k_photon_store<<<blocks_for(q.capacity, 128), 128, 0, s>>>(ls, q);
+}
+
+uint32_t trace_photons_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_photons<false>, 128, 0) != cudaSuccess) n = 4;
+    return n > 0 ? (uint32_t)n : 1u;
 }
 void launch_gather_fp32(const LaunchSet& ls, cudaStream_t s) {
     if (ls.total) k_gather<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls);

@@ -31,8 +31,9 @@ PRECISION_FP32, PRECISION_MIXED = 0, 1
 RADIUS_FOOTPRINT, RADIUS_DIAGONAL = 0, 1
 SEED_XORSHIFT, SEED_HASH = 0, 1
 FLAG_GL_DEPTH_CLIP = 0x1
+FLAG_FUSED_PHOTON = 0x2
 IMAGE_RADIANCE, IMAGE_DISPLAY = 0, 1
-STAGES = ("frame_begin", "eye", "grid", "photon", "gather", "resolve")
+STAGES = ("frame_begin", "eye", "grid", "photon", "gather", "resolve", "photon_trace", "photon_store")
 
 STATE = {
     "hit_position": 0, "hit_reflectance": 1, "hit_normal": 2, "eye_rng": 3, "hit_triangle": 4,

@@ -73,6 +73,8 @@ typedef enum sppm_seed_mode {
 } sppm_seed_mode;
 
 /* Flags */
+#define SPPM_FLAG_FUSED_PHOTON 0x2u  /* one photon kernel per pass instead of the wavefront
+                                        generate -> trace -> store (same results) */
 #define SPPM_FLAG_GL_DEPTH_CLIP 0x1u /* scatter.vs: photons whose depth z >= 1 (last row, i >= w/2)
                                         are counted but never become a slot's stored photon */
 
@@ -234,10 +236,12 @@ typedef enum sppm_stage {
     SPPM_STAGE_FRAME_BEGIN = 0, /* hash clear + per-frame scalars                          */
     SPPM_STAGE_EYE = 1,         /* eyeraytrace.fs + max/min reductions                      */
     SPPM_STAGE_GRID = 2,        /* InitialRadius / GridScale (glslppm.cpp:294-311)          */
-    SPPM_STAGE_PHOTON = 3,      /* photontrace.fs + sum reduction + hash.fs/scatter/correction */
+    SPPM_STAGE_PHOTON = 3,      /* photontrace.fs emit/bounce (+ trace, store, hash when fused) */
     SPPM_STAGE_GATHER = 4,      /* progressive.fs                                          */
     SPPM_STAGE_RESOLVE = 5,     /* re.fs                                                   */
-    SPPM_STAGE_COUNT = 6
+    SPPM_STAGE_PHOTON_TRACE = 6, /* photon segment traversal (wavefront pass)              */
+    SPPM_STAGE_PHOTON_STORE = 7, /* photon store + hash.fs/scatter/correction (wavefront)  */
+    SPPM_STAGE_COUNT = 8
 } sppm_stage;
 int sppm_enable_stage_timing(sppm_ctx* ctx, int enable);
 int sppm_read_stage_times(sppm_ctx* ctx, float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]);

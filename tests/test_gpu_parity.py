@@ -77,6 +77,17 @@ def test_state_bit_exact_cornell_box_diagonal_radius(cornell_c1_mesh):
     run_pair(cfg, mesh.scene(), cam, [1, 12, 30])
 
 
+def test_fused_photon_kernel_bit_exact(cornell_c1_mesh):
+    """The single-kernel photon pass (SPPM_FLAG_FUSED_PHOTON) and the default wavefront
+    (generate -> persistent trace -> store) produce the same state."""
+    sc, mesh = cornell_c1_mesh
+    cfg = g.default_config(32, photon_width=64, photon_height=64, radius_rule=N.RADIUS_DIAGONAL,
+                           radius_fraction=0.01)
+    cfg.flags |= N.FLAG_FUSED_PHOTON
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 32, 32, sc.fov)
+    run_pair(cfg, mesh.scene(), cam, [1, 11])
+
+
 def test_state_bit_exact_non_square_and_hash_seed(cornell_c1_mesh):
     sc, mesh = cornell_c1_mesh
     cfg = g.default_config(40, height=24, photon_width=48, photon_height=20, hash_slots=1500,
