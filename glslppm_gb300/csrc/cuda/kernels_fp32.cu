@@ -758,71 +758,53 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
             }
         }
         if (__all_sync(0xFFFFFFFFu, idx == kDone)) break;
-        // node phase: lanes walk nodes until about half of the lanes still tracing wait on a
-        // triangle test (postponed leaf test): a lane that reaches a leaf whose box it hits
-        // stops there and tests the triangle in the leaf phase below together with the other
-        // waiting lanes, then continues at node + 1 -- the order in which each ray visits nodes
-        // and tests triangles is unchanged
+        if (idx == kDone) continue;
         bool finished = false;
-        int32_t pend_tri = -1;
 #pragma unroll 1
-        for (int it = 0; it < 64; it++) {
-            if (idx < kDone && pend_tri < 0 && !finished) {
-                if (steps++ > nn) {
-                    err |= kErrWatchdogTraverse;
-                    finished = true;
-                } else {
-                    const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + node));
-                    const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + node) + 1);
-                    if (COUNT) tc.nodes++;
-                    const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y),
-                                lz = xadd(xmul(rcp.z, A.z), t0.z);
-                    const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y),
-                                hz = xadd(xmul(rcp.z, B.z), t0.z);
-                    const float tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
-                    const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
-                    const bool hit = (tmin <= tmax) && (tmin <= h.t) && (tmax >= 0.0f);
-                    const int32_t tri = __float_as_int(B.w);
-                    if (hit && tri >= 0 && !(tri & kEmitterBit)) {
-                        pend_tri = tri;  // test in the leaf phase, then continue at node + 1
-                    } else {
-                        const int32_t next = hit ? node + 1 : __float_as_int(A.w);
-                        if (next < 0 || next >= nn) finished = true;
-                        else node = next;
-                    }
+        for (int it = 0; it < 32; it++) {
+            if (steps++ > nn) {
+                err |= kErrWatchdogTraverse;
+                finished = true;
+                break;
+            }
+            const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + node));
+            const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + node) + 1);
+            if (COUNT) tc.nodes++;
+            const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
+            const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
+            const float tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
+            const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
+            const bool hit = (tmin <= tmax) && (tmin <= h.t) && (tmax >= 0.0f);
+            const int32_t tri = __float_as_int(B.w);
+            if (hit && tri >= 0 && !(tri & kEmitterBit)) {
+                if (COUNT) tc.tris++;
+                const float4 a = __ldg(&tri_isect[(size_t)tri * 3 + 0]);
+                const float4 b = __ldg(&tri_isect[(size_t)tri * 3 + 1]);
+                const float4 c = __ldg(&tri_isect[(size_t)tri * 3 + 2]);
+                const f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
+                const f3 pv = cross(dir, e1);
+                const float det = dot(e0, pv);
+                const f3 tv = sub(org, v0);
+                const f3 qv = cross(tv, e0);
+                const float u = xdiv(dot(tv, pv), det);
+                const float v = xdiv(dot(dir, qv), det);
+                const float tt = xdiv(dot(e1, qv), det);
+                const float w = xsub(xsub(1.0f, u), v);
+                if (u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt < h.t) {
+                    h.t = tt;
+                    h.tri = tri;
+                    h.mat = __float_as_int(c.y);
+                    h.bu = v;
+                    h.bv = w;
+                    h.bw = u;
                 }
             }
-            // leave the walk once idle lanes (waiting for a test, or finished and waiting for a new
-            // ray) are as many as the walking ones
-            const unsigned waiting = __ballot_sync(0xFFFFFFFFu, pend_tri >= 0 || (finished && idx < kDone));
-            const unsigned walking = __ballot_sync(0xFFFFFFFFu, idx < kDone && pend_tri < 0 && !finished);
-            if (!walking || __popc(waiting) >= __popc(walking)) break;
-        }
-        // leaf phase: the waiting lanes test their triangles together
-        if (pend_tri >= 0) {
-            if (COUNT) tc.tris++;
-            const float4 a = __ldg(&tri_isect[(size_t)pend_tri * 3 + 0]);
-            const float4 b = __ldg(&tri_isect[(size_t)pend_tri * 3 + 1]);
-            const float4 c = __ldg(&tri_isect[(size_t)pend_tri * 3 + 2]);
-            const f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
-            const f3 pv = cross(dir, e1);
-            const float det = dot(e0, pv);
-            const f3 tv = sub(org, v0);
-            const f3 qv = cross(tv, e0);
-            const float u = xdiv(dot(tv, pv), det);
-            const float v = xdiv(dot(dir, qv), det);
-            const float tt = xdiv(dot(e1, qv), det);
-            const float w = xsub(xsub(1.0f, u), v);
-            if (u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt < h.t) {
-                h.t = tt;
-                h.tri = pend_tri;
-                h.mat = __float_as_int(c.y);
-                h.bu = v;
-                h.bv = w;
-                h.bw = u;
+            const int32_t next = hit ? node + 1 : __float_as_int(A.w);
+            if (next < 0 || next >= nn) {
+                finished = true;
+                break;
             }
-            if (node + 1 >= nn) finished = true;  // a leaf's successor is node + 1 (hit or miss)
-            else node = node + 1;
+            node = next;
         }
         if (finished) {
             q.hit[idx] = make_float4(__int_as_float(h.tri), h.bu, h.bv, h.bw);
