@@ -18,6 +18,7 @@
 #include "../host/scene_internal.h"
 #include "device_common.cuh"
 #include "kernels.h"
+#include "../host/scene_bvh4.h"
 
 using namespace sppm_dev;
 using sppm::fail;
@@ -187,8 +188,6 @@ int validate_config(const sppm_config* c) {
     if (c->max_path_length == 0 || c->max_path_length > 1024) return fail(SPPM_ERR_ARG, "max_path_length must be 1..1024");
     if (c->precision != SPPM_PRECISION_FP32 && c->precision != SPPM_PRECISION_MIXED)
         return fail(SPPM_ERR_ARG, "unknown precision %u", c->precision);
-    if (c->precision == SPPM_PRECISION_MIXED)
-        return fail(SPPM_ERR_UNSUPPORTED, "mixed precision is not available in this build");
     if (c->seed_mode > SPPM_SEED_HASH) return fail(SPPM_ERR_ARG, "unknown seed mode %u", c->seed_mode);
     if (c->radius_rule > SPPM_RADIUS_DIAGONAL) return fail(SPPM_ERR_ARG, "unknown radius rule %u", c->radius_rule);
     if (!(c->alpha > 0.0f && c->alpha <= 1.0f)) return fail(SPPM_ERR_ARG, "alpha must be in (0, 1]");
@@ -232,6 +231,12 @@ int reset_state(sppm_ctx* c) {
     SPPM_CK(cudaMemsetAsync(pp.hit, 0, (size_t)c->P * sizeof(int2), s));
     SPPM_CK(cudaMemsetAsync(c->job.winner, 0xFF, (size_t)c->hash_num * 4, s));
     SPPM_CK(cudaMemsetAsync(c->job.count, 0, (size_t)c->hash_num * 4, s));
+    if (c->job.slots) {
+        SPPM_CK(cudaMemsetAsync(c->job.slots, 0, (size_t)c->hash_num * sizeof(SlotRec), s));
+        SPPM_CK(cudaMemsetAsync(px.stat_n, 0, (size_t)c->npix * 8, s));
+        SPPM_CK(cudaMemsetAsync(px.stat_r2, 0, (size_t)c->npix * 8, s));
+        SPPM_CK(cudaMemsetAsync(px.stat_tau, 0, (size_t)c->npix * 24, s));
+    }
     st.initial_radius = c->fixed_radius;
     SPPM_CK(cudaMemcpyAsync(c->d_state, &st, sizeof(st), cudaMemcpyHostToDevice, s));
     SPPM_CK(cudaStreamSynchronize(s));  // the host vectors go out of scope
@@ -414,6 +419,8 @@ int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out) {
     bytes += 4 * Arena::align(P * 16) + Arena::align(P * 8);
     bytes += 2 * Arena::align(hn * 4);
     bytes += 3 * Arena::align(P * 16) + Arena::align(64);  // ray queue of the wavefront photon pass
+    const bool mixed = cfg->precision == SPPM_PRECISION_MIXED;
+    if (mixed) bytes += Arena::align(hn * sizeof(SlotRec)) + 2 * Arena::align(np * 8) + Arena::align(np * 24);
     if ((st = c->state_mem.reserve(bytes))) return st;
     Arena& a = c->state_mem;
     c->d_job = a.take<JobDesc>(1);
@@ -442,6 +449,13 @@ int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out) {
     c->queue.hit = a.take<float4>(P);
     c->queue.counters = a.take<uint32_t>(16);
     c->queue.capacity = c->P;
+    if (mixed) {
+        J.slots = a.take<SlotRec>(hn);
+        J.px.stat_n = a.take<double>(np);
+        J.px.stat_r2 = a.take<double>(np);
+        J.px.stat_tau = a.take<double>(np * 3);
+        if (!J.px.stat_tau) return fail(SPPM_ERR_OOM, "state arena sizing error (mixed)");
+    }
     {
         int sms = 0;
         SPPM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
@@ -476,10 +490,26 @@ int sppm_upload_scene(sppm_ctx* c, const sppm_scene* scene) {
     Packed pk;
     int st = pack_scene(scene, pk);
     if (st) return st;
+    std::vector<sppm::Node4> nodes4;
+    if (c->cfg.precision == SPPM_PRECISION_MIXED) {
+        uint32_t depth = 0;
+        const int b4 = sppm::build_bvh4(*scene, nodes4, &depth);
+        if (b4) return fail(SPPM_ERR_ARG, "4-wide BVH construction failed (%d): inconsistent BVH arrays", b4);
+        if (depth > sppm::kBvh4MaxDepth)
+            return fail(SPPM_ERR_UNSUPPORTED, "4-wide BVH depth %u exceeds the traversal stack (%u levels)", depth,
+                        sppm::kBvh4MaxDepth);
+        for (auto& n : nodes4)  // photon rays pass through lights: mark leaf triangles of emitters
+            for (int k = 0; k < n.count; k++)
+                if (n.child[k] < 0 && n.child[k] != sppm::kChildEmpty) {
+                    const int32_t tri = ~n.child[k];
+                    if (scene->materials[scene->material_ids[tri]].brdf == -1) n.child[k] = ~(tri | kEmitterBit);
+                }
+    }
     size_t bytes = Arena::align(pk.nodes.size() * sizeof(NodeX)) + Arena::align(pk.isect.size() * 16) +
                    Arena::align(pk.shade.size() * 16) + Arena::align(pk.mats.size() * sizeof(DevMaterial)) +
                    Arena::align(std::max<size_t>(pk.light_cdf.size(), 1) * 4) +
-                   Arena::align(std::max<size_t>(pk.light_tri.size(), 1) * 4) + 1024;
+                   Arena::align(std::max<size_t>(pk.light_tri.size(), 1) * 4) +
+                   Arena::align(std::max<size_t>(nodes4.size(), 1) * sizeof(sppm::Node4)) + 1024;
     SPPM_CK(cudaStreamSynchronize(c->stream));
     if ((st = c->scene_mem.reserve(bytes))) return st;
     DevScene& S = c->job.scene;
@@ -494,6 +524,11 @@ int sppm_upload_scene(sppm_ctx* c, const sppm_scene* scene) {
     if ((st = put(c->scene_mem, pk.mats, &mats, c->stream))) return st;
     if ((st = put(c->scene_mem, pk.light_cdf, &lcdf, c->stream))) return st;
     if ((st = put(c->scene_mem, pk.light_tri, &ltri, c->stream))) return st;
+    sppm::Node4* n4 = nullptr;
+    if ((st = put(c->scene_mem, nodes4, &n4, c->stream))) return st;
+    S.nodes4 = nodes4.empty() ? nullptr : reinterpret_cast<const Node4Dev*>(n4);
+    S.flux_unscale = scene->light_area != 0.0f ? scene->light_area * 3.141592f : 1.0f;
+    S.flux_unscale_inv = 1.0f / S.flux_unscale;
     S.nodes = nodes;
     S.tri_isect = isect;
     S.tri_shade = shade;
@@ -579,7 +614,8 @@ int sppm_run_passes(sppm_ctx* c, uint32_t n) {
             launch_grid(c->d_job, c->d_tables, 1, c->stream);
             timed(c, SPPM_STAGE_GRID, false);
         }
-        if (c->cfg.flags & SPPM_FLAG_FUSED_PHOTON) {
+        const bool mixed = c->cfg.precision == SPPM_PRECISION_MIXED;
+        if ((c->cfg.flags & SPPM_FLAG_FUSED_PHOTON) && !mixed) {
             timed(c, SPPM_STAGE_PHOTON, true);
             launch_photon_fp32(pho, c->count_traversal, c->stream);
             timed(c, SPPM_STAGE_PHOTON, false);
@@ -588,14 +624,17 @@ int sppm_run_passes(sppm_ctx* c, uint32_t n) {
             launch_photon_gen_fp32(pho, c->queue, c->stream);
             timed(c, SPPM_STAGE_PHOTON, false);
             timed(c, SPPM_STAGE_PHOTON_TRACE, true);
-            launch_trace_photons_fp32(pho, c->queue, c->count_traversal, c->trace_blocks, c->stream);
+            if (mixed) launch_trace_photons4(pho, c->queue, c->stream);
+            else launch_trace_photons_fp32(pho, c->queue, c->count_traversal, c->trace_blocks, c->stream);
             timed(c, SPPM_STAGE_PHOTON_TRACE, false);
             timed(c, SPPM_STAGE_PHOTON_STORE, true);
             launch_photon_store_fp32(pho, c->queue, c->stream);
+            if (mixed) launch_slot_fill(pho, c->queue, c->stream);
             timed(c, SPPM_STAGE_PHOTON_STORE, false);
         }
         timed(c, SPPM_STAGE_GATHER, true);
-        launch_gather_fp32(pix, c->stream);
+        if (mixed) launch_gather_mixed(pix, c->stream);
+        else launch_gather_fp32(pix, c->stream);
         timed(c, SPPM_STAGE_GATHER, false);
         if ((st = launch_check("SPPM frame"))) return st;
         c->frames++;
@@ -621,7 +660,8 @@ int sppm_read_image(sppm_ctx* c, uint32_t kind, float* rgb, size_t num_floats) {
     if (num_floats != (size_t)c->npix * 3) return fail(SPPM_ERR_ARG, "image needs %zu floats", (size_t)c->npix * 3);
     SPPM_CK(cudaSetDevice(c->device));
     timed(c, SPPM_STAGE_RESOLVE, true);
-    launch_resolve_fp32(c->set(0), kind, c->stream);
+    if (c->cfg.precision == SPPM_PRECISION_MIXED) launch_resolve_mixed(c->set(0), kind, c->stream);
+    else launch_resolve_fp32(c->set(0), kind, c->stream);
     timed(c, SPPM_STAGE_RESOLVE, false);
     int st = launch_check("resolve");
     if (st) return st;
@@ -648,6 +688,9 @@ static void* state_ptr(const sppm_ctx* c, uint32_t kind, size_t* bytes) {
         case SPPM_STATE_SLOT_WINNER: *bytes = hn * 4; return J.winner;
         case SPPM_STATE_SLOT_COUNT: *bytes = hn * 4; return J.count;
         case SPPM_STATE_HIT_T: *bytes = np * 4; return J.px.t;
+        case SPPM_STATE_STATS_N: *bytes = J.px.stat_n ? np * 8 : 0; return J.px.stat_n;
+        case SPPM_STATE_STATS_R2: *bytes = J.px.stat_r2 ? np * 8 : 0; return J.px.stat_r2;
+        case SPPM_STATE_STATS_TAU: *bytes = J.px.stat_tau ? np * 24 : 0; return J.px.stat_tau;
         default: *bytes = 0; return nullptr;
     }
 }

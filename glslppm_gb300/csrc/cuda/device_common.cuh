@@ -44,8 +44,24 @@ struct __align__(16) DevMaterial {
     float pad[2];
 };
 
+// 4-wide quantised BVH node of the mixed path (host layout: csrc/host/scene_bvh4.h, 64 bytes):
+// w[0] = origin xyz, exponent bytes x|y|z|count; w[1] = children; w[2] = qlo x,y,z, qhi x;
+// w[3] = qhi y,z
+struct __align__(16) Node4Dev {
+    float4 w[4];
+};
+
+// the photon a hash slot keeps, as the mixed-path gather reads it (32 bytes):
+// w0 = cell x|y (int16), cell z (int16) | count (uint16), offset x|y, offset z (unorm16)
+// w1 = flux r|g, b (FP16, scaled), direction x|y, z (snorm16)
+struct __align__(16) SlotRec {
+    uint4 w0, w1;
+};
+
 struct DevScene {
     const NodeX* nodes;       // [6][num_nodes]
+    const Node4Dev* nodes4;   // mixed path
+    float flux_unscale, flux_unscale_inv;  // FP16 flux scale of the mixed path (light area * pi)
     const float4* tri_isect;  // [num_tris][3]
     const float4* tri_shade;  // [num_tris][6]
     const DevMaterial* mats;
@@ -93,6 +109,7 @@ struct JobDesc {
     DevPhotons ph;
     uint32_t* winner;
     uint32_t* count;
+    SlotRec* slots;  // mixed path
     JobState* state;
     float* image;  // W*H*3 resolve target
     float cam_pos[3], cam_u[3], cam_v[3], cam_w[3];

@@ -17,6 +17,12 @@ void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool coun
                                uint32_t persistent_blocks, cudaStream_t s);
 void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
 uint32_t trace_photons_blocks_per_sm();
+
+// mixed-precision path (kernels_mixed.cu)
+void launch_trace_photons4(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
+void launch_slot_fill(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
+void launch_gather_mixed(const LaunchSet& ls, cudaStream_t s);
+void launch_resolve_mixed(const LaunchSet& ls, uint32_t display, cudaStream_t s);
 void launch_gather_fp32(const LaunchSet& ls, cudaStream_t s);
 void launch_resolve_fp32(const LaunchSet& ls, uint32_t display, cudaStream_t s);
 void launch_hash_build(const float4* pos, const float4* flux, uint32_t pw, uint32_t ph, uint32_t hash_num,

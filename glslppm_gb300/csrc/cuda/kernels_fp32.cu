@@ -840,6 +840,7 @@ __global__ void __launch_bounds__(128) k_photon_store(LaunchSet ls, RayQueue q) 
     const float4 f = J.ph.flux[sidx];
     const int depth = J.ph.hit[sidx].y;
     const uint32_t slot = photon_store(J, st, sidx, h, mk(d.x, d.y, d.z), mk(f.x, f.y, f.z), (float)depth);
+    q.hit[qi].x = __uint_as_float(slot);  // for the slot records of the mixed path
     hash_insert(J, k, sidx, slot, __activemask());
 }
 

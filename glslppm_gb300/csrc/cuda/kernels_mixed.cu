@@ -1,0 +1,321 @@
+// Mixed-precision SPPM kernels (sppm_config.precision = SPPM_PRECISION_MIXED).
+//
+// What changes against the plain FP32 path, and why:
+//  * photon segments are traced through a 4-wide BVH whose child boxes are 8-bit outward-rounded
+//    offsets (64-byte nodes: one node fetch tests four boxes), closest-child-first with a stack,
+//    slab tests and the triangle test in fused multiply-adds with one reciprocal per triangle --
+//    the boxes are conservative and the triangle test is single precision, so the reported
+//    triangle is the true closest one up to ties at equal distance;
+//  * the photon a hash slot keeps is stored once per slot as a 32-byte record -- cell (int16 x3),
+//    position inside the cell (unorm16 x3), flux (FP16 x3, scaled by 1/(light area * pi)),
+//    direction (snorm16 x3) and the slot's photon count -- so the gather reads one sector per cell
+//    instead of the winner index, three photon arrays and the count; the in-cell test becomes an
+//    integer compare;
+//  * flux is gathered in FP32 and the per-pixel statistics N, R^2 and tau are kept in FP64.
+// Emission/bounce (photon generation), photon records and hashing stay the plain FP32 kernels.
+#include <cstdint>
+
+#include <cuda_fp16.h>
+
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace sppm_dev {
+
+namespace {
+
+constexpr int kStack = 128;  // >= 3 * kBvh4MaxDepth + 1
+
+struct Hit4 {
+    float t;
+    int32_t tri;
+    float bu, bv, bw;  // (v, w, u) as the plain path stores them
+};
+
+__device__ __forceinline__ float node_scale(uint8_t e) { return __uint_as_float((uint32_t)e << 23); }
+
+// closest hit through the 4-wide BVH; PHOTON rays skip emitters, eye rays of the first bounce
+// cull back faces (eyeraytrace.fs:130)
+template <bool PHOTON>
+__device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const float4* __restrict__ tri_isect, f3 org,
+                                       f3 dir, bool cull, float tmax0, uint32_t& err) {
+    Hit4 h;
+    h.t = tmax0;
+    h.tri = -1;
+    h.bu = h.bv = h.bw = 0.0f;
+    const float rx = 1.0f / dir.x, ry = 1.0f / dir.y, rz = 1.0f / dir.z;
+    const float nx = -org.x * rx, ny = -org.y * ry, nz = -org.z * rz;
+    int32_t stack_node[kStack];
+    float stack_t[kStack];
+    int sp = 0;
+    int32_t cur = 0;
+    uint32_t visits = 0;
+    for (;;) {
+        if (++visits > 4u * (1u << 20)) {  // bounded: no tree here has this many nodes
+            err |= kErrWatchdogTraverse;
+            break;
+        }
+        const float4* np = reinterpret_cast<const float4*>(nodes + cur);
+        const float4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3);
+        const uint32_t eb = __float_as_uint(w0.w);
+        const float sx = node_scale(eb & 0xFF), sy = node_scale((eb >> 8) & 0xFF), sz = node_scale((eb >> 16) & 0xFF);
+        const int cnt = (int)(eb >> 24);
+        const int32_t ch[4] = {__float_as_int(w1.x), __float_as_int(w1.y), __float_as_int(w1.z), __float_as_int(w1.w)};
+        const uint32_t qlx = __float_as_uint(w2.x), qly = __float_as_uint(w2.y), qlz = __float_as_uint(w2.z);
+        const uint32_t qhx = __float_as_uint(w2.w), qhy = __float_as_uint(w3.x), qhz = __float_as_uint(w3.y);
+        // slab test of the (up to) four children
+        float tnear[4];
+        bool hit[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float lx = fmaf((float)((qlx >> (8 * k)) & 0xFF), sx, w0.x);
+            const float ly = fmaf((float)((qly >> (8 * k)) & 0xFF), sy, w0.y);
+            const float lz = fmaf((float)((qlz >> (8 * k)) & 0xFF), sz, w0.z);
+            const float hx = fmaf((float)((qhx >> (8 * k)) & 0xFF), sx, w0.x);
+            const float hy = fmaf((float)((qhy >> (8 * k)) & 0xFF), sy, w0.y);
+            const float hz = fmaf((float)((qhz >> (8 * k)) & 0xFF), sz, w0.z);
+            const float ax = fmaf(lx, rx, nx), bx = fmaf(hx, rx, nx);
+            const float ay = fmaf(ly, ry, ny), by = fmaf(hy, ry, ny);
+            const float az = fmaf(lz, rz, nz), bz = fmaf(hz, rz, nz);
+            const float t0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), 0.0f));
+            // widen the far bound by a few ulps so that rounding never rejects a grazing hit
+            const float t1 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz)) * 1.00000036f;
+            tnear[k] = t0;
+            hit[k] = k < cnt && t0 <= t1 && t0 <= h.t;
+        }
+        // leaf children: test their triangle now (a closer hit shrinks the search)
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (!hit[k] || ch[k] >= 0) continue;
+            hit[k] = false;
+            const int32_t code = ~ch[k];
+            if (PHOTON && (code & kEmitterBit)) continue;
+            const int32_t tri = code & kTriMask;
+            const float4 a = __ldg(&tri_isect[(size_t)tri * 3 + 0]);
+            const float4 b = __ldg(&tri_isect[(size_t)tri * 3 + 1]);
+            const float4 c = __ldg(&tri_isect[(size_t)tri * 3 + 2]);
+            const f3 e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
+            const float pvx = dir.y * e1.z - dir.z * e1.y, pvy = dir.z * e1.x - dir.x * e1.z,
+                        pvz = dir.x * e1.y - dir.y * e1.x;
+            const float det = e0.x * pvx + e0.y * pvy + e0.z * pvz;
+            if (!PHOTON && cull && !(det > 1e-10f)) continue;
+            const float inv = 1.0f / det;
+            const float tvx = org.x - a.x, tvy = org.y - a.y, tvz = org.z - a.z;
+            const float u = (tvx * pvx + tvy * pvy + tvz * pvz) * inv;
+            if (!(u >= 0.0f && u <= 1.0f)) continue;
+            const float qx = tvy * e0.z - tvz * e0.y, qy = tvz * e0.x - tvx * e0.z, qz = tvx * e0.y - tvy * e0.x;
+            const float v = (dir.x * qx + dir.y * qy + dir.z * qz) * inv;
+            const float t = (e1.x * qx + e1.y * qy + e1.z * qz) * inv;
+            const float w = 1.0f - u - v;
+            if (v >= 0.0f && w >= 0.0f && t >= 0.0f && t < h.t) {
+                h.t = t;
+                h.tri = tri;
+                h.bu = v;
+                h.bv = w;
+                h.bw = u;
+            }
+        }
+        // internal children: nearest next, the others on the stack (farthest first)
+        int32_t order[4];
+        float ot[4];
+        int n = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (hit[k] && tnear[k] <= h.t) {
+                int j = n++;
+                while (j > 0 && ot[j - 1] < tnear[k]) {  // descending distance
+                    ot[j] = ot[j - 1];
+                    order[j] = order[j - 1];
+                    j--;
+                }
+                ot[j] = tnear[k];
+                order[j] = ch[k];
+            }
+        }
+        if (n > 0) {
+            if (sp + n - 1 > kStack) {
+                err |= kErrWatchdogTraverse;
+                break;
+            }
+            for (int j = 0; j < n - 1; j++) {
+                stack_node[sp] = order[j];
+                stack_t[sp] = ot[j];
+                sp++;
+            }
+            cur = order[n - 1];
+            continue;
+        }
+        bool found = false;
+        while (sp > 0) {
+            sp--;
+            if (stack_t[sp] <= h.t) {
+                cur = stack_node[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    return h;
+}
+
+}  // namespace
+
+// trace every queued photon ray through the 4-wide BVH (one thread per ray)
+__global__ void __launch_bounds__(128) k_trace_photons4(LaunchSet ls, RayQueue q) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t total = q.counters[0];
+    if (i >= total) return;
+    const float4 o = q.org[i], d = q.dir[i];
+    const uint32_t g = __float_as_uint(o.w);
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    uint32_t err = 0;
+    const Hit4 h = trace4<true>(J.scene.nodes4, J.scene.tri_isect, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), false,
+                                1.0e30f, err);
+    q.hit[i] = make_float4(__int_as_float(h.tri), h.bu, h.bv, h.bw);
+    if (err) atomicOr(&J.state->err, err);
+}
+
+// the winner of each slot writes the slot's 32-byte record (after all photons are hashed)
+__global__ void __launch_bounds__(256) k_slot_fill(LaunchSet ls, RayQueue q) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= q.counters[0]) return;
+    const uint32_t slot = __float_as_uint(q.hit[i].x);  // k_photon_store left the slot here
+    if (slot == 0xFFFFFFFFu) return;
+    const uint32_t g = __float_as_uint(q.org[i].w);
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    const uint32_t sidx = g - ls.prefix[k];
+    if (J.winner[slot] != sidx) return;
+    const JobState* st = J.state;
+    const float4 p = J.ph.pos[sidx], f = J.ph.flux[sidx], dd = J.ph.dir[sidx];
+    const float G = st->grid_scale;
+    const float fx = (p.x - st->bbmin[0]) * G, fy = (p.y - st->bbmin[1]) * G, fz = (p.z - st->bbmin[2]) * G;
+    const float cx = floorf(fx), cy = floorf(fy), cz = floorf(fz);
+    auto unorm16 = [](float x) { return (uint32_t)fminf(fmaxf(x * 65536.0f, 0.0f), 65535.0f); };
+    auto snorm16 = [](float x) { return (uint32_t)(uint16_t)(int16_t)__float2int_rn(fminf(fmaxf(x, -1.0f), 1.0f) * 32767.0f); };
+    const float fs = J.scene.flux_unscale_inv;
+    const __half2 frg = __floats2half2_rn(f.x * fs, f.y * fs);
+    const __half2 fb_ = __floats2half2_rn(f.z * fs, 0.0f);
+    SlotRec r;
+    r.w0 = make_uint4(((uint32_t)(uint16_t)(int16_t)cx) | ((uint32_t)(uint16_t)(int16_t)cy << 16),
+                      ((uint32_t)(uint16_t)(int16_t)cz) | (min(J.count[slot], 65535u) << 16),
+                      unorm16(fx - cx) | (unorm16(fy - cy) << 16), unorm16(fz - cz));
+    r.w1 = make_uint4(*reinterpret_cast<const uint32_t*>(&frg), *reinterpret_cast<const uint32_t*>(&fb_),
+                      snorm16(dd.x) | (snorm16(dd.y) << 16), snorm16(dd.z));
+    J.slots[slot] = r;
+}
+
+// progressive.fs with the slot records, FP32 flux gathering and FP64 statistics
+__global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
+    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gi >= ls.total) return;
+    const int k = find_job(ls, gi);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    JobState* st = J.state;
+    const uint32_t p = gi - ls.prefix[k];
+    const uint32_t frame = st->frame;
+    if (p == 0) {
+        const uint32_t e = st->emitted_frame;
+        st->num_photons_f32 = __fadd_rn(st->num_photons_f32, (float)(int)e);
+        st->num_photons += e;
+        st->photon_segments += st->segments_frame;
+    }
+    double N = J.px.stat_n[p];
+    double R2 = frame == 0 ? (double)st->r0 * (double)st->r0 : J.px.stat_r2[p];
+    double tx = frame == 0 ? 0.0 : J.px.stat_tau[3 * (size_t)p + 0];
+    double ty = frame == 0 ? 0.0 : J.px.stat_tau[3 * (size_t)p + 1];
+    double tz = frame == 0 ? 0.0 : J.px.stat_tau[3 * (size_t)p + 2];
+    if (J.px.tri[p] >= 0) {
+        const float G = st->grid_scale;
+        const float hs1 = st->hash_scale1;
+        const float hn = (float)J.hash_num;
+        const float4 qp4 = J.px.pos[p], qn4 = J.px.nrm[p], qr4 = J.px.refl[p];
+        const float gx = fabsf(qp4.x - st->bbmin[0]) * G, gy = fabsf(qp4.y - st->bbmin[1]) * G,
+                    gz = fabsf(qp4.z - st->bbmin[2]) * G;
+        const float ix = floorf(gx - 0.5f), iy = floorf(gy - 0.5f), iz = floorf(gz - 0.5f);
+        const float R = (float)sqrt(R2);
+        const float R2f = R * R;
+        const float invG = 1.0f / G;
+        float fx = 0.0f, fy = 0.0f, fz = 0.0f, M = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const float cx = ix + (float)(c & 1), cy = iy + (float)((c >> 1) & 1), cz = iz + (float)(c >> 2);
+            const uint32_t slot = hash_cell(mk(cx, cy, cz), G, hs1, hn);
+            const SlotRec r = J.slots[slot];
+            const uint32_t cnt = r.w0.y >> 16;
+            if (cnt == 0 || J.winner[slot] == kEmptySlot) continue;
+            if ((int)(int16_t)(r.w0.x & 0xFFFF) != (int)cx || (int)(int16_t)(r.w0.x >> 16) != (int)cy ||
+                (int)(int16_t)(r.w0.y & 0xFFFF) != (int)cz)
+                continue;  // the slot holds a photon of another cell (hash collision)
+            const float px = (cx + (float)(r.w0.z & 0xFFFF) * (1.0f / 65536.0f)) * invG + st->bbmin[0];
+            const float py = (cy + (float)(r.w0.z >> 16) * (1.0f / 65536.0f)) * invG + st->bbmin[1];
+            const float pz = (cz + (float)(r.w0.w & 0xFFFF) * (1.0f / 65536.0f)) * invG + st->bbmin[2];
+            const float dx = px - qp4.x, dy = py - qp4.y, dz = pz - qp4.z;
+            if (dx * dx + dy * dy + dz * dz >= R2f) continue;
+            const float ddx = (float)(int16_t)(r.w1.z & 0xFFFF), ddy = (float)(int16_t)(r.w1.z >> 16),
+                        ddz = (float)(int16_t)(r.w1.w & 0xFFFF);
+            if (!(qn4.x * ddx + qn4.y * ddy + qn4.z * ddz < 0.0f)) continue;
+            const float2 frg = __half22float2(*reinterpret_cast<const __half2*>(&r.w1.x));
+            const float2 fb_ = __half22float2(*reinterpret_cast<const __half2*>(&r.w1.y));
+            const float cf = (float)cnt;
+            fx += frg.x * cf;
+            fy += frg.y * cf;
+            fz += fb_.x * cf;
+            M += cf;
+        }
+        const double scale = (double)J.scene.flux_unscale;
+        const double alpha = (double)J.alpha;
+        const double Md = (double)M;
+        const double gg = fmin((N + alpha * Md) / (N + Md), 1.0);
+        R2 *= gg;
+        N += alpha * Md;
+        const double ip = 0.31830988618379067;
+        tx = (tx + (double)fx * scale * (double)qr4.x * ip) * gg;
+        ty = (ty + (double)fy * scale * (double)qr4.y * ip) * gg;
+        tz = (tz + (double)fz * scale * (double)qr4.z * ip) * gg;
+        J.px.stat_n[p] = N;
+    }
+    J.px.stat_r2[p] = R2;
+    J.px.stat_tau[3 * (size_t)p + 0] = tx;
+    J.px.stat_tau[3 * (size_t)p + 1] = ty;
+    J.px.stat_tau[3 * (size_t)p + 2] = tz;
+}
+
+// re.fs from the FP64 statistics
+__global__ void k_resolve_mixed(LaunchSet ls, uint32_t display) {
+    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gi >= ls.total) return;
+    const int k = find_job(ls, gi);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    const uint32_t p = gi - ls.prefix[k];
+    const double den = J.px.stat_r2[p] * 3.141592653589793 * (double)J.state->num_photons;
+    const float4 qe = J.px.emi_n[p];
+    const float e[3] = {qe.x, qe.y, qe.z};
+    for (int c = 0; c < 3; c++) {
+        float v = (float)(J.px.stat_tau[3 * (size_t)p + c] / den) + e[c];
+        if (display) {
+            v = 1.0f - sppm_fexp(-v * 60000.0f);
+            v = v < 0.0031308f ? 12.92f * v : 1.055f * sppm_fpow(v, 0.416666666667f) - 0.055f;
+        }
+        J.image[(size_t)p * 3 + c] = v;
+    }
+}
+
+static inline uint32_t blocks_for(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
+
+void launch_trace_photons4(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
+    if (q.capacity) k_trace_photons4<<<blocks_for(q.capacity, 128), 128, 0, s>>>(ls, q);
+}
+void launch_slot_fill(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
+    if (q.capacity) k_slot_fill<<<blocks_for(q.capacity, 256), 256, 0, s>>>(ls, q);
+}
+void launch_gather_mixed(const LaunchSet& ls, cudaStream_t s) {
+    if (ls.total) k_gather_mixed<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls);
+}
+void launch_resolve_mixed(const LaunchSet& ls, uint32_t display, cudaStream_t s) {
+    if (ls.total) k_resolve_mixed<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls, display);
+}
+
+}  // namespace sppm_dev
