@@ -459,7 +459,7 @@ int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out) {
     {
         int sms = 0;
         SPPM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        c->trace_blocks = (uint32_t)sms * trace_photons_blocks_per_sm();
+        c->trace_blocks = (uint32_t)sms * (mixed ? trace_photons4_blocks_per_sm() : trace_photons_blocks_per_sm());
     }
     if (!J.count) return fail(SPPM_ERR_OOM, "state arena sizing error");
     J.state = c->d_state;
@@ -624,7 +624,7 @@ int sppm_run_passes(sppm_ctx* c, uint32_t n) {
             launch_photon_gen_fp32(pho, c->queue, c->stream);
             timed(c, SPPM_STAGE_PHOTON, false);
             timed(c, SPPM_STAGE_PHOTON_TRACE, true);
-            if (mixed) launch_trace_photons4(pho, c->queue, c->stream);
+            if (mixed) launch_trace_photons4(pho, c->queue, c->trace_blocks, c->stream);
             else launch_trace_photons_fp32(pho, c->queue, c->count_traversal, c->trace_blocks, c->stream);
             timed(c, SPPM_STAGE_PHOTON_TRACE, false);
             timed(c, SPPM_STAGE_PHOTON_STORE, true);

@@ -161,20 +161,198 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
 
 }  // namespace
 
-// trace every queued photon ray through the 4-wide BVH (one thread per ray)
-__global__ void __launch_bounds__(128) k_trace_photons4(LaunchSet ls, RayQueue q) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// byte k of w as an exact float: the byte placed in the low mantissa of 2^23, minus 2^23
+__device__ __forceinline__ float byte_f(uint32_t w, uint32_t sel) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f;
+}
+
+constexpr int kTraceBlock = 128;
+constexpr int kSmemStack = 16;  // top of each thread's stack, in shared memory (16 KB per block)
+constexpr int kLocalStack = kStack - kSmemStack;  // deeper entries, in local memory (rarely touched)
+
+template <int K>
+__device__ __forceinline__ void child_box(const float4& w0, const float4& w2, const float4& w3, float sx, float sy,
+                                          float sz, float rx, float ry, float rz, float nx, float ny, float nz,
+                                          float tbest, float& tn, bool& hit) {
+    constexpr uint32_t sel = 0x7650u | (uint32_t)K;  // byte K of the word into byte 0, 0x4B into byte 3
+    const float lx = fmaf(byte_f(__float_as_uint(w2.x), sel), sx, w0.x);
+    const float ly = fmaf(byte_f(__float_as_uint(w2.y), sel), sy, w0.y);
+    const float lz = fmaf(byte_f(__float_as_uint(w2.z), sel), sz, w0.z);
+    const float hx = fmaf(byte_f(__float_as_uint(w2.w), sel), sx, w0.x);
+    const float hy = fmaf(byte_f(__float_as_uint(w3.x), sel), sy, w0.y);
+    const float hz = fmaf(byte_f(__float_as_uint(w3.y), sel), sz, w0.z);
+    const float ax = fmaf(lx, rx, nx), bx = fmaf(hx, rx, nx);
+    const float ay = fmaf(ly, ry, ny), by = fmaf(hy, ry, ny);
+    const float az = fmaf(lz, rz, nz), bz = fmaf(hz, rz, nz);
+    const float t0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), 0.0f));
+    // the far bound widened by a few ulps so that rounding never rejects a grazing hit
+    const float t1 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz)) * 1.00000036f;
+    tn = t0;
+    hit = t0 <= t1 && t0 <= tbest;
+}
+
+__device__ __forceinline__ void cswap(float& ta, int32_t& ca, float& tb, int32_t& cb) {
+    if (tb < ta) {
+        const float t = ta;
+        ta = tb;
+        tb = t;
+        const int32_t c = ca;
+        ca = cb;
+        cb = c;
+    }
+}
+
+// photon segments through the 4-wide BVH: persistent warps with dynamic ray fetch (a lane whose
+// ray finished takes the next queued ray), one node per lane per step, closest child first, the
+// other hit children on a per-thread stack in shared memory
+__global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, RayQueue q) {
+    __shared__ int32_t s_node[kSmemStack][kTraceBlock];
+    __shared__ float s_t[kSmemStack][kTraceBlock];
+    int32_t l_node[kLocalStack];
+    float l_t[kLocalStack];
+    auto push = [&](int sp_, int32_t n, float t) {
+        if (sp_ < kSmemStack) {
+            s_node[sp_][threadIdx.x] = n;
+            s_t[sp_][threadIdx.x] = t;
+        } else {
+            l_node[sp_ - kSmemStack] = n;
+            l_t[sp_ - kSmemStack] = t;
+        }
+    };
     const uint32_t total = q.counters[0];
-    if (i >= total) return;
-    const float4 o = q.org[i], d = q.dir[i];
-    const uint32_t g = __float_as_uint(o.w);
-    const int k = find_job(ls, g);
-    const JobDesc& J = ls.jobs[ls.job_ids[k]];
-    uint32_t err = 0;
-    const Hit4 h = trace4<true>(J.scene.nodes4, J.scene.tri_isect, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), false,
-                                1.0e30f, err);
-    q.hit[i] = make_float4(__int_as_float(h.tri), h.bu, h.bv, h.bw);
-    if (err) atomicOr(&J.state->err, err);
+    const unsigned lane = threadIdx.x & 31, tid = threadIdx.x;
+    const uint32_t kNeed = 0xFFFFFFFFu, kDone = 0xFFFFFFFEu;
+    uint32_t idx = kNeed;
+    const Node4Dev* nodes = nullptr;
+    const float4* tri_isect = nullptr;
+    float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, rx = 0, ry = 0, rz = 0, nx = 0, ny = 0, nz = 0;
+    float ht = 1.0e30f, hbu = 0, hbv = 0, hbw = 0;
+    int32_t htri = -1, cur = 0;
+    int sp = 0;
+    uint32_t visits = 0, err = 0;
+    int job_k = 0;
+    for (;;) {
+        const bool need = idx == kNeed;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(&q.counters[1], __popc(m));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (need) {
+                idx = base + __popc(m & ((1u << lane) - 1));
+                if (idx >= total) {
+                    idx = kDone;
+                } else {
+                    const float4 o = q.org[idx], d = q.dir[idx];
+                    job_k = find_job(ls, __float_as_uint(o.w));
+                    const DevScene& S = ls.jobs[ls.job_ids[job_k]].scene;
+                    nodes = S.nodes4;
+                    tri_isect = S.tri_isect;
+                    ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
+                    rx = 1.0f / dx, ry = 1.0f / dy, rz = 1.0f / dz;
+                    nx = -ox * rx, ny = -oy * ry, nz = -oz * rz;
+                    ht = 1.0e30f;
+                    htri = -1;
+                    hbu = hbv = hbw = 0.0f;
+                    cur = 0;
+                    sp = 0;
+                    visits = 0;
+                }
+            }
+        }
+        if (__all_sync(0xFFFFFFFFu, idx == kDone)) break;
+        if (idx == kDone) continue;
+        bool finished = false;
+#pragma unroll 1
+        for (int it = 0; it < 16 && !finished; it++) {
+            if (++visits > (1u << 22)) {
+                err |= kErrWatchdogTraverse;
+                finished = true;
+                break;
+            }
+            const float4* np = reinterpret_cast<const float4*>(nodes + cur);
+            const float4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3);
+            const uint32_t eb = __float_as_uint(w0.w);
+            const float sx = node_scale(eb & 0xFF), sy = node_scale((eb >> 8) & 0xFF), sz = node_scale((eb >> 16) & 0xFF);
+            const int cnt = (int)(eb >> 24);
+            float t[4];
+            bool hit[4];
+            child_box<0>(w0, w2, w3, sx, sy, sz, rx, ry, rz, nx, ny, nz, ht, t[0], hit[0]);
+            child_box<1>(w0, w2, w3, sx, sy, sz, rx, ry, rz, nx, ny, nz, ht, t[1], hit[1]);
+            child_box<2>(w0, w2, w3, sx, sy, sz, rx, ry, rz, nx, ny, nz, ht, t[2], hit[2]);
+            child_box<3>(w0, w2, w3, sx, sy, sz, rx, ry, rz, nx, ny, nz, ht, t[3], hit[3]);
+            int32_t c[4] = {__float_as_int(w1.x), __float_as_int(w1.y), __float_as_int(w1.z), __float_as_int(w1.w)};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                hit[k] = hit[k] && k < cnt;
+                if (!hit[k] || c[k] >= 0) continue;
+                // a leaf child: its triangle (photons pass through emitters)
+                hit[k] = false;
+                const int32_t code = ~c[k];
+                if (code & kEmitterBit) continue;
+                const float4 a = __ldg(&tri_isect[(size_t)code * 3 + 0]);
+                const float4 b = __ldg(&tri_isect[(size_t)code * 3 + 1]);
+                const float4 cc = __ldg(&tri_isect[(size_t)code * 3 + 2]);
+                const float e0x = a.w, e0y = b.x, e0z = b.y, e1x = b.z, e1y = b.w, e1z = cc.x;
+                const float pvx = dy * e1z - dz * e1y, pvy = dz * e1x - dx * e1z, pvz = dx * e1y - dy * e1x;
+                const float det = e0x * pvx + e0y * pvy + e0z * pvz;
+                const float inv = 1.0f / det;
+                const float tvx = ox - a.x, tvy = oy - a.y, tvz = oz - a.z;
+                const float u = (tvx * pvx + tvy * pvy + tvz * pvz) * inv;
+                const float qx = tvy * e0z - tvz * e0y, qy = tvz * e0x - tvx * e0z, qz = tvx * e0y - tvy * e0x;
+                const float v = (dx * qx + dy * qy + dz * qz) * inv;
+                const float tt = (e1x * qx + e1y * qy + e1z * qz) * inv;
+                const float w = 1.0f - u - v;
+                if (u >= 0.0f && v >= 0.0f && w >= 0.0f && tt >= 0.0f && tt < ht) {
+                    ht = tt;
+                    htri = code;
+                    hbu = v;
+                    hbv = w;
+                    hbw = u;
+                }
+            }
+            // internal children hit before the current closest hit, sorted near to far
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (!(hit[k] && t[k] <= ht)) t[k] = __int_as_float(0x7f800000);
+            cswap(t[0], c[0], t[1], c[1]);
+            cswap(t[2], c[2], t[3], c[3]);
+            cswap(t[0], c[0], t[2], c[2]);
+            cswap(t[1], c[1], t[3], c[3]);
+            cswap(t[1], c[1], t[2], c[2]);
+            const float inf = __int_as_float(0x7f800000);
+            if (t[0] < inf) {
+                const int pushes = (t[1] < inf) + (t[2] < inf) + (t[3] < inf);
+                if (sp + pushes > kStack) {
+                    err |= kErrWatchdogTraverse;
+                    finished = true;
+                    break;
+                }
+                if (t[3] < inf) push(sp++, c[3], t[3]);
+                if (t[2] < inf) push(sp++, c[2], t[2]);
+                if (t[1] < inf) push(sp++, c[1], t[1]);
+                cur = c[0];
+                continue;
+            }
+            bool found = false;
+            while (sp > 0) {
+                sp--;
+                const float st_t = sp < kSmemStack ? s_t[sp][tid] : l_t[sp - kSmemStack];
+                if (st_t <= ht) {
+                    cur = sp < kSmemStack ? s_node[sp][tid] : l_node[sp - kSmemStack];
+                    found = true;
+                    break;
+                }
+            }
+            if (!found) finished = true;
+        }
+        if (finished) {
+            q.hit[idx] = make_float4(__int_as_float(htri), hbu, hbv, hbw);
+            idx = kNeed;
+        }
+    }
+    if (err) atomicOr(&ls.jobs[ls.job_ids[job_k]].state->err, err);
 }
 
 // the winner of each slot writes the slot's 32-byte record (after all photons are hashed)
@@ -305,8 +483,13 @@ __global__ void k_resolve_mixed(LaunchSet ls, uint32_t display) {
 
 static inline uint32_t blocks_for(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
 
-void launch_trace_photons4(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
-    if (q.capacity) k_trace_photons4<<<blocks_for(q.capacity, 128), 128, 0, s>>>(ls, q);
+void launch_trace_photons4(const LaunchSet& ls, const RayQueue& q, uint32_t persistent_blocks, cudaStream_t s) {
+    if (ls.total) k_trace_photons4<<<persistent_blocks, kTraceBlock, 0, s>>>(ls, q);
+}
+uint32_t trace_photons4_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_photons4, kTraceBlock, 0) != cudaSuccess) n = 4;
+    return n > 0 ? (uint32_t)n : 1u;
 }
 void launch_slot_fill(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
     if (q.capacity) k_slot_fill<<<blocks_for(q.capacity, 256), 256, 0, s>>>(ls, q);
