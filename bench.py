@@ -248,16 +248,18 @@ def run_gpu(args, rank, world, local):
         r.run_passes(align)
     r.synchronize()
     fi0 = r.frame_info()
-    # device-timed region (CUDA events on the library's stream), per-stage events for the roofline
-    r.enable_stage_timing(True)
+    # device-timed region (CUDA events on the library's stream; each frame replays its CUDA
+    # graph); the photon traversal kernel carries its own events for the roofline
+    roof_stage = "photon_trace"
+    r.time_stages([roof_stage])
     r.read_stage_times()
     barrier(world)
     t_wall = time.time()
     ms = r.time_passes(K)
     clocks.mark(t_wall, time.time())
     clocks.__exit__(None, None, None)
-    stages = r.read_stage_times()
-    r.enable_stage_timing(False)
+    roof_times = r.read_stage_times()[roof_stage]
+    r.time_stages([])
     fi1 = r.frame_info()
     photons = fi1.photons_emitted - fi0.photons_emitted
     segments = (fi1.photon_segments + fi1.eye_segments) - (fi0.photon_segments + fi0.eye_segments)
@@ -266,7 +268,14 @@ def run_gpu(args, rank, world, local):
     segs_all = sum_over_ranks(segments, world)
     value = photons_all / t / 1e6
     mrays = segs_all / t / 1e6
-    launches = sum(n for (_, n) in stages.values())
+    launches = fi1.kernel_launches - fi0.kernel_launches
+
+    # per-stage breakdown (every stage timed) over a further 10-pass cycle, outside the timed region
+    r.enable_stage_timing(True)
+    r.read_stage_times()
+    r.run_passes(10)
+    stages = r.read_stage_times()
+    r.enable_stage_timing(False)
 
     # end to end through the public API with host buffers
     image = np.empty((cfg.height, cfg.width, 3), dtype=np.float32)
@@ -288,8 +297,8 @@ def run_gpu(args, rank, world, local):
     # roofline of the photon kernel: algorithmic bytes per photon segment = 64 + 32 V + 36 T
     # (ray state in/out, 32-byte nodes, 36-byte triangles), V/T from the traversal counters
     peak, peak_kind = measured_peaks()
-    kernel = "k_trace_photons" if stages["photon_trace"][1] else "k_photon"
-    ph_ms, ph_n = stages["photon_trace"] if stages["photon_trace"][1] else stages["photon"]
+    kernel = "k_trace_photons4" if args.precision == "mixed" else "k_trace_photons"
+    ph_ms, ph_n = roof_times
     roof = None
     cnt = traversal_counters(r)
     if ph_n and cnt:

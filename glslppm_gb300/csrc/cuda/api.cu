@@ -71,6 +71,22 @@ struct StageEvent {
     cudaEvent_t a, b;
 };
 
+// one frame's launches as an instantiated CUDA graph; stages being timed carry event record
+// nodes whose events are swapped for pooled ones before every replay
+struct FrameGraph {
+    cudaGraph_t graph = nullptr;  // kept: the event record nodes below belong to it
+    cudaGraphExec_t exec = nullptr;
+    uint32_t mask = 0;
+    uint32_t kernels = 0;  // kernel nodes (launches per replay)
+    bool counting = false;  // captured with the traversal-counting kernels
+    cudaGraphNode_t ev_a[SPPM_STAGE_COUNT] = {}, ev_b[SPPM_STAGE_COUNT] = {};
+    void drop() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        *this = FrameGraph{};
+    }
+};
+
 }  // namespace
 
 struct sppm_ctx {
@@ -88,10 +104,15 @@ struct sppm_ctx {
     float* d_image = nullptr;
     bool have_scene = false, have_camera = false;
     uint32_t frames = 0;  // host mirror of frames queued since reset
+    uint64_t kernel_launches = 0;  // kernels launched by sppm_run_passes since creation
     float fixed_radius = 0.0f;
     // stage timing
-    bool timing = false;
+    uint32_t timing_mask = 0;  // bit k: time stage k
     bool count_traversal = false;
+    // frame graphs: [0] photon-only frame, [1] frame with an eye pass
+    FrameGraph graphs[2];
+    bool capturing = false;
+    cudaEvent_t placeholder[2 * SPPM_STAGE_COUNT] = {};
     std::vector<StageEvent> pending;
     std::vector<cudaEvent_t> event_pool;
     float stage_ms[SPPM_STAGE_COUNT] = {0};
@@ -116,8 +137,15 @@ struct sppm_ctx {
         cudaEventCreate(&e);
         return e;
     }
+    void drop_graphs() {
+        graphs[0].drop();
+        graphs[1].drop();
+    }
     ~sppm_ctx() {
         if (device >= 0) cudaSetDevice(device);
+        drop_graphs();
+        for (auto e : placeholder)
+            if (e) cudaEventDestroy(e);
         for (auto& p : pending) {
             cudaEventDestroy(p.a);
             cudaEventDestroy(p.b);
@@ -418,7 +446,9 @@ int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out) {
     bytes += 6 * Arena::align(np * 16) + 2 * Arena::align(np * 4) + Arena::align(np * 12);
     bytes += 4 * Arena::align(P * 16) + Arena::align(P * 8);
     bytes += 2 * Arena::align(hn * 4);
-    bytes += 3 * Arena::align(P * 16) + Arena::align(64);  // ray queue of the wavefront photon pass
+    bytes += 3 * Arena::align(P * 16) + Arena::align(64) + Arena::align(P * 4);  // ray queue of the wavefront pass
+    const bool binned = !(cfg->flags & SPPM_FLAG_UNBINNED_RAYS);
+    if (binned) bytes += Arena::align(P * 8) + Arena::align(P * 4) + Arena::align(kRayBins * 4);
     const bool mixed = cfg->precision == SPPM_PRECISION_MIXED;
     if (mixed) bytes += Arena::align(hn * sizeof(SlotRec)) + 2 * Arena::align(np * 8) + Arena::align(np * 24);
     if ((st = c->state_mem.reserve(bytes))) return st;
@@ -449,6 +479,12 @@ int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out) {
     c->queue.hit = a.take<float4>(P);
     c->queue.counters = a.take<uint32_t>(16);
     c->queue.capacity = c->P;
+    c->queue.slow = a.take<uint32_t>(P);
+    if (binned) {
+        c->queue.key = a.take<uint2>(P);
+        c->queue.perm = a.take<uint32_t>(P);
+        c->queue.bins = a.take<uint32_t>(kRayBins);
+    }
     if (mixed) {
         J.slots = a.take<SlotRec>(hn);
         J.px.stat_n = a.take<double>(np);
@@ -487,6 +523,7 @@ int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out) {
 int sppm_upload_scene(sppm_ctx* c, const sppm_scene* scene) {
     if (!c) return fail(SPPM_ERR_ARG, "null context");
     SPPM_CK(cudaSetDevice(c->device));
+    c->drop_graphs();
     Packed pk;
     int st = pack_scene(scene, pk);
     if (st) return st;
@@ -583,8 +620,14 @@ int sppm_reset(sppm_ctx* c) {
     return reset_state(c);
 }
 
+// start or end of a timed stage: while a frame graph is being captured, an event record node
+// with a placeholder event; otherwise a pooled event recorded on the stream
 static void timed(sppm_ctx* c, int stage, bool start) {
-    if (!c->timing) return;
+    if (!((c->timing_mask >> stage) & 1u)) return;
+    if (c->capturing) {
+        cudaEventRecordWithFlags(c->placeholder[2 * stage + (start ? 0 : 1)], c->stream, cudaEventRecordExternal);
+        return;
+    }
     if (start) {
         StageEvent e{stage, c->get_event(), c->get_event()};
         cudaEventRecord(e.a, c->stream);
@@ -594,49 +637,130 @@ static void timed(sppm_ctx* c, int stage, bool start) {
     }
 }
 
+}  // extern "C"
+
+namespace {
+
+// the launches of one frame (m_display, glslppm.cpp:214-536) on the context's stream
+int enqueue_frame(sppm_ctx* c, bool eye) {
+    const LaunchSet pix = c->set(0), pho = c->set(1), hsh = c->set(2);
+    timed(c, SPPM_STAGE_FRAME_BEGIN, true);
+    launch_frame_begin(hsh, c->queue, c->stream);
+    timed(c, SPPM_STAGE_FRAME_BEGIN, false);
+    if (eye) {
+        timed(c, SPPM_STAGE_EYE, true);
+        launch_eye_fp32(pix, c->stream);
+        timed(c, SPPM_STAGE_EYE, false);
+        timed(c, SPPM_STAGE_GRID, true);
+        launch_grid(c->d_job, c->d_tables, 1, c->stream);
+        timed(c, SPPM_STAGE_GRID, false);
+    }
+    const bool mixed = c->cfg.precision == SPPM_PRECISION_MIXED;
+    if ((c->cfg.flags & SPPM_FLAG_FUSED_PHOTON) && !mixed) {
+        timed(c, SPPM_STAGE_PHOTON, true);
+        launch_photon_fp32(pho, c->count_traversal, c->stream);
+        timed(c, SPPM_STAGE_PHOTON, false);
+    } else {
+        timed(c, SPPM_STAGE_PHOTON, true);
+        launch_photon_gen_fp32(pho, c->queue, c->stream);
+        timed(c, SPPM_STAGE_PHOTON, false);
+        if (c->queue.key) {
+            timed(c, SPPM_STAGE_RAY_BINS, true);
+            launch_ray_bins(c->queue, c->stream);
+            timed(c, SPPM_STAGE_RAY_BINS, false);
+        }
+        timed(c, SPPM_STAGE_PHOTON_TRACE, true);
+        if (mixed) launch_trace_photons4(pho, c->queue, c->trace_blocks, c->stream);
+        else launch_trace_photons_fp32(pho, c->queue, c->count_traversal, c->trace_blocks, c->stream);
+        timed(c, SPPM_STAGE_PHOTON_TRACE, false);
+        timed(c, SPPM_STAGE_PHOTON_STORE, true);
+        launch_photon_store_fp32(pho, c->queue, c->stream);
+        if (mixed) launch_slot_fill(pho, c->queue, c->stream);
+        timed(c, SPPM_STAGE_PHOTON_STORE, false);
+    }
+    timed(c, SPPM_STAGE_GATHER, true);
+    if (mixed) launch_gather_mixed(pix, c->stream);
+    else launch_gather_fp32(pix, c->stream);
+    timed(c, SPPM_STAGE_GATHER, false);
+    return launch_check("SPPM frame");
+}
+
+int build_frame_graph(sppm_ctx* c, bool eye) {
+    FrameGraph& g = c->graphs[eye ? 1 : 0];
+    g.drop();
+    for (auto& e : c->placeholder)
+        if (!e) SPPM_CK(cudaEventCreate(&e));
+    SPPM_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    c->capturing = true;
+    const int st = enqueue_frame(c, eye);
+    c->capturing = false;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (st || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return st ? st : fail(SPPM_ERR_CUDA, "frame graph capture failed: %s", cudaGetErrorString(e));
+    }
+    g.graph = graph;
+    g.mask = c->timing_mask;
+    g.counting = c->count_traversal;
+    size_t n = 0;
+    SPPM_CK(cudaGraphGetNodes(graph, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    SPPM_CK(cudaGraphGetNodes(graph, nodes.data(), &n));
+    for (cudaGraphNode_t node : nodes) {
+        cudaGraphNodeType type;
+        SPPM_CK(cudaGraphNodeGetType(node, &type));
+        if (type == cudaGraphNodeTypeKernel) g.kernels++;
+        if (type != cudaGraphNodeTypeEventRecord) continue;
+        cudaEvent_t ev = nullptr;
+        SPPM_CK(cudaGraphEventRecordNodeGetEvent(node, &ev));
+        for (int k = 0; k < SPPM_STAGE_COUNT; k++) {
+            if (ev == c->placeholder[2 * k]) g.ev_a[k] = node;
+            if (ev == c->placeholder[2 * k + 1]) g.ev_b[k] = node;
+        }
+    }
+    SPPM_CK(cudaGraphInstantiate(&g.exec, graph, 0));
+    return SPPM_OK;
+}
+
+int replay_frame_graph(sppm_ctx* c, bool eye) {
+    FrameGraph& g = c->graphs[eye ? 1 : 0];
+    if (!g.exec || g.mask != c->timing_mask || g.counting != c->count_traversal) {
+        const int st = build_frame_graph(c, eye);
+        if (st) return st;
+    }
+    for (int k = 0; k < SPPM_STAGE_COUNT; k++) {
+        if (!g.ev_a[k] || !g.ev_b[k]) continue;
+        StageEvent se{k, c->get_event(), c->get_event()};
+        SPPM_CK(cudaGraphExecEventRecordNodeSetEvent(g.exec, g.ev_a[k], se.a));
+        SPPM_CK(cudaGraphExecEventRecordNodeSetEvent(g.exec, g.ev_b[k], se.b));
+        c->pending.push_back(se);
+    }
+    SPPM_CK(cudaGraphLaunch(g.exec, c->stream));
+    return SPPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int sppm_run_passes(sppm_ctx* c, uint32_t n) {
     if (!c) return fail(SPPM_ERR_ARG, "null context");
     if (!c->have_scene || !c->have_camera) return fail(SPPM_ERR_STATE, "upload a scene and set a camera before running passes");
     SPPM_CK(cudaSetDevice(c->device));
-    const LaunchSet pix = c->set(0), pho = c->set(1), hsh = c->set(2);
     const uint32_t interval = c->cfg.eye_pass_interval ? c->cfg.eye_pass_interval : 1u;
-    int st;
+    // the traversal-counting kernels run eagerly (they are a measurement pass)
+    const bool graphs = !(c->cfg.flags & SPPM_FLAG_EAGER_LAUNCH) && !c->count_traversal;
     for (uint32_t k = 0; k < n; k++) {
         const bool eye = (c->frames % interval) == 0;
-        timed(c, SPPM_STAGE_FRAME_BEGIN, true);
-        launch_frame_begin(hsh, c->queue, c->stream);
-        timed(c, SPPM_STAGE_FRAME_BEGIN, false);
-        if (eye) {
-            timed(c, SPPM_STAGE_EYE, true);
-            launch_eye_fp32(pix, c->stream);
-            timed(c, SPPM_STAGE_EYE, false);
-            timed(c, SPPM_STAGE_GRID, true);
-            launch_grid(c->d_job, c->d_tables, 1, c->stream);
-            timed(c, SPPM_STAGE_GRID, false);
+        FrameGraph& g = c->graphs[eye ? 1 : 0];
+        if (!graphs && !g.exec) {  // captured (not launched) once to count the frame's kernels
+            const int st = build_frame_graph(c, eye);
+            if (st) return st;
         }
-        const bool mixed = c->cfg.precision == SPPM_PRECISION_MIXED;
-        if ((c->cfg.flags & SPPM_FLAG_FUSED_PHOTON) && !mixed) {
-            timed(c, SPPM_STAGE_PHOTON, true);
-            launch_photon_fp32(pho, c->count_traversal, c->stream);
-            timed(c, SPPM_STAGE_PHOTON, false);
-        } else {
-            timed(c, SPPM_STAGE_PHOTON, true);
-            launch_photon_gen_fp32(pho, c->queue, c->stream);
-            timed(c, SPPM_STAGE_PHOTON, false);
-            timed(c, SPPM_STAGE_PHOTON_TRACE, true);
-            if (mixed) launch_trace_photons4(pho, c->queue, c->trace_blocks, c->stream);
-            else launch_trace_photons_fp32(pho, c->queue, c->count_traversal, c->trace_blocks, c->stream);
-            timed(c, SPPM_STAGE_PHOTON_TRACE, false);
-            timed(c, SPPM_STAGE_PHOTON_STORE, true);
-            launch_photon_store_fp32(pho, c->queue, c->stream);
-            if (mixed) launch_slot_fill(pho, c->queue, c->stream);
-            timed(c, SPPM_STAGE_PHOTON_STORE, false);
-        }
-        timed(c, SPPM_STAGE_GATHER, true);
-        if (mixed) launch_gather_mixed(pix, c->stream);
-        else launch_gather_fp32(pix, c->stream);
-        timed(c, SPPM_STAGE_GATHER, false);
-        if ((st = launch_check("SPPM frame"))) return st;
+        const int st = graphs ? replay_frame_graph(c, eye) : enqueue_frame(c, eye);
+        if (st) return st;
+        c->kernel_launches += g.kernels;
         c->frames++;
     }
     return SPPM_OK;
@@ -736,6 +860,8 @@ int sppm_get_frame_info(sppm_ctx* c, sppm_frame_info* fi) {
     fi->counted_segments = st.count_segments;
     fi->counted_nodes = st.count_nodes;
     fi->counted_triangles = st.count_tris;
+    fi->coop_segments = st.coop_segments;
+    fi->kernel_launches = c->kernel_launches;
     return SPPM_OK;
 }
 
@@ -747,7 +873,13 @@ int sppm_enable_traversal_counters(sppm_ctx* c, int enable) {
 
 int sppm_enable_stage_timing(sppm_ctx* c, int enable) {
     if (!c) return fail(SPPM_ERR_ARG, "null context");
-    c->timing = enable != 0;
+    c->timing_mask = enable ? (1u << SPPM_STAGE_COUNT) - 1u : 0u;
+    return SPPM_OK;
+}
+
+int sppm_set_stage_timing_mask(sppm_ctx* c, uint32_t mask) {
+    if (!c) return fail(SPPM_ERR_ARG, "null context");
+    c->timing_mask = mask & ((1u << SPPM_STAGE_COUNT) - 1u);
     return SPPM_OK;
 }
 
@@ -826,6 +958,46 @@ int sppm_debug_fpmath(int fn, const float* x, const float* y, float* out, size_t
     cudaFree(dy);
     cudaFree(dout);
     if (e != cudaSuccess) return fail(SPPM_ERR_CUDA, "fpmath kernel failed: %s", cudaGetErrorString(e));
+    return SPPM_OK;
+}
+
+int sppm_debug_trace(sppm_ctx* c, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
+                     int32_t* tri, float* t) {
+    if (!c || !org || !dir || !tri || !t) return fail(SPPM_ERR_ARG, "null argument");
+    if (!c->have_scene) return fail(SPPM_ERR_STATE, "upload a scene first");
+    if (mode != 0 && mode != 1) return fail(SPPM_ERR_ARG, "mode must be 0 (thread per ray) or 1 (warp per ray)");
+    if (n == 0) return SPPM_OK;
+    if (n > (1u << 26)) return fail(SPPM_ERR_ARG, "n too large");
+    SPPM_CK(cudaSetDevice(c->device));
+    SPPM_CK(cudaStreamSynchronize(c->stream));
+    float *d_org = nullptr, *d_dir = nullptr, *d_t = nullptr;
+    int32_t* d_tri = nullptr;
+    uint32_t* d_err = nullptr;
+    cudaError_t e = cudaMalloc(&d_org, n * 12);
+    if (e == cudaSuccess) e = cudaMalloc(&d_dir, n * 12);
+    if (e == cudaSuccess) e = cudaMalloc(&d_t, n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&d_tri, n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&d_err, 4);
+    if (e == cudaSuccess) e = cudaMemcpy(d_org, org, n * 12, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_dir, dir, n * 12, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(d_err, 0, 4);
+    uint32_t err = 0;
+    if (e == cudaSuccess) {
+        launch_debug_trace(c->job.scene, d_org, d_dir, (uint32_t)n, photon != 0, cull != 0, mode, d_tri, d_t, d_err,
+                           c->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(tri, d_tri, n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(t, d_t, n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&err, d_err, 4, cudaMemcpyDeviceToHost);
+    cudaFree(d_org);
+    cudaFree(d_dir);
+    cudaFree(d_t);
+    cudaFree(d_tri);
+    cudaFree(d_err);
+    if (e != cudaSuccess) return fail(SPPM_ERR_CUDA, "debug trace failed: %s", cudaGetErrorString(e));
+    if (err) return fail(SPPM_ERR_WATCHDOG, "BVH traversal exceeded its step bound");
     return SPPM_OK;
 }
 

@@ -101,6 +101,7 @@ struct JobState {
     uint32_t err;
     unsigned long long num_photons, photon_segments, eye_segments;
     unsigned long long count_nodes, count_tris, count_segments;  // traversal counters (when enabled)
+    unsigned long long coop_segments;  // photon segments traced one per warp
 };
 
 struct JobDesc {
@@ -119,13 +120,26 @@ struct JobDesc {
     float alpha, footprint, focal, aperture, fixed_radius;
 };
 
+// Ray binning: a counting sort of the queued rays by (direction class, origin cell) so that the
+// rays one warp fetches start close together and walk the same node ordering. 24 direction
+// classes (cube face of the direction x the signs of its two minor components) x 8^3 origin
+// cells of the scene's bounding cube, Morton-ordered.
+constexpr uint32_t kRayDirClasses = 24;
+constexpr uint32_t kRayCellBits = 3;
+constexpr uint32_t kRayBins = kRayDirClasses << (3 * kRayCellBits);
+
 // ray queue of the wavefront photon pass: org.w holds the photon's global item index
 struct RayQueue {
     float4* org;
     float4* dir;
     float4* hit;          // (triangle or -1 as int bits, barycentrics v, w, u)
-    uint32_t* counters;   // [0] rays queued, [1] fetch head of the trace kernel
+    uint32_t* counters;   // [0] rays queued, [1] fetch head of the trace kernel, [2] rays set aside
     uint32_t capacity;
+    uint32_t* slow;       // [capacity] queue indices of the rays traced one per warp
+    // binning (all null when the rays are traced in queue order)
+    uint2* key;           // [capacity] (bin, rank within the bin)
+    uint32_t* bins;       // [kRayBins] counts, then exclusive offsets
+    uint32_t* perm;       // [capacity] queue index of the i-th ray in bin order
 };
 
 // the work of one launch: items [prefix[k], prefix[k+1]) belong to jobs[job_ids[k]]

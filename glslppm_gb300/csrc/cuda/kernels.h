@@ -15,6 +15,8 @@ void launch_photon_fp32(const LaunchSet& ls, bool count_traversal, cudaStream_t 
 void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
 void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool count_traversal,
                                uint32_t persistent_blocks, cudaStream_t s);
+void launch_ray_bins(const RayQueue& q, cudaStream_t s);
+void launch_trace_photons_coop(const LaunchSet& ls, const RayQueue& q, bool count_traversal, cudaStream_t s);
 void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
 uint32_t trace_photons_blocks_per_sm();
 
@@ -29,6 +31,8 @@ void launch_resolve_fp32(const LaunchSet& ls, uint32_t display, cudaStream_t s);
 void launch_hash_build(const float4* pos, const float4* flux, uint32_t pw, uint32_t ph, uint32_t hash_num,
                        const float bbmin[3], float grid_scale, uint32_t flags, uint32_t* winner, uint32_t* count,
                        cudaStream_t s);
+void launch_debug_trace(const DevScene& sc, const float* org, const float* dir, uint32_t n, bool photon, bool cull,
+                        int mode, int32_t* tri, float* t, uint32_t* err, cudaStream_t s);
 void launch_fpmath(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t s);
 
 }  // namespace sppm_dev

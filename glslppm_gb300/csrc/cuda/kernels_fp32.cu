@@ -38,6 +38,27 @@ __device__ __forceinline__ int cube_face(f3 d) {
     return d.z < 0.0f ? 5 : 4;
 }
 
+// bin of a queued ray: direction class (cube face x signs of the two minor components) and the
+// Morton index of its origin's cell in a grid over the scene's bounding cube
+__device__ __forceinline__ uint32_t spread_bits4(uint32_t v) {  // bits 0..3 -> 0, 3, 6, 9
+    v = (v | (v << 4)) & 0x0C3u;
+    return (v | (v << 2)) & 0x249u;
+}
+__device__ __forceinline__ uint32_t ray_bin(const DevScene& s, f3 o, f3 d) {
+    const float* bs = s.bsphere;
+    const float half = (float)(1u << (kRayCellBits - 1));
+    const float sc = half / fmaxf(bs[3], 1e-30f);
+    const float top = 2.0f * half - 1.0f;
+    const uint32_t cx = (uint32_t)fminf(fmaxf((o.x - bs[0]) * sc + half, 0.0f), top);
+    const uint32_t cy = (uint32_t)fminf(fmaxf((o.y - bs[1]) * sc + half, 0.0f), top);
+    const uint32_t cz = (uint32_t)fminf(fmaxf((o.z - bs[2]) * sc + half, 0.0f), top);
+    const int face = cube_face(d);
+    const int axis = face >> 1;
+    const float m1 = axis == 0 ? d.y : d.x, m2 = axis == 2 ? d.y : d.z;
+    const uint32_t cls = (uint32_t)face * 4u + (m1 < 0.0f ? 2u : 0u) + (m2 < 0.0f ? 1u : 0u);
+    return (cls << (3 * kRayCellBits)) | (spread_bits4(cx) << 2) | (spread_bits4(cy) << 1) | spread_bits4(cz);
+}
+
 struct TraversalCount {
     uint32_t nodes = 0, tris = 0;
 };
@@ -98,6 +119,153 @@ __device__ __forceinline__ Hit trace_exact(const DevScene& s, f3 org, f3 dir, bo
         const int32_t next = hit ? i + 1 : __float_as_int(A.w);
         if (next < 0 || next >= nn) break;
         i = next;
+    }
+    return h;
+}
+
+// A ray with a zero (or denormal-small) direction component has an infinite reciprocal, and
+// 0 * inf or inf - inf turn that axis' slab into NaN, which fminf/fmaxf then ignore: the box test
+// passes for every box the other axes allow (for a photon leaving the light straight down,
+// every box), and the walk visits nearly the whole tree.  Such rays are rare (a few per 10^7)
+// but each costs thousands of dependent node fetches, so they are traced by coop_trace_exact.
+__device__ __forceinline__ bool slab_degenerate(f3 d) {
+    return fabsf(d.x) < 1e-30f || fabsf(d.y) < 1e-30f || fabsf(d.z) < 1e-30f;
+}
+
+// Warp-cooperative form of trace_exact for one ray (all 32 lanes call it with the same
+// arguments and get the same result).  The lanes evaluate the box and triangle tests of 32
+// consecutive nodes at once; the walk itself -- which nodes are visited, in which order, and
+// which triangle hit replaces the current one -- is then resolved with ballots in exactly the
+// order of the scalar loop, so the result is the same bit for bit.  A node is visited as a hit
+// when its box passes with the t of the closest hit so far; a visited leaf replaces the closest
+// hit when its triangle test passes with that t; the walk goes to node + 1 after a hit and to
+// the miss link otherwise.
+template <bool PHOTON, bool COUNT>
+__device__ __noinline__ Hit coop_trace_exact(const DevScene& s, f3 org, f3 dir, bool cull, uint32_t& err,
+                                             TraversalCount* cnt) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    const int lane = (int)(threadIdx.x & 31);
+    Hit h;
+    h.t = PHOTON ? 1.0e30f : 1.0e20f;
+    h.tri = -1;
+    h.mat = -1;
+    h.bu = h.bv = h.bw = 0.0f;
+    const NodeX* nodes = s.nodes + (size_t)cube_face(dir) * s.num_nodes;
+    const f3 rcp = mk(xdiv(1.0f, dir.x), xdiv(1.0f, dir.y), xdiv(1.0f, dir.z));
+    const f3 t0 = mul(neg(rcp), org);
+    const int32_t nn = (int32_t)s.num_nodes;
+    int32_t cur = 0;
+    uint32_t steps = 0;
+    bool done = false;
+    while (!done) {
+        const int32_t base = cur;
+        const int32_t j = base + lane;
+        bool box = false, leaf = false, ok = false;
+        float tmin = 0.0f, tt = 0.0f, bu = 0.0f, bv = 0.0f, bw = 0.0f;
+        int32_t miss = -1, tri = -1, mat = -1;
+        if (j < nn) {
+            const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + j));
+            const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + j) + 1);
+            const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
+            const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
+            tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
+            const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
+            box = (tmin <= tmax) && (tmax >= 0.0f);
+            miss = __float_as_int(A.w);
+            const int32_t raw = __float_as_int(B.w);
+            leaf = raw >= 0 && (!PHOTON || !(raw & kEmitterBit));
+            if (leaf && box) {
+                tri = raw & kTriMask;
+                const float4 a = __ldg(&s.tri_isect[(size_t)tri * 3 + 0]);
+                const float4 b = __ldg(&s.tri_isect[(size_t)tri * 3 + 1]);
+                const float4 c = __ldg(&s.tri_isect[(size_t)tri * 3 + 2]);
+                const f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
+                const f3 pv = cross(dir, e1);
+                const float det = dot(e0, pv);
+                if (PHOTON || !cull || det > 1e-10f) {
+                    const f3 tv = sub(org, v0);
+                    const f3 qv = cross(tv, e0);
+                    const float u = xdiv(dot(tv, pv), det);
+                    const float v = xdiv(dot(dir, qv), det);
+                    tt = xdiv(dot(e1, qv), det);
+                    const float w = xsub(xsub(1.0f, u), v);
+                    ok = u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f;
+                    mat = __float_as_int(c.y);
+                    bu = v;
+                    bv = w;
+                    bw = u;
+                }
+            }
+        }
+        const unsigned inwin = __ballot_sync(kFull, j < nn);
+        const unsigned leaves = __ballot_sync(kFull, leaf);
+        int pos = 0;
+        for (;;) {
+            const unsigned ge = kFull << pos;
+            const unsigned M = __ballot_sync(kFull, box && tmin <= h.t) & ge & inwin;  // hits with the current t
+            const unsigned U = __ballot_sync(kFull, ok && tt < h.t) & M;               // hits that replace it
+            const unsigned notM = ~M & ge;
+            const int stop = notM ? __ffs(notM) - 1 : 32;  // first lane >= pos that is not a hit
+            const unsigned run = (stop == 32 ? kFull : ((1u << stop) - 1u)) & ge;
+            const unsigned ur = U & run;
+            if (ur) {
+                const int p = __ffs(ur) - 1;  // visits pos..p, the leaf at p replaces the hit
+                const unsigned vis = run & (p == 31 ? kFull : ((2u << p) - 1u));
+                steps += __popc(vis);
+                if (COUNT) {
+                    cnt->nodes += __popc(vis);
+                    cnt->tris += __popc(vis & leaves);
+                }
+                h.t = __shfl_sync(kFull, tt, p);
+                h.tri = __shfl_sync(kFull, tri, p);
+                h.mat = __shfl_sync(kFull, mat, p);
+                h.bu = __shfl_sync(kFull, bu, p);
+                h.bv = __shfl_sync(kFull, bv, p);
+                h.bw = __shfl_sync(kFull, bw, p);
+                if (p == 31) {
+                    cur = base + 32;
+                    done = cur >= nn;
+                    break;
+                }
+                pos = p + 1;
+                if (base + pos >= nn) {
+                    done = true;
+                    break;
+                }
+                continue;
+            }
+            steps += __popc(run);  // pos..stop-1 visited as hits, none replaces the hit
+            if (COUNT) {
+                cnt->nodes += __popc(run);
+                cnt->tris += __popc(run & leaves);
+            }
+            if (stop == 32) {
+                cur = base + 32;
+                done = cur >= nn;
+                break;
+            }
+            if (!((inwin >> stop) & 1u)) {  // the walk stepped past the last node
+                done = true;
+                break;
+            }
+            steps += 1;  // lane `stop` is visited and missed: follow its miss link
+            if (COUNT) cnt->nodes += 1;
+            const int32_t nx = __shfl_sync(kFull, miss, stop);
+            if (nx < 0 || nx >= nn) {
+                done = true;
+                break;
+            }
+            if (nx > base + stop && nx < base + 32) {
+                pos = nx - base;
+                continue;
+            }
+            cur = nx;
+            break;
+        }
+        if (steps > (uint32_t)nn + 1u) {
+            err |= kErrWatchdogTraverse;
+            done = true;
+        }
     }
     return h;
 }
@@ -182,7 +350,9 @@ __global__ void k_frame_begin(LaunchSet ls, RayQueue q) {
     if (g == 0 && q.counters) {
         q.counters[0] = 0;
         q.counters[1] = 0;
+        q.counters[2] = 0;
     }
+    if (q.bins && g < kRayBins) q.bins[g] = 0u;
     if (g >= ls.total) return;
     const int k = find_job(ls, g);
     const JobDesc& J = ls.jobs[ls.job_ids[k]];
@@ -703,8 +873,71 @@ __global__ void __launch_bounds__(128) k_photon_gen(LaunchSet ls, RayQueue q) {
         const uint32_t qi = base + __popc(live & ((1u << (threadIdx.x & 31)) - 1));
         q.org[qi] = make_float4(R.org.x, R.org.y, R.org.z, __uint_as_float(g));
         q.dir[qi] = make_float4(R.dir.x, R.dir.y, R.dir.z, 0.0f);
+        if (q.key) {
+            // lanes with the same bin take consecutive ranks from one atomic
+            const uint32_t bin = ray_bin(J.scene, R.org, R.dir);
+            const unsigned same = __match_any_sync(live, bin);
+            const int lead = __ffs(same) - 1;
+            uint32_t rb = 0;
+            if ((int)(threadIdx.x & 31) == lead) rb = atomicAdd(&q.bins[bin], __popc(same));
+            rb = __shfl_sync(same, rb, lead);
+            q.key[qi] = make_uint2(bin, rb + __popc(same & ((1u << (threadIdx.x & 31)) - 1)));
+        }
     }
     photon_counters(st, k, active, R.emitted, R.cont ? 1u : 0u, err);
+}
+
+// exclusive scan of the bin counts in place (one block of 1024 threads, 96 bins per thread)
+__global__ void __launch_bounds__(1024) k_ray_bins_scan(uint32_t* bins) {
+    constexpr uint32_t kPer = kRayBins / 1024;
+    static_assert(kRayBins % 1024 == 0 && kPer % 4 == 0, "bin count must split into uint4 chunks");
+    __shared__ uint32_t warp_sums[32];
+    uint4* v = reinterpret_cast<uint4*>(bins) + threadIdx.x * (kPer / 4);
+    uint32_t sum = 0;
+#pragma unroll 4
+    for (uint32_t i = 0; i < kPer / 4; i++) {
+        const uint4 x = v[i];
+        sum += x.x + x.y + x.z + x.w;
+    }
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if ((int)lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane], wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+            if ((int)lane >= o) wi += y;
+        }
+        warp_sums[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = warp_sums[warp] + incl - sum;
+#pragma unroll 4
+    for (uint32_t i = 0; i < kPer / 4; i++) {
+        uint4 x = v[i];
+        const uint32_t a = x.x, b = x.y, c = x.z, d = x.w;
+        x.x = run;
+        x.y = run + a;
+        x.z = run + a + b;
+        x.w = run + a + b + c;
+        run += a + b + c + d;
+        v[i] = x;
+    }
+}
+
+// perm[offset of the bin + rank] = queue index
+__global__ void __launch_bounds__(256) k_ray_bins_scatter(RayQueue q) {
+    const uint32_t qi = grid_tid();
+    if (qi >= q.counters[0]) return;
+    const uint2 kr = q.key[qi];
+    q.perm[q.bins[kr.x] + kr.y] = qi;
 }
 
 // trace: persistent warps; a lane whose ray finished fetches the next one from the queue, so
@@ -723,7 +956,21 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
     int32_t node = 0, steps = 0;
     uint32_t err = 0;
     int job_k = 0;
+    // traversal counters: summed per lane, added to the job's totals when the lane moves to
+    // another job's rays and at the end (three 64-bit atomics per ray would serialise the kernel)
     TraversalCount tc;
+    uint32_t tc_segs = 0;
+    int tc_job = -1;
+    auto flush_counts = [&]() {
+        if (tc_job >= 0 && tc_segs) {
+            JobState* st = ls.jobs[ls.job_ids[tc_job]].state;
+            atomicAdd(&st->count_nodes, (unsigned long long)tc.nodes);
+            atomicAdd(&st->count_tris, (unsigned long long)tc.tris);
+            atomicAdd(&st->count_segments, (unsigned long long)tc_segs);
+        }
+        tc.nodes = tc.tris = 0;
+        tc_segs = 0;
+    };
     for (;;) {
         const bool need = idx == kNeed;
         const unsigned m = __ballot_sync(0xFFFFFFFFu, need);
@@ -737,9 +984,14 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
                 if (idx >= total) {
                     idx = kDone;
                 } else {
+                    if (q.perm) idx = q.perm[idx];
                     const float4 o = q.org[idx], d = q.dir[idx];
                     const uint32_t g = __float_as_uint(o.w);
                     job_k = find_job(ls, g);
+                    if (COUNT && job_k != tc_job) {
+                        flush_counts();
+                        tc_job = job_k;
+                    }
                     const DevScene& S = ls.jobs[ls.job_ids[job_k]].scene;
                     org = mk(o.x, o.y, o.z);
                     dir = mk(d.x, d.y, d.z);
@@ -754,11 +1006,16 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
                     h.bu = h.bv = h.bw = 0.0f;
                     node = 0;
                     steps = 0;
+                    if (slab_degenerate(dir)) {
+                        // walks most of the tree: left to k_trace_photons_coop
+                        q.slow[atomicAdd(&q.counters[2], 1u)] = idx;
+                        idx = kNeed;
+                    }
                 }
             }
         }
         if (__all_sync(0xFFFFFFFFu, idx == kDone)) break;
-        if (idx == kDone) continue;
+        if (idx >= kDone) continue;
         bool finished = false;
 #pragma unroll 1
         for (int it = 0; it < 32; it++) {
@@ -808,17 +1065,39 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
         }
         if (finished) {
             q.hit[idx] = make_float4(__int_as_float(h.tri), h.bu, h.bv, h.bw);
-            if (COUNT) {
-                JobState* st = ls.jobs[ls.job_ids[job_k]].state;
-                atomicAdd(&st->count_nodes, (unsigned long long)tc.nodes);
-                atomicAdd(&st->count_tris, (unsigned long long)tc.tris);
-                atomicAdd(&st->count_segments, 1ull);
-                tc.nodes = tc.tris = 0;
-            }
+            if (COUNT) tc_segs++;
             idx = kNeed;
         }
     }
+    if (COUNT) flush_counts();
     if (err) atomicOr(&ls.jobs[ls.job_ids[job_k]].state->err, err);
+}
+
+// the rays k_trace_photons set aside (slab_degenerate directions), one warp per ray
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_photons_coop(LaunchSet ls, RayQueue q) {
+    const uint32_t n = q.counters[2];
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    const unsigned lane = threadIdx.x & 31;
+    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += warps) {
+        const uint32_t idx = q.slow[w];
+        const float4 o = q.org[idx], d = q.dir[idx];
+        const int job_k = find_job(ls, __float_as_uint(o.w));
+        const JobDesc& J = ls.jobs[ls.job_ids[job_k]];
+        uint32_t err = 0;
+        TraversalCount ct;
+        const Hit h = coop_trace_exact<true, COUNT>(J.scene, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), false, err, &ct);
+        if (lane == 0) {
+            q.hit[idx] = make_float4(__int_as_float(h.tri), h.bu, h.bv, h.bw);
+            atomicAdd(&J.state->coop_segments, 1ull);
+            if (err) atomicOr(&J.state->err, err);
+            if (COUNT) {
+                atomicAdd(&J.state->count_nodes, (unsigned long long)ct.nodes);
+                atomicAdd(&J.state->count_tris, (unsigned long long)ct.tris);
+                atomicAdd(&J.state->count_segments, 1ull);
+            }
+        }
+    }
 }
 
 // store: shade the hit of each queued ray, write the photon record, insert it into the grid
@@ -988,13 +1267,43 @@ __global__ void k_fpmath(int fn, const float* x, const float* y, float* out, uin
     out[i] = r;
 }
 
+// single rays through the exact traversal: mode 0 one thread per ray (trace_exact), mode 1 one
+// warp per ray (coop_trace_exact); photon rays skip emitters, eye rays may cull back faces
+template <bool PHOTON>
+__global__ void __launch_bounds__(128) k_debug_trace(DevScene s, const float* org, const float* dir, uint32_t n,
+                                                     int cull, int mode, int32_t* tri, float* t, uint32_t* err) {
+    uint32_t e = 0;
+    if (mode == 0) {
+        const uint32_t i = grid_tid();
+        if (i >= n) return;
+        const Hit h = trace_exact<PHOTON>(s, mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]),
+                                          mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]), cull != 0, e);
+        tri[i] = h.tri;
+        t[i] = h.t;
+    } else {
+        const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+        for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+            TraversalCount ct;
+            const Hit h = coop_trace_exact<PHOTON, false>(s, mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]),
+                                                          mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]), cull != 0,
+                                                          e, &ct);
+            if ((threadIdx.x & 31) == 0) {
+                tri[i] = h.tri;
+                t[i] = h.t;
+            }
+        }
+    }
+    if (e) atomicOr(err, e);
+}
+
 // ----------------------------------------------------------------------------------------------
 // launchers
 // ----------------------------------------------------------------------------------------------
 static inline uint32_t blocks_for(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
 
 void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
-    if (ls.total) k_frame_begin<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls, q);
+    const uint32_t n = q.bins && ls.total < kRayBins ? kRayBins : ls.total;
+    if (ls.total) k_frame_begin<<<blocks_for(n, 256), 256, 0, s>>>(ls, q);
 }
 void launch_eye_fp32(const LaunchSet& ls, cudaStream_t s) {
     if (ls.total) k_eye<<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
@@ -1011,12 +1320,23 @@ void launch_photon_fp32(const LaunchSet& ls, bool count, cudaStream_t s) {
 void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
     if (ls.total) k_photon_gen<<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q);
 }
+void launch_ray_bins(const RayQueue& q, cudaStream_t s) {
+    if (!q.key || !q.capacity) return;
+    k_ray_bins_scan<<<1, 1024, 0, s>>>(q.bins);
+    k_ray_bins_scatter<<<blocks_for(q.capacity, 256), 256, 0, s>>>(q);
+}
 
 void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool count, uint32_t persistent_blocks,
                                cudaStream_t s) {
     if (!ls.total) return;
     if (count) k_trace_photons<true><<<persistent_blocks, 128, 0, s>>>(ls, q);
     else k_trace_photons<false><<<persistent_blocks, 128, 0, s>>>(ls, q);
+    launch_trace_photons_coop(ls, q, count, s);
+}
+void launch_trace_photons_coop(const LaunchSet& ls, const RayQueue& q, bool count, cudaStream_t s) {
+    if (!ls.total || !q.slow) return;
+    if (count) k_trace_photons_coop<true><<<32, 128, 0, s>>>(ls, q);
+    else k_trace_photons_coop<false><<<32, 128, 0, s>>>(ls, q);
 }
 
 void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
@@ -1042,6 +1362,14 @@ void launch_hash_build(const float4* pos, const float4* flux, uint32_t pw, uint3
 }
 void launch_fpmath(int fn, const float* x, const float* y, float* out, uint32_t n, cudaStream_t s) {
     if (n) k_fpmath<<<blocks_for(n, 256), 256, 0, s>>>(fn, x, y, out, n);
+}
+
+void launch_debug_trace(const DevScene& sc, const float* org, const float* dir, uint32_t n, bool photon, bool cull,
+                        int mode, int32_t* tri, float* t, uint32_t* err, cudaStream_t s) {
+    if (!n) return;
+    const uint32_t blocks = mode == 0 ? blocks_for(n, 128) : blocks_for(n, 4);
+    if (photon) k_debug_trace<true><<<blocks, 128, 0, s>>>(sc, org, dir, n, cull, mode, tri, t, err);
+    else k_debug_trace<false><<<blocks, 128, 0, s>>>(sc, org, dir, n, cull, mode, tri, t, err);
 }
 
 }  // namespace sppm_dev

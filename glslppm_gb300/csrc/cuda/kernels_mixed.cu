@@ -166,6 +166,11 @@ __device__ __forceinline__ float byte_f(uint32_t w, uint32_t sel) {
     return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f;
 }
 
+// direction component used for the slab reciprocals: a zero (or denormal-small) component is
+// replaced by +-1e-30 so that the slab of that axis is +-huge instead of NaN (a NaN slab would be
+// ignored by fminf/fmaxf and the ray would enter every box the other axes allow)
+__device__ __forceinline__ float slab_dir(float d) { return fabsf(d) < 1e-30f ? copysignf(1e-30f, d) : d; }
+
 constexpr int kTraceBlock = 128;
 constexpr int kSmemStack = 16;  // top of each thread's stack, in shared memory (16 KB per block)
 constexpr int kLocalStack = kStack - kSmemStack;  // deeper entries, in local memory (rarely touched)
@@ -244,13 +249,14 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
                 if (idx >= total) {
                     idx = kDone;
                 } else {
+                    if (q.perm) idx = q.perm[idx];
                     const float4 o = q.org[idx], d = q.dir[idx];
                     job_k = find_job(ls, __float_as_uint(o.w));
                     const DevScene& S = ls.jobs[ls.job_ids[job_k]].scene;
                     nodes = S.nodes4;
                     tri_isect = S.tri_isect;
                     ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
-                    rx = 1.0f / dx, ry = 1.0f / dy, rz = 1.0f / dz;
+                    rx = 1.0f / slab_dir(dx), ry = 1.0f / slab_dir(dy), rz = 1.0f / slab_dir(dz);
                     nx = -ox * rx, ny = -oy * ry, nz = -oz * rz;
                     ht = 1.0e30f;
                     htri = -1;

@@ -32,8 +32,10 @@ RADIUS_FOOTPRINT, RADIUS_DIAGONAL = 0, 1
 SEED_XORSHIFT, SEED_HASH = 0, 1
 FLAG_GL_DEPTH_CLIP = 0x1
 FLAG_FUSED_PHOTON = 0x2
+FLAG_UNBINNED_RAYS = 0x4
+FLAG_EAGER_LAUNCH = 0x8
 IMAGE_RADIANCE, IMAGE_DISPLAY = 0, 1
-STAGES = ("frame_begin", "eye", "grid", "photon", "gather", "resolve", "photon_trace", "photon_store")
+STAGES = ("frame_begin", "eye", "grid", "photon", "gather", "resolve", "photon_trace", "photon_store", "ray_bins")
 
 STATE = {
     "hit_position": 0, "hit_reflectance": 1, "hit_normal": 2, "eye_rng": 3, "hit_triangle": 4,
@@ -86,6 +88,7 @@ class FrameInfo(C.Structure):
         ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3), ("aa_offset", C.c_float * 2),
         ("photon_segments", C.c_uint64), ("eye_segments", C.c_uint64),
         ("counted_segments", C.c_uint64), ("counted_nodes", C.c_uint64), ("counted_triangles", C.c_uint64),
+        ("coop_segments", C.c_uint64), ("kernel_launches", C.c_uint64),
     ]
 
 
@@ -111,6 +114,7 @@ SIGNATURES = {
     "sppm_state_bytes": (C.c_size_t, [P, C.c_uint32]),
     "sppm_get_frame_info": (C.c_int, [P, C.POINTER(FrameInfo)]),
     "sppm_enable_stage_timing": (C.c_int, [P, C.c_int]),
+    "sppm_set_stage_timing_mask": (C.c_int, [P, C.c_uint32]),
     "sppm_enable_traversal_counters": (C.c_int, [P, C.c_int]),
     "sppm_read_stage_times": (C.c_int, [P, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     "sppm_time_passes": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_float)]),
@@ -121,6 +125,7 @@ SIGNATURES = {
     "sppm_reduce_texture_noalloc": (C.c_int, [P, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), P]),
     "sppm_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "sppm_debug_fpmath": (C.c_int, [C.c_int, P, P, P, C.c_size_t]),
+    "sppm_debug_trace": (C.c_int, [P, P, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P]),
     "sppm_device_count": (C.c_int, []),
     "sppm_abi_version": (C.c_uint32, []),
 }

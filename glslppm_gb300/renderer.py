@@ -246,6 +246,19 @@ class Renderer:
         N.check(N.lib.sppm_read_state(self._h, k, out.ctypes.data, nbytes))
         return out
 
+    def debug_trace(self, org: np.ndarray, dir: np.ndarray, photon: bool = True, cull: bool = False,
+                    mode: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        """Single rays through the exact traversal of the uploaded scene: (triangle or -1, t).
+        mode 0 traces one ray per thread, mode 1 one ray per warp."""
+        org = np.ascontiguousarray(org, dtype=np.float32).reshape(-1, 3)
+        dir = np.ascontiguousarray(dir, dtype=np.float32).reshape(-1, 3)
+        n = org.shape[0]
+        tri = np.empty(n, dtype=np.int32)
+        t = np.empty(n, dtype=np.float32)
+        N.check(N.lib.sppm_debug_trace(self._h, org.ctypes.data, dir.ctypes.data, n, int(photon), int(cull), mode,
+                                       tri.ctypes.data, t.ctypes.data))
+        return tri, t
+
     def frame_info(self) -> N.FrameInfo:
         fi = N.FrameInfo()
         N.check(N.lib.sppm_get_frame_info(self._h, C.byref(fi)))
@@ -253,6 +266,13 @@ class Renderer:
 
     def enable_stage_timing(self, enable: bool = True) -> None:
         N.check(N.lib.sppm_enable_stage_timing(self._h, 1 if enable else 0))
+
+    def time_stages(self, stages) -> None:
+        """Times only the named stages (see native.STAGES); an empty list turns timing off."""
+        mask = 0
+        for s in stages:
+            mask |= 1 << N.STAGES.index(s)
+        N.check(N.lib.sppm_set_stage_timing_mask(self._h, mask))
 
     def read_stage_times(self) -> dict:
         ms = (C.c_float * len(N.STAGES))()

@@ -77,6 +77,10 @@ typedef enum sppm_seed_mode {
                                         generate -> trace -> store (same results) */
 #define SPPM_FLAG_GL_DEPTH_CLIP 0x1u /* scatter.vs: photons whose depth z >= 1 (last row, i >= w/2)
                                         are counted but never become a slot's stored photon */
+#define SPPM_FLAG_EAGER_LAUNCH 0x8u  /* launch each frame's kernels one by one instead of replaying the
+                                        frame's CUDA graph (same results) */
+#define SPPM_FLAG_UNBINNED_RAYS 0x4u /* wavefront pass: trace the photon rays in queue order instead
+                                        of binned by direction class and origin cell (same results) */
 
 typedef struct sppm_config {
     uint32_t width, height;               /* image (ImageResolution x ImageResolution in the ref)  */
@@ -224,6 +228,9 @@ typedef struct sppm_frame_info {
     uint64_t counted_segments;    /* photon segments traced while traversal counters were on   */
     uint64_t counted_nodes;       /* BVH nodes those segments visited                          */
     uint64_t counted_triangles;   /* triangles those segments tested                           */
+    uint64_t coop_segments;       /* photon segments traced one per warp (a zero direction
+                                     component, see sppm_debug_trace)                          */
+    uint64_t kernel_launches;     /* kernels launched by sppm_run_passes since sppm_create      */
 } sppm_frame_info;
 int sppm_get_frame_info(sppm_ctx* ctx, sppm_frame_info* info);
 /* While enabled, the photon pass also counts BVH nodes visited and triangles tested (a separate
@@ -241,9 +248,12 @@ typedef enum sppm_stage {
     SPPM_STAGE_RESOLVE = 5,     /* re.fs                                                   */
     SPPM_STAGE_PHOTON_TRACE = 6, /* photon segment traversal (wavefront pass)              */
     SPPM_STAGE_PHOTON_STORE = 7, /* photon store + hash.fs/scatter/correction (wavefront)  */
-    SPPM_STAGE_COUNT = 8
+    SPPM_STAGE_RAY_BINS = 8,     /* counting sort of the photon rays into bins (wavefront)  */
+    SPPM_STAGE_COUNT = 9
 } sppm_stage;
 int sppm_enable_stage_timing(sppm_ctx* ctx, int enable);
+/* Times only the stages whose bit (1 << stage) is set; 0 turns timing off. */
+int sppm_set_stage_timing_mask(sppm_ctx* ctx, uint32_t mask);
 int sppm_read_stage_times(sppm_ctx* ctx, float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]);
 
 /* Device time (ms) of `n` frames measured with CUDA events on the context's stream. */
@@ -293,6 +303,13 @@ size_t sppm_last_error(char* buf, size_t buf_size);
 /* Runs the pinned FP32 functions of sppm_fpmath.h on the GPU: fn 0 sin, 1 cos, 2 pow(x,y),
    3 exp, 4 log2, 5 exp2.  x, y, out are host arrays of n floats. */
 int sppm_debug_fpmath(int fn, const float* x, const float* y, float* out, size_t n);
+/* Traces n single rays (org, dir: 3 floats each, host arrays) through the uploaded scene's exact
+   FP32 traversal (raytrace() of photontrace.fs:123-255 when photon != 0, of eyeraytrace.fs:67-290
+   with back-face culling when cull != 0 otherwise): tri[i] = closest triangle or -1, t[i] = its
+   t (the initial bound when nothing is hit).  mode 0 traces one ray per thread, mode 1 one ray
+   per warp (the form used for rays with a zero direction component); both give the same result. */
+int sppm_debug_trace(sppm_ctx* ctx, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
+                     int32_t* tri, float* t);
 /* Number of CUDA devices (0 when none); never fails. */
 int sppm_device_count(void);
 uint32_t sppm_abi_version(void);

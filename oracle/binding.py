@@ -37,6 +37,7 @@ def load(fp64: bool = False) -> C.CDLL:
             "gpurnd_sequence": (None, [P, C.c_uint32, P, P]),
             "hash_of_cell": (C.c_uint32, [C.c_float, C.c_float, C.c_float, C.c_float, C.c_uint32]),
             "fpmath": (None, [C.c_int, P, P, P, C.c_size_t]),
+            "trace": (None, [P, P, P, C.c_size_t, C.c_int, C.c_int, P, P]),
             "destroy": (None, [P]),
         }
         for name, (res, args) in sig.items():
@@ -99,6 +100,17 @@ class Oracle:
         fi = FrameInfo()
         self.lib.frame_info(self._h, C.addressof(fi))
         return fi
+
+    def trace(self, org: np.ndarray, dir: np.ndarray, photon: bool = True, cull: bool = False):
+        """raytrace() on single rays: (closest triangle or -1, its t) per ray."""
+        org = np.ascontiguousarray(org, dtype=np.float32).reshape(-1, 3)
+        dir = np.ascontiguousarray(dir, dtype=np.float32).reshape(-1, 3)
+        n = org.shape[0]
+        tri = np.empty(n, dtype=np.int32)
+        t = np.empty(n, dtype=np.float32)
+        self.lib.trace(self._h, org.ctypes.data, dir.ctypes.data, n, int(photon), int(cull), tri.ctypes.data,
+                       t.ctypes.data)
+        return tri, t
 
     def close(self) -> None:
         if self._h:

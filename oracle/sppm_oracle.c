@@ -1228,6 +1228,20 @@ EXPORT int ORACLE_API(reduce_texture)(const float* tex, uint32_t R, uint32_t op,
     return 0;
 }
 
+/* raytrace() on single rays against the context's scene: the closest triangle (-1 = none) and
+   its t (the initial bound when nothing is hit); photon / cull as in raytrace() */
+EXPORT void ORACLE_API(trace)(oracle_ctx* c, const float* org, const float* dir, size_t n, int photon, int cull,
+                              int32_t* tri, float* t) {
+    for (size_t i = 0; i < n; i++) {
+        LastIsect last;
+        const vec3 o = v3((real)org[3 * i], (real)org[3 * i + 1], (real)org[3 * i + 2]);
+        const vec3 d = v3((real)dir[3 * i], (real)dir[3 * i + 1], (real)dir[3 * i + 2]);
+        (void)raytrace(c, o, d, photon, cull, &last);
+        tri[i] = last.tri;
+        t[i] = (float)last.t;
+    }
+}
+
 /* the pinned single-precision functions of sppm_fpmath.h evaluated on the host:
    fn 0 sin, 1 cos, 2 pow(x,y), 3 exp, 4 log2, 5 exp2 */
 EXPORT void ORACLE_API(fpmath)(int fn, const float* x, const float* y, float* out, size_t n) {

@@ -88,6 +88,17 @@ def test_fused_photon_kernel_bit_exact(cornell_c1_mesh):
     run_pair(cfg, mesh.scene(), cam, [1, 11])
 
 
+def test_unbinned_photon_rays_bit_exact(cornell_c1_mesh):
+    """Tracing the photon rays in queue order (SPPM_FLAG_UNBINNED_RAYS) instead of binned by
+    direction class and origin cell changes only the order of work: the state is the same."""
+    sc, mesh = cornell_c1_mesh
+    cfg = g.default_config(32, photon_width=64, photon_height=64, radius_rule=N.RADIUS_DIAGONAL,
+                           radius_fraction=0.01)
+    cfg.flags |= N.FLAG_UNBINNED_RAYS
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 32, 32, sc.fov)
+    run_pair(cfg, mesh.scene(), cam, [1, 11])
+
+
 def test_state_bit_exact_non_square_and_hash_seed(cornell_c1_mesh):
     sc, mesh = cornell_c1_mesh
     cfg = g.default_config(40, height=24, photon_width=48, photon_height=20, hash_slots=1500,
