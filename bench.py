@@ -277,8 +277,8 @@ def run_gpu(args, rank, world, local):
     stages = r.read_stage_times()
     r.enable_stage_timing(False)
 
-    # end to end through the public API with host buffers
-    image = np.empty((cfg.height, cfg.width, 3), dtype=np.float32)
+    # end to end through the public API with (page-locked) host buffers
+    image = g.pinned_empty((cfg.height, cfg.width, 3), np.float32)
     E = max(10, min(K, 100))
     r.synchronize()
     fe0 = r.frame_info()
@@ -300,7 +300,14 @@ def run_gpu(args, rank, world, local):
     kernel = "k_trace_photons4" if args.precision == "mixed" else "k_trace_photons"
     ph_ms, ph_n = roof_times
     roof = None
-    cnt = traversal_counters(r)
+    if args.precision == "mixed":
+        # the algorithmic bytes are those of the exact traversal of the same workload
+        r32 = make_renderer(dev, precision=0)[0]
+        r32.run_passes(W)
+        cnt = traversal_counters(r32)
+        r32.close()
+    else:
+        cnt = traversal_counters(r)
     if ph_n and cnt:
         seg_per_launch = cnt["photon_segments"] / cnt["passes"]
         bytes_per_launch = seg_per_launch * (64 + 32 * cnt["nodes_per_segment"] + 36 * cnt["tris_per_segment"])

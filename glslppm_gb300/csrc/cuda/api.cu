@@ -961,6 +961,24 @@ int sppm_debug_fpmath(int fn, const float* x, const float* y, float* out, size_t
     return SPPM_OK;
 }
 
+int sppm_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr) return fail(SPPM_ERR_ARG, "null argument");
+    *ptr = nullptr;
+    if (bytes == 0) return SPPM_OK;
+    if (sppm_device_count() == 0) return fail(SPPM_ERR_NO_DEVICE, "no CUDA device is visible");
+    const cudaError_t e = cudaMallocHost(ptr, bytes);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return fail(e == cudaErrorMemoryAllocation ? SPPM_ERR_OOM : SPPM_ERR_CUDA, "cudaMallocHost(%zu) failed: %s",
+                    bytes, cudaGetErrorString(e));
+    }
+    return SPPM_OK;
+}
+
+void sppm_host_free(void* ptr) {
+    if (ptr) cudaFreeHost(ptr);
+}
+
 int sppm_debug_trace(sppm_ctx* c, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
                      int32_t* tri, float* t) {
     if (!c || !org || !dir || !tri || !t) return fail(SPPM_ERR_ARG, "null argument");

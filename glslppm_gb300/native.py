@@ -126,6 +126,8 @@ SIGNATURES = {
     "sppm_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "sppm_debug_fpmath": (C.c_int, [C.c_int, P, P, P, C.c_size_t]),
     "sppm_debug_trace": (C.c_int, [P, P, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P]),
+    "sppm_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
+    "sppm_host_free": (None, [P]),
     "sppm_device_count": (C.c_int, []),
     "sppm_abi_version": (C.c_uint32, []),
 }

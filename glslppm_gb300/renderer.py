@@ -337,6 +337,27 @@ def reduce_texture(d_texture: int, resolution: int, op: int, stream: int = 0) ->
     return np.array(list(out), dtype=np.float32)
 
 
+class _PinnedBlock:
+    def __init__(self, nbytes: int):
+        self.ptr = C.c_void_p()
+        N.check(N.lib.sppm_host_alloc(nbytes, C.byref(self.ptr)))
+
+    def __del__(self):
+        if getattr(self, "ptr", None) is not None and self.ptr.value:
+            N.lib.sppm_host_free(self.ptr)
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype=np.float32) -> np.ndarray:
+    """A numpy array in page-locked host memory (freed with the array)."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) * dtype.itemsize
+    block = _PinnedBlock(max(n, 1))
+    buf = (C.c_char * max(n, 1)).from_address(block.ptr.value)
+    buf._block = block  # the ctypes buffer keeps the allocation alive; numpy keeps the buffer
+    return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+
 def debug_fpmath(fn: int, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
     x = np.ascontiguousarray(x, dtype=np.float32)
     yy = None if y is None else np.ascontiguousarray(y, dtype=np.float32)

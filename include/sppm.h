@@ -310,6 +310,10 @@ int sppm_debug_fpmath(int fn, const float* x, const float* y, float* out, size_t
    per warp (the form used for rays with a zero direction component); both give the same result. */
 int sppm_debug_trace(sppm_ctx* ctx, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
                      int32_t* tri, float* t);
+/* Page-locked host memory (cudaMallocHost) for the host buffers of sppm_read_image and friends:
+   copies to it run at the interconnect's DMA rate instead of being staged through the driver. */
+int sppm_host_alloc(size_t bytes, void** ptr);
+void sppm_host_free(void* ptr);
 /* Number of CUDA devices (0 when none); never fails. */
 int sppm_device_count(void);
 uint32_t sppm_abi_version(void);
