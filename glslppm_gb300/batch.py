@@ -1,0 +1,136 @@
+"""Batched SPPM (include/sppm_batch.h): many render jobs advanced by one launch per stage."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import native as N
+from .renderer import Mesh, SceneArrays, _state_array, scene_from_arrays
+
+
+def _scene(scene):
+    if isinstance(scene, Mesh):
+        return scene.scene()
+    if isinstance(scene, SceneArrays):
+        return scene_from_arrays(scene)
+    return scene
+
+
+class Batch:
+    """A set of resident render jobs on one GPU.  Job ids are small integers (slots)."""
+
+    def __init__(self, precision: int = N.PRECISION_FP32, flags: int = 0, eye_pass_interval: int = 10,
+                 max_jobs: int = 256, memory_budget: int = 0, device: int = 0):
+        cfg = N.BatchConfig()
+        N.lib.sppm_batch_config_defaults(C.byref(cfg))
+        cfg.precision, cfg.flags, cfg.eye_pass_interval = precision, flags, eye_pass_interval
+        cfg.max_jobs, cfg.memory_budget = max_jobs, memory_budget
+        out = C.c_void_p()
+        N.check(N.lib.sppm_batch_create(C.byref(cfg), device, C.byref(out)))
+        self._h = out
+        self.config = cfg
+        self._sizes: dict[int, tuple[int, int]] = {}
+
+    def job_bytes(self, config: N.Config, scene) -> int:
+        n = C.c_uint64()
+        N.check(N.lib.sppm_batch_job_bytes(self._h, C.byref(config), C.byref(_scene(scene)), C.byref(n)))
+        return int(n.value)
+
+    def add_job(self, config: N.Config, scene, camera: N.Camera) -> int:
+        job = C.c_uint32()
+        N.check(N.lib.sppm_batch_add_job(self._h, C.byref(config), C.byref(_scene(scene)), C.byref(camera),
+                                         C.byref(job)))
+        self._sizes[job.value] = (config.width, config.height)
+        return int(job.value)
+
+    def remove_job(self, job: int) -> None:
+        N.check(N.lib.sppm_batch_remove_job(self._h, job))
+        self._sizes.pop(job, None)
+
+    def reset_job(self, job: int) -> None:
+        N.check(N.lib.sppm_batch_reset_job(self._h, job))
+
+    def set_camera(self, job: int, camera: N.Camera) -> None:
+        N.check(N.lib.sppm_batch_set_camera(self._h, job, C.byref(camera)))
+
+    def run_passes(self, n: int = 1) -> None:
+        N.check(N.lib.sppm_batch_run_passes(self._h, n))
+
+    def time_passes(self, n: int) -> float:
+        ms = C.c_float()
+        N.check(N.lib.sppm_batch_time_passes(self._h, n, C.byref(ms)))
+        return float(ms.value)
+
+    def synchronize(self) -> None:
+        N.check(N.lib.sppm_batch_synchronize(self._h))
+
+    def read_image(self, job: int, kind: int = N.IMAGE_RADIANCE, out: np.ndarray | None = None) -> np.ndarray:
+        w, h = self._sizes[job]
+        if out is None:
+            out = np.empty((h, w, 3), dtype=np.float32)
+        N.check(N.lib.sppm_batch_read_image(self._h, job, kind, out.ctypes.data, w * h * 3))
+        return out
+
+    def read_state(self, job: int, kind: str) -> np.ndarray:
+        k = N.STATE[kind]
+        nbytes = int(N.lib.sppm_batch_state_bytes(self._h, job, k))
+        if nbytes == 0:
+            raise N.SppmError(N.ERR_ARG, f"state {kind} is not kept by job {job}")
+        out = _state_array(kind, nbytes)
+        N.check(N.lib.sppm_batch_read_state(self._h, job, k, out.ctypes.data, nbytes))
+        return out
+
+    def frame_info(self, job: int) -> N.FrameInfo:
+        fi = N.FrameInfo()
+        N.check(N.lib.sppm_batch_get_frame_info(self._h, job, C.byref(fi)))
+        return fi
+
+    def info(self) -> N.BatchInfo:
+        bi = N.BatchInfo()
+        N.check(N.lib.sppm_batch_get_info(self._h, C.byref(bi)))
+        return bi
+
+    def time_stages(self, stages) -> None:
+        mask = 0
+        for s in stages:
+            mask |= 1 << N.STAGES.index(s)
+        N.check(N.lib.sppm_batch_set_stage_timing_mask(self._h, mask))
+
+    def read_stage_times(self) -> dict:
+        ms = (C.c_float * len(N.STAGES))()
+        n = (C.c_uint32 * len(N.STAGES))()
+        N.check(N.lib.sppm_batch_read_stage_times(self._h, ms, n))
+        return {name: (float(ms[i]), int(n[i])) for i, name in enumerate(N.STAGES)}
+
+    def traversal_counters(self, passes: int = 10) -> dict:
+        """Mean BVH nodes visited and triangles tested per photon segment over every job."""
+        jobs = list(self._sizes)
+        f0 = [self.frame_info(j) for j in jobs]
+        N.check(N.lib.sppm_batch_enable_traversal_counters(self._h, 1))
+        try:
+            self.run_passes(passes)
+            self.synchronize()
+        finally:
+            N.check(N.lib.sppm_batch_enable_traversal_counters(self._h, 0))
+        f1 = [self.frame_info(j) for j in jobs]
+        segs = sum(b.counted_segments - a.counted_segments for a, b in zip(f0, f1))
+        nodes = sum(b.counted_nodes - a.counted_nodes for a, b in zip(f0, f1))
+        tris = sum(b.counted_triangles - a.counted_triangles for a, b in zip(f0, f1))
+        return {"passes": passes, "photon_segments": segs, "nodes_per_segment": nodes / max(segs, 1),
+                "tris_per_segment": tris / max(segs, 1)}
+
+    @property
+    def jobs(self) -> list[int]:
+        return sorted(self._sizes)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            N.lib.sppm_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,261 @@
+// C ABI of the batched SPPM path (include/sppm_batch.h): a Runner holding many Jobs.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "runtime.h"
+#include "sppm_batch.h"
+
+using namespace sppm_dev;
+using namespace sppm_rt;
+using sppm::fail;
+
+struct sppm_batch {
+    Runner rt;
+    sppm_batch_config cfg{};
+    std::vector<std::unique_ptr<Job>> slots;  // [max_jobs]; null = free
+    uint64_t budget = 0;
+};
+
+namespace {
+
+// ray queue bytes per photon slot: org, dir, hit (3 x 16), set-aside list (4), binning key (8)
+// and permutation (4)
+constexpr uint64_t kQueueBytesPerSlot = 3 * 16 + 4 + 8 + 4;
+
+Job* job_of(const sppm_batch* b, uint32_t id) {
+    if (!b || id >= b->slots.size()) return nullptr;
+    return b->slots[id].get();
+}
+
+uint64_t used_bytes(const sppm_batch* b) {
+    uint64_t u = b->rt.desc_mem.size + b->rt.table_mem.size + b->rt.queue_mem.size;
+    for (const auto& j : b->slots)
+        if (j) u += j->bytes();
+    return u;
+}
+
+uint64_t queued_slots(const sppm_batch* b) {
+    uint64_t p = 0;
+    for (const auto& j : b->slots)
+        if (j) p += j->P;
+    return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+void sppm_batch_config_defaults(sppm_batch_config* c) {
+    if (!c) return;
+    memset(c, 0, sizeof(*c));
+    c->precision = SPPM_PRECISION_FP32;
+    c->flags = 0;
+    c->eye_pass_interval = 10;
+    c->max_jobs = 256;
+    c->memory_budget = 0;
+}
+
+int sppm_batch_create(const sppm_batch_config* cfg, int device, sppm_batch** out) {
+    if (!cfg || !out) return fail(SPPM_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (cfg->precision != SPPM_PRECISION_FP32 && cfg->precision != SPPM_PRECISION_MIXED)
+        return fail(SPPM_ERR_ARG, "unknown precision %u", cfg->precision);
+    if (cfg->max_jobs == 0 || cfg->max_jobs > 65536) return fail(SPPM_ERR_ARG, "max_jobs must be 1..65536");
+    if (cfg->eye_pass_interval > 4096) return fail(SPPM_ERR_ARG, "eye_pass_interval must be at most 4096");
+    const int ndev = sppm_device_count();
+    if (ndev == 0) return fail(SPPM_ERR_NO_DEVICE, "no CUDA device is visible");
+    if (device < 0 || device >= ndev) return fail(SPPM_ERR_ARG, "device %d out of range (%d devices)", device, ndev);
+    std::unique_ptr<sppm_batch> b(new (std::nothrow) sppm_batch());
+    if (!b) return fail(SPPM_ERR_OOM, "host allocation failed");
+    b->cfg = *cfg;
+    const uint32_t interval = cfg->eye_pass_interval ? cfg->eye_pass_interval : 1u;
+    b->cfg.eye_pass_interval = interval;
+    int st = b->rt.init(device, cfg->precision, cfg->flags, interval, cfg->max_jobs);
+    if (st) return st;
+    b->slots.resize(cfg->max_jobs);
+    b->budget = cfg->memory_budget;
+    if (b->budget == 0) {
+        size_t free_b = 0, total_b = 0;
+        SPPM_CK(cudaMemGetInfo(&free_b, &total_b));
+        b->budget = (uint64_t)((double)free_b * 0.9);
+    }
+    *out = b.release();
+    return SPPM_OK;
+}
+
+void sppm_batch_destroy(sppm_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->rt.device);
+    if (b->rt.stream) cudaStreamSynchronize(b->rt.stream);
+    b->rt.active.clear();
+    b->slots.clear();
+    delete b;
+}
+
+int sppm_batch_job_bytes(const sppm_batch* b, const sppm_config* cfg, const sppm_scene* scene, uint64_t* bytes) {
+    if (!b || !cfg || !scene || !bytes) return fail(SPPM_ERR_ARG, "null argument");
+    int st = validate_config(cfg);
+    if (st) return st;
+    *bytes = Job::state_bytes(*cfg) + Job::scene_bytes(*scene, cfg->precision) +
+             kQueueBytesPerSlot * (uint64_t)cfg->photon_width * cfg->photon_height;
+    return SPPM_OK;
+}
+
+int sppm_batch_add_job(sppm_batch* b, const sppm_config* cfg, const sppm_scene* scene, const sppm_camera* cam,
+                       uint32_t* job) {
+    if (!b || !cfg || !scene || !cam || !job) return fail(SPPM_ERR_ARG, "null argument");
+    int st = validate_config(cfg);
+    if (st) return st;
+    if (cfg->precision != b->cfg.precision)
+        return fail(SPPM_ERR_ARG, "job precision %u differs from the batch's %u", cfg->precision, b->cfg.precision);
+    const uint32_t interval = cfg->eye_pass_interval ? cfg->eye_pass_interval : 1u;
+    if (interval != b->cfg.eye_pass_interval)
+        return fail(SPPM_ERR_ARG, "job eye_pass_interval %u differs from the batch's %u", interval,
+                    b->cfg.eye_pass_interval);
+    uint32_t id = 0;
+    while (id < b->slots.size() && b->slots[id]) id++;
+    if (id == b->slots.size()) return fail(SPPM_ERR_STATE, "every one of the %u job slots is taken", (uint32_t)id);
+    uint64_t need = 0;
+    if ((st = sppm_batch_job_bytes(b, cfg, scene, &need))) return st;
+    const uint64_t used = used_bytes(b);
+    if (used + need > b->budget)
+        return fail(SPPM_ERR_OOM, "admission: job needs %llu bytes, %llu of the %llu-byte budget are in use",
+                    (unsigned long long)need, (unsigned long long)used, (unsigned long long)b->budget);
+    SPPM_CK(cudaSetDevice(b->rt.device));
+    SPPM_CK(cudaStreamSynchronize(b->rt.stream));
+    std::unique_ptr<Job> j(new (std::nothrow) Job());
+    if (!j) return fail(SPPM_ERR_OOM, "host allocation failed");
+    if ((st = j->init(*cfg, b->rt.d_jobs + id, id, b->rt.stream))) return st;
+    if ((st = j->upload_scene(scene, b->rt.stream))) return st;
+    if ((st = j->set_camera(cam, b->rt.stream))) return st;
+    j->start_frame = b->rt.frames;
+    b->rt.active.push_back(j.get());
+    b->slots[id] = std::move(j);
+    b->rt.dirty = true;
+    *job = id;
+    return SPPM_OK;
+}
+
+int sppm_batch_remove_job(sppm_batch* b, uint32_t id) {
+    Job* j = job_of(b, id);
+    if (!j) return fail(SPPM_ERR_ARG, "no job %u", id);
+    SPPM_CK(cudaSetDevice(b->rt.device));
+    SPPM_CK(cudaStreamSynchronize(b->rt.stream));
+    auto& a = b->rt.active;
+    a.erase(std::remove(a.begin(), a.end(), j), a.end());
+    b->slots[id].reset();
+    b->rt.dirty = true;
+    return SPPM_OK;
+}
+
+int sppm_batch_reset_job(sppm_batch* b, uint32_t id) {
+    Job* j = job_of(b, id);
+    if (!j) return fail(SPPM_ERR_ARG, "no job %u", id);
+    SPPM_CK(cudaSetDevice(b->rt.device));
+    SPPM_CK(cudaStreamSynchronize(b->rt.stream));
+    int st = j->reset(b->rt.stream);
+    if (st) return st;
+    j->start_frame = b->rt.frames;
+    b->rt.dirty = true;
+    return SPPM_OK;
+}
+
+int sppm_batch_set_camera(sppm_batch* b, uint32_t id, const sppm_camera* cam) {
+    Job* j = job_of(b, id);
+    if (!j || !cam) return fail(SPPM_ERR_ARG, "no job %u or null camera", id);
+    SPPM_CK(cudaSetDevice(b->rt.device));
+    return j->set_camera(cam, b->rt.stream);
+}
+
+int sppm_batch_run_passes(sppm_batch* b, uint32_t n) {
+    if (!b) return fail(SPPM_ERR_ARG, "null batch");
+    return b->rt.run(n);
+}
+
+int sppm_batch_time_passes(sppm_batch* b, uint32_t n, float* ms) {
+    if (!b || !ms) return fail(SPPM_ERR_ARG, "null argument");
+    return b->rt.time(n, ms);
+}
+
+int sppm_batch_synchronize(sppm_batch* b) {
+    if (!b) return fail(SPPM_ERR_ARG, "null batch");
+    return b->rt.synchronize();
+}
+
+int sppm_batch_read_image(sppm_batch* b, uint32_t id, uint32_t kind, float* rgb, size_t num_floats) {
+    Job* j = job_of(b, id);
+    if (!j || !rgb) return fail(SPPM_ERR_ARG, "no job %u or null buffer", id);
+    if (kind > SPPM_IMAGE_DISPLAY) return fail(SPPM_ERR_ARG, "unknown image kind %u", kind);
+    if (num_floats != (size_t)j->npix * 3) return fail(SPPM_ERR_ARG, "image needs %zu floats", (size_t)j->npix * 3);
+    int st = b->rt.resolve(*j, kind);
+    if (st) return st;
+    SPPM_CK(cudaMemcpyAsync(rgb, j->d_image, num_floats * 4, cudaMemcpyDeviceToHost, b->rt.stream));
+    return b->rt.synchronize();
+}
+
+size_t sppm_batch_state_bytes(const sppm_batch* b, uint32_t id, uint32_t kind) {
+    const Job* j = job_of(b, id);
+    if (!j) return 0;
+    size_t n = 0;
+    return j->state_ptr(kind, &n) ? n : 0;
+}
+
+int sppm_batch_read_state(sppm_batch* b, uint32_t id, uint32_t kind, void* dst, size_t bytes) {
+    Job* j = job_of(b, id);
+    if (!j || !dst) return fail(SPPM_ERR_ARG, "no job %u or null buffer", id);
+    size_t need = 0;
+    void* src = j->state_ptr(kind, &need);
+    if (!src) return fail(SPPM_ERR_ARG, "state kind %u is not kept by this job", kind);
+    if (bytes != need) return fail(SPPM_ERR_ARG, "state kind %u has %zu bytes, %zu requested", kind, need, bytes);
+    SPPM_CK(cudaSetDevice(b->rt.device));
+    SPPM_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, b->rt.stream));
+    return b->rt.synchronize();
+}
+
+int sppm_batch_get_frame_info(sppm_batch* b, uint32_t id, sppm_frame_info* fi) {
+    Job* j = job_of(b, id);
+    if (!j || !fi) return fail(SPPM_ERR_ARG, "no job %u or null output", id);
+    SPPM_CK(cudaSetDevice(b->rt.device));
+    int st = j->frame_info(fi, b->rt.stream);
+    if (st) return st;
+    fi->kernel_launches = b->rt.kernel_launches;
+    return SPPM_OK;
+}
+
+int sppm_batch_get_info(sppm_batch* b, sppm_batch_info* info) {
+    if (!b || !info) return fail(SPPM_ERR_ARG, "null argument");
+    memset(info, 0, sizeof(*info));
+    info->num_jobs = (uint32_t)b->rt.active.size();
+    info->max_jobs = (uint32_t)b->slots.size();
+    info->bytes_used = used_bytes(b);
+    info->memory_budget = b->budget;
+    info->frames = b->rt.frames;
+    info->kernel_launches = b->rt.kernel_launches;
+    info->photon_slots = queued_slots(b);
+    for (const Job* j : b->rt.active) info->pixels += j->npix;
+    return SPPM_OK;
+}
+
+int sppm_batch_set_stage_timing_mask(sppm_batch* b, uint32_t mask) {
+    if (!b) return fail(SPPM_ERR_ARG, "null batch");
+    b->rt.timing_mask = mask & ((1u << SPPM_STAGE_COUNT) - 1u);
+    return SPPM_OK;
+}
+
+int sppm_batch_read_stage_times(sppm_batch* b, float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]) {
+    if (!b || !ms || !launches) return fail(SPPM_ERR_ARG, "null argument");
+    return b->rt.read_stage_times(ms, launches);
+}
+
+int sppm_batch_enable_traversal_counters(sppm_batch* b, int enable) {
+    if (!b) return fail(SPPM_ERR_ARG, "null batch");
+    b->rt.count_traversal = enable != 0;
+    return SPPM_OK;
+}
+
+}  // extern "C"

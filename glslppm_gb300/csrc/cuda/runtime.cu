@@ -1,0 +1,850 @@
+// Render jobs in device memory and the runner that queues the passes of a set of jobs.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../host/scene_bvh4.h"
+#include "kernels.h"
+#include "runtime.h"
+
+using sppm::fail;
+
+namespace sppm_rt {
+
+int Arena::reserve(size_t bytes) {
+    release();
+    size = bytes;
+    if (bytes == 0) return SPPM_OK;
+    cudaError_t e = cudaMalloc(&base, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        base = nullptr;
+        size = 0;
+        return fail(e == cudaErrorMemoryAllocation ? SPPM_ERR_OOM : SPPM_ERR_CUDA, "cudaMalloc(%zu bytes) failed: %s",
+                    bytes, cudaGetErrorString(e));
+    }
+    return SPPM_OK;
+}
+
+int launch_check(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(SPPM_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+    return SPPM_OK;
+}
+
+int validate_config(const sppm_config* c) {
+    if (!c) return fail(SPPM_ERR_ARG, "null config");
+    if (c->width == 0 || c->height == 0 || c->photon_width == 0 || c->photon_height == 0)
+        return fail(SPPM_ERR_ARG, "image and photon buffer sizes must be positive");
+    if ((uint64_t)c->width * c->height > (1u << 28) || (uint64_t)c->photon_width * c->photon_height > (1u << 28))
+        return fail(SPPM_ERR_ARG, "image or photon buffer larger than 2^28 elements");
+    if (c->hash_slots > (1u << 28)) return fail(SPPM_ERR_ARG, "hash_slots larger than 2^28");
+    if (c->max_path_length == 0 || c->max_path_length > 1024) return fail(SPPM_ERR_ARG, "max_path_length must be 1..1024");
+    if (c->precision != SPPM_PRECISION_FP32 && c->precision != SPPM_PRECISION_MIXED)
+        return fail(SPPM_ERR_ARG, "unknown precision %u", c->precision);
+    if (c->seed_mode > SPPM_SEED_HASH) return fail(SPPM_ERR_ARG, "unknown seed mode %u", c->seed_mode);
+    if (c->radius_rule > SPPM_RADIUS_DIAGONAL) return fail(SPPM_ERR_ARG, "unknown radius rule %u", c->radius_rule);
+    if (!(c->alpha > 0.0f && c->alpha <= 1.0f)) return fail(SPPM_ERR_ARG, "alpha must be in (0, 1]");
+    if (c->eye_pass_interval > 4096) return fail(SPPM_ERR_ARG, "eye_pass_interval must be at most 4096");
+    return SPPM_OK;
+}
+
+namespace {
+
+// ---- seeding (RandomizeTextures, glslppm.cpp:77-140) -----------------------------------------
+float xorshift_frand(uint32_t* s) {
+    const uint32_t t = s[0] ^ (s[0] << 11);
+    s[0] = s[1];
+    s[1] = s[2];
+    s[2] = s[3];
+    s[3] = (s[3] ^ (s[3] >> 19)) ^ (t ^ (t >> 8));
+    return (float)s[3] * (1.0f / 4294967295.0f);
+}
+
+uint32_t mix32(uint32_t h) {  // MurmurHash3 fmix32 finaliser
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+
+void seed_streams(const sppm_config& cfg, uint32_t npix, uint32_t P, std::vector<float>& eye, std::vector<float>& ph,
+                  uint32_t xs[4]) {
+    xs[0] = 123456789u;
+    xs[1] = 362436069u;
+    xs[2] = 521288629u;
+    xs[3] = 88675123u;
+    if (cfg.seed != 0) {
+        for (int k = 0; k < 4; k++) xs[k] ^= mix32(cfg.seed * 4u + (uint32_t)k + 0x9E3779B9u);
+        if ((xs[0] | xs[1] | xs[2] | xs[3]) == 0) xs[0] = 1;
+    }
+    eye.resize((size_t)npix * 4);
+    ph.resize((size_t)P * 4);
+    if (cfg.seed_mode == SPPM_SEED_XORSHIFT) {
+        // the reference's TVector4(rand, rand, rand, rand) evaluates its arguments right to left
+        for (size_t i = 0; i < eye.size(); i += 4)
+            for (int k = 3; k >= 0; k--) eye[i + k] = (float)((double)xorshift_frand(xs) * 4194304.0);
+        for (size_t i = 0; i < ph.size(); i += 4)
+            for (int k = 3; k >= 0; k--) ph[i + k] = (float)((double)xorshift_frand(xs) * 4194304.0);
+    } else {
+        static const uint32_t mlane[4] = {4194287u, 4194277u, 4194191u, 4194167u};
+        for (size_t e = 0; e < (size_t)npix + P; e++) {
+            for (int k = 0; k < 4; k++) {
+                const uint32_t h = mix32(mix32((uint32_t)e * 4u + (uint32_t)k) ^ mix32(cfg.seed + 0x51ED27u * (e >= npix)));
+                const float v = (float)(1u + h % (mlane[k] - 1u));
+                if (e < npix) eye[e * 4 + k] = v;
+                else ph[(e - npix) * 4 + k] = v;
+            }
+        }
+    }
+}
+
+// ---- scene packing (CGPURT::CreateTextures, gpurt.cpp:47-552, in the traversal layout) --------
+struct Packed {
+    std::vector<NodeX> nodes;
+    std::vector<float4> isect, shade;
+    std::vector<DevMaterial> mats;
+    std::vector<float> light_cdf;
+    std::vector<int32_t> light_tri;
+};
+
+int check_scene(const sppm_scene* s) {
+    if (!s) return fail(SPPM_ERR_ARG, "null scene");
+    const uint32_t nt = s->num_triangles, nn = s->num_nodes, nm = s->num_materials, nl = s->num_lights;
+    if (nt == 0) return fail(SPPM_ERR_ARG, "scene has no triangles");
+    if (nt > (uint32_t)kTriMask) return fail(SPPM_ERR_ARG, "scene has more than 2^30 triangles");
+    if (nn != 2 * nt - 1) return fail(SPPM_ERR_ARG, "num_nodes %u must be 2*num_triangles-1 = %u", nn, 2 * nt - 1);
+    if (!s->positions || !s->normals || !s->material_ids || !s->materials || nm == 0 || !s->node_bounds ||
+        !s->node_triangle || !s->order_base || !s->order_miss)
+        return fail(SPPM_ERR_ARG, "scene array missing (positions, normals, materials, BVH)");
+    if (nl && (!s->light_triangles || !s->light_cdf)) return fail(SPPM_ERR_ARG, "light table missing");
+    if (s->light_area != 0.0f && nl == 0) return fail(SPPM_ERR_ARG, "light_area != 0 with an empty light table");
+    return SPPM_OK;
+}
+
+int pack_scene(const sppm_scene* s, Packed& out) {
+    int st = check_scene(s);
+    if (st) return st;
+    const uint32_t nt = s->num_triangles, nn = s->num_nodes, nm = s->num_materials, nl = s->num_lights;
+    out.mats.resize(nm);
+    for (uint32_t m = 0; m < nm; m++) {
+        const sppm_material& sm = s->materials[m];
+        if (sm.brdf < -1 || sm.brdf > 6) return fail(SPPM_ERR_UNSUPPORTED, "material %u: brdf %d not supported", m, sm.brdf);
+        DevMaterial& d = out.mats[m];
+        memset(&d, 0, sizeof(d));
+        d.color[0] = sm.color[0];
+        d.color[1] = sm.color[1];
+        d.color[2] = sm.color[2];
+        d.eta = sm.eta;
+        d.brdf = sm.brdf;
+        d.g = sm.glossiness;
+    }
+    out.isect.resize((size_t)nt * 3);
+    out.shade.resize((size_t)nt * 6);
+    for (uint32_t t = 0; t < nt; t++) {
+        const int32_t mi = s->material_ids[t];
+        if (mi < 0 || (uint32_t)mi >= nm) return fail(SPPM_ERR_ARG, "triangle %u: material %d out of range", t, mi);
+        const float* p = s->positions + (size_t)t * 9;
+        const sppm::V3 v0 = sppm::v3(p[0], p[1], p[2]), v1 = sppm::v3(p[3], p[4], p[5]), v2 = sppm::v3(p[6], p[7], p[8]);
+        const sppm::V3 e0 = v1 - v0, e1 = v2 - v0;
+        float mbits;
+        memcpy(&mbits, &mi, 4);
+        out.isect[(size_t)t * 3 + 0] = make_float4(v0.x, v0.y, v0.z, e0.x);
+        out.isect[(size_t)t * 3 + 1] = make_float4(e0.y, e0.z, e1.x, e1.y);
+        out.isect[(size_t)t * 3 + 2] = make_float4(e1.z, mbits, 0.0f, 0.0f);
+        // geometric normal normalize(cross(V1-V0, V2-V0)) (eyeraytrace.fs:275)
+        const sppm::V3 gn = sppm::normalize3(sppm::cross3(e0, e1));
+        // shading normals as the shader decodes them: z = sgn(nz) * sqrt(|1 - x*x - y*y|)
+        // with sgn(0) = -1 as gpurt.cpp packs it (eyeraytrace.fs:268-270, gpurt.cpp:35-45, 85)
+        float N[9];
+        const float* n = s->normals + (size_t)t * 9;
+        for (int k = 0; k < 3; k++) {
+            const float x = n[k * 3], y = n[k * 3 + 1];
+            const float sg = n[k * 3 + 2] > 0.0f ? 1.0f : -1.0f;
+            N[k * 3] = x;
+            N[k * 3 + 1] = y;
+            N[k * 3 + 2] = sg * sppm::sqrt_f32(std::fabs(1.0f - x * x - y * y));
+        }
+        out.shade[(size_t)t * 6 + 0] = make_float4(gn.x, gn.y, gn.z, mbits);
+        out.shade[(size_t)t * 6 + 1] = make_float4(v0.x, v0.y, v0.z, v1.x);
+        out.shade[(size_t)t * 6 + 2] = make_float4(v1.y, v1.z, v2.x, v2.y);
+        out.shade[(size_t)t * 6 + 3] = make_float4(v2.z, N[0], N[1], N[2]);
+        out.shade[(size_t)t * 6 + 4] = make_float4(N[3], N[4], N[5], N[6]);
+        out.shade[(size_t)t * 6 + 5] = make_float4(N[7], N[8], 0.0f, 0.0f);
+    }
+    out.nodes.resize((size_t)6 * nn);
+    std::vector<uint8_t> seen(nn);
+    for (int o = 0; o < 6; o++) {
+        std::fill(seen.begin(), seen.end(), 0);
+        for (uint32_t i = 0; i < nn; i++) {
+            const int32_t c = s->order_base[(size_t)o * nn + i];
+            if (c < 0 || (uint32_t)c >= nn || seen[c])
+                return fail(SPPM_ERR_ARG, "ordering %d: node %u has an invalid or repeated base id %d", o, i, c);
+            seen[c] = 1;
+            const int32_t raw = s->order_miss[(size_t)o * nn + i];
+            NodeX& d = out.nodes[(size_t)o * nn + i];
+            const float* b = s->node_bounds + (size_t)c * 6;
+            d.bmin[0] = b[0];
+            d.bmin[1] = b[1];
+            d.bmin[2] = b[2];
+            d.bmax[0] = b[3];
+            d.bmax[1] = b[4];
+            d.bmax[2] = b[5];
+            d.miss = (raw < 0 || (uint32_t)raw >= nn) ? -1 : raw;
+            int32_t tri = s->node_triangle[c];
+            if (tri >= (int32_t)nt) return fail(SPPM_ERR_ARG, "node %d: triangle %d out of range", c, tri);
+            if (tri >= 0 && s->materials[s->material_ids[tri]].brdf == -1) tri |= kEmitterBit;
+            d.tri = tri < 0 ? -1 : tri;
+        }
+    }
+    out.light_cdf.assign(s->light_cdf, s->light_cdf + nl);
+    out.light_tri.assign(s->light_triangles, s->light_triangles + nl);
+    for (uint32_t l = 0; l < nl; l++)
+        if (out.light_tri[l] < 0 || (uint32_t)out.light_tri[l] >= nt)
+            return fail(SPPM_ERR_ARG, "light %u: triangle %d out of range", l, out.light_tri[l]);
+    return SPPM_OK;
+}
+
+template <class T>
+int put(Arena& a, const std::vector<T>& v, T** dst, cudaStream_t s) {
+    *dst = a.take<T>(std::max<size_t>(v.size(), 1));
+    if (!*dst) return fail(SPPM_ERR_OOM, "scene arena exhausted");
+    if (!v.empty()) SPPM_CK(cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return SPPM_OK;
+}
+
+constexpr size_t kSelfWords = 8;
+
+}  // namespace
+
+// ================================================================================================
+// Job
+// ================================================================================================
+uint64_t Job::state_bytes(const sppm_config& cfg) {
+    const size_t np = (size_t)cfg.width * cfg.height, P = (size_t)cfg.photon_width * cfg.photon_height;
+    const size_t hn = cfg.hash_slots ? cfg.hash_slots : P;
+    size_t b = Arena::align(sizeof(JobState)) + Arena::align(kSelfWords * 4);
+    b += 6 * Arena::align(np * 16) + 2 * Arena::align(np * 4) + Arena::align(np * 12);
+    b += 4 * Arena::align(P * 16) + Arena::align(P * 8);
+    b += 2 * Arena::align(hn * 4);
+    if (cfg.precision == SPPM_PRECISION_MIXED)
+        b += Arena::align(hn * sizeof(SlotRec)) + 2 * Arena::align(np * 8) + Arena::align(np * 24);
+    return b;
+}
+
+uint64_t Job::scene_bytes(const sppm_scene& s, uint32_t precision) {
+    const uint64_t nt = s.num_triangles, nn = s.num_nodes;
+    uint64_t b = Arena::align(6 * nn * sizeof(NodeX)) + Arena::align(nt * 48) + Arena::align(nt * 96) +
+                 Arena::align(std::max<uint64_t>(s.num_materials, 1) * sizeof(DevMaterial)) +
+                 2 * Arena::align(std::max<uint64_t>(s.num_lights, 1) * 4) + 1024;
+    // the 4-wide tree has at most one node per internal binary node
+    if (precision == SPPM_PRECISION_MIXED) b += Arena::align(std::max<uint64_t>(nn, 1) * sizeof(sppm::Node4));
+    else b += Arena::align(sizeof(sppm::Node4));
+    return b;
+}
+
+int Job::init(const sppm_config& c, JobDesc* dd, uint32_t sl, cudaStream_t s) {
+    int st = validate_config(&c);
+    if (st) return st;
+    cfg = c;
+    d_desc = dd;
+    slot = sl;
+    W = c.width;
+    H = c.height;
+    PW = c.photon_width;
+    PH = c.photon_height;
+    P = PW * PH;
+    npix = W * H;
+    hash_num = c.hash_slots ? c.hash_slots : P;
+    const size_t np = npix, hn = hash_num;
+    if ((st = state_mem.reserve(state_bytes(c)))) return st;
+    Arena& a = state_mem;
+    d_state = a.take<JobState>(1);
+    d_self = a.take<uint32_t>(kSelfWords);
+    JobDesc& J = desc;
+    memset(&J, 0, sizeof(J));
+    J.px.pos = a.take<float4>(np);
+    J.px.refl = a.take<float4>(np);
+    J.px.nrm = a.take<float4>(np);
+    J.px.rng = a.take<float4>(np);
+    J.px.emi_n = a.take<float4>(np);
+    J.px.flux_r = a.take<float4>(np);
+    J.px.tri = a.take<int32_t>(np);
+    J.px.t = a.take<float>(np);
+    d_image = a.take<float>(np * 3);
+    J.ph.pos = a.take<float4>(P);
+    J.ph.flux = a.take<float4>(P);
+    J.ph.dir = a.take<float4>(P);
+    J.ph.rng = a.take<float4>(P);
+    J.ph.hit = a.take<int2>(P);
+    J.winner = a.take<uint32_t>(hn);
+    J.count = a.take<uint32_t>(hn);
+    if (c.precision == SPPM_PRECISION_MIXED) {
+        J.slots = a.take<SlotRec>(hn);
+        J.px.stat_n = a.take<double>(np);
+        J.px.stat_r2 = a.take<double>(np);
+        J.px.stat_tau = a.take<double>(np * 3);
+        if (!J.px.stat_tau) return fail(SPPM_ERR_OOM, "state arena sizing error (mixed)");
+    }
+    if (!J.count) return fail(SPPM_ERR_OOM, "state arena sizing error");
+    J.state = d_state;
+    J.image = d_image;
+    J.W = W;
+    J.H = H;
+    J.PW = PW;
+    J.PH = PH;
+    J.hash_num = hash_num;
+    J.max_path = c.max_path_length;
+    J.eye_interval = c.eye_pass_interval;
+    J.radius_rule = c.radius_rule;
+    J.flags = c.flags;
+    J.precision = c.precision;
+    J.alpha = c.alpha;
+    J.footprint = c.initial_footprint;
+    J.focal = c.focal_length;
+    J.aperture = c.aperture;
+    const uint32_t self[kSelfWords] = {slot, 0u, npix, 0u, P, 0u, hash_num, 0u};
+    SPPM_CK(cudaMemcpyAsync(d_self, self, sizeof(self), cudaMemcpyHostToDevice, s));
+    if ((st = write_desc(s))) return st;
+    return reset(s);
+}
+
+int Job::write_desc(cudaStream_t s) {
+    SPPM_CK(cudaMemcpyAsync(d_desc, &desc, sizeof(JobDesc), cudaMemcpyHostToDevice, s));
+    SPPM_CK(cudaStreamSynchronize(s));  // the host copy may change right after this call
+    return SPPM_OK;
+}
+
+int Job::reset(cudaStream_t s) {
+    std::vector<float> eye, ph;
+    JobState st;
+    memset(&st, 0, sizeof(st));
+    seed_streams(cfg, npix, P, eye, ph, st.xs);
+    const DevPixels& px = desc.px;
+    const DevPhotons& pp = desc.ph;
+    SPPM_CK(cudaMemcpyAsync(px.rng, eye.data(), eye.size() * 4, cudaMemcpyHostToDevice, s));
+    SPPM_CK(cudaMemcpyAsync(pp.rng, ph.data(), ph.size() * 4, cudaMemcpyHostToDevice, s));
+    const size_t n4 = (size_t)npix * sizeof(float4);
+    SPPM_CK(cudaMemsetAsync(px.pos, 0, n4, s));
+    SPPM_CK(cudaMemsetAsync(px.refl, 0, n4, s));
+    SPPM_CK(cudaMemsetAsync(px.nrm, 0, n4, s));
+    SPPM_CK(cudaMemsetAsync(px.emi_n, 0, n4, s));
+    SPPM_CK(cudaMemsetAsync(px.flux_r, 0, n4, s));
+    SPPM_CK(cudaMemsetAsync(px.tri, 0xFF, (size_t)npix * 4, s));
+    SPPM_CK(cudaMemsetAsync(px.t, 0, (size_t)npix * 4, s));
+    const size_t p4 = (size_t)P * sizeof(float4);
+    SPPM_CK(cudaMemsetAsync(pp.pos, 0, p4, s));
+    SPPM_CK(cudaMemsetAsync(pp.flux, 0, p4, s));
+    SPPM_CK(cudaMemsetAsync(pp.dir, 0, p4, s));
+    SPPM_CK(cudaMemsetAsync(pp.hit, 0, (size_t)P * sizeof(int2), s));
+    SPPM_CK(cudaMemsetAsync(desc.winner, 0xFF, (size_t)hash_num * 4, s));
+    SPPM_CK(cudaMemsetAsync(desc.count, 0, (size_t)hash_num * 4, s));
+    if (desc.slots) {
+        SPPM_CK(cudaMemsetAsync(desc.slots, 0, (size_t)hash_num * sizeof(SlotRec), s));
+        SPPM_CK(cudaMemsetAsync(px.stat_n, 0, (size_t)npix * 8, s));
+        SPPM_CK(cudaMemsetAsync(px.stat_r2, 0, (size_t)npix * 8, s));
+        SPPM_CK(cudaMemsetAsync(px.stat_tau, 0, (size_t)npix * 24, s));
+    }
+    st.initial_radius = fixed_radius;
+    SPPM_CK(cudaMemcpyAsync(d_state, &st, sizeof(st), cudaMemcpyHostToDevice, s));
+    SPPM_CK(cudaStreamSynchronize(s));  // the host vectors go out of scope
+    return SPPM_OK;
+}
+
+int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
+    Packed pk;
+    int st = pack_scene(scene, pk);
+    if (st) return st;
+    std::vector<sppm::Node4> nodes4;
+    if (cfg.precision == SPPM_PRECISION_MIXED) {
+        uint32_t depth = 0;
+        const int b4 = sppm::build_bvh4(*scene, nodes4, &depth);
+        if (b4) return fail(SPPM_ERR_ARG, "4-wide BVH construction failed (%d): inconsistent BVH arrays", b4);
+        if (depth > sppm::kBvh4MaxDepth)
+            return fail(SPPM_ERR_UNSUPPORTED, "4-wide BVH depth %u exceeds the traversal stack (%u levels)", depth,
+                        sppm::kBvh4MaxDepth);
+        for (auto& n : nodes4)  // photon rays pass through lights: mark leaf triangles of emitters
+            for (int k = 0; k < n.count; k++)
+                if (n.child[k] < 0 && n.child[k] != sppm::kChildEmpty) {
+                    const int32_t tri = ~n.child[k];
+                    if (scene->materials[scene->material_ids[tri]].brdf == -1) n.child[k] = ~(tri | kEmitterBit);
+                }
+    }
+    const size_t bytes = Arena::align(pk.nodes.size() * sizeof(NodeX)) + Arena::align(pk.isect.size() * 16) +
+                         Arena::align(pk.shade.size() * 16) + Arena::align(pk.mats.size() * sizeof(DevMaterial)) +
+                         Arena::align(std::max<size_t>(pk.light_cdf.size(), 1) * 4) +
+                         Arena::align(std::max<size_t>(pk.light_tri.size(), 1) * 4) +
+                         Arena::align(std::max<size_t>(nodes4.size(), 1) * sizeof(sppm::Node4)) + 1024;
+    SPPM_CK(cudaStreamSynchronize(s));
+    if ((st = scene_mem.reserve(bytes))) return st;
+    scene_bytes_used = bytes;
+    DevScene& S = desc.scene;
+    NodeX* nodes;
+    float4 *isect, *shade;
+    DevMaterial* mats;
+    float* lcdf;
+    int32_t* ltri;
+    if ((st = put(scene_mem, pk.nodes, &nodes, s))) return st;
+    if ((st = put(scene_mem, pk.isect, &isect, s))) return st;
+    if ((st = put(scene_mem, pk.shade, &shade, s))) return st;
+    if ((st = put(scene_mem, pk.mats, &mats, s))) return st;
+    if ((st = put(scene_mem, pk.light_cdf, &lcdf, s))) return st;
+    if ((st = put(scene_mem, pk.light_tri, &ltri, s))) return st;
+    sppm::Node4* n4 = nullptr;
+    if ((st = put(scene_mem, nodes4, &n4, s))) return st;
+    S.nodes4 = nodes4.empty() ? nullptr : reinterpret_cast<const Node4Dev*>(n4);
+    S.flux_unscale = scene->light_area != 0.0f ? scene->light_area * 3.141592f : 1.0f;
+    S.flux_unscale_inv = 1.0f / S.flux_unscale;
+    S.nodes = nodes;
+    S.tri_isect = isect;
+    S.tri_shade = shade;
+    S.mats = mats;
+    S.light_cdf = lcdf;
+    S.light_tri = ltri;
+    S.num_nodes = scene->num_nodes;
+    S.num_tris = scene->num_triangles;
+    S.num_lights = scene->num_lights;
+    S.num_mats = scene->num_materials;
+    S.light_area = scene->light_area;
+    S.light_stride = scene->num_lights ? 1.0f / (float)scene->num_lights : 0.0f;
+    // SceneBSphere (glslppm.cpp:388-393)
+    const float* mn = scene->bbox_min;
+    const float* mx = scene->bbox_max;
+    const float dx = mx[0] - mn[0], dy = mx[1] - mn[1], dz = mx[2] - mn[2];
+    S.bsphere[0] = (mx[0] + mn[0]) * 0.5f;
+    S.bsphere[1] = (mx[1] + mn[1]) * 0.5f;
+    S.bsphere[2] = (mx[2] + mn[2]) * 0.5f;
+    S.bsphere[3] = sppm::sqrt_f32(dx * dx + dy * dy + dz * dz) * 0.5f;
+    fixed_radius = cfg.radius_rule == SPPM_RADIUS_DIAGONAL
+                       ? cfg.radius_fraction * sppm::sqrt_f32(dx * dx + dy * dy + dz * dz)
+                       : 0.0f;
+    desc.fixed_radius = fixed_radius;
+    have_scene = true;
+    if ((st = write_desc(s))) return st;
+    return reset(s);
+}
+
+int Job::set_camera(const sppm_camera* cam, cudaStream_t s) {
+    JobDesc& J = desc;
+    for (int k = 0; k < 3; k++) {
+        J.cam_pos[k] = cam->origin[k];
+        J.cam_u[k] = cam->u[k];
+        J.cam_v[k] = cam->v[k];
+        J.cam_w[k] = cam->w[k];
+    }
+    J.cam_cx = (float)cam->width * 0.5f;
+    J.cam_cy = (float)cam->height * 0.5f;
+    J.cam_dist = cam->distance;
+    have_camera = true;
+    SPPM_CK(cudaStreamSynchronize(s));
+    return write_desc(s);
+}
+
+void* Job::state_ptr(uint32_t kind, size_t* bytes) const {
+    const JobDesc& J = desc;
+    const size_t np = npix, hn = hash_num, p = P;
+    switch (kind) {
+        case SPPM_STATE_HIT_POSITION: *bytes = np * 16; return J.px.pos;
+        case SPPM_STATE_HIT_REFLECTANCE: *bytes = np * 16; return J.px.refl;
+        case SPPM_STATE_HIT_NORMAL: *bytes = np * 16; return J.px.nrm;
+        case SPPM_STATE_EYE_RNG: *bytes = np * 16; return J.px.rng;
+        case SPPM_STATE_HIT_TRIANGLE: *bytes = np * 4; return J.px.tri;
+        case SPPM_STATE_EMISSION_N: *bytes = np * 16; return J.px.emi_n;
+        case SPPM_STATE_FLUX_RADIUS: *bytes = np * 16; return J.px.flux_r;
+        case SPPM_STATE_PHOTON_POSITION: *bytes = p * 16; return J.ph.pos;
+        case SPPM_STATE_PHOTON_FLUX: *bytes = p * 16; return J.ph.flux;
+        case SPPM_STATE_PHOTON_DIRECTION: *bytes = p * 16; return J.ph.dir;
+        case SPPM_STATE_PHOTON_RNG: *bytes = p * 16; return J.ph.rng;
+        case SPPM_STATE_PHOTON_HIT: *bytes = p * 8; return J.ph.hit;
+        case SPPM_STATE_SLOT_WINNER: *bytes = hn * 4; return J.winner;
+        case SPPM_STATE_SLOT_COUNT: *bytes = hn * 4; return J.count;
+        case SPPM_STATE_HIT_T: *bytes = np * 4; return J.px.t;
+        case SPPM_STATE_STATS_N: *bytes = J.px.stat_n ? np * 8 : 0; return J.px.stat_n;
+        case SPPM_STATE_STATS_R2: *bytes = J.px.stat_r2 ? np * 8 : 0; return J.px.stat_r2;
+        case SPPM_STATE_STATS_TAU: *bytes = J.px.stat_tau ? np * 24 : 0; return J.px.stat_tau;
+        default: *bytes = 0; return nullptr;
+    }
+}
+
+int Job::frame_info(sppm_frame_info* fi, cudaStream_t s) const {
+    JobState st;
+    SPPM_CK(cudaMemcpyAsync(&st, d_state, sizeof(st), cudaMemcpyDeviceToHost, s));
+    SPPM_CK(cudaStreamSynchronize(s));
+    memset(fi, 0, sizeof(*fi));
+    fi->frames = st.frames_started;
+    fi->eye_samples = st.eye_samples;
+    fi->photons_emitted = st.num_photons;
+    fi->num_photons_f32 = st.num_photons_f32;
+    fi->initial_radius = st.initial_radius;
+    fi->grid_scale = st.grid_scale;
+    for (int k = 0; k < 3; k++) {
+        fi->bbox_min[k] = st.bbmin[k];
+        fi->bbox_max[k] = st.bbmax[k];
+    }
+    fi->aa_offset[0] = st.aa[0];
+    fi->aa_offset[1] = st.aa[1];
+    fi->photon_segments = st.photon_segments;
+    fi->eye_segments = st.eye_segments;
+    fi->counted_segments = st.count_segments;
+    fi->counted_nodes = st.count_nodes;
+    fi->counted_triangles = st.count_tris;
+    fi->coop_segments = st.coop_segments;
+    return SPPM_OK;
+}
+
+LaunchSet Job::self_set(const JobDesc* table, uint32_t which) const {
+    LaunchSet ls;
+    ls.jobs = table;
+    ls.job_ids = d_self;
+    ls.prefix = d_self + 1 + 2 * which;
+    ls.njobs = 1;
+    ls.total = which == 0 ? npix : (which == 1 ? P : hash_num);
+    return ls;
+}
+
+// ================================================================================================
+// Runner
+// ================================================================================================
+void FrameGraph::drop() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    *this = FrameGraph{};
+}
+
+Runner::~Runner() {
+    cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    drop_graphs();
+    for (auto& p : pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (auto e : event_pool) cudaEventDestroy(e);
+    for (auto e : placeholder)
+        if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+int Runner::init(int dev, uint32_t prec, uint32_t fl, uint32_t interval, uint32_t jobs_max) {
+    device = dev;
+    precision = prec;
+    flags = fl;
+    eye_interval = interval ? interval : 1u;
+    max_jobs = jobs_max;
+    SPPM_CK(cudaSetDevice(device));
+    SPPM_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    int st = desc_mem.reserve(Arena::align(sizeof(JobDesc) * std::max<uint32_t>(max_jobs, 1)));
+    if (st) return st;
+    d_jobs = desc_mem.take<JobDesc>(std::max<uint32_t>(max_jobs, 1));
+    int sms = 0;
+    SPPM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    trace_blocks = (uint32_t)sms * (precision == SPPM_PRECISION_MIXED ? trace_photons4_blocks_per_sm()
+                                                                      : trace_photons_blocks_per_sm());
+    graphs.resize(eye_interval + 1);
+    dirty = true;
+    return SPPM_OK;
+}
+
+void Runner::drop_graphs() {
+    for (auto& g : graphs) g.drop();
+}
+
+bool Runner::phase_has_eye(uint32_t phase) const { return phase < eye_pix.size() && eye_pix[phase].njobs > 0; }
+
+int Runner::rebuild() {
+    SPPM_CK(cudaSetDevice(device));
+    SPPM_CK(cudaStreamSynchronize(stream));
+    drop_graphs();
+    const uint32_t n = (uint32_t)active.size(), L = eye_interval;
+    // launch tables: ids[n], prefix pixels/photons/hash [n+1] each, then per phase the ids and
+    // pixel prefix of the jobs that start an eye pass at that phase
+    std::vector<uint32_t> t;
+    t.reserve(4 * (size_t)n + 3 + (size_t)L * (2 * n + 1));
+    uint64_t tot[3] = {0, 0, 0};
+    for (Job* j : active) t.push_back(j->slot);
+    const size_t pre = t.size();
+    for (int w = 0; w < 3; w++) {
+        uint64_t acc = 0;
+        for (Job* j : active) {
+            t.push_back((uint32_t)acc);
+            acc += w == 0 ? j->npix : (w == 1 ? j->P : j->hash_num);
+        }
+        t.push_back((uint32_t)acc);
+        tot[w] = acc;
+    }
+    if (tot[0] > 0xFFFFFFFFull || tot[1] > (1ull << 31) || tot[2] > 0xFFFFFFFFull)
+        return fail(SPPM_ERR_OOM, "jobs exceed 2^32 pixels or hash slots or 2^31 photon slots in one launch");
+    std::vector<size_t> eye_off(L), eye_cnt(L);
+    for (uint32_t p = 0; p < L; p++) {
+        eye_off[p] = t.size();
+        std::vector<uint32_t> ids, pref;
+        uint64_t acc = 0;
+        for (Job* j : active) {
+            if ((j->start_frame % L) != (uint64_t)p) continue;
+            ids.push_back(j->slot);
+            pref.push_back((uint32_t)acc);
+            acc += j->npix;
+        }
+        pref.push_back((uint32_t)acc);
+        eye_cnt[p] = ids.size();
+        t.insert(t.end(), ids.begin(), ids.end());
+        t.insert(t.end(), pref.begin(), pref.end());
+    }
+    int st = table_mem.reserve(Arena::align(std::max<size_t>(t.size(), 1) * 4));
+    if (st) return st;
+    uint32_t* d_t = table_mem.take<uint32_t>(std::max<size_t>(t.size(), 1));
+    SPPM_CK(cudaMemcpy(d_t, t.data(), t.size() * 4, cudaMemcpyHostToDevice));
+    auto mk = [&](size_t ids, size_t prefix, uint32_t nj, uint64_t total) {
+        LaunchSet ls;
+        ls.jobs = d_jobs;
+        ls.job_ids = d_t + ids;
+        ls.prefix = d_t + prefix;
+        ls.njobs = nj;
+        ls.total = (uint32_t)total;
+        return ls;
+    };
+    pix = mk(0, pre, n, tot[0]);
+    pho = mk(0, pre + (n + 1), n, tot[1]);
+    hsh = mk(0, pre + 2 * (n + 1), n, tot[2]);
+    eye_pix.assign(L, LaunchSet{});
+    eye_ids.assign(L, nullptr);
+    for (uint32_t p = 0; p < L; p++) {
+        const uint32_t m = (uint32_t)eye_cnt[p];
+        uint64_t px = 0;
+        for (Job* j : active)
+            if ((j->start_frame % L) == (uint64_t)p) px += j->npix;
+        eye_pix[p] = mk(eye_off[p], eye_off[p] + m, m, px);
+        eye_ids[p] = d_t + eye_off[p];
+    }
+    // the ray queue: one entry per photon slot of every job
+    const uint32_t cap = (uint32_t)tot[1];
+    if (cap > queue.capacity || !queue.org) {
+        const bool binned = !(flags & SPPM_FLAG_UNBINNED_RAYS);
+        const size_t c = std::max<uint32_t>(cap, 1);
+        size_t bytes = 3 * Arena::align(c * 16) + Arena::align(64) + Arena::align(c * 4);
+        if (binned) bytes += Arena::align(c * 8) + Arena::align(c * 4) + Arena::align(kRayBins * 4);
+        if ((st = queue_mem.reserve(bytes))) return st;
+        Arena& a = queue_mem;
+        queue = RayQueue{};
+        queue.org = a.take<float4>(c);
+        queue.dir = a.take<float4>(c);
+        queue.hit = a.take<float4>(c);
+        queue.counters = a.take<uint32_t>(16);
+        queue.slow = a.take<uint32_t>(c);
+        if (binned) {
+            queue.key = a.take<uint2>(c);
+            queue.perm = a.take<uint32_t>(c);
+            queue.bins = a.take<uint32_t>(kRayBins);
+        }
+        queue.capacity = (uint32_t)c;
+        SPPM_CK(cudaMemset(queue.counters, 0, 64));
+    }
+    dirty = false;
+    return SPPM_OK;
+}
+
+cudaEvent_t Runner::get_event() {
+    if (!event_pool.empty()) {
+        cudaEvent_t e = event_pool.back();
+        event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// start or end of a timed stage: while a frame graph is being captured, an event record node
+// with a placeholder event; otherwise a pooled event recorded on the stream
+void Runner::timed(int stage, bool start) {
+    if (!((timing_mask >> stage) & 1u)) return;
+    if (capturing) {
+        cudaEventRecordWithFlags(placeholder[2 * stage + (start ? 0 : 1)], stream, cudaEventRecordExternal);
+        return;
+    }
+    if (start) {
+        StageEvent e{stage, get_event(), get_event()};
+        cudaEventRecord(e.a, stream);
+        pending.push_back(e);
+    } else {
+        cudaEventRecord(pending.back().b, stream);
+    }
+}
+
+// the launches of one frame (m_display, glslppm.cpp:214-536) for every active job
+int Runner::enqueue_frame(uint32_t phase) {
+    timed(SPPM_STAGE_FRAME_BEGIN, true);
+    launch_frame_begin(hsh, queue, stream);
+    timed(SPPM_STAGE_FRAME_BEGIN, false);
+    if (phase_has_eye(phase)) {
+        timed(SPPM_STAGE_EYE, true);
+        launch_eye_fp32(eye_pix[phase], stream);
+        timed(SPPM_STAGE_EYE, false);
+        timed(SPPM_STAGE_GRID, true);
+        launch_grid(d_jobs, eye_ids[phase], eye_pix[phase].njobs, stream);
+        timed(SPPM_STAGE_GRID, false);
+    }
+    const bool mixed = precision == SPPM_PRECISION_MIXED;
+    if ((flags & SPPM_FLAG_FUSED_PHOTON) && !mixed) {
+        timed(SPPM_STAGE_PHOTON, true);
+        launch_photon_fp32(pho, count_traversal, stream);
+        timed(SPPM_STAGE_PHOTON, false);
+    } else {
+        timed(SPPM_STAGE_PHOTON, true);
+        launch_photon_gen_fp32(pho, queue, stream);
+        timed(SPPM_STAGE_PHOTON, false);
+        if (queue.key) {
+            timed(SPPM_STAGE_RAY_BINS, true);
+            launch_ray_bins(queue, stream);
+            timed(SPPM_STAGE_RAY_BINS, false);
+        }
+        timed(SPPM_STAGE_PHOTON_TRACE, true);
+        if (mixed) launch_trace_photons4(pho, queue, trace_blocks, stream);
+        else launch_trace_photons_fp32(pho, queue, count_traversal, trace_blocks, stream);
+        timed(SPPM_STAGE_PHOTON_TRACE, false);
+        timed(SPPM_STAGE_PHOTON_STORE, true);
+        launch_photon_store_fp32(pho, queue, stream);
+        if (mixed) launch_slot_fill(pho, queue, stream);
+        timed(SPPM_STAGE_PHOTON_STORE, false);
+    }
+    timed(SPPM_STAGE_GATHER, true);
+    if (mixed) launch_gather_mixed(pix, stream);
+    else launch_gather_fp32(pix, stream);
+    timed(SPPM_STAGE_GATHER, false);
+    return launch_check("SPPM frame");
+}
+
+int Runner::build_graph(uint32_t phase, FrameGraph& g) {
+    g.drop();
+    for (auto& e : placeholder)
+        if (!e) SPPM_CK(cudaEventCreate(&e));
+    SPPM_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    capturing = true;
+    const int st = enqueue_frame(phase);
+    capturing = false;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(stream, &graph);
+    if (st || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return st ? st : fail(SPPM_ERR_CUDA, "frame graph capture failed: %s", cudaGetErrorString(e));
+    }
+    g.graph = graph;
+    g.mask = timing_mask;
+    g.counting = count_traversal;
+    size_t n = 0;
+    SPPM_CK(cudaGraphGetNodes(graph, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    SPPM_CK(cudaGraphGetNodes(graph, nodes.data(), &n));
+    for (cudaGraphNode_t node : nodes) {
+        cudaGraphNodeType type;
+        SPPM_CK(cudaGraphNodeGetType(node, &type));
+        if (type == cudaGraphNodeTypeKernel) g.kernels++;
+        if (type != cudaGraphNodeTypeEventRecord) continue;
+        cudaEvent_t ev = nullptr;
+        SPPM_CK(cudaGraphEventRecordNodeGetEvent(node, &ev));
+        for (int k = 0; k < SPPM_STAGE_COUNT; k++) {
+            if (ev == placeholder[2 * k]) g.ev_a[k] = node;
+            if (ev == placeholder[2 * k + 1]) g.ev_b[k] = node;
+        }
+    }
+    SPPM_CK(cudaGraphInstantiate(&g.exec, graph, 0));
+    return SPPM_OK;
+}
+
+int Runner::run(uint32_t n) {
+    SPPM_CK(cudaSetDevice(device));
+    int st;
+    if (dirty && (st = rebuild())) return st;
+    if (active.empty()) return SPPM_OK;
+    // the traversal-counting kernels run eagerly (they are a measurement pass)
+    const bool use_graphs = !(flags & SPPM_FLAG_EAGER_LAUNCH) && !count_traversal;
+    for (uint32_t k = 0; k < n; k++) {
+        const uint32_t phase = (uint32_t)(frames % eye_interval);
+        FrameGraph& g = graphs[phase_has_eye(phase) ? phase : eye_interval];
+        if (!g.exec || g.mask != timing_mask || g.counting != count_traversal) {
+            // captured, and launched only in graph mode; eager mode keeps it to count kernels
+            if ((st = build_graph(phase, g))) return st;
+        }
+        if (use_graphs) {
+            for (int s = 0; s < SPPM_STAGE_COUNT; s++) {
+                if (!g.ev_a[s] || !g.ev_b[s]) continue;
+                StageEvent se{s, get_event(), get_event()};
+                SPPM_CK(cudaGraphExecEventRecordNodeSetEvent(g.exec, g.ev_a[s], se.a));
+                SPPM_CK(cudaGraphExecEventRecordNodeSetEvent(g.exec, g.ev_b[s], se.b));
+                pending.push_back(se);
+            }
+            SPPM_CK(cudaGraphLaunch(g.exec, stream));
+        } else if ((st = enqueue_frame(phase))) {
+            return st;
+        }
+        kernel_launches += g.kernels;
+        frames++;
+    }
+    return SPPM_OK;
+}
+
+int Runner::synchronize() {
+    SPPM_CK(cudaSetDevice(device));
+    SPPM_CK(cudaStreamSynchronize(stream));
+    std::vector<uint32_t> errs(active.size(), 0);
+    for (size_t i = 0; i < active.size(); i++)
+        SPPM_CK(cudaMemcpyAsync(&errs[i], &active[i]->d_state->err, 4, cudaMemcpyDeviceToHost, stream));
+    SPPM_CK(cudaStreamSynchronize(stream));
+    for (size_t i = 0; i < active.size(); i++) {
+        if (errs[i] & kErrWatchdogTraverse)
+            return fail(SPPM_ERR_WATCHDOG, "job %u: BVH traversal exceeded its step bound (corrupt or cyclic links)",
+                        active[i]->slot);
+        if (errs[i] & kErrWatchdogLight)
+            return fail(SPPM_ERR_WATCHDOG, "job %u: light-table search exceeded its step bound", active[i]->slot);
+    }
+    return SPPM_OK;
+}
+
+int Runner::time(uint32_t n, float* ms) {
+    SPPM_CK(cudaSetDevice(device));
+    cudaEvent_t a = get_event(), b = get_event();
+    SPPM_CK(cudaEventRecord(a, stream));
+    int st = run(n);
+    if (st) return st;
+    SPPM_CK(cudaEventRecord(b, stream));
+    SPPM_CK(cudaEventSynchronize(b));
+    SPPM_CK(cudaEventElapsedTime(ms, a, b));
+    event_pool.push_back(a);
+    event_pool.push_back(b);
+    return synchronize();
+}
+
+int Runner::read_stage_times(float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]) {
+    SPPM_CK(cudaSetDevice(device));
+    SPPM_CK(cudaStreamSynchronize(stream));
+    for (auto& p : pending) {
+        float t = 0.0f;
+        SPPM_CK(cudaEventElapsedTime(&t, p.a, p.b));
+        stage_ms[p.stage] += t;
+        stage_launches[p.stage] += 1;
+        event_pool.push_back(p.a);
+        event_pool.push_back(p.b);
+    }
+    pending.clear();
+    for (int k = 0; k < SPPM_STAGE_COUNT; k++) {
+        ms[k] = stage_ms[k];
+        launches[k] = stage_launches[k];
+        stage_ms[k] = 0.0f;
+        stage_launches[k] = 0;
+    }
+    return SPPM_OK;
+}
+
+int Runner::resolve(Job& j, uint32_t kind) {
+    SPPM_CK(cudaSetDevice(device));
+    timed(SPPM_STAGE_RESOLVE, true);
+    if (precision == SPPM_PRECISION_MIXED) launch_resolve_mixed(j.self_set(d_jobs, 0), kind, stream);
+    else launch_resolve_fp32(j.self_set(d_jobs, 0), kind, stream);
+    timed(SPPM_STAGE_RESOLVE, false);
+    return launch_check("resolve");
+}
+
+}  // namespace sppm_rt

@@ -1,0 +1,162 @@
+// Host runtime of the SPPM path: render jobs in device memory and the runner that queues the
+// passes of a set of jobs.
+//
+// A Job owns one scene (traversal layout), camera, progressive state and hashed grid in two
+// device arenas.  A Runner owns a stream, a table of job descriptors, the launch tables (job ids
+// and prefix sums of each job's pixels, photon slots and hash slots), the shared wavefront ray
+// queue and the per-frame CUDA graphs: every stage of a frame is ONE launch over all of its jobs
+// (the kernels find an item's job by binary search in the prefix table).  The single-job context
+// of sppm.h is a Runner with one job; the batch of sppm_batch.h is a Runner with many.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../host/scene_internal.h"
+#include "device_common.cuh"
+#include "sppm.h"
+
+#define SPPM_CK(call)                                                                                  \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            return sppm::fail(SPPM_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),   \
+                              __FILE__, __LINE__);                                                     \
+    } while (0)
+
+namespace sppm_rt {
+
+using namespace sppm_dev;
+
+// bump allocator over one cudaMalloc
+struct Arena {
+    char* base = nullptr;
+    size_t size = 0, used = 0;
+    Arena() = default;
+    Arena(const Arena&) = delete;
+    Arena& operator=(const Arena&) = delete;
+    ~Arena() { release(); }
+    static size_t align(size_t n) { return (n + 255) & ~size_t(255); }
+    void release() {
+        if (base) cudaFree(base);
+        base = nullptr;
+        size = used = 0;
+    }
+    int reserve(size_t bytes);
+    template <class T>
+    T* take(size_t count) {
+        const size_t b = align(sizeof(T) * count);
+        if (used + b > size) return nullptr;
+        T* p = reinterpret_cast<T*>(base + used);
+        used += b;
+        return p;
+    }
+};
+
+int validate_config(const sppm_config* c);
+int launch_check(const char* what);
+
+// one render job (scene + camera + progressive state)
+struct Job {
+    sppm_config cfg{};
+    uint32_t W = 0, H = 0, PW = 0, PH = 0, P = 0, npix = 0, hash_num = 0;
+    Arena state_mem, scene_mem;
+    JobDesc desc{};                // host copy of the device descriptor
+    JobDesc* d_desc = nullptr;     // the descriptor's slot in the runner's table
+    JobState* d_state = nullptr;
+    uint32_t* d_self = nullptr;    // launch tables of this job alone: {slot, 0, npix, 0, P, 0, hash}
+    float* d_image = nullptr;
+    uint32_t slot = 0;
+    bool have_scene = false, have_camera = false;
+    float fixed_radius = 0.0f;
+    uint64_t start_frame = 0;      // runner frame at which the job's frame 0 is queued
+    uint64_t scene_bytes_used = 0;
+
+    // device bytes of the state arena for a configuration
+    static uint64_t state_bytes(const sppm_config& cfg);
+    // device bytes of the scene arena for a scene (mixed precision adds the 4-wide BVH, bounded
+    // by the binary node count)
+    static uint64_t scene_bytes(const sppm_scene& s, uint32_t precision);
+
+    int init(const sppm_config& cfg, JobDesc* d_desc, uint32_t slot, cudaStream_t s);
+    int upload_scene(const sppm_scene* scene, cudaStream_t s);
+    int set_camera(const sppm_camera* cam, cudaStream_t s);
+    int reset(cudaStream_t s);
+    int write_desc(cudaStream_t s);
+    void* state_ptr(uint32_t kind, size_t* bytes) const;
+    int frame_info(sppm_frame_info* fi, cudaStream_t s) const;
+    LaunchSet self_set(const JobDesc* table, uint32_t which) const;  // 0 pixels, 1 photons, 2 hash
+    uint64_t bytes() const { return state_mem.size + scene_mem.size; }
+};
+
+struct StageEvent {
+    int stage;
+    cudaEvent_t a, b;
+};
+
+// one frame's launches as an instantiated CUDA graph; stages being timed carry event record
+// nodes whose events are swapped for pooled ones before every replay
+struct FrameGraph {
+    cudaGraph_t graph = nullptr;  // kept: the event record nodes below belong to it
+    cudaGraphExec_t exec = nullptr;
+    uint32_t mask = 0;
+    uint32_t kernels = 0;   // kernel nodes (launches per replay)
+    bool counting = false;  // captured with the traversal-counting kernels
+    cudaGraphNode_t ev_a[SPPM_STAGE_COUNT] = {}, ev_b[SPPM_STAGE_COUNT] = {};
+    void drop();
+};
+
+// queues the frames of a set of jobs on one stream
+struct Runner {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t precision = SPPM_PRECISION_FP32, flags = 0, eye_interval = 10, max_jobs = 0;
+    Arena desc_mem;                // JobDesc[max_jobs]
+    JobDesc* d_jobs = nullptr;
+    Arena table_mem, queue_mem;    // rebuilt when the set of jobs changes
+    RayQueue queue{};
+    std::vector<Job*> active;      // launch order
+    LaunchSet pix{}, pho{}, hsh{};
+    std::vector<LaunchSet> eye_pix;          // per phase (frame mod eye_interval)
+    std::vector<const uint32_t*> eye_ids;    // per phase: the job ids of eye_pix
+    uint64_t frames = 0;                     // frames queued
+    uint64_t kernel_launches = 0;
+    uint32_t trace_blocks = 0;
+    bool dirty = true;
+    // stage timing
+    uint32_t timing_mask = 0;  // bit k: time stage k
+    bool count_traversal = false;
+    std::vector<StageEvent> pending;
+    std::vector<cudaEvent_t> event_pool;
+    float stage_ms[SPPM_STAGE_COUNT] = {0};
+    uint32_t stage_launches[SPPM_STAGE_COUNT] = {0};
+    // frame graphs: one per phase with eye jobs, and one for phases without
+    std::vector<FrameGraph> graphs;
+    bool capturing = false;
+    cudaEvent_t placeholder[2 * SPPM_STAGE_COUNT] = {};
+
+    Runner() = default;
+    Runner(const Runner&) = delete;
+    Runner& operator=(const Runner&) = delete;
+    ~Runner();
+    int init(int device, uint32_t precision, uint32_t flags, uint32_t eye_interval, uint32_t max_jobs);
+    void drop_graphs();
+    int rebuild();                 // launch tables and queue for `active`
+    int run(uint32_t n);           // queue n frames of every active job
+    int synchronize();             // waits and reports device-side watchdog errors of every job
+    int time(uint32_t n, float* ms);
+    int read_stage_times(float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]);
+    int resolve(Job& j, uint32_t kind);
+    cudaEvent_t get_event();
+    void timed(int stage, bool start);
+
+  private:
+    int enqueue_frame(uint32_t phase);
+    int build_graph(uint32_t phase, FrameGraph& g);
+    bool phase_has_eye(uint32_t phase) const;
+};
+
+}  // namespace sppm_rt

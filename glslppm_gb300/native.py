@@ -92,7 +92,18 @@ class FrameInfo(C.Structure):
     ]
 
 
-# every exported symbol of include/sppm.h with its ctypes signature
+class BatchConfig(C.Structure):
+    _fields_ = [("precision", C.c_uint32), ("flags", C.c_uint32), ("eye_pass_interval", C.c_uint32),
+                ("max_jobs", C.c_uint32), ("memory_budget", C.c_uint64)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("num_jobs", C.c_uint32), ("max_jobs", C.c_uint32), ("bytes_used", C.c_uint64),
+                ("memory_budget", C.c_uint64), ("frames", C.c_uint64), ("kernel_launches", C.c_uint64),
+                ("photon_slots", C.c_uint64), ("pixels", C.c_uint64)]
+
+
+# every exported symbol of include/sppm.h and include/sppm_batch.h with its ctypes signature
 P = C.c_void_p
 SIGNATURES = {
     "sppm_config_defaults": (None, [C.POINTER(Config), C.c_uint32]),
@@ -129,6 +140,27 @@ SIGNATURES = {
     "sppm_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
     "sppm_host_free": (None, [P]),
     "sppm_device_count": (C.c_int, []),
+    # include/sppm_batch.h
+    "sppm_batch_config_defaults": (None, [C.POINTER(BatchConfig)]),
+    "sppm_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.c_int, C.POINTER(P)]),
+    "sppm_batch_destroy": (None, [P]),
+    "sppm_batch_job_bytes": (C.c_int, [P, C.POINTER(Config), C.POINTER(Scene), C.POINTER(C.c_uint64)]),
+    "sppm_batch_add_job": (C.c_int, [P, C.POINTER(Config), C.POINTER(Scene), C.POINTER(Camera),
+                                     C.POINTER(C.c_uint32)]),
+    "sppm_batch_remove_job": (C.c_int, [P, C.c_uint32]),
+    "sppm_batch_reset_job": (C.c_int, [P, C.c_uint32]),
+    "sppm_batch_set_camera": (C.c_int, [P, C.c_uint32, C.POINTER(Camera)]),
+    "sppm_batch_run_passes": (C.c_int, [P, C.c_uint32]),
+    "sppm_batch_time_passes": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_float)]),
+    "sppm_batch_synchronize": (C.c_int, [P]),
+    "sppm_batch_read_image": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.c_size_t]),
+    "sppm_batch_state_bytes": (C.c_size_t, [P, C.c_uint32, C.c_uint32]),
+    "sppm_batch_read_state": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.c_size_t]),
+    "sppm_batch_get_frame_info": (C.c_int, [P, C.c_uint32, C.POINTER(FrameInfo)]),
+    "sppm_batch_get_info": (C.c_int, [P, C.POINTER(BatchInfo)]),
+    "sppm_batch_set_stage_timing_mask": (C.c_int, [P, C.c_uint32]),
+    "sppm_batch_read_stage_times": (C.c_int, [P, P, P]),
+    "sppm_batch_enable_traversal_counters": (C.c_int, [P, C.c_int]),
     "sppm_abi_version": (C.c_uint32, []),
 }
 

@@ -180,6 +180,21 @@ def scene_from_arrays(a: SceneArrays) -> N.Scene:
     return s
 
 
+def _state_array(kind: str, nbytes: int) -> np.ndarray:
+    """An empty host array of the element type and shape of a state kind."""
+    if kind in ("hit_triangle",):
+        return np.empty(nbytes // 4, dtype=np.int32)
+    if kind in ("slot_winner", "slot_count"):
+        return np.empty(nbytes // 4, dtype=np.uint32)
+    if kind == "photon_hit":
+        return np.empty((nbytes // 8, 2), dtype=np.int32)
+    if kind == "hit_t":
+        return np.empty(nbytes // 4, dtype=np.float32)
+    if kind.startswith("stats_"):
+        return np.empty(nbytes // 8, dtype=np.float64)
+    return np.empty((nbytes // 16, 4), dtype=np.float32)
+
+
 class Renderer:
     """One SPPM render job on one GPU (CGPURT + m_display)."""
 
@@ -231,18 +246,7 @@ class Renderer:
         nbytes = self.state_bytes(kind)
         if nbytes == 0:
             raise N.SppmError(N.ERR_ARG, f"state {kind} is not kept by this context")
-        if kind in ("hit_triangle",):
-            out = np.empty(nbytes // 4, dtype=np.int32)
-        elif kind in ("slot_winner", "slot_count"):
-            out = np.empty(nbytes // 4, dtype=np.uint32)
-        elif kind == "photon_hit":
-            out = np.empty((nbytes // 8, 2), dtype=np.int32)
-        elif kind == "hit_t":
-            out = np.empty(nbytes // 4, dtype=np.float32)
-        elif kind.startswith("stats_"):
-            out = np.empty(nbytes // 8, dtype=np.float64)
-        else:
-            out = np.empty((nbytes // 16, 4), dtype=np.float32)
+        out = _state_array(kind, nbytes)
         N.check(N.lib.sppm_read_state(self._h, k, out.ctypes.data, nbytes))
         return out
 

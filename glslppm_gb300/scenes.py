@@ -107,35 +107,39 @@ def _quad(p0, p1, p2, p3, n):
 
 
 def uv_sphere(center, radius, segments=64, rings=32):
-    """UV sphere with outward winding and smooth normals: 2*segments + 2*segments*(rings-2) triangles."""
+    """UV sphere with outward winding and smooth normals: 2*segments + 2*segments*(rings-2) triangles.
+
+    Triangle order, per segment j: the north cap (0,j)(1,j)(1,j+1), the south cap
+    (R,j)(R-1,j+1)(R-1,j), then rings 1..R-2 as two triangles each; a triangle whose winding
+    faces inwards is reversed (vertices and normals)."""
     c = np.asarray(center, dtype=np.float64)
-
-    def vert(i, j):
+    # unit directions of the (rings+1) x segments vertex grid (the trigonometry of Python's math)
+    d = np.empty((rings + 1, segments, 3), dtype=np.float64)
+    for i in range(rings + 1):
         th = math.pi * i / rings
-        ph = 2.0 * math.pi * (j % segments) / segments
-        d = np.array([math.sin(th) * math.cos(ph), math.cos(th), math.sin(th) * math.sin(ph)])
-        return c + radius * d, d
-
-    tris, nrms = [], []
-
-    def add(a, b, cc):
-        (pa, na), (pb, nb), (pc, nc) = a, b, cc
-        t = np.array([pa, pb, pc])
-        if np.dot(np.cross(pb - pa, pc - pa), (pa + pb + pc) / 3.0 - c) < 0:
-            t = t[::-1]
-            nn = np.array([nc, nb, na])
-        else:
-            nn = np.array([na, nb, nc])
-        tris.append(t)
-        nrms.append(nn)
-
-    for j in range(segments):
-        add(vert(0, j), vert(1, j), vert(1, j + 1))
-        add(vert(rings, j), vert(rings - 1, j + 1), vert(rings - 1, j))
+        st, ct = math.sin(th), math.cos(th)
+        for j in range(segments):
+            ph = 2.0 * math.pi * j / segments
+            d[i, j] = (st * math.cos(ph), ct, st * math.sin(ph))
+    p = c + radius * d
+    j = np.arange(segments)
+    j1 = (j + 1) % segments
+    idx = []  # per segment: caps, then the rings
+    for jj, jn in zip(j, j1):
+        idx.append(((0, jj), (1, jj), (1, jn)))
+        idx.append(((rings, jj), (rings - 1, jn), (rings - 1, jj)))
         for i in range(1, rings - 1):
-            add(vert(i, j), vert(i + 1, j), vert(i + 1, j + 1))
-            add(vert(i, j), vert(i + 1, j + 1), vert(i, j + 1))
-    return np.array(tris), np.array(nrms)
+            idx.append(((i, jj), (i + 1, jj), (i + 1, jn)))
+            idx.append(((i, jj), (i + 1, jn), (i, jn)))
+    idx = np.array(idx, dtype=np.int64)  # [n, 3, 2]
+    tris = p[idx[..., 0], idx[..., 1]]
+    nrms = d[idx[..., 0], idx[..., 1]]
+    cen = (tris[:, 0] + tris[:, 1] + tris[:, 2]) / 3.0
+    face = np.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0])
+    flip = np.einsum("ij,ij->i", face, cen - c) < 0
+    tris[flip] = tris[flip][:, ::-1]
+    nrms[flip] = nrms[flip][:, ::-1]
+    return tris, nrms
 
 
 def cornell_box(segments: int = 64, rings: int = 32) -> SceneSpec:
@@ -165,3 +169,79 @@ def cornell_box(segments: int = 64, rings: int = 32) -> SceneSpec:
     nrm = np.concatenate([p[1] for p in parts]).astype(np.float32)
     mid = np.concatenate([np.full(len(p[0]), p[2], dtype=np.int32) for p in parts])
     return SceneSpec(pos, nrm, mid, mats)
+
+
+@dataclass
+class JobSpec:
+    """One job of the batched workload: a scene and its image / photon sizes."""
+    scene: SceneSpec
+    width: int
+    height: int
+    photon_width: int
+    photon_height: int
+    seed: int
+
+
+def _box(lo, hi):
+    """axis-aligned box as 12 outward-facing triangles with flat normals"""
+    lo, hi = np.asarray(lo, dtype=np.float64), np.asarray(hi, dtype=np.float64)
+    P = lambda x, y, z: np.array([[lo, hi][x][0], [lo, hi][y][1], [lo, hi][z][2]])
+    faces = [((0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1), (0, -1, 0)),
+             ((0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1), (0, 1, 0)),
+             ((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, -1)),
+             ((0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1), (0, 0, 1)),
+             ((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1), (-1, 0, 0)),
+             ((1, 0, 0), (1, 1, 0), (1, 1, 1), (1, 0, 1), (1, 0, 0))]
+    tris, nrms = [], []
+    for a, b, c, d, n in faces:
+        t, nn = _quad(P(*a), P(*b), P(*c), P(*d), n)
+        tris.append(t)
+        nrms.append(nn)
+    return np.concatenate(tris), np.concatenate(nrms)
+
+
+def cornell_variant(seed: int, min_tris: int = 10_000, max_tris: int = 500_000) -> JobSpec:
+    """A procedurally generated Cornell box of the batched workload: the five walls and ceiling
+    light of cornell_box() plus 1-40 random spheres and boxes, with a triangle count drawn
+    log-uniformly from [min_tris, max_tris] (spread over the spheres' tessellation), an image of
+    128^2, 256^2, 512^2 or 1024^2 pixels and 2^14 .. 2^19 photon slots per pass (a 2^(e/2)
+    square, or 2^((e+1)/2) x 2^((e-1)/2) for odd e).  Materials: Lambertian albedo uniform in
+    [0.2, 0.8] (75 %), mirror (15 %), glass of index 1.5 (10 %)."""
+    rng = np.random.default_rng(0x5eed0000 + seed)
+    base = cornell_box(segments=8, rings=4)
+    keep = base.material_ids <= 3  # walls and light
+    pos, nrm, mid = [base.positions[keep]], [base.normals[keep]], [base.material_ids[keep]]
+    mats = list(base.materials[:4])
+    target = int(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris))))
+    n_obj = int(rng.integers(1, 41))
+    kinds = rng.random(n_obj) < 0.7  # True: sphere
+    if not kinds.any():
+        kinds[0] = True
+    n_sph = int(kinds.sum())
+    budget = max(target - 12 * (n_obj - n_sph) - 12, 64)
+    seg = max(8, int(math.sqrt(budget / n_sph)) // 2 * 2)
+    for k in range(n_obj):
+        u = rng.random()
+        if u < 0.75:
+            alb = tuple(float(x) for x in rng.uniform(0.2, 0.8, 3))
+            mats.append(MaterialSpec(f"m{k}", BRDF_MATTE, alb))
+        elif u < 0.9:
+            mats.append(MaterialSpec(f"m{k}", BRDF_MIRROR, (0.95, 0.95, 0.95)))
+        else:
+            mats.append(MaterialSpec(f"m{k}", 2, (0.98, 0.98, 0.98), eta=1.5))
+        m = len(mats) - 1
+        if kinds[k]:
+            r = float(rng.uniform(0.03, 0.15))
+            c = (rng.uniform(r, 1 - r), rng.uniform(r, 0.9 - r), rng.uniform(r, 1 - r))
+            t, n = uv_sphere(c, r, seg, seg // 2)
+        else:
+            h = rng.uniform(0.03, 0.15, 3)
+            c = np.array([rng.uniform(h[0], 1 - h[0]), rng.uniform(h[1], 0.9 - h[1]), rng.uniform(h[2], 1 - h[2])])
+            t, n = _box(c - h, c + h)
+        pos.append(t.astype(np.float32))
+        nrm.append(n.astype(np.float32))
+        mid.append(np.full(len(t), m, dtype=np.int32))
+    sc = SceneSpec(np.concatenate(pos), np.concatenate(nrm), np.concatenate(mid), mats)
+    res = int(rng.choice([128, 256, 512, 1024]))
+    e = int(rng.integers(14, 20))
+    return JobSpec(sc, res, res, 1 << ((e + 1) // 2), 1 << (e // 2), seed)

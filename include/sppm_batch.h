@@ -1,0 +1,79 @@
+/* Batched SPPM: many render jobs -- each with its own scene, camera, image size and photon
+ * budget -- advanced together, every stage of a pass being ONE launch over all jobs.
+ *
+ * No counterpart in the reference: glslppm renders one scene per process (CGPURT, gpurt.h:29-67,
+ * driven by m_display, glslppm.cpp:214-536).  A batch job follows exactly the single-job pass
+ * sequence of sppm.h; a job's state after n passes in a batch is the same as after n passes of
+ * a single-job context with the same configuration, scene and camera.
+ *
+ * Jobs are admitted against a device-memory budget (sppm_batch_job_bytes gives a job's
+ * footprint) and keep their scene, hit points and progressive state resident until removed.
+ * Passes are queued on the batch's stream as one CUDA graph per eye-pass phase.  All calls on
+ * one batch must come from one host thread at a time. */
+#ifndef SPPM_BATCH_H
+#define SPPM_BATCH_H
+
+#include "sppm.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sppm_batch sppm_batch;
+
+typedef struct sppm_batch_config {
+    uint32_t precision;         /* SPPM_PRECISION_* of every job                               */
+    uint32_t flags;             /* SPPM_FLAG_UNBINNED_RAYS, SPPM_FLAG_EAGER_LAUNCH,
+                                   SPPM_FLAG_FUSED_PHOTON (the job flags stay per job)         */
+    uint32_t eye_pass_interval; /* shared by every job (MaxNumberOfBounces)                    */
+    uint32_t max_jobs;          /* job slots (job ids are 0 .. max_jobs-1)                     */
+    uint64_t memory_budget;     /* device bytes jobs may hold; 0 = 90% of the free memory
+                                   when the batch is created                                   */
+} sppm_batch_config;
+
+typedef struct sppm_batch_info {
+    uint32_t num_jobs;          /* jobs resident                                               */
+    uint32_t max_jobs;
+    uint64_t bytes_used;        /* device bytes of the jobs, launch tables and ray queue       */
+    uint64_t memory_budget;
+    uint64_t frames;            /* passes queued since creation                                */
+    uint64_t kernel_launches;   /* kernels launched by sppm_batch_run_passes                   */
+    uint64_t photon_slots;      /* photon slots per pass over all jobs                         */
+    uint64_t pixels;            /* pixels over all jobs                                        */
+} sppm_batch_info;
+
+void sppm_batch_config_defaults(sppm_batch_config* cfg);
+int sppm_batch_create(const sppm_batch_config* cfg, int device, sppm_batch** out);
+void sppm_batch_destroy(sppm_batch* b);
+
+/* Device bytes a job with this configuration and scene holds in the batch (state + scene +
+   its share of the ray queue). */
+int sppm_batch_job_bytes(const sppm_batch* b, const sppm_config* cfg, const sppm_scene* scene, uint64_t* bytes);
+/* Uploads the scene and camera, seeds the job's state and admits it: SPPM_ERR_OOM when the
+   budget (or the device) has no room, SPPM_ERR_STATE when every slot is taken.  The job's first
+   pass is the batch's next pass. */
+int sppm_batch_add_job(sppm_batch* b, const sppm_config* cfg, const sppm_scene* scene, const sppm_camera* cam,
+                       uint32_t* job);
+int sppm_batch_remove_job(sppm_batch* b, uint32_t job);
+int sppm_batch_reset_job(sppm_batch* b, uint32_t job);
+int sppm_batch_set_camera(sppm_batch* b, uint32_t job, const sppm_camera* cam);
+
+/* Queues n passes of every resident job. */
+int sppm_batch_run_passes(sppm_batch* b, uint32_t n);
+int sppm_batch_time_passes(sppm_batch* b, uint32_t n, float* ms);
+int sppm_batch_synchronize(sppm_batch* b);
+
+int sppm_batch_read_image(sppm_batch* b, uint32_t job, uint32_t kind, float* rgb, size_t num_floats);
+size_t sppm_batch_state_bytes(const sppm_batch* b, uint32_t job, uint32_t kind);
+int sppm_batch_read_state(sppm_batch* b, uint32_t job, uint32_t kind, void* dst, size_t bytes);
+int sppm_batch_get_frame_info(sppm_batch* b, uint32_t job, sppm_frame_info* info);
+int sppm_batch_get_info(sppm_batch* b, sppm_batch_info* info);
+
+int sppm_batch_set_stage_timing_mask(sppm_batch* b, uint32_t mask);
+int sppm_batch_read_stage_times(sppm_batch* b, float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]);
+int sppm_batch_enable_traversal_counters(sppm_batch* b, int enable);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPPM_BATCH_H */

@@ -46,8 +46,10 @@ def test_struct_layouts_match_the_header(native_lib, tmp_path):
     import subprocess
     N = native_lib
     structs = {"sppm_config": N.Config, "sppm_material": N.Material, "sppm_scene": N.Scene,
-               "sppm_camera": N.Camera, "sppm_frame_info": N.FrameInfo}
-    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sppm.h"', "int main(void) {"]
+               "sppm_camera": N.Camera, "sppm_frame_info": N.FrameInfo, "sppm_batch_config": N.BatchConfig,
+               "sppm_batch_info": N.BatchInfo}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sppm.h"', '#include "sppm_batch.h"',
+             "int main(void) {"]
     for cname, cls in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
         for fname, _ in cls._fields_:

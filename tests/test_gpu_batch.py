@@ -1,0 +1,130 @@
+"""Batched SPPM: jobs advanced together by one launch per stage have, word for word, the state
+that single-job contexts with the same configuration, scene and camera reach -- whatever the
+other jobs in the batch, when a job joins, and after other jobs leave."""
+import numpy as np
+import pytest
+
+import glslppm_gb300 as g
+from glslppm_gb300 import native as N, scenes
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["hit_position", "hit_triangle", "emission_n", "flux_radius", "photon_position", "photon_flux",
+         "photon_rng", "photon_hit", "slot_winner", "slot_count"]
+
+
+def small_jobs():
+    """Three jobs of different scenes, image sizes and photon buffers (two random variants and the
+    Cornell box of the main workload)."""
+    out = []
+    for seed, (w, h, pw, ph) in zip((1, 2), ((24, 16, 32, 16), (32, 32, 16, 16))):
+        j = scenes.cornell_variant(seed, min_tris=800, max_tris=3000)
+        out.append((j.scene, w, h, pw, ph))
+    out.append((scenes.cornell_box(), 40, 24, 48, 20))
+    return out
+
+
+def config_for(w, h, pw, ph, precision=N.PRECISION_FP32, seed=0):
+    return g.default_config(w, height=h, photon_width=pw, photon_height=ph, radius_rule=N.RADIUS_DIAGONAL,
+                            radius_fraction=0.01, precision=precision, seed=seed)
+
+
+def camera_for(sc, w, h):
+    return g.look_at(sc.camera_origin, sc.camera_lookat, w, h, sc.fov)
+
+
+def single_states(spec, passes, precision=N.PRECISION_FP32, kinds=KINDS):
+    sc, w, h, pw, ph = spec
+    r = g.Renderer(config_for(w, h, pw, ph, precision))
+    r.upload_scene(sc.to_mesh())
+    r.set_camera(camera_for(sc, w, h))
+    r.run_passes(passes)
+    r.synchronize()
+    st = {k: r.read_state(k) for k in kinds}
+    st["image"] = r.read_image()
+    return st, r.frame_info()
+
+
+def assert_same(a, b, what):
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    assert a.shape == b.shape, what
+    assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), what
+
+
+@pytest.mark.parametrize("precision", [N.PRECISION_FP32, N.PRECISION_MIXED])
+def test_batch_equals_single_contexts(precision):
+    specs = small_jobs()
+    meshes = [s[0].to_mesh() for s in specs]
+    b = g.Batch(precision=precision, max_jobs=8)
+    ids = [b.add_job(config_for(w, h, pw, ph, precision), m, camera_for(sc, w, h))
+           for (sc, w, h, pw, ph), m in zip(specs, meshes)]
+    passes = 23  # three eye passes
+    b.run_passes(passes)
+    b.synchronize()
+    kinds = KINDS + (["stats_n", "stats_r2", "stats_tau"] if precision == N.PRECISION_MIXED else [])
+    for jid, spec in zip(ids, specs):
+        ref, fi_ref = single_states(spec, passes, precision, kinds)
+        for k in kinds:
+            assert_same(b.read_state(jid, k), ref[k], f"job {jid} {k}")
+        assert_same(b.read_image(jid), ref["image"], f"job {jid} image")
+        fi = b.frame_info(jid)
+        assert fi.frames == fi_ref.frames == passes
+        assert fi.photons_emitted == fi_ref.photons_emitted
+        assert fi.photon_segments == fi_ref.photon_segments
+    info = b.info()
+    assert info.num_jobs == 3 and info.frames == passes
+    assert info.photon_slots == sum(s[3] * s[4] for s in specs)
+    # one launch per stage: the batch launched as many kernels as one single-job context
+    assert info.kernel_launches == fi_ref.kernel_launches
+
+
+def test_jobs_joining_and_leaving_keep_their_own_schedule():
+    specs = small_jobs()
+    b = g.Batch(max_jobs=4)
+    (sa, wa, ha, pwa, pha), (sb, wb, hb, pwb, phb), (sc_, wc, hc, pwc, phc) = specs
+    a = b.add_job(config_for(wa, ha, pwa, pha), sa.to_mesh(), camera_for(sa, wa, ha))
+    c = b.add_job(config_for(wc, hc, pwc, phc), sc_.to_mesh(), camera_for(sc_, wc, hc))
+    b.run_passes(7)
+    j = b.add_job(config_for(wb, hb, pwb, phb), sb.to_mesh(), camera_for(sb, wb, hb))  # joins at batch frame 7
+    b.run_passes(6)
+    b.remove_job(c)  # leaves
+    b.run_passes(9)
+    b.synchronize()
+    ref_a, _ = single_states(specs[0], 22)
+    ref_j, _ = single_states(specs[1], 15)
+    for k in KINDS:
+        assert_same(b.read_state(a, k), ref_a[k], f"job a {k}")
+        assert_same(b.read_state(j, k), ref_j[k], f"joined job {k}")
+    assert b.frame_info(j).frames == 15 and b.frame_info(j).eye_samples == 2
+    with pytest.raises(N.SppmError):
+        b.read_state(c, "hit_position")
+    # the freed slot is reused
+    assert b.add_job(config_for(wc, hc, pwc, phc), sc_.to_mesh(), camera_for(sc_, wc, hc)) == c
+
+
+def test_admission_by_memory_budget():
+    sc, w, h, pw, ph = small_jobs()[2]
+    mesh = sc.to_mesh()
+    cfg = config_for(w, h, pw, ph)
+    probe = g.Batch(max_jobs=2)
+    need = probe.job_bytes(cfg, mesh)
+    probe.close()
+    b = g.Batch(max_jobs=8, memory_budget=int(need * 2.5))
+    b.add_job(cfg, mesh, camera_for(sc, w, h))
+    b.add_job(cfg, mesh, camera_for(sc, w, h))
+    with pytest.raises(N.SppmError) as e:
+        b.add_job(cfg, mesh, camera_for(sc, w, h))
+    assert e.value.status == N.ERR_OOM
+    info = b.info()
+    assert info.num_jobs == 2 and info.bytes_used <= info.memory_budget
+
+
+def test_batch_rejects_mismatched_jobs():
+    sc, w, h, pw, ph = small_jobs()[2]
+    b = g.Batch(precision=N.PRECISION_FP32, max_jobs=2)
+    with pytest.raises(N.SppmError):
+        b.add_job(config_for(w, h, pw, ph, precision=N.PRECISION_MIXED), sc.to_mesh(), camera_for(sc, w, h))
+    cfg = config_for(w, h, pw, ph)
+    cfg.eye_pass_interval = 5
+    with pytest.raises(N.SppmError):
+        b.add_job(cfg, sc.to_mesh(), camera_for(sc, w, h))

@@ -126,3 +126,20 @@ def test_drop_in_gpurt_header_with_reference_host_code(tmp_path):
     a, b = read_dump(out), run_ref_host_dump(REFERENCE / "cornell_metal.obj", 0.01)
     for k in FIELDS:
         assert np.array_equal(np.asarray(a[k]).view(np.uint8), np.asarray(b[k]).view(np.uint8)), k
+
+
+def test_cornell_variants_are_seeded_and_in_range():
+    from glslppm_gb300 import scenes
+    a, b = scenes.cornell_variant(7), scenes.cornell_variant(7)
+    assert np.array_equal(a.scene.positions, b.scene.positions) and a.width == b.width
+    sizes = set()
+    for s in range(12):
+        j = scenes.cornell_variant(s, min_tris=2_000, max_tris=20_000)
+        n = j.scene.num_triangles
+        assert 1_500 <= n <= 25_000, n
+        assert j.width == j.height and j.width in (128, 256, 512, 1024)
+        e = int(np.log2(j.photon_width * j.photon_height))
+        assert 14 <= e <= 19 and j.photon_width in (j.photon_height, 2 * j.photon_height)
+        assert j.scene.material_ids.max() < len(j.scene.materials)
+        sizes.add(j.width)
+    assert len(sizes) >= 3
