@@ -343,8 +343,167 @@ def run_gpu(args, rank, world, local):
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
         }
+    if not args.no_batched:
+        prec = N.PRECISION_MIXED if args.precision == "mixed" else N.PRECISION_FP32
+        res = run_batched(args, dev, args.batch_steps, W, prec)
+        if rank == 0:
+            out["batched"] = {k: v for k, v in res.items() if not k.startswith("_")}
+    if rank == 0:
         print(json.dumps(out), flush=True)
     return out
+
+
+BATCHED = {"workload": "cornell-variants-64", "jobs": 64, "triangles_per_job": "10k-500k (log-uniform)",
+           "objects_per_job": "1-40 spheres/boxes", "images": "128^2/256^2/512^2/1024^2",
+           "photons_per_pass_per_job": "2^14..2^19", "eye_pass_every": 10, "alpha": 0.7,
+           "radius": "0.5% of scene diagonal"}
+
+
+def build_jobs(n_jobs: int, seed0: int = 0):
+    """The batched workload's jobs: seeded Cornell variants, host BVH builds in parallel threads
+    (the native build releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    import glslppm_gb300 as g
+    from glslppm_gb300 import scenes
+    specs = [scenes.cornell_variant(seed0 + i) for i in range(n_jobs)]
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        meshes = list(ex.map(lambda s: s.scene.to_mesh(), specs))
+    jobs = []
+    for s, m in zip(specs, meshes):
+        cfg = g.default_config(s.width, height=s.height, photon_width=s.photon_width, photon_height=s.photon_height,
+                               radius_rule=1, radius_fraction=0.005, seed=s.seed)
+        cam = g.look_at(s.scene.camera_origin, s.scene.camera_lookat, s.width, s.height, s.scene.fov)
+        jobs.append((s, m, cfg, cam))
+    return jobs
+
+
+def run_batched(args, device: int, K: int, W: int, precision: int):
+    """The batched workload: 64 jobs advanced by one launch per stage (CUDA graph per pass),
+    against the plain single-job path looped over the same jobs."""
+    import glslppm_gb300 as g
+    from glslppm_gb300 import native as N
+    t_setup = time.perf_counter()
+    jobs = build_jobs(args.batch_jobs)
+    for (_, _, cfg, _) in jobs:
+        cfg.precision = precision
+    b = g.Batch(precision=precision, max_jobs=len(jobs), device=device)
+    ids = [b.add_job(cfg, m, cam) for (_, m, cfg, cam) in jobs]
+    setup_s = time.perf_counter() - t_setup
+    b.run_passes(W)
+    b.synchronize()
+    f0 = [b.frame_info(j) for j in ids]
+    info_k0 = b.info().kernel_launches
+    b.time_stages(["photon_trace"])
+    b.read_stage_times()
+    ms = b.time_passes(K)
+    tr = b.read_stage_times()["photon_trace"]
+    b.time_stages([])
+    f1 = [b.frame_info(j) for j in ids]
+    launches = b.info().kernel_launches - info_k0
+    photons = sum(y.photons_emitted - x.photons_emitted for x, y in zip(f0, f1))
+    segs = sum((y.photon_segments + y.eye_segments) - (x.photon_segments + x.eye_segments) for x, y in zip(f0, f1))
+    info = b.info()
+    batched = photons / (ms / 1000.0) / 1e6
+    # end to end: every step sets each job's camera (host->device), runs one pass and reads each
+    # job's progress counters back (device->host)
+    E = max(5, min(K, 30))
+    fe0 = [b.frame_info(j) for j in ids]
+    t0 = time.perf_counter()
+    for _ in range(E):
+        for j, (_, _, _, cam) in zip(ids, jobs):
+            b.set_camera(j, cam)
+        b.run_passes(1)
+        fe = [b.frame_info(j) for j in ids]
+    te = time.perf_counter() - t0
+    e2e = sum(y.photons_emitted - x.photons_emitted for x, y in zip(fe0, fe)) / te / 1e6
+    # per-stage breakdown over a further 10-pass cycle (every stage timed, outside the timed region)
+    b.time_stages(list(N.STAGES))
+    b.read_stage_times()
+    b.run_passes(10)
+    st = b.read_stage_times()
+    b.time_stages([])
+    cnt = b.traversal_counters(5) if precision == N.PRECISION_FP32 else None
+    b.close()
+    # the plain FP32 single-job path looped over the same jobs: each job's device time per pass,
+    # summed
+    loop_ms, loop_photons = 0.0, 0
+    for (s, m, cfg, cam) in jobs:
+        cfg.precision = N.PRECISION_FP32
+        r = g.Renderer(cfg, device=device)
+        r.upload_scene(m)
+        r.set_camera(cam)
+        r.run_passes(W)
+        r.synchronize()
+        a = r.frame_info()
+        k = max(10, K // 4)
+        t = r.time_passes(k)
+        z = r.frame_info()
+        loop_ms += t / k
+        loop_photons += (z.photons_emitted - a.photons_emitted) / k
+        r.close()
+    loop = loop_photons / (loop_ms / 1000.0) / 1e6
+    return {
+        "config": dict(BATCHED, precision="mixed" if precision == N.PRECISION_MIXED else "fp32",
+                       triangles_total=int(sum(s.scene.num_triangles for (s, _, _, _) in jobs)),
+                       photon_slots_per_pass=int(info.photon_slots), pixels=int(info.pixels),
+                       device_bytes=int(info.bytes_used)),
+        "value": round(batched, 3), "unit": "Mphotons/s", "mrays_per_s": round(segs / (ms / 1000.0) / 1e6, 3),
+        "steps": K, "warmup": W, "ms_per_step": round(ms / K, 4),
+        "photon_trace_ms_per_launch": round(tr[0] / max(tr[1], 1), 4),
+        "stage_ms_per_launch": {k: round(v[0] / v[1], 4) for k, v in st.items() if v[1]},
+        "traversal": ({"nodes_per_segment": round(cnt["nodes_per_segment"], 2),
+                       "tris_per_segment": round(cnt["tris_per_segment"], 2)} if cnt else None),
+        "plain_loop": {"value": round(loop, 3), "unit": "Mphotons/s", "ms_per_pass_all_jobs": round(loop_ms, 4),
+                       "note": "plain FP32 single-job contexts run one after another, device time per pass summed"},
+        "speedup_vs_plain_loop": round(batched / loop, 3),
+        "e2e": {"value": round(e2e, 3), "unit": "Mphotons/s", "h2d_bytes_per_step": 64 * len(ids),
+                "d2h_bytes_per_step": 128 * len(ids), "steps": E},
+        "setup_seconds": round(setup_s, 2),
+        "_launches": int(launches), "_trace": tr, "_counters": cnt, "_photons": photons, "_ms": ms,
+    }
+
+
+def run_batched_line(args, rank, world, local):
+    """--workload batched: the batched workload as the headline JSON line."""
+    from glslppm_gb300 import native as N
+    prec = N.PRECISION_MIXED if args.precision == "mixed" else N.PRECISION_FP32
+    clocks = ClockSampler(local).__enter__()
+    barrier(world)
+    t_wall = time.time()
+    res = run_batched(args, local, args.steps, args.warmup, prec)
+    clocks.mark(t_wall, time.time())
+    clocks.__exit__(None, None, None)
+    t = max_over_ranks(res["_ms"] / 1000.0, world)
+    photons = sum_over_ranks(res["_photons"], world)
+    value = photons / t / 1e6
+    peak, peak_kind = measured_peaks()
+    roof = None
+    cnt = res["_counters"]
+    tr_ms, tr_n = res["_trace"]
+    if cnt and tr_n:
+        seg_per_launch = cnt["photon_segments"] / cnt["passes"]
+        bpl = seg_per_launch * (64 + 32 * cnt["nodes_per_segment"] + 36 * cnt["tris_per_segment"])
+        achieved = bpl / (tr_ms / tr_n / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "kernel": "k_trace_photons",
+                "peak_kind": peak_kind, "nodes_per_segment": round(cnt["nodes_per_segment"], 2),
+                "tris_per_segment": round(cnt["tris_per_segment"], 2),
+                "algorithmic_bytes_per_launch": round(bpl)}
+    if rank == 0:
+        line = {
+            "metric": "SPPM Mphotons/s + Mrays/s at fixed RMSE vs FP64 oracle, plain vs batched",
+            "value": round(value, 3), "unit": "Mphotons/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000.0 * t / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(res["config"], l2="working set > 129 MB L2 (no flush)",
+                           parallelism=f"replicas x{world}"),
+            "mrays_per_s": res["mrays_per_s"], "plain_loop": res["plain_loop"],
+            "speedup_vs_plain_loop": res["speedup_vs_plain_loop"],
+            "photon_trace_ms_per_launch": res["photon_trace_ms_per_launch"],
+            "gpu_launches": res["_launches"], "e2e": res["e2e"], "roofline": roof, "cpu_baseline": None,
+            "clocks": clocks.summary(), "setup_seconds": res["setup_seconds"],
+        }
+        print(json.dumps(line), flush=True)
 
 
 def traversal_counters(r):
@@ -364,6 +523,12 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="cornell-1024", choices=["cornell-1024", "batched"],
+                    help="the JSON line's headline workload; the default line also carries the batched "
+                         "workload's summary under 'batched' unless --no-batched")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-jobs", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=100)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -373,6 +538,8 @@ def main():
         dist.init_process_group("gloo" if args.impl == "reference" else "gloo")
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "batched":
+        run_batched_line(args, rank, world, local)
     else:
         run_gpu(args, rank, world, local)
     if world > 1:

@@ -122,16 +122,25 @@ def uv_sphere(center, radius, segments=64, rings=32):
             ph = 2.0 * math.pi * j / segments
             d[i, j] = (st * math.cos(ph), ct, st * math.sin(ph))
     p = c + radius * d
-    j = np.arange(segments)
-    j1 = (j + 1) % segments
-    idx = []  # per segment: caps, then the rings
-    for jj, jn in zip(j, j1):
-        idx.append(((0, jj), (1, jj), (1, jn)))
-        idx.append(((rings, jj), (rings - 1, jn), (rings - 1, jj)))
-        for i in range(1, rings - 1):
-            idx.append(((i, jj), (i + 1, jj), (i + 1, jn)))
-            idx.append(((i, jj), (i + 1, jn), (i, jn)))
-    idx = np.array(idx, dtype=np.int64)  # [n, 3, 2]
+    # per segment: the two caps, then rings 1..R-2 as two triangles each; (ring, segment) pairs
+    nr = rings - 2
+    jj = np.arange(segments)[:, None]
+    jn = (jj + 1) % segments
+    i = np.arange(1, rings - 1)[None, :]
+    idx = np.empty((segments, 2 + 2 * nr, 3, 2), dtype=np.int64)
+    idx[:, 0] = np.stack([np.stack([np.zeros_like(jj[:, 0]), jj[:, 0]], -1),
+                          np.stack([np.ones_like(jj[:, 0]), jj[:, 0]], -1),
+                          np.stack([np.ones_like(jj[:, 0]), jn[:, 0]], -1)], 1)
+    idx[:, 1] = np.stack([np.stack([np.full_like(jj[:, 0], rings), jj[:, 0]], -1),
+                          np.stack([np.full_like(jj[:, 0], rings - 1), jn[:, 0]], -1),
+                          np.stack([np.full_like(jj[:, 0], rings - 1), jj[:, 0]], -1)], 1)
+    if nr > 0:
+        I, J, JN = np.broadcast_arrays(i, jj, jn)
+        a = np.stack([np.stack([I, J], -1), np.stack([I + 1, J], -1), np.stack([I + 1, JN], -1)], 2)
+        b = np.stack([np.stack([I, J], -1), np.stack([I + 1, JN], -1), np.stack([I, JN], -1)], 2)
+        idx[:, 2::2] = a
+        idx[:, 3::2] = b
+    idx = idx.reshape(-1, 3, 2)
     tris = p[idx[..., 0], idx[..., 1]]
     nrms = d[idx[..., 0], idx[..., 1]]
     cen = (tris[:, 0] + tris[:, 1] + tris[:, 2]) / 3.0
