@@ -7,7 +7,7 @@ ABI of ``include/sppm.h``); this package is its host-side mirror.  Importing the
 from .native import NativeLibraryMissing, SppmError, device_count  # noqa: F401
 from .renderer import Mesh, Renderer, default_config, look_at, pinned_empty, scene_from_arrays  # noqa: F401
 from . import native, scenes  # noqa: F401
-from .batch import Batch  # noqa: F401
+from .batch import Batch, Server  # noqa: F401
 
-__all__ = ["Batch", "Mesh", "Renderer", "default_config", "look_at", "pinned_empty", "scene_from_arrays", "SppmError",
+__all__ = ["Batch", "Server", "Mesh", "Renderer", "default_config", "look_at", "pinned_empty", "scene_from_arrays", "SppmError",
            "NativeLibraryMissing", "device_count", "native", "scenes"]

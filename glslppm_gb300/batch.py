@@ -134,3 +134,62 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Continuous-batching render server (include/sppm_server.h): submit requests from any thread;
+    a native thread admits them into a batch as slots and memory free up, runs passes of every
+    resident job and retires finished ones."""
+
+    def __init__(self, precision: int = N.PRECISION_FP32, flags: int = 0, eye_pass_interval: int = 10,
+                 max_jobs: int = 256, memory_budget: int = 0, passes_per_step: int = 1, max_queue: int = 4096,
+                 device: int = 0):
+        cfg = N.ServerConfig()
+        N.lib.sppm_server_config_defaults(C.byref(cfg))
+        cfg.batch.precision, cfg.batch.flags, cfg.batch.eye_pass_interval = precision, flags, eye_pass_interval
+        cfg.batch.max_jobs, cfg.batch.memory_budget = max_jobs, memory_budget
+        cfg.passes_per_step, cfg.max_queue = passes_per_step, max_queue
+        out = C.c_void_p()
+        N.check(N.lib.sppm_server_create(C.byref(cfg), device, C.byref(out)))
+        self._h = out
+        self._sizes: dict[int, tuple[int, int]] = {}
+
+    def submit(self, config: N.Config, scene, camera: N.Camera, target_passes: int) -> int:
+        t = C.c_uint64()
+        N.check(N.lib.sppm_server_submit(self._h, C.byref(config), C.byref(_scene(scene)), C.byref(camera),
+                                         target_passes, C.byref(t)))
+        self._sizes[t.value] = (config.width, config.height)
+        return int(t.value)
+
+    def poll(self, ticket: int) -> N.RequestInfo:
+        info = N.RequestInfo()
+        N.check(N.lib.sppm_server_poll(self._h, ticket, C.byref(info)))
+        return info
+
+    def wait(self, ticket: int, timeout: float = 60.0) -> N.RequestInfo:
+        info = N.RequestInfo()
+        N.check(N.lib.sppm_server_wait(self._h, ticket, timeout, C.byref(info)))
+        return info
+
+    def fetch_image(self, ticket: int) -> np.ndarray:
+        w, h = self._sizes[ticket]
+        out = np.empty((h, w, 3), dtype=np.float32)
+        N.check(N.lib.sppm_server_fetch_image(self._h, ticket, out.ctypes.data, w * h * 3))
+        del self._sizes[ticket]
+        return out
+
+    def stats(self) -> N.ServerStats:
+        s = N.ServerStats()
+        N.check(N.lib.sppm_server_get_stats(self._h, C.byref(s)))
+        return s
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            N.lib.sppm_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

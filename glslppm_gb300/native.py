@@ -103,7 +103,28 @@ class BatchInfo(C.Structure):
                 ("photon_slots", C.c_uint64), ("pixels", C.c_uint64)]
 
 
-# every exported symbol of include/sppm.h and include/sppm_batch.h with its ctypes signature
+class ServerConfig(C.Structure):
+    _fields_ = [("batch", BatchConfig), ("passes_per_step", C.c_uint32), ("max_queue", C.c_uint32)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("status", C.c_int32), ("passes_done", C.c_uint32),
+                ("target_passes", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("photons_emitted", C.c_uint64), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
+                ("failed", C.c_uint64), ("resident", C.c_uint32), ("queued", C.c_uint32),
+                ("bytes_used", C.c_uint64), ("memory_budget", C.c_uint64), ("passes", C.c_uint64),
+                ("photons", C.c_uint64), ("busy_seconds", C.c_double)]
+
+
+REQUEST_QUEUED, REQUEST_RUNNING, REQUEST_DONE, REQUEST_FAILED = 0, 1, 2, 3
+
+
+# every exported symbol of include/sppm.h, sppm_batch.h and sppm_server.h with its ctypes signature
 P = C.c_void_p
 SIGNATURES = {
     "sppm_config_defaults": (None, [C.POINTER(Config), C.c_uint32]),
@@ -161,6 +182,16 @@ SIGNATURES = {
     "sppm_batch_set_stage_timing_mask": (C.c_int, [P, C.c_uint32]),
     "sppm_batch_read_stage_times": (C.c_int, [P, P, P]),
     "sppm_batch_enable_traversal_counters": (C.c_int, [P, C.c_int]),
+    # include/sppm_server.h
+    "sppm_server_config_defaults": (None, [C.POINTER(ServerConfig)]),
+    "sppm_server_create": (C.c_int, [C.POINTER(ServerConfig), C.c_int, C.POINTER(P)]),
+    "sppm_server_destroy": (None, [P]),
+    "sppm_server_submit": (C.c_int, [P, C.POINTER(Config), C.POINTER(Scene), C.POINTER(Camera), C.c_uint32,
+                                     C.POINTER(C.c_uint64)]),
+    "sppm_server_poll": (C.c_int, [P, C.c_uint64, C.POINTER(RequestInfo)]),
+    "sppm_server_wait": (C.c_int, [P, C.c_uint64, C.c_double, C.POINTER(RequestInfo)]),
+    "sppm_server_fetch_image": (C.c_int, [P, C.c_uint64, P, C.c_size_t]),
+    "sppm_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
     "sppm_abi_version": (C.c_uint32, []),
 }
 
