@@ -463,6 +463,96 @@ def run_batched(args, device: int, K: int, W: int, precision: int):
     }
 
 
+SERVING = {"workload": "serving-poisson", "scene_pool": "seeded Cornell variants as in the batched workload",
+           "camera": "random origin within 0.15 of the default, looking at the box centre",
+           "target": "passes to 2% relative RMSE against the FP64 oracle (calibrated rule)",
+           "memory_budget_gb": 180, "eye_pass_every": 10}
+
+
+def target_passes(photons_per_pass: int) -> int:
+    """Passes for a job to reach the serving target (2% relative RMSE against the FP64 oracle):
+    the rule fitted by tests/golden/make_rmse_calibration.py (passes = a * P^-b, P photons per
+    pass), read from its committed result."""
+    p = REPO / "tests" / "golden" / "rmse_calibration.json"
+    d = json.loads(p.read_text())
+    a, b = d["fit_2pct"]["a"], d["fit_2pct"]["b"]
+    return int(max(1, math.ceil(a * photons_per_pass ** (-b))))
+
+
+def run_serving(args, device: int):
+    """Poisson arrivals of render requests into the continuous-batching server; per arrival rate,
+    p50/p99 time to target and aggregate Mphotons/s."""
+    import glslppm_gb300 as g
+    from glslppm_gb300 import native as N
+    rng = np.random.default_rng(12345)
+    pool = build_jobs(args.serve_pool)
+    prec = N.PRECISION_MIXED if args.precision == "mixed" else N.PRECISION_FP32
+    rates = [float(x) for x in args.serve_rates.split(",")]
+    out = []
+    for lam in rates:
+        srv = g.Server(precision=prec, max_jobs=256, memory_budget=180 << 30, passes_per_step=1, device=device)
+        n = args.serve_requests
+        gaps = rng.exponential(1.0 / lam, n)
+        reqs = []
+        for i in range(n):
+            s, m, cfg0, _ = pool[int(rng.integers(len(pool)))]
+            cfg = g.default_config(cfg0.width, height=cfg0.height, photon_width=cfg0.photon_width,
+                                   photon_height=cfg0.photon_height, radius_rule=1, radius_fraction=0.005,
+                                   seed=int(rng.integers(1, 1 << 30)), precision=prec)
+            o = np.array(s.scene.camera_origin) + rng.uniform(-0.15, 0.15, 3)
+            cam = g.look_at(tuple(o), (0.5, 0.5, 0.5), cfg.width, cfg.height, s.scene.fov)
+            reqs.append((cfg, m, cam, target_passes(cfg.photon_width * cfg.photon_height)))
+        t0 = time.perf_counter()
+        tickets = []
+        due = 0.0
+        for (cfg, m, cam, tp), gap in zip(reqs, gaps):
+            due += gap
+            d = due - (time.perf_counter() - t0)
+            if d > 0:
+                time.sleep(d)
+            tickets.append(srv.submit(cfg, m, cam, tp))
+        infos = [srv.wait(t, timeout=3600) for t in tickets]
+        st = srv.stats()
+        srv.close()
+        ok = [i for i in infos if i.state == N.REQUEST_DONE]
+        ttt = np.array([i.t_done - i.t_submit for i in ok])
+        span = max(i.t_done for i in ok) - min(i.t_submit for i in infos)
+        out.append({"rate_per_s": lam, "requests": n, "completed": len(ok),
+                    "p50_time_to_target_s": round(float(np.percentile(ttt, 50)), 4),
+                    "p99_time_to_target_s": round(float(np.percentile(ttt, 99)), 4),
+                    "mean_queue_wait_s": round(float(np.mean([i.t_admit - i.t_submit for i in ok])), 4),
+                    "mphotons_per_s": round(sum(i.photons_emitted for i in ok) / span / 1e6, 3),
+                    "busy_fraction": round(st.busy_seconds / span, 3),
+                    "mean_target_passes": round(float(np.mean([r[3] for r in reqs])), 1)})
+    return out
+
+
+def run_serving_line(args, rank, world, local):
+    """--workload serving: the serving sweep; value = aggregate Mphotons/s at the highest rate."""
+    clocks = ClockSampler(local).__enter__()
+    t_wall = time.time()
+    rows = run_serving(args, local)
+    clocks.mark(t_wall, time.time())
+    clocks.__exit__(None, None, None)
+    top = rows[-1]
+    value = sum_over_ranks(top["mphotons_per_s"], world)
+    if rank == 0:
+        line = {
+            "metric": "SPPM Mphotons/s + Mrays/s at fixed RMSE vs FP64 oracle, plain vs batched",
+            "value": round(value, 3), "unit": "Mphotons/s", "n_gpus": world, "steps": top["requests"],
+            "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(SERVING, precision=args.precision, rates=args.serve_rates,
+                           requests_per_rate=args.serve_requests, parallelism=f"replicas x{world}"),
+            "serving": rows,
+            "e2e": {"value": round(value, 3), "unit": "Mphotons/s", "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": None,
+                    "note": "requests submitted and images fetched through the server API; a step is a request"},
+            "roofline": None, "cpu_baseline": None, "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
 def run_batched_line(args, rank, world, local):
     """--workload batched: the batched workload as the headline JSON line."""
     from glslppm_gb300 import native as N
@@ -500,6 +590,7 @@ def run_batched_line(args, rank, world, local):
             "mrays_per_s": res["mrays_per_s"], "plain_loop": res["plain_loop"],
             "speedup_vs_plain_loop": res["speedup_vs_plain_loop"],
             "photon_trace_ms_per_launch": res["photon_trace_ms_per_launch"],
+            "stage_ms_per_launch": res["stage_ms_per_launch"], "traversal": res["traversal"],
             "gpu_launches": res["_launches"], "e2e": res["e2e"], "roofline": roof, "cpu_baseline": None,
             "clocks": clocks.summary(), "setup_seconds": res["setup_seconds"],
         }
@@ -523,12 +614,15 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="cornell-1024", choices=["cornell-1024", "batched"],
+    ap.add_argument("--workload", default="cornell-1024", choices=["cornell-1024", "batched", "serving"],
                     help="the JSON line's headline workload; the default line also carries the batched "
                          "workload's summary under 'batched' unless --no-batched")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--serve-rates", default="1,10,50,200")
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-pool", type=int, default=32)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -540,6 +634,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "batched":
         run_batched_line(args, rank, world, local)
+    elif args.workload == "serving":
+        run_serving_line(args, rank, world, local)
     else:
         run_gpu(args, rank, world, local)
     if world > 1:

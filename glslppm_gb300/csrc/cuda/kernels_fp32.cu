@@ -16,6 +16,7 @@
 //   k_resolve       re.fs (on demand)
 #include <cstdint>
 
+#include "bvh4_trace.cuh"
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -402,6 +403,20 @@ __device__ __forceinline__ void warp_bbox_atomics(JobState* st, f3 p, int job_k)
     }
 }
 
+// eye rays of the mixed path walk the 4-wide quantised BVH (the material comes from the triangle)
+__device__ __forceinline__ Hit trace_eye4(const DevScene& s, f3 org, f3 dir, bool cull, uint32_t& err) {
+    const Hit4 h4 = trace4<false>(s.nodes4, s.tri_isect, org, dir, cull, 1.0e20f, err);
+    Hit h;
+    h.t = h4.t;
+    h.tri = h4.tri;
+    h.mat = h4.tri >= 0 ? __float_as_int(__ldg(&s.tri_isect[(size_t)h4.tri * 3 + 2]).y) : -1;
+    h.bu = h4.bu;
+    h.bv = h4.bv;
+    h.bw = h4.bw;
+    return h;
+}
+
+template <bool MIXED>
 __global__ void __launch_bounds__(128) k_eye(LaunchSet ls) {
     const uint32_t g = grid_tid();
     if (g >= ls.total) return;
@@ -439,7 +454,7 @@ __global__ void __launch_bounds__(128) k_eye(LaunchSet ls) {
     last.t = 1.0e20f;
     uint32_t segs = 0;
     for (uint32_t j = 0; j < J.max_path; j++) {
-        const Hit h = trace_exact<false>(S, rorg, rdir, j == 0, err);
+        const Hit h = MIXED ? trace_eye4(S, rorg, rdir, j == 0, err) : trace_exact<false>(S, rorg, rdir, j == 0, err);
         last = h;
         segs++;
         if (h.tri < 0) {
@@ -1305,8 +1320,10 @@ void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) 
     const uint32_t n = q.bins && ls.total < kRayBins ? kRayBins : ls.total;
     if (ls.total) k_frame_begin<<<blocks_for(n, 256), 256, 0, s>>>(ls, q);
 }
-void launch_eye_fp32(const LaunchSet& ls, cudaStream_t s) {
-    if (ls.total) k_eye<<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
+void launch_eye(const LaunchSet& ls, bool mixed, cudaStream_t s) {
+    if (!ls.total) return;
+    if (mixed) k_eye<true><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
+    else k_eye<false><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
 }
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s) {
     if (njobs) k_grid<<<blocks_for(njobs, 64), 64, 0, s>>>(jobs, job_ids, njobs);

@@ -681,7 +681,7 @@ int Runner::enqueue_frame(uint32_t phase) {
     timed(SPPM_STAGE_FRAME_BEGIN, false);
     if (phase_has_eye(phase)) {
         timed(SPPM_STAGE_EYE, true);
-        launch_eye_fp32(eye_pix[phase], stream);
+        launch_eye(eye_pix[phase], precision == SPPM_PRECISION_MIXED, stream);
         timed(SPPM_STAGE_EYE, false);
         timed(SPPM_STAGE_GRID, true);
         launch_grid(d_jobs, eye_ids[phase], eye_pix[phase].njobs, stream);

@@ -19,8 +19,8 @@ def render(cfg, mesh, cam, passes):
 
 
 def test_mixed_photon_hits_equal_fp32_on_the_same_rays(cornell_c1_mesh):
-    """One frame from the same seeds: identical eye pass and photon rays; the quantised-box FMA
-    traversal must report the same triangle as the exact traversal for (almost) every segment."""
+    """One frame from the same seeds: the same eye and photon rays; the quantised-box FMA traversal
+    must report the same triangle as the exact traversal for (almost) every segment."""
     sc, mesh = cornell_c1_mesh
     cam = g.look_at(sc.camera_origin, sc.camera_lookat, 64, 64, sc.fov)
     base = dict(photon_width=256, photon_height=256, radius_rule=N.RADIUS_DIAGONAL, radius_fraction=0.005)
@@ -33,8 +33,10 @@ def test_mixed_photon_hits_equal_fp32_on_the_same_rays(cornell_c1_mesh):
     both = same & (h32[:, 0] >= 0)
     rel = np.abs(p32[both, :3] - pmx[both, :3]).max() / np.abs(p32[both, :3]).max()
     assert rel < 1e-5, rel
-    # eye pass is the same kernel: hit points identical
-    assert np.array_equal(r32.read_state("hit_triangle"), rmx.read_state("hit_triangle"))
+    # the eye pass of the mixed path walks the 4-wide BVH too: the same visible triangle for
+    # (almost) every pixel
+    e32, emx = r32.read_state("hit_triangle"), rmx.read_state("hit_triangle")
+    assert (e32 == emx).mean() > 0.999, f"{(e32 != emx).sum()} of {len(e32)} eye hits differ"
 
 
 def test_mixed_image_error_vs_fp64_oracle_matches_fp32(cornell_c1_mesh):
