@@ -465,18 +465,9 @@ def run_batched(args, device: int, K: int, W: int, precision: int):
 
 SERVING = {"workload": "serving-poisson", "scene_pool": "seeded Cornell variants as in the batched workload",
            "camera": "random origin within 0.15 of the default, looking at the box centre",
-           "target": "passes to 2% relative RMSE against the FP64 oracle (calibrated rule)",
+           "target": "a fixed pass count per request (--serve-passes); the relative RMSE against the FP64 "
+                     "oracle that a pass count reaches is measured in tests/golden/rmse_calibration.json",
            "memory_budget_gb": 180, "eye_pass_every": 10}
-
-
-def target_passes(photons_per_pass: int) -> int:
-    """Passes for a job to reach the serving target (2% relative RMSE against the FP64 oracle):
-    the rule fitted by tests/golden/make_rmse_calibration.py (passes = a * P^-b, P photons per
-    pass), read from its committed result."""
-    p = REPO / "tests" / "golden" / "rmse_calibration.json"
-    d = json.loads(p.read_text())
-    a, b = d["fit_2pct"]["a"], d["fit_2pct"]["b"]
-    return int(max(1, math.ceil(a * photons_per_pass ** (-b))))
 
 
 def run_serving(args, device: int):
@@ -501,7 +492,7 @@ def run_serving(args, device: int):
                                    seed=int(rng.integers(1, 1 << 30)), precision=prec)
             o = np.array(s.scene.camera_origin) + rng.uniform(-0.15, 0.15, 3)
             cam = g.look_at(tuple(o), (0.5, 0.5, 0.5), cfg.width, cfg.height, s.scene.fov)
-            reqs.append((cfg, m, cam, target_passes(cfg.photon_width * cfg.photon_height)))
+            reqs.append((cfg, m, cam, args.serve_passes))
         t0 = time.perf_counter()
         tickets = []
         due = 0.0
@@ -543,7 +534,8 @@ def run_serving_line(args, rank, world, local):
             "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(SERVING, precision=args.precision, rates=args.serve_rates,
-                           requests_per_rate=args.serve_requests, parallelism=f"replicas x{world}"),
+                           requests_per_rate=args.serve_requests, passes_per_request=args.serve_passes,
+                           parallelism=f"replicas x{world}"),
             "serving": rows,
             "e2e": {"value": round(value, 3), "unit": "Mphotons/s", "h2d_bytes_per_step": None,
                     "d2h_bytes_per_step": None,
@@ -623,6 +615,7 @@ def main():
     ap.add_argument("--serve-rates", default="1,10,50,200")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-pool", type=int, default=32)
+    ap.add_argument("--serve-passes", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
