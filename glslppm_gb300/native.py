@@ -133,6 +133,7 @@ SIGNATURES = {
     "sppm_mesh_load_obj": (C.c_int, [C.c_char_p, C.POINTER(C.c_float), C.c_float, C.POINTER(P)]),
     "sppm_mesh_from_arrays": (C.c_int, [C.c_uint32, P, P, P, C.c_uint32, P, C.POINTER(P)]),
     "sppm_mesh_build_bvh": (C.c_int, [P]),
+    "sppm_mesh_build_bvh_gpu": (C.c_int, [P, C.c_int]),
     "sppm_mesh_get_scene": (C.c_int, [P, C.POINTER(Scene)]),
     "sppm_mesh_destroy": (None, [P]),
     "sppm_create": (C.c_int, [C.POINTER(Config), C.c_int, C.POINTER(P)]),

@@ -89,8 +89,14 @@ class Mesh:
                                             mid.ctypes.data, len(mats), mats.ctypes.data, C.byref(out)))
         return cls(out.value)
 
-    def build_bvh(self) -> "Mesh":
-        N.check(N.lib.sppm_mesh_build_bvh(self._h))
+    def build_bvh(self, gpu: bool = False, device: int = 0) -> "Mesh":
+        """TBVH::Build on the host (the reference's exact-SAH tree), or with gpu=True the same
+        arrays from a linear BVH built on the GPU (a different tree, milliseconds per million
+        triangles)."""
+        if gpu:
+            N.check(N.lib.sppm_mesh_build_bvh_gpu(self._h, device))
+        else:
+            N.check(N.lib.sppm_mesh_build_bvh(self._h))
         return self
 
     def scene(self) -> N.Scene:

@@ -160,6 +160,12 @@ int sppm_mesh_from_arrays(uint32_t num_triangles, const float* positions, const 
 /* TBVH::Build (bvh.cpp:244-317): exact-SAH binary BVH, one triangle per leaf, 6 threaded
    orderings.  Stores the node arrays in the mesh. */
 int sppm_mesh_build_bvh(sppm_mesh* mesh);
+/* The same BVH arrays (node boxes and triangles, six threaded orderings with the reference's
+   child-order rules) from a linear BVH built on the GPU: Morton-ordered triangles and a radix
+   tree instead of the exact-SAH splits, so the tree differs from sppm_mesh_build_bvh's (rays
+   find the same closest triangle except at exact ties) and is built in milliseconds for
+   multi-million-triangle meshes.  No counterpart in the reference (bvh.cpp builds on the host). */
+int sppm_mesh_build_bvh_gpu(sppm_mesh* mesh, int device);
 /* Fills *scene with pointers into the mesh (valid until sppm_mesh_destroy). */
 int sppm_mesh_get_scene(const sppm_mesh* mesh, sppm_scene* scene);
 void sppm_mesh_destroy(sppm_mesh* mesh);
