@@ -518,6 +518,112 @@ def run_serving(args, device: int):
     return out
 
 
+LARGE = {"workload": "large-mesh", "triangles": "4.1M (displaced geodesic sphere 2.01M + heightfield 2.09M)",
+         "image": "1920x1080", "photons_per_pass": 2 ** 21, "passes_in_config": 200, "materials": 4005,
+         "lights": "4 quads, emission 5-20", "radius": "0.5% of scene diagonal", "eye_pass_every": 10,
+         "bvh": "linear BVH built on the GPU"}
+
+
+def run_large_line(args, rank, world, local):
+    """--workload large: the large-mesh scene at 1920x1080 with 2^21 photons per pass."""
+    import glslppm_gb300 as g
+    from glslppm_gb300 import native as N, scenes
+    prec = N.PRECISION_MIXED if args.precision == "mixed" else N.PRECISION_FP32
+    t0 = time.perf_counter()
+    sc = scenes.large_mesh(1)
+    t_gen = time.perf_counter() - t0
+    mesh = g.Mesh.from_arrays(sc.positions, sc.material_ids, sc.material_array(), sc.normals)
+    t1 = time.perf_counter()
+    mesh.build_bvh(gpu=True, device=local)
+    t_bvh = time.perf_counter() - t1
+    cfg = g.default_config(1920, height=1080, photon_width=2048, photon_height=1024, radius_rule=1,
+                           radius_fraction=0.005, precision=prec)
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 1920, 1080, sc.fov)
+    r = g.Renderer(cfg, device=local)
+    t2 = time.perf_counter()
+    r.upload_scene(mesh)
+    t_up = time.perf_counter() - t2
+    r.set_camera(cam)
+    K, W = args.steps, args.warmup
+    clocks = ClockSampler(local).__enter__()
+    r.run_passes(W)
+    fi0 = r.frame_info()
+    align = (10 - fi0.frames % 10) % 10
+    if align:
+        r.run_passes(align)
+    r.synchronize()
+    fi0 = r.frame_info()
+    r.time_stages(["photon_trace"])
+    r.read_stage_times()
+    barrier(world)
+    t_wall = time.time()
+    ms = r.time_passes(K)
+    clocks.mark(t_wall, time.time())
+    clocks.__exit__(None, None, None)
+    tr_ms, tr_n = r.read_stage_times()["photon_trace"]
+    r.time_stages([])
+    fi1 = r.frame_info()
+    launches = fi1.kernel_launches - fi0.kernel_launches
+    t = max_over_ranks(ms / 1000.0, world)
+    photons = sum_over_ranks(fi1.photons_emitted - fi0.photons_emitted, world)
+    segs = sum_over_ranks((fi1.photon_segments + fi1.eye_segments) - (fi0.photon_segments + fi0.eye_segments), world)
+    value = photons / t / 1e6
+    r.enable_stage_timing(True)
+    r.read_stage_times()
+    r.run_passes(10)
+    stages = r.read_stage_times()
+    r.enable_stage_timing(False)
+    # end to end: camera up, one pass, radiance image down (pinned host buffer)
+    image = g.pinned_empty((cfg.height, cfg.width, 3), np.float32)
+    E = max(5, min(K, 20))
+    fe0 = r.frame_info()
+    te0 = time.perf_counter()
+    for _ in range(E):
+        r.set_camera(cam)
+        r.run_passes(1)
+        r.read_image(N.IMAGE_RADIANCE, out=image)
+    te = max_over_ranks(time.perf_counter() - te0, world)
+    fe1 = r.frame_info()
+    e2e = sum_over_ranks(fe1.photons_emitted - fe0.photons_emitted, world) / te / 1e6
+    peak, peak_kind = measured_peaks()
+    roof = None
+    if prec == N.PRECISION_FP32:
+        cnt = traversal_counters(r)
+    else:
+        r32 = g.Renderer(g.default_config(1920, height=1080, photon_width=2048, photon_height=1024, radius_rule=1,
+                                          radius_fraction=0.005), device=local)
+        r32.upload_scene(mesh)
+        r32.set_camera(cam)
+        r32.run_passes(W)
+        cnt = traversal_counters(r32)
+        r32.close()
+    if cnt and tr_n:
+        bpl = cnt["photon_segments"] / cnt["passes"] * (64 + 32 * cnt["nodes_per_segment"] + 36 * cnt["tris_per_segment"])
+        achieved = bpl / (tr_ms / tr_n / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None,
+                "kernel": "k_trace_photons4" if prec == N.PRECISION_MIXED else "k_trace_photons",
+                "peak_kind": peak_kind, "nodes_per_segment": round(cnt["nodes_per_segment"], 2),
+                "tris_per_segment": round(cnt["tris_per_segment"], 2), "algorithmic_bytes_per_launch": round(bpl)}
+    if rank == 0:
+        line = {
+            "metric": "SPPM Mphotons/s + Mrays/s at fixed RMSE vs FP64 oracle, plain vs batched",
+            "value": round(value, 3), "unit": "Mphotons/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": round(1000.0 * t / K, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(LARGE, precision=args.precision, triangles_exact=sc.num_triangles,
+                           l2="BVH + triangles 2.2 GB > 129 MB L2 (no flush)", parallelism=f"replicas x{world}"),
+            "mrays_per_s": round(segs / t / 1e6, 3),
+            "stage_ms_per_launch": {k: round(v[0] / v[1], 4) for k, v in stages.items() if v[1]},
+            "setup_seconds": {"generate": round(t_gen, 2), "gpu_bvh_build": round(t_bvh, 3), "upload": round(t_up, 2)},
+            "gpu_launches": int(launches),
+            "e2e": {"value": round(e2e, 3), "unit": "Mphotons/s", "h2d_bytes_per_step": 64,
+                    "d2h_bytes_per_step": int(cfg.width * cfg.height * 12), "steps": E},
+            "roofline": roof, "cpu_baseline": None, "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
 def run_serving_line(args, rank, world, local):
     """--workload serving: the serving sweep; value = aggregate Mphotons/s at the highest rate."""
     clocks = ClockSampler(local).__enter__()
@@ -606,7 +712,7 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="cornell-1024", choices=["cornell-1024", "batched", "serving"],
+    ap.add_argument("--workload", default="cornell-1024", choices=["cornell-1024", "batched", "serving", "large"],
                     help="the JSON line's headline workload; the default line also carries the batched "
                          "workload's summary under 'batched' unless --no-batched")
     ap.add_argument("--no-batched", action="store_true")
@@ -629,6 +735,8 @@ def main():
         run_batched_line(args, rank, world, local)
     elif args.workload == "serving":
         run_serving_line(args, rank, world, local)
+    elif args.workload == "large":
+        run_large_line(args, rank, world, local)
     else:
         run_gpu(args, rank, world, local)
     if world > 1:

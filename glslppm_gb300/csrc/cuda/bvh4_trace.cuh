@@ -11,7 +11,7 @@
 
 namespace sppm_dev {
 
-constexpr int kStack = 128;  // >= 3 * kBvh4MaxDepth + 1
+constexpr int kStack = 196;  // >= 3 * kBvh4MaxDepth + 1 (kBvh4MaxDepth = 64)
 
 struct Hit4 {
     float t;

@@ -10,7 +10,7 @@
 namespace sppm {
 
 constexpr int32_t kChildEmpty = INT32_MIN;  // unused child slot
-constexpr uint32_t kBvh4MaxDepth = 40;      // traversal stack holds 3 entries per level
+constexpr uint32_t kBvh4MaxDepth = 64;      // traversal stack holds 3 entries per level
 
 // 64 bytes: a child k's box is origin + q * 2^(exponent - 127) per axis, q in [qlo, qhi]
 struct alignas(16) Node4 {

@@ -254,3 +254,113 @@ def cornell_variant(seed: int, min_tris: int = 10_000, max_tris: int = 500_000) 
     res = int(rng.choice([128, 256, 512, 1024]))
     e = int(rng.integers(14, 20))
     return JobSpec(sc, res, res, 1 << ((e + 1) // 2), 1 << (e // 2), seed)
+
+
+def perlin(p: np.ndarray, seed: int) -> np.ndarray:
+    """Classic gradient noise (Perlin 2002: quintic fade, 12 edge gradients, a seeded permutation
+    of 256) at the points p [..., 3]; values roughly in [-1, 1]."""
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(256)
+    perm = np.concatenate([perm, perm]).astype(np.int64)
+    grad = np.array([[1, 1, 0], [-1, 1, 0], [1, -1, 0], [-1, -1, 0], [1, 0, 1], [-1, 0, 1], [1, 0, -1], [-1, 0, -1],
+                     [0, 1, 1], [0, -1, 1], [0, 1, -1], [0, -1, -1]], dtype=np.float64)
+    p = np.asarray(p, dtype=np.float64)
+    pi = np.floor(p).astype(np.int64)
+    pf = p - pi
+    pi &= 255
+    fade = pf * pf * pf * (pf * (pf * 6 - 15) + 10)
+    out = 0.0
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                h = perm[perm[perm[pi[..., 0] + dx] + pi[..., 1] + dy] + pi[..., 2] + dz] % 12
+                g = grad[h]
+                d = pf - np.array([dx, dy, dz], dtype=np.float64)
+                w = np.where(dx, fade[..., 0], 1 - fade[..., 0]) * np.where(dy, fade[..., 1], 1 - fade[..., 1]) * \
+                    np.where(dz, fade[..., 2], 1 - fade[..., 2])
+                out = out + w * np.einsum("...k,...k->...", g, d)
+    return out
+
+
+def _face_normals(tris: np.ndarray) -> np.ndarray:
+    n = np.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0])
+    n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-30)
+    return np.repeat(n[:, None, :], 3, axis=1)
+
+
+def geodesic_sphere(center, radius, freq: int, displace, seed: int):
+    """Icosahedron with every face split into freq^2 triangles, projected to the sphere and
+    displaced radially by radius * displace * noise(3 * direction): 20 * freq^2 triangles."""
+    t = (1 + 5 ** 0.5) / 2
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], dtype=np.float64)
+    f = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2],
+                  [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5],
+                  [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]])
+    m = freq
+    i, j = np.meshgrid(np.arange(m), np.arange(m), indexing="ij")
+    up = (i + j) < m
+    dn = (i + j) < m - 1
+    ui, uj = i[up], j[up]
+    di, dj = i[dn], j[dn]
+    # barycentric (a, b) of the lattice points of one face, per triangle corner
+    up_ab = np.stack([np.stack([ui, uj], -1), np.stack([ui + 1, uj], -1), np.stack([ui, uj + 1], -1)], 1)
+    dn_ab = np.stack([np.stack([di + 1, dj], -1), np.stack([di + 1, dj + 1], -1), np.stack([di, dj + 1], -1)], 1)
+    ab = np.concatenate([up_ab, dn_ab]).astype(np.float64) / m  # [m^2, 3, 2]
+    A, B, Cc = v[f[:, 0]], v[f[:, 1]], v[f[:, 2]]  # [20, 3]
+    pts = (A[:, None, None, :] + ab[None, ..., 0:1] * (B - A)[:, None, None, :] +
+           ab[None, ..., 1:2] * (Cc - A)[:, None, None, :]).reshape(-1, 3, 3)
+    d = pts / np.linalg.norm(pts, axis=-1, keepdims=True)
+    r = radius * (1.0 + displace * perlin(3.0 * d + 17.0, seed))
+    tris = np.asarray(center, dtype=np.float64) + d * r[..., None]
+    # outward winding
+    cen = tris.mean(1) - np.asarray(center)
+    fn = np.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0])
+    flip = np.einsum("ij,ij->i", fn, cen) < 0
+    tris[flip] = tris[flip][:, ::-1]
+    return tris
+
+
+def heightfield(size: float, verts: int, height: float, seed: int):
+    """A verts x verts grid over [-size, size]^2 at y = height * noise: 2 (verts-1)^2 triangles."""
+    x = np.linspace(-size, size, verts)
+    X, Z = np.meshgrid(x, x, indexing="ij")
+    Y = height * perlin(np.stack([X * 3.0, np.full_like(X, 0.5), Z * 3.0], -1), seed + 1)
+    P = np.stack([X, Y, Z], -1)
+    a, b, c, d = P[:-1, :-1], P[1:, :-1], P[1:, 1:], P[:-1, 1:]
+    t1 = np.stack([a, d, c], 2).reshape(-1, 3, 3)  # y-up winding
+    t2 = np.stack([a, c, b], 2).reshape(-1, 3, 3)
+    return np.concatenate([t1, t2])
+
+
+def large_mesh(seed: int = 1, sphere_freq: int = 317, floor_verts: int = 1024, n_albedo: int = 4000) -> SceneSpec:
+    """The large-mesh workload: a Perlin-displaced geodesic sphere (20 * 317^2 = 2.01M triangles)
+    on a Perlin heightfield floor of 1024 x 1024 vertices (2.09M triangles), per-triangle albedo
+    uniform in [0.2, 0.8] quantised to 4000 materials, 10% of the triangles mirrors, and four
+    random quad area lights of emission 5-20 above the scene."""
+    rng = np.random.default_rng(0x1a46e000 + seed)
+    sph = geodesic_sphere((0.0, 0.75, 0.0), 0.6, sphere_freq, 0.08, seed)
+    flo = heightfield(2.0, floor_verts, 0.1, seed)
+    geo = np.concatenate([sph, flo])
+    n = len(geo)
+    alb = rng.uniform(0.2, 0.8, size=(n_albedo, 3))
+    mats = [MaterialSpec(f"a{k}", BRDF_MATTE, tuple(float(c) for c in alb[k])) for k in range(n_albedo)]
+    mats.append(MaterialSpec("mirror", BRDF_MIRROR, (0.95, 0.95, 0.95)))
+    mid = rng.integers(0, n_albedo, n).astype(np.int32)
+    mid[rng.random(n) < 0.1] = n_albedo
+    lights = []
+    for k in range(4):
+        e = float(rng.uniform(5.0, 20.0))
+        mats.append(MaterialSpec(f"light{k}", BRDF_LIGHT, (e, e, e)))
+        cx, cz = rng.uniform(-1.2, 1.2, 2)
+        h = float(rng.uniform(0.15, 0.3))
+        y = float(rng.uniform(2.0, 2.6))
+        t, _ = _quad(np.array([cx - h, y, cz - h]), np.array([cx + h, y, cz - h]), np.array([cx + h, y, cz + h]),
+                     np.array([cx - h, y, cz + h]), (0, -1, 0))
+        lights.append((t, len(mats) - 1))
+    ltris = np.concatenate([t for t, _ in lights])
+    lmid = np.concatenate([np.full(2, m, dtype=np.int32) for _, m in lights])
+    pos = np.concatenate([geo, ltris]).astype(np.float32)
+    mid = np.concatenate([mid, lmid])
+    return SceneSpec(pos, _face_normals(pos.astype(np.float64)).astype(np.float32), mid, mats,
+                     camera_origin=(0.0, 1.6, 3.2), camera_lookat=(0.0, 0.6, 0.0), fov=45.0)
