@@ -5,9 +5,10 @@ ABI of ``include/sppm.h``); this package is its host-side mirror.  Importing the
 ``NativeLibraryMissing`` when the library has not been built.
 """
 from .native import NativeLibraryMissing, SppmError, device_count  # noqa: F401
-from .renderer import Mesh, Renderer, default_config, look_at, pinned_empty, scene_from_arrays  # noqa: F401
+from .renderer import (Mesh, Renderer, default_config, look_at, pinned_empty, scene_from_arrays,  # noqa: F401
+                       write_image)
 from . import native, scenes  # noqa: F401
 from .batch import Batch, Server  # noqa: F401
 
-__all__ = ["Batch", "Server", "Mesh", "Renderer", "default_config", "look_at", "pinned_empty", "scene_from_arrays", "SppmError",
+__all__ = ["Batch", "Server", "Mesh", "Renderer", "default_config", "look_at", "pinned_empty", "scene_from_arrays", "write_image", "SppmError",
            "NativeLibraryMissing", "device_count", "native", "scenes"]

@@ -3,17 +3,22 @@
 // so each per-pixel and per-photon value is bit-identical to the CPU restatement.  This
 // translation unit is also compiled with -fmad=false.
 //
-// One SPPM frame (m_display, glslppm.cpp:214-536) is four to six launches over all jobs of a
+// One SPPM frame (m_display, glslppm.cpp:214-536) is one launch per stage over all jobs of a
 // batch:
-//   k_frame_begin   hash-slot clear + per-job frame bookkeeping (AA offset of the eye pass)
-//   k_eye           eyeraytrace.fs, fused with the max/min reductions (warp shuffles + one
-//                   atomic per warp) that replace ReduceTexture's 2x2 passes and 18 readbacks
-//   k_grid          InitialRadius / grid (glslppm.cpp:294-311), on the device: no host round trip
-//   k_photon        photontrace.fs, fused with the sum reduction of emitted photons and with the
-//                   hashed-grid build of hash.fs + scatter.vs (depth test = atomicMin of the photon
-//                   index) + correction.vs (additive blend = atomicAdd), warp-aggregated per slot
-//   k_gather        progressive.fs
-//   k_resolve       re.fs (on demand)
+//   k_frame_begin        hash-slot clear + per-job frame bookkeeping (AA offset of the eye pass)
+//   k_eye                eyeraytrace.fs, fused with the max/min reductions (warp shuffles + one
+//                        atomic per warp) that replace ReduceTexture's 2x2 passes and 18 readbacks
+//   k_grid               InitialRadius / grid (glslppm.cpp:294-311), on the device
+//   k_photon_gen         photontrace.fs emission / bounce / Russian roulette + the sum reduction;
+//                        queues each live photon's ray (with its bin for the counting sort)
+//   k_ray_bins_*         counting sort of the queued rays by direction class and origin cell
+//   k_trace_photons      persistent traversal of the queued rays (dynamic fetch); rays with a zero
+//                        direction component are set aside for k_trace_photons_coop (one warp each)
+//   k_photon_store       store rule + hash.fs + scatter.vs (depth test = atomicMin of the photon
+//                        index) + correction.vs (additive blend = atomicAdd), warp-aggregated
+//   k_gather             progressive.fs
+//   k_resolve            re.fs (on demand)
+// k_photon is the single-kernel form of gen + trace + store (SPPM_FLAG_FUSED_PHOTON).
 #include <cstdint>
 
 #include "bvh4_trace.cuh"

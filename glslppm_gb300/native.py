@@ -160,6 +160,7 @@ SIGNATURES = {
     "sppm_debug_fpmath": (C.c_int, [C.c_int, P, P, P, C.c_size_t]),
     "sppm_debug_trace": (C.c_int, [P, P, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P]),
     "sppm_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
+    "sppm_write_image_file": (C.c_int, [C.c_char_p, P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "sppm_host_free": (None, [P]),
     "sppm_device_count": (C.c_int, []),
     # include/sppm_batch.h

@@ -368,6 +368,14 @@ def pinned_empty(shape, dtype=np.float32) -> np.ndarray:
     return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
 
 
+def write_image(path, rgb: np.ndarray, fmt: str = "pfm") -> None:
+    """Writes an [h, w, 3] image as read_image returns it (row 0 = bottom): 'pfm' keeps the linear
+    floats, 'ppm' writes 8-bit values (for display images)."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+    h, w = rgb.shape[:2]
+    N.check(N.lib.sppm_write_image_file(str(path).encode(), rgb.ctypes.data, w, h, {"pfm": 0, "ppm": 1}[fmt]))
+
+
 def debug_fpmath(fn: int, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
     x = np.ascontiguousarray(x, dtype=np.float32)
     yy = None if y is None else np.ascontiguousarray(y, dtype=np.float32)

@@ -194,6 +194,13 @@ typedef enum sppm_image_kind {
 /* Resolves the image and copies width*height*3 floats (row 0 = bottom row, as GL) to rgb. */
 int sppm_read_image(sppm_ctx* ctx, uint32_t kind, float* rgb, size_t num_floats);
 
+/* Writes an image as sppm_read_image returns it to a file (no counterpart in the reference,
+   which only displays):  SPPM_FILE_PFM keeps the linear floats (little-endian, bottom row first,
+   as the format stores rows); SPPM_FILE_PPM writes binary 8-bit P6, top row first, with
+   clamp(v, 0, 1) * 255 rounded -- meant for SPPM_IMAGE_DISPLAY images. */
+typedef enum sppm_file_format { SPPM_FILE_PFM = 0, SPPM_FILE_PPM = 1 } sppm_file_format;
+int sppm_write_image_file(const char* path, const float* rgb, uint32_t width, uint32_t height, uint32_t format);
+
 /* Per-pixel / per-photon / per-slot state, for parity checks and checkpointing. */
 typedef enum sppm_state_kind {
     SPPM_STATE_HIT_POSITION = 0,    /* float4/pixel  QueryPositionTexture (pos.xyz, dir.x)      */

@@ -143,3 +143,23 @@ def test_cornell_variants_are_seeded_and_in_range():
         assert j.scene.material_ids.max() < len(j.scene.materials)
         sizes.add(j.width)
     assert len(sizes) >= 3
+
+
+def test_image_files(tmp_path):
+    img = np.random.default_rng(0).random((5, 7, 3)).astype(np.float32) * 2.0
+    img[0, 0] = (np.nan, -1.0, 0.5)
+    g.write_image(tmp_path / "a.pfm", img, "pfm")
+    raw = (tmp_path / "a.pfm").read_bytes()
+    head = b"PF\n7 5\n-1.0\n"
+    assert raw.startswith(head)
+    data = np.frombuffer(raw[len(head):], dtype="<f4").reshape(5, 7, 3)
+    assert np.array_equal(data.view(np.uint32), img.view(np.uint32))  # bottom row first, as stored
+    g.write_image(tmp_path / "a.ppm", img, "ppm")
+    raw = (tmp_path / "a.ppm").read_bytes()
+    head = b"P6\n7 5\n255\n"
+    assert raw.startswith(head)
+    px = np.frombuffer(raw[len(head):], dtype=np.uint8).reshape(5, 7, 3)
+    ref = np.round(np.clip(np.nan_to_num(img, nan=0.0), 0, 1) * 255).astype(np.uint8)[::-1]
+    assert np.array_equal(px, ref)
+    with pytest.raises(g.SppmError):
+        g.write_image(tmp_path / "missing" / "x.pfm", img)
