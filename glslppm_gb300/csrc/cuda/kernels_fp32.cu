@@ -675,6 +675,8 @@ __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t 
     R.org = mk(0, 0, 0);
     R.dir = mk(0, 0, 0);
     const int2 hitin = frame == 0 ? make_int2(-1, 0) : J.ph.hit[sidx];
+    // the previous segment's record, loaded with the hit (a bounce needs it; an emission does not)
+    const float4 PP = J.ph.pos[sidx], PF = J.ph.flux[sidx], PD = J.ph.dir[sidx];
     R.depth = xadd((float)hitin.y, 1.0f);
     if (hitin.x < 0 || R.depth >= (float)J.max_path) {
         if (S.light_area != 0.0f) light_sample(J, rndv, R.flux, R.dir, R.org, err);
@@ -684,7 +686,6 @@ __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t 
         R.cont = true;
         return R;
     }
-    const float4 PP = J.ph.pos[sidx], PF = J.ph.flux[sidx], PD = J.ph.dir[sidx];
     f3 flux = mk(fabsf(PF.x), fabsf(PF.y), fabsf(PF.z));
     const f3 ipos = xyz(PP);
     f3 inrm = mk(PP.w, PF.w, PD.w);
@@ -1146,7 +1147,7 @@ __global__ void __launch_bounds__(128) k_photon_store(LaunchSet ls, RayQueue q) 
 // ----------------------------------------------------------------------------------------------
 // k_gather: progressive.fs (:98-142, AccumulatePhotons :65-95)
 // ----------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_gather(LaunchSet ls) {
+__global__ void __launch_bounds__(256, 4) k_gather(LaunchSet ls) {
     const uint32_t g = grid_tid();
     if (g >= ls.total) return;
     const int k = find_job(ls, g);
@@ -1177,25 +1178,39 @@ __global__ void __launch_bounds__(256) k_gather(LaunchSet ls) {
                          floorf(xsub(xmul(fabsf(xsub(qp.z, bbmin.z)), G), 0.5f)));
         f3 flux = mk(0, 0, 0);
         float M = 0.0f;
+        // the eight cells' slots and winners first (independent loads in flight together), then
+        // the candidate photons' positions, then the accumulation in cell order (the sum's order
+        // is progressive.fs's)
+        uint32_t slot[8], win[8];
 #pragma unroll
         for (int c = 0; c < 8; c++) {
             const f3 cell = mk(xadd(ii.x, (float)(c & 1)), xadd(ii.y, (float)((c >> 1) & 1)), xadd(ii.z, (float)(c >> 2)));
-            const uint32_t slot = hash_cell(cell, G, hs1, hn);
-            const uint32_t w = J.winner[slot];
-            if (w == kEmptySlot) continue;  // the cleared texel: photon 0 weighted by count 0
-            const float4 pp = J.ph.pos[w];
+            slot[c] = hash_cell(cell, G, hs1, hn);
+        }
+#pragma unroll
+        for (int c = 0; c < 8; c++) win[c] = __ldg(&J.winner[slot[c]]);
+        uint32_t inside = 0;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            if (win[c] == kEmptySlot) continue;  // the cleared texel: photon 0 weighted by count 0
+            const f3 cell = mk(xadd(ii.x, (float)(c & 1)), xadd(ii.y, (float)((c >> 1) & 1)), xadd(ii.z, (float)(c >> 2)));
+            const float4 pp = __ldg(&J.ph.pos[win[c]]);
             const f3 rmin = mk(xadd(xdiv(cell.x, G), bbmin.x), xadd(xdiv(cell.y, G), bbmin.y), xadd(xdiv(cell.z, G), bbmin.z));
             const f3 rmax = mk(xadd(xdiv(xadd(cell.x, 1.0f), G), bbmin.x), xadd(xdiv(xadd(cell.y, 1.0f), G), bbmin.y),
                                xadd(xdiv(xadd(cell.z, 1.0f), G), bbmin.z));
-            if (pp.x > rmin.x && pp.y > rmin.y && pp.z > rmin.z && pp.x < rmax.x && pp.y < rmax.y && pp.z < rmax.z) {
-                const f3 diff = sub(xyz(pp), qp);
-                const float4 pd = J.ph.dir[w];
-                if (length(diff) < R && dot(qn, neg(xyz(pd))) > 0.0f) {
-                    const float4 pf = J.ph.flux[w];
-                    const float cnt = (float)J.count[slot];
-                    flux = add(flux, scl(xyz(pf), cnt));
-                    M = xadd(M, cnt);
-                }
+            if (pp.x > rmin.x && pp.y > rmin.y && pp.z > rmin.z && pp.x < rmax.x && pp.y < rmax.y && pp.z < rmax.z &&
+                length(sub(xyz(pp), qp)) < R)
+                inside |= 1u << c;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            if (!((inside >> c) & 1u)) continue;
+            const float4 pd = __ldg(&J.ph.dir[win[c]]);
+            if (dot(qn, neg(xyz(pd))) > 0.0f) {
+                const float4 pf = __ldg(&J.ph.flux[win[c]]);
+                const float cnt = (float)__ldg(&J.count[slot[c]]);
+                flux = add(flux, scl(xyz(pf), cnt));
+                M = xadd(M, cnt);
             }
         }
         flux = mul(flux, scl(qr, 3.183099627e-01f));
