@@ -243,7 +243,8 @@ int sppm_debug_trace(sppm_ctx* c, const float* org, const float* dir, size_t n, 
                      int32_t* tri, float* t) {
     if (!c || !org || !dir || !tri || !t) return fail(SPPM_ERR_ARG, "null argument");
     if (!c->job.have_scene) return fail(SPPM_ERR_STATE, "upload a scene first");
-    if (mode != 0 && mode != 1) return fail(SPPM_ERR_ARG, "mode must be 0 (thread per ray) or 1 (warp per ray)");
+    if (mode < 0 || mode > 2)
+        return fail(SPPM_ERR_ARG, "mode must be 0 (thread per ray), 1 (warp per ray) or 2 (block per ray)");
     if (n == 0) return SPPM_OK;
     if (n > (1u << 26)) return fail(SPPM_ERR_ARG, "n too large");
     SPPM_CK(cudaSetDevice(c->rt.device));

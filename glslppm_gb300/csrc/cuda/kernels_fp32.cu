@@ -276,6 +276,234 @@ __device__ __noinline__ Hit coop_trace_exact(const DevScene& s, f3 org, f3 dir, 
     return h;
 }
 
+// Block-wide form of the same walk (1024 threads, one ray, the same result bit for bit): the
+// threads evaluate the box and triangle tests of 1024 consecutive nodes into shared memory; one
+// warp then resolves the walk with 32-bit masks of the window -- M = nodes whose box passes with
+// the current closest t, U = those of M whose triangle would replace the closest hit -- jumping
+// straight to the next "event" (first node at or after the walk's position that is not in M, or
+// is in U).  All nodes before an event are visited as hits without effect, so a window costs a
+// few mask operations per event instead of a step per node; M and U are recomputed only when the
+// closest hit changes.
+constexpr int kBlockWalk = 1024;
+constexpr int kBlockWords = kBlockWalk / 32;
+
+struct BlockWalkShared {
+    float tmin[kBlockWalk], tt[kBlockWalk], bu[kBlockWalk], bv[kBlockWalk], bw[kBlockWalk];
+    int32_t miss[kBlockWalk], tri[kBlockWalk], mat[kBlockWalk];
+    uint32_t box[kBlockWords], leaf[kBlockWords], ok[kBlockWords], inwin[kBlockWords];
+    uint32_t M[kBlockWords], U[kBlockWords];  // with the closest t at the window's start
+    // the walk's state, broadcast to the block between windows
+    Hit h;
+    int32_t cur;
+    uint32_t steps, nodes, tris;
+    int done;
+};
+
+template <bool PHOTON, bool COUNT>
+__device__ __noinline__ Hit block_trace_exact(const DevScene& s, f3 org, f3 dir, bool cull, uint32_t& err,
+                                              TraversalCount* cnt, BlockWalkShared& sh) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    const int t = (int)threadIdx.x;
+    const int lane = t & 31;
+    const NodeX* nodes = s.nodes + (size_t)cube_face(dir) * s.num_nodes;
+    const f3 rcp = mk(xdiv(1.0f, dir.x), xdiv(1.0f, dir.y), xdiv(1.0f, dir.z));
+    const f3 t0 = mul(neg(rcp), org);
+    const int32_t nn = (int32_t)s.num_nodes;
+    if (t == 0) {
+        sh.h.t = PHOTON ? 1.0e30f : 1.0e20f;
+        sh.h.tri = -1;
+        sh.h.mat = -1;
+        sh.h.bu = sh.h.bv = sh.h.bw = 0.0f;
+        sh.cur = 0;
+        sh.steps = sh.nodes = sh.tris = 0;
+        sh.done = 0;
+    }
+    __syncthreads();
+    while (!sh.done) {
+        const int32_t base = sh.cur;
+        // ---- evaluate the window's nodes (every thread one node) ----
+        {
+            const int32_t j = base + t;
+            bool box = false, leaf = false, ok = false;
+            float tmin = 0.0f, tt = 0.0f, bu = 0.0f, bv = 0.0f, bw = 0.0f;
+            int32_t miss = -1, tri = -1, mat = -1;
+            if (j < nn) {
+                const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + j));
+                const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + j) + 1);
+                const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
+                const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
+                tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
+                const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
+                box = (tmin <= tmax) && (tmax >= 0.0f);
+                miss = __float_as_int(A.w);
+                const int32_t raw = __float_as_int(B.w);
+                leaf = raw >= 0 && (!PHOTON || !(raw & kEmitterBit));
+                if (leaf && box) {
+                    tri = raw & kTriMask;
+                    const float4 a = __ldg(&s.tri_isect[(size_t)tri * 3 + 0]);
+                    const float4 b = __ldg(&s.tri_isect[(size_t)tri * 3 + 1]);
+                    const float4 c = __ldg(&s.tri_isect[(size_t)tri * 3 + 2]);
+                    const f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
+                    const f3 pv = cross(dir, e1);
+                    const float det = dot(e0, pv);
+                    if (PHOTON || !cull || det > 1e-10f) {
+                        const f3 tv = sub(org, v0);
+                        const f3 qv = cross(tv, e0);
+                        const float u = xdiv(dot(tv, pv), det);
+                        const float v = xdiv(dot(dir, qv), det);
+                        tt = xdiv(dot(e1, qv), det);
+                        const float w = xsub(xsub(1.0f, u), v);
+                        ok = u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f;
+                        mat = __float_as_int(c.y);
+                        bu = v;
+                        bv = w;
+                        bw = u;
+                    }
+                }
+            }
+            sh.tmin[t] = tmin;
+            sh.tt[t] = tt;
+            sh.bu[t] = bu;
+            sh.bv[t] = bv;
+            sh.bw[t] = bw;
+            sh.miss[t] = miss;
+            sh.tri[t] = tri;
+            sh.mat[t] = mat;
+            const float ht = sh.h.t;
+            const bool m = box && j < nn && tmin <= ht;
+            const unsigned bx = __ballot_sync(kFull, box), lf = __ballot_sync(kFull, leaf),
+                           okm = __ballot_sync(kFull, ok), in = __ballot_sync(kFull, j < nn),
+                           mm = __ballot_sync(kFull, m), um = __ballot_sync(kFull, m && ok && tt < ht);
+            if (lane == 0) {
+                sh.box[t >> 5] = bx;
+                sh.leaf[t >> 5] = lf;
+                sh.ok[t >> 5] = okm;
+                sh.inwin[t >> 5] = in;
+                sh.M[t >> 5] = mm;
+                sh.U[t >> 5] = um;
+            }
+        }
+        __syncthreads();
+        // ---- one warp resolves the walk through the window ----
+        if (t < 32) {
+            const int w = lane;  // this lane's 32-node word
+            Hit h = sh.h;
+            uint32_t steps = sh.steps, cn = 0, ct = 0;
+            int32_t next_window = -1;
+            bool done = false;
+            // M and U of words from..31 for the current closest t: word k from node k*32 + lane of
+            // every lane (conflict-free shared reads), kept by lane k
+            auto masks = [&](uint32_t& M, uint32_t& U, int from) {
+                for (int k = from; k < kBlockWords; k++) {
+                    const int n = k * 32 + lane;
+                    const bool in = (sh.inwin[k] >> lane) & 1u, bx = (sh.box[k] >> lane) & 1u;
+                    const bool m = in && bx && sh.tmin[n] <= h.t;
+                    const bool u = m && ((sh.ok[k] >> lane) & 1u) && sh.tt[n] < h.t;
+                    const unsigned bm = __ballot_sync(kFull, m), bu = __ballot_sync(kFull, u);
+                    if (lane == k) {
+                        M = bm;
+                        U = bu;
+                    }
+                }
+            };
+            uint32_t M = sh.M[w], U = sh.U[w];
+            const uint32_t leafw = sh.leaf[w], inw = sh.inwin[w];
+            int pos = 0;
+            for (;;) {
+                // nodes at or after pos in this lane's word
+                const int pw = pos >> 5;
+                const uint32_t ge = w < pw ? 0u : (w > pw ? kFull : (kFull << (pos & 31)));
+                const uint32_t ev = (~M | U) & ge;
+                const unsigned has = __ballot_sync(kFull, ev != 0u);
+                int e = kBlockWalk;  // event position (window end when none)
+                if (has) {
+                    const int fw = __ffs(has) - 1;
+                    const uint32_t evw = __shfl_sync(kFull, ev, fw);
+                    e = fw * 32 + __ffs(evw) - 1;
+                }
+                // nodes pos .. e-1 are visited as hits that change nothing
+                {
+                    const uint32_t lo = ge;
+                    const uint32_t hi = (e >> 5) > w ? kFull : ((e >> 5) < w ? 0u : ((1u << (e & 31)) - 1u));
+                    const uint32_t vis = lo & hi;
+                    const uint32_t nv = __reduce_add_sync(kFull, __popc(vis));
+                    steps += nv;
+                    if (COUNT) {
+                        cn += nv;
+                        ct += __reduce_add_sync(kFull, __popc(vis & leafw));
+                    }
+                }
+                if (e == kBlockWalk) {  // ran off the window's end: continue at the next node
+                    next_window = base + kBlockWalk;
+                    done = next_window >= nn;
+                    break;
+                }
+                const int ew = e >> 5, eb = e & 31;
+                const bool e_in = (__shfl_sync(kFull, inw, ew) >> eb) & 1u;
+                if (!e_in) {  // the walk stepped past the last node
+                    done = true;
+                    break;
+                }
+                const bool e_upd = (__shfl_sync(kFull, U, ew) >> eb) & 1u;
+                steps += 1;
+                if (COUNT) cn += 1;
+                if (e_upd) {  // a hit whose triangle replaces the closest hit
+                    if (COUNT) ct += 1;
+                    h.t = sh.tt[e];
+                    h.tri = sh.tri[e];
+                    h.mat = sh.mat[e];
+                    h.bu = sh.bu[e];
+                    h.bv = sh.bv[e];
+                    h.bw = sh.bw[e];
+                    pos = e + 1;
+                    if (base + pos >= nn) {
+                        done = true;
+                        break;
+                    }
+                    if (pos == kBlockWalk) {
+                        next_window = base + kBlockWalk;
+                        break;
+                    }
+                    masks(M, U, pos >> 5);
+                    continue;
+                }
+                // a node whose box misses: follow its miss link
+                const int32_t nx = sh.miss[e];
+                if (nx < 0 || nx >= nn) {
+                    done = true;
+                    break;
+                }
+                if (nx > base + e && nx < base + kBlockWalk) {
+                    pos = nx - base;
+                    continue;
+                }
+                next_window = nx;
+                break;
+            }
+            if (lane == 0) {
+                sh.h = h;
+                sh.steps = steps;
+                if (COUNT) {
+                    sh.nodes += cn;
+                    sh.tris += ct;
+                }
+                sh.cur = next_window;
+                sh.done = done || steps > (uint32_t)nn + 1u;
+                if (steps > (uint32_t)nn + 1u) sh.steps = 0xFFFFFFFFu;
+            }
+        }
+        __syncthreads();
+    }
+    const Hit out = sh.h;
+    if (sh.steps == 0xFFFFFFFFu) err |= kErrWatchdogTraverse;
+    if (COUNT) {
+        cnt->nodes += sh.nodes;
+        cnt->tris += sh.tris;
+    }
+    __syncthreads();  // the shared state is read by every thread before a next ray reuses it
+    return out;
+}
+
 struct Shade {
     f3 pos, nrm, gnrm, col;
     int brdf;
@@ -1094,21 +1322,22 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
     if (err) atomicOr(&ls.jobs[ls.job_ids[job_k]].state->err, err);
 }
 
-// the rays k_trace_photons set aside (slab_degenerate directions), one warp per ray
+// the rays k_trace_photons set aside (slab_degenerate directions), one block of 1024 threads per
+// ray (block_trace_exact)
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_trace_photons_coop(LaunchSet ls, RayQueue q) {
+__global__ void __launch_bounds__(kBlockWalk) k_trace_photons_coop(LaunchSet ls, RayQueue q) {
+    __shared__ BlockWalkShared sh;
     const uint32_t n = q.counters[2];
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    const unsigned lane = threadIdx.x & 31;
-    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += warps) {
+    for (uint32_t w = blockIdx.x; w < n; w += gridDim.x) {
         const uint32_t idx = q.slow[w];
         const float4 o = q.org[idx], d = q.dir[idx];
         const int job_k = find_job(ls, __float_as_uint(o.w));
         const JobDesc& J = ls.jobs[ls.job_ids[job_k]];
         uint32_t err = 0;
         TraversalCount ct;
-        const Hit h = coop_trace_exact<true, COUNT>(J.scene, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), false, err, &ct);
-        if (lane == 0) {
+        const Hit h = block_trace_exact<true, COUNT>(J.scene, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), false, err, &ct,
+                                                     sh);
+        if (threadIdx.x == 0) {
             q.hit[idx] = make_float4(__int_as_float(h.tri), h.bu, h.bv, h.bw);
             atomicAdd(&J.state->coop_segments, 1ull);
             if (err) atomicOr(&J.state->err, err);
@@ -1305,10 +1534,22 @@ __global__ void k_fpmath(int fn, const float* x, const float* y, float* out, uin
 // single rays through the exact traversal: mode 0 one thread per ray (trace_exact), mode 1 one
 // warp per ray (coop_trace_exact); photon rays skip emitters, eye rays may cull back faces
 template <bool PHOTON>
-__global__ void __launch_bounds__(128) k_debug_trace(DevScene s, const float* org, const float* dir, uint32_t n,
+__global__ void __launch_bounds__(1024) k_debug_trace(DevScene s, const float* org, const float* dir, uint32_t n,
                                                      int cull, int mode, int32_t* tri, float* t, uint32_t* err) {
     uint32_t e = 0;
-    if (mode == 0) {
+    if (mode == 2) {
+        __shared__ BlockWalkShared sh;
+        for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+            TraversalCount ct;
+            const Hit h = block_trace_exact<PHOTON, false>(s, mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]),
+                                                           mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]), cull != 0, e,
+                                                           &ct, sh);
+            if (threadIdx.x == 0) {
+                tri[i] = h.tri;
+                t[i] = h.t;
+            }
+        }
+    } else if (mode == 0) {
         const uint32_t i = grid_tid();
         if (i >= n) return;
         const Hit h = trace_exact<PHOTON>(s, mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]),
@@ -1372,8 +1613,8 @@ void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool coun
 }
 void launch_trace_photons_coop(const LaunchSet& ls, const RayQueue& q, bool count, cudaStream_t s) {
     if (!ls.total || !q.slow) return;
-    if (count) k_trace_photons_coop<true><<<32, 128, 0, s>>>(ls, q);
-    else k_trace_photons_coop<false><<<32, 128, 0, s>>>(ls, q);
+    if (count) k_trace_photons_coop<true><<<64, kBlockWalk, 0, s>>>(ls, q);
+    else k_trace_photons_coop<false><<<64, kBlockWalk, 0, s>>>(ls, q);
 }
 
 void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
@@ -1404,9 +1645,10 @@ void launch_fpmath(int fn, const float* x, const float* y, float* out, uint32_t 
 void launch_debug_trace(const DevScene& sc, const float* org, const float* dir, uint32_t n, bool photon, bool cull,
                         int mode, int32_t* tri, float* t, uint32_t* err, cudaStream_t s) {
     if (!n) return;
-    const uint32_t blocks = mode == 0 ? blocks_for(n, 128) : blocks_for(n, 4);
-    if (photon) k_debug_trace<true><<<blocks, 128, 0, s>>>(sc, org, dir, n, cull, mode, tri, t, err);
-    else k_debug_trace<false><<<blocks, 128, 0, s>>>(sc, org, dir, n, cull, mode, tri, t, err);
+    const uint32_t threads = mode == 2 ? kBlockWalk : 128;
+    const uint32_t blocks = mode == 0 ? blocks_for(n, 128) : (mode == 1 ? blocks_for(n, 4) : (n < 256 ? n : 256u));
+    if (photon) k_debug_trace<true><<<blocks, threads, 0, s>>>(sc, org, dir, n, cull, mode, tri, t, err);
+    else k_debug_trace<false><<<blocks, threads, 0, s>>>(sc, org, dir, n, cull, mode, tri, t, err);
 }
 
 }  // namespace sppm_dev

@@ -259,7 +259,7 @@ class Renderer:
     def debug_trace(self, org: np.ndarray, dir: np.ndarray, photon: bool = True, cull: bool = False,
                     mode: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """Single rays through the exact traversal of the uploaded scene: (triangle or -1, t).
-        mode 0 traces one ray per thread, mode 1 one ray per warp."""
+        mode 0 traces one ray per thread, mode 1 one ray per warp, mode 2 one ray per block."""
         org = np.ascontiguousarray(org, dtype=np.float32).reshape(-1, 3)
         dir = np.ascontiguousarray(dir, dtype=np.float32).reshape(-1, 3)
         n = org.shape[0]

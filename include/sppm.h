@@ -320,7 +320,8 @@ int sppm_debug_fpmath(int fn, const float* x, const float* y, float* out, size_t
    FP32 traversal (raytrace() of photontrace.fs:123-255 when photon != 0, of eyeraytrace.fs:67-290
    with back-face culling when cull != 0 otherwise): tri[i] = closest triangle or -1, t[i] = its
    t (the initial bound when nothing is hit).  mode 0 traces one ray per thread, mode 1 one ray
-   per warp (the form used for rays with a zero direction component); both give the same result. */
+   per warp, mode 2 one ray per block of 1024 threads (the form the photon pass uses for rays
+   with a zero direction component); all give the same result. */
 int sppm_debug_trace(sppm_ctx* ctx, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
                      int32_t* tri, float* t);
 /* Page-locked host memory (cudaMallocHost) for the host buffers of sppm_read_image and friends:

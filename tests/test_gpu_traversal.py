@@ -56,26 +56,46 @@ def test_thread_warp_and_oracle_agree_on_generic_rays(traced, photon, cull):
     d = rng.normal(size=(4096, 3))
     d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
     tri0, t0 = r.debug_trace(org, d, photon, cull, mode=0)
-    tri1, t1 = r.debug_trace(org, d, photon, cull, mode=1)
     trio, to = o.trace(org, d, photon, cull)
     assert (tri0 >= 0).mean() > 0.5
     np.testing.assert_array_equal(tri0, trio)
     np.testing.assert_array_equal(t0.view(np.uint32), to.view(np.uint32))
-    np.testing.assert_array_equal(tri1, trio)
-    np.testing.assert_array_equal(t1.view(np.uint32), to.view(np.uint32))
+    for mode in (1, 2):
+        trim, tm = r.debug_trace(org, d, photon, cull, mode=mode)
+        np.testing.assert_array_equal(trim, trio, err_msg=f"mode {mode}")
+        np.testing.assert_array_equal(tm.view(np.uint32), to.view(np.uint32), err_msg=f"mode {mode}")
 
 
 @pytest.mark.parametrize("photon", [True, False])
 def test_thread_warp_and_oracle_agree_on_zero_direction_components(traced, photon):
     r, o, lo, hi = traced
     org, d = degenerate_rays(np.random.default_rng(11), lo, hi)
-    tri1, t1 = r.debug_trace(org, d, photon, False, mode=1)
     trio, to = o.trace(org, d, photon, False)
-    np.testing.assert_array_equal(tri1, trio)
-    np.testing.assert_array_equal(t1.view(np.uint32), to.view(np.uint32))
-    tri0, t0 = r.debug_trace(org, d, photon, False, mode=0)
-    np.testing.assert_array_equal(tri0, trio)
-    np.testing.assert_array_equal(t0.view(np.uint32), to.view(np.uint32))
+    for mode in (2, 1, 0):
+        trim, tm = r.debug_trace(org, d, photon, False, mode=mode)
+        np.testing.assert_array_equal(trim, trio, err_msg=f"mode {mode}")
+        np.testing.assert_array_equal(tm.view(np.uint32), to.view(np.uint32), err_msg=f"mode {mode}")
+
+
+def test_block_walk_on_a_large_scene(cornell_c1_mesh):
+    """The block-per-ray walk over a 100k-triangle scene (windows of 1024 nodes, jumps between
+    windows, several closest-hit updates per window) equals the thread-per-ray walk."""
+    from glslppm_gb300 import scenes
+    sc = scenes.cornell_variant(5, min_tris=90_000, max_tris=110_000).scene
+    r = g.Renderer(g.default_config(16, photon_width=16, photon_height=16))
+    r.upload_scene(sc.to_mesh())
+    pos = sc.positions.reshape(-1, 3)
+    org, d = degenerate_rays(np.random.default_rng(4), pos.min(0), pos.max(0), n_each=8)
+    rng = np.random.default_rng(6)
+    og = rng.uniform(0.05, 0.95, size=(512, 3)).astype(np.float32)
+    dg = rng.normal(size=(512, 3))
+    dg = (dg / np.linalg.norm(dg, axis=1, keepdims=True)).astype(np.float32)
+    org, d = np.concatenate([org, og]), np.concatenate([d, dg])
+    for photon in (True, False):
+        tri0, t0 = r.debug_trace(org, d, photon, False, mode=0)
+        tri2, t2 = r.debug_trace(org, d, photon, False, mode=2)
+        np.testing.assert_array_equal(tri2, tri0)
+        np.testing.assert_array_equal(t2.view(np.uint32), t0.view(np.uint32))
 
 
 def test_photon_pass_with_warp_traced_segments_matches_fused_kernel(cornell_c1_mesh):
