@@ -276,8 +276,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
         const float gx = fabsf(qp4.x - st->bbmin[0]) * G, gy = fabsf(qp4.y - st->bbmin[1]) * G,
                     gz = fabsf(qp4.z - st->bbmin[2]) * G;
         const float ix = floorf(gx - 0.5f), iy = floorf(gy - 0.5f), iz = floorf(gz - 0.5f);
-        const float R = (float)sqrt(R2);
-        const float R2f = R * R;
+        const float R2f = (float)R2;  // the in-radius test in FP32 (no FP64 square root)
         const float invG = 1.0f / G;
         float fx = 0.0f, fy = 0.0f, fz = 0.0f, M = 0.0f;
 #pragma unroll
@@ -306,16 +305,18 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
             fz += fb_.x * cf;
             M += cf;
         }
-        const double scale = (double)J.scene.flux_unscale;
-        const double alpha = (double)J.alpha;
-        const double Md = (double)M;
-        const double gg = fmin((N + alpha * Md) / (N + Md), 1.0);
+        // shrink ratio (N + alpha M) / (N + M) = 1 - (1 - alpha) M / (N + M), computed in FP32 (its
+        // relative error ~1e-7 per pass); the statistics themselves accumulate in FP64 with fused
+        // multiply-adds, so GB300's slow FP64 units see no division and no square root
+        const float denom = (float)(N + (double)M);
+        const float ggf = M > 0.0f ? fminf(1.0f - (1.0f - J.alpha) * (M / denom), 1.0f) : 1.0f;
+        const double gg = (double)ggf;
         R2 *= gg;
-        N += alpha * Md;
-        const double ip = 0.31830988618379067;
-        tx = (tx + (double)fx * scale * (double)qr4.x * ip) * gg;
-        ty = (ty + (double)fy * scale * (double)qr4.y * ip) * gg;
-        tz = (tz + (double)fz * scale * (double)qr4.z * ip) * gg;
+        N = fma((double)J.alpha, (double)M, N);
+        const float s = J.scene.flux_unscale * 0.318309886f;
+        tx = fma(tx, gg, (double)(fx * s * qr4.x * ggf));
+        ty = fma(ty, gg, (double)(fy * s * qr4.y * ggf));
+        tz = fma(tz, gg, (double)(fz * s * qr4.z * ggf));
         J.px.stat_n[p] = N;
     }
     J.px.stat_r2[p] = R2;
