@@ -69,9 +69,9 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
             const float ax = fmaf(lx, rx, nx), bx = fmaf(hx, rx, nx);
             const float ay = fmaf(ly, ry, ny), by = fmaf(hy, ry, ny);
             const float az = fmaf(lz, rz, nz), bz = fmaf(hz, rz, nz);
-            const float t0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), 0.0f));
+            const float t0 = fmaxf(fmax3(fminf(ax, bx), fminf(ay, by), fminf(az, bz)), 0.0f);
             // widen the far bound by a few ulps so that rounding never rejects a grazing hit
-            const float t1 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz)) * 1.00000036f;
+            const float t1 = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fmaxf(az, bz)) * 1.00000036f;
             tnear[k] = t0;
             hit[k] = k < cnt && t0 <= t1 && t0 <= h.t;
         }

@@ -161,6 +161,19 @@ __device__ __forceinline__ int find_job(const LaunchSet& ls, uint32_t g) {
     return lo;
 }
 
+// three-input minimum / maximum (one instruction on sm_100+); like fminf/fmaxf a NaN operand is
+// ignored, so fmax3(a, b, c) == fmaxf(fmaxf(a, b), c) for every input that can compare equal
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 // ---- exact single-precision vector helpers (pinned evaluation order, never fused) ----------
 struct f3 {
     float x, y, z;

@@ -92,8 +92,8 @@ __device__ __forceinline__ Hit trace_exact(const DevScene& s, f3 org, f3 dir, bo
         if (COUNT) cnt->nodes++;
         const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
         const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
-        const float tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
-        const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
+        const float tmin = fmax3(fminf(lx, hx), fminf(ly, hy), fminf(lz, hz));
+        const float tmax = fmin3(fmaxf(lx, hx), fmaxf(ly, hy), fmaxf(lz, hz));
         const bool hit = (tmin <= tmax) && (tmin <= h.t) && (tmax >= 0.0f);
         const int32_t tri = __float_as_int(B.w);
         if (hit && tri >= 0 && (!PHOTON || !(tri & kEmitterBit))) {
@@ -174,8 +174,8 @@ __device__ __noinline__ Hit coop_trace_exact(const DevScene& s, f3 org, f3 dir, 
             const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + j) + 1);
             const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
             const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
-            tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
-            const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
+            tmin = fmax3(fminf(lx, hx), fminf(ly, hy), fminf(lz, hz));
+            const float tmax = fmin3(fmaxf(lx, hx), fmaxf(ly, hy), fmaxf(lz, hz));
             box = (tmin <= tmax) && (tmax >= 0.0f);
             miss = __float_as_int(A.w);
             const int32_t raw = __float_as_int(B.w);
@@ -332,8 +332,8 @@ __device__ __noinline__ Hit block_trace_exact(const DevScene& s, f3 org, f3 dir,
                 const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + j) + 1);
                 const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
                 const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
-                tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
-                const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
+                tmin = fmax3(fminf(lx, hx), fminf(ly, hy), fminf(lz, hz));
+                const float tmax = fmin3(fmaxf(lx, hx), fmaxf(ly, hy), fmaxf(lz, hz));
                 box = (tmin <= tmax) && (tmax >= 0.0f);
                 miss = __float_as_int(A.w);
                 const int32_t raw = __float_as_int(B.w);
@@ -1278,8 +1278,8 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
             if (COUNT) tc.nodes++;
             const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
             const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
-            const float tmin = fmaxf(fmaxf(fminf(lx, hx), fminf(ly, hy)), fminf(lz, hz));
-            const float tmax = fminf(fminf(fmaxf(lx, hx), fmaxf(ly, hy)), fmaxf(lz, hz));
+            const float tmin = fmax3(fminf(lx, hx), fminf(ly, hy), fminf(lz, hz));
+            const float tmax = fmin3(fmaxf(lx, hx), fmaxf(ly, hy), fmaxf(lz, hz));
             const bool hit = (tmin <= tmax) && (tmin <= h.t) && (tmax >= 0.0f);
             const int32_t tri = __float_as_int(B.w);
             if (hit && tri >= 0 && !(tri & kEmitterBit)) {

@@ -46,9 +46,9 @@ __device__ __forceinline__ void child_box(const float4& w0, const float4& w2, co
     const float ax = fmaf(lx, rx, nx), bx = fmaf(hx, rx, nx);
     const float ay = fmaf(ly, ry, ny), by = fmaf(hy, ry, ny);
     const float az = fmaf(lz, rz, nz), bz = fmaf(hz, rz, nz);
-    const float t0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), 0.0f));
+    const float t0 = fmaxf(fmax3(fminf(ax, bx), fminf(ay, by), fminf(az, bz)), 0.0f);
     // the far bound widened by a few ulps so that rounding never rejects a grazing hit
-    const float t1 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz)) * 1.00000036f;
+    const float t1 = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fmaxf(az, bz)) * 1.00000036f;
     tn = t0;
     hit = t0 <= t1 && t0 <= tbest;
 }
