@@ -86,6 +86,15 @@ class Batch:
         N.check(N.lib.sppm_batch_get_frame_info(self._h, job, C.byref(fi)))
         return fi
 
+    def save_checkpoint(self, job: int) -> bytes:
+        n = int(N.lib.sppm_batch_checkpoint_bytes(self._h, job))
+        buf = C.create_string_buffer(n)
+        N.check(N.lib.sppm_batch_save_checkpoint(self._h, job, buf, n))
+        return buf.raw
+
+    def load_checkpoint(self, job: int, data: bytes) -> None:
+        N.check(N.lib.sppm_batch_load_checkpoint(self._h, job, data, len(data)))
+
     def info(self) -> N.BatchInfo:
         bi = N.BatchInfo()
         N.check(N.lib.sppm_batch_get_info(self._h, C.byref(bi)))

@@ -66,7 +66,7 @@ int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out) {
     if (!c) return fail(SPPM_ERR_OOM, "host allocation failed");
     if ((st = c->rt.init(device, cfg->precision, cfg->flags, cfg->eye_pass_interval, 1))) return st;
     if ((st = c->job.init(*cfg, c->rt.d_jobs, 0, c->rt.stream))) return st;
-    c->job.start_frame = c->rt.frames;
+    c->job.start_frame = (int64_t)c->rt.frames;
     c->rt.active.push_back(&c->job);
     c->rt.dirty = true;
     *out = c.release();
@@ -79,7 +79,7 @@ int sppm_upload_scene(sppm_ctx* c, const sppm_scene* scene) {
     SPPM_CK(cudaStreamSynchronize(c->rt.stream));
     int st = c->job.upload_scene(scene, c->rt.stream);
     if (st) return st;
-    c->job.start_frame = c->rt.frames;
+    c->job.start_frame = (int64_t)c->rt.frames;
     c->rt.dirty = true;
     return SPPM_OK;
 }
@@ -96,7 +96,7 @@ int sppm_reset(sppm_ctx* c) {
     SPPM_CK(cudaStreamSynchronize(c->rt.stream));
     int st = c->job.reset(c->rt.stream);
     if (st) return st;
-    c->job.start_frame = c->rt.frames;
+    c->job.start_frame = (int64_t)c->rt.frames;
     c->rt.dirty = true;
     return SPPM_OK;
 }
@@ -139,6 +139,27 @@ int sppm_read_state(sppm_ctx* c, uint32_t kind, void* dst, size_t bytes) {
     SPPM_CK(cudaSetDevice(c->rt.device));
     SPPM_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->rt.stream));
     return c->rt.synchronize();
+}
+
+size_t sppm_checkpoint_bytes(const sppm_ctx* c) { return c ? c->job.checkpoint_bytes() : 0; }
+
+int sppm_save_checkpoint(sppm_ctx* c, void* dst, size_t bytes) {
+    if (!c || !dst) return fail(SPPM_ERR_ARG, "null argument");
+    SPPM_CK(cudaSetDevice(c->rt.device));
+    SPPM_CK(cudaStreamSynchronize(c->rt.stream));
+    return c->job.save_checkpoint(dst, bytes, c->rt.stream);
+}
+
+int sppm_load_checkpoint(sppm_ctx* c, const void* src, size_t bytes) {
+    if (!c || !src) return fail(SPPM_ERR_ARG, "null argument");
+    SPPM_CK(cudaSetDevice(c->rt.device));
+    uint32_t frames = 0;
+    int st = c->job.load_checkpoint(src, bytes, c->rt.stream, &frames);
+    if (st) return st;
+    // the job's next frame is frame `frames`: its eye-pass phase follows
+    c->job.start_frame = (int64_t)c->rt.frames - (int64_t)frames;
+    c->rt.dirty = true;
+    return SPPM_OK;
 }
 
 int sppm_get_frame_info(sppm_ctx* c, sppm_frame_info* fi) {

@@ -133,7 +133,7 @@ int sppm_batch_add_job(sppm_batch* b, const sppm_config* cfg, const sppm_scene* 
     if ((st = j->init(*cfg, b->rt.d_jobs + id, id, b->rt.stream))) return st;
     if ((st = j->upload_scene(scene, b->rt.stream))) return st;
     if ((st = j->set_camera(cam, b->rt.stream))) return st;
-    j->start_frame = b->rt.frames;
+    j->start_frame = (int64_t)b->rt.frames;
     b->rt.active.push_back(j.get());
     b->slots[id] = std::move(j);
     b->rt.dirty = true;
@@ -160,7 +160,7 @@ int sppm_batch_reset_job(sppm_batch* b, uint32_t id) {
     SPPM_CK(cudaStreamSynchronize(b->rt.stream));
     int st = j->reset(b->rt.stream);
     if (st) return st;
-    j->start_frame = b->rt.frames;
+    j->start_frame = (int64_t)b->rt.frames;
     b->rt.dirty = true;
     return SPPM_OK;
 }
@@ -215,6 +215,31 @@ int sppm_batch_read_state(sppm_batch* b, uint32_t id, uint32_t kind, void* dst, 
     SPPM_CK(cudaSetDevice(b->rt.device));
     SPPM_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, b->rt.stream));
     return b->rt.synchronize();
+}
+
+size_t sppm_batch_checkpoint_bytes(const sppm_batch* b, uint32_t id) {
+    const Job* j = job_of(b, id);
+    return j ? j->checkpoint_bytes() : 0;
+}
+
+int sppm_batch_save_checkpoint(sppm_batch* b, uint32_t id, void* dst, size_t bytes) {
+    Job* j = job_of(b, id);
+    if (!j || !dst) return fail(SPPM_ERR_ARG, "no job %u or null buffer", id);
+    SPPM_CK(cudaSetDevice(b->rt.device));
+    SPPM_CK(cudaStreamSynchronize(b->rt.stream));
+    return j->save_checkpoint(dst, bytes, b->rt.stream);
+}
+
+int sppm_batch_load_checkpoint(sppm_batch* b, uint32_t id, const void* src, size_t bytes) {
+    Job* j = job_of(b, id);
+    if (!j || !src) return fail(SPPM_ERR_ARG, "no job %u or null buffer", id);
+    SPPM_CK(cudaSetDevice(b->rt.device));
+    uint32_t frames = 0;
+    int st = j->load_checkpoint(src, bytes, b->rt.stream, &frames);
+    if (st) return st;
+    j->start_frame = (int64_t)b->rt.frames - (int64_t)frames;
+    b->rt.dirty = true;
+    return SPPM_OK;
 }
 
 int sppm_batch_get_frame_info(sppm_batch* b, uint32_t id, sppm_frame_info* fi) {

@@ -495,6 +495,81 @@ int Job::frame_info(sppm_frame_info* fi, cudaStream_t s) const {
     return SPPM_OK;
 }
 
+namespace {
+struct CheckpointHeader {
+    char magic[8];
+    uint32_t version, W, H, PW, PH, hash_num, precision, state_bytes;
+};
+constexpr char kCheckpointMagic[8] = {'S', 'P', 'P', 'M', 'C', 'K', 'P', '1'};
+constexpr uint32_t kCheckpointKinds = SPPM_STATE_STATS_TAU + 1;
+}  // namespace
+
+size_t Job::checkpoint_bytes() const {
+    size_t b = sizeof(CheckpointHeader) + sizeof(JobState);
+    for (uint32_t k = 0; k < kCheckpointKinds; k++) {
+        size_t n = 0;
+        if (state_ptr(k, &n)) b += n;
+    }
+    return b;
+}
+
+int Job::save_checkpoint(void* dst, size_t bytes, cudaStream_t s) const {
+    if (bytes != checkpoint_bytes()) return fail(SPPM_ERR_ARG, "checkpoint needs %zu bytes", checkpoint_bytes());
+    char* p = static_cast<char*>(dst);
+    CheckpointHeader h;
+    memcpy(h.magic, kCheckpointMagic, 8);
+    h.version = 1;
+    h.W = W;
+    h.H = H;
+    h.PW = PW;
+    h.PH = PH;
+    h.hash_num = hash_num;
+    h.precision = cfg.precision;
+    h.state_bytes = (uint32_t)sizeof(JobState);
+    memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    SPPM_CK(cudaMemcpyAsync(p, d_state, sizeof(JobState), cudaMemcpyDeviceToHost, s));
+    p += sizeof(JobState);
+    for (uint32_t k = 0; k < kCheckpointKinds; k++) {
+        size_t n = 0;
+        void* src = state_ptr(k, &n);
+        if (!src) continue;
+        SPPM_CK(cudaMemcpyAsync(p, src, n, cudaMemcpyDeviceToHost, s));
+        p += n;
+    }
+    SPPM_CK(cudaStreamSynchronize(s));
+    return SPPM_OK;
+}
+
+int Job::load_checkpoint(const void* src, size_t bytes, cudaStream_t s, uint32_t* frames_started) {
+    if (bytes != checkpoint_bytes()) return fail(SPPM_ERR_ARG, "checkpoint has %zu bytes, this job's %zu", bytes,
+                                                  checkpoint_bytes());
+    const char* p = static_cast<const char*>(src);
+    CheckpointHeader h;
+    memcpy(&h, p, sizeof(h));
+    if (memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != 1 || h.state_bytes != sizeof(JobState))
+        return fail(SPPM_ERR_ARG, "not a checkpoint of this build");
+    if (h.W != W || h.H != H || h.PW != PW || h.PH != PH || h.hash_num != hash_num || h.precision != cfg.precision)
+        return fail(SPPM_ERR_ARG, "checkpoint of a %ux%u image with %ux%u photons (%u slots, precision %u) does not "
+                    "fit this job", h.W, h.H, h.PW, h.PH, h.hash_num, h.precision);
+    p += sizeof(h);
+    JobState st;
+    memcpy(&st, p, sizeof(st));
+    p += sizeof(JobState);
+    SPPM_CK(cudaStreamSynchronize(s));
+    SPPM_CK(cudaMemcpyAsync(d_state, &st, sizeof(st), cudaMemcpyHostToDevice, s));
+    for (uint32_t k = 0; k < kCheckpointKinds; k++) {
+        size_t n = 0;
+        void* dst = state_ptr(k, &n);
+        if (!dst) continue;
+        SPPM_CK(cudaMemcpyAsync(dst, p, n, cudaMemcpyHostToDevice, s));
+        p += n;
+    }
+    SPPM_CK(cudaStreamSynchronize(s));
+    *frames_started = st.frames_started;
+    return SPPM_OK;
+}
+
 LaunchSet Job::self_set(const JobDesc* table, uint32_t which) const {
     LaunchSet ls;
     ls.jobs = table;
@@ -583,7 +658,7 @@ int Runner::rebuild() {
         std::vector<uint32_t> ids, pref;
         uint64_t acc = 0;
         for (Job* j : active) {
-            if ((j->start_frame % L) != (uint64_t)p) continue;
+            if (j->eye_phase(L) != p) continue;
             ids.push_back(j->slot);
             pref.push_back((uint32_t)acc);
             acc += j->npix;
@@ -615,7 +690,7 @@ int Runner::rebuild() {
         const uint32_t m = (uint32_t)eye_cnt[p];
         uint64_t px = 0;
         for (Job* j : active)
-            if ((j->start_frame % L) == (uint64_t)p) px += j->npix;
+            if (j->eye_phase(L) == p) px += j->npix;
         eye_pix[p] = mk(eye_off[p], eye_off[p] + m, m, px);
         eye_ids[p] = d_t + eye_off[p];
     }

@@ -72,7 +72,13 @@ struct Job {
     uint32_t slot = 0;
     bool have_scene = false, have_camera = false;
     float fixed_radius = 0.0f;
-    uint64_t start_frame = 0;      // runner frame at which the job's frame 0 is queued
+    int64_t start_frame = 0;       // runner frame at which the job's frame 0 is (or was) queued;
+                                   // negative for a job resumed with more frames than the runner
+    // the runner phase (frame mod interval) at which this job's eye passes fall
+    uint32_t eye_phase(uint32_t interval) const {
+        const int64_t L = (int64_t)interval;
+        return (uint32_t)(((start_frame % L) + L) % L);
+    }
     uint64_t scene_bytes_used = 0;
 
     // device bytes of the state arena for a configuration
@@ -88,6 +94,10 @@ struct Job {
     int write_desc(cudaStream_t s);
     void* state_ptr(uint32_t kind, size_t* bytes) const;
     int frame_info(sppm_frame_info* fi, cudaStream_t s) const;
+    // checkpoint: header + JobState + every state array (flat binary, this build's layout)
+    size_t checkpoint_bytes() const;
+    int save_checkpoint(void* dst, size_t bytes, cudaStream_t s) const;
+    int load_checkpoint(const void* src, size_t bytes, cudaStream_t s, uint32_t* frames_started);
     LaunchSet self_set(const JobDesc* table, uint32_t which) const;  // 0 pixels, 1 photons, 2 hash
     uint64_t bytes() const { return state_mem.size + scene_mem.size; }
 };

@@ -145,6 +145,9 @@ SIGNATURES = {
     "sppm_read_image": (C.c_int, [P, C.c_uint32, P, C.c_size_t]),
     "sppm_read_state": (C.c_int, [P, C.c_uint32, P, C.c_size_t]),
     "sppm_state_bytes": (C.c_size_t, [P, C.c_uint32]),
+    "sppm_checkpoint_bytes": (C.c_size_t, [P]),
+    "sppm_save_checkpoint": (C.c_int, [P, P, C.c_size_t]),
+    "sppm_load_checkpoint": (C.c_int, [P, P, C.c_size_t]),
     "sppm_get_frame_info": (C.c_int, [P, C.POINTER(FrameInfo)]),
     "sppm_enable_stage_timing": (C.c_int, [P, C.c_int]),
     "sppm_set_stage_timing_mask": (C.c_int, [P, C.c_uint32]),
@@ -181,6 +184,9 @@ SIGNATURES = {
     "sppm_batch_read_state": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.c_size_t]),
     "sppm_batch_get_frame_info": (C.c_int, [P, C.c_uint32, C.POINTER(FrameInfo)]),
     "sppm_batch_get_info": (C.c_int, [P, C.POINTER(BatchInfo)]),
+    "sppm_batch_checkpoint_bytes": (C.c_size_t, [P, C.c_uint32]),
+    "sppm_batch_save_checkpoint": (C.c_int, [P, C.c_uint32, P, C.c_size_t]),
+    "sppm_batch_load_checkpoint": (C.c_int, [P, C.c_uint32, P, C.c_size_t]),
     "sppm_batch_set_stage_timing_mask": (C.c_int, [P, C.c_uint32]),
     "sppm_batch_read_stage_times": (C.c_int, [P, P, P]),
     "sppm_batch_enable_traversal_counters": (C.c_int, [P, C.c_int]),

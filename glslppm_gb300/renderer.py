@@ -269,6 +269,16 @@ class Renderer:
                                        tri.ctypes.data, t.ctypes.data))
         return tri, t
 
+    def save_checkpoint(self) -> bytes:
+        """The progressive state as a flat binary (sppm_save_checkpoint)."""
+        n = int(N.lib.sppm_checkpoint_bytes(self._h))
+        buf = C.create_string_buffer(n)
+        N.check(N.lib.sppm_save_checkpoint(self._h, buf, n))
+        return buf.raw
+
+    def load_checkpoint(self, data: bytes) -> None:
+        N.check(N.lib.sppm_load_checkpoint(self._h, data, len(data)))
+
     def frame_info(self) -> N.FrameInfo:
         fi = N.FrameInfo()
         N.check(N.lib.sppm_get_frame_info(self._h, C.byref(fi)))

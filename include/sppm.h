@@ -246,6 +246,15 @@ typedef struct sppm_frame_info {
     uint64_t kernel_launches;     /* kernels launched by sppm_run_passes since sppm_create      */
 } sppm_frame_info;
 int sppm_get_frame_info(sppm_ctx* ctx, sppm_frame_info* info);
+
+/* Checkpoint / resume of the progressive state (no counterpart in the reference): a flat binary
+   image of the frame counters, RNG states, hit points, photon records, hashed grid and
+   progressive statistics -- not the scene or camera, which a resuming context uploads itself.
+   Loading it into a context of the same image, photon and hash sizes and precision continues the
+   render exactly where it was saved (the next frames are bit-identical to an uninterrupted run). */
+size_t sppm_checkpoint_bytes(const sppm_ctx* ctx);
+int sppm_save_checkpoint(sppm_ctx* ctx, void* dst, size_t bytes);
+int sppm_load_checkpoint(sppm_ctx* ctx, const void* src, size_t bytes);
 /* While enabled, the photon pass also counts BVH nodes visited and triangles tested (a separate
    kernel instantiation; results are unchanged).  Used for the algorithmic-byte roofline. */
 int sppm_enable_traversal_counters(sppm_ctx* ctx, int enable);

@@ -68,6 +68,11 @@ size_t sppm_batch_state_bytes(const sppm_batch* b, uint32_t job, uint32_t kind);
 int sppm_batch_read_state(sppm_batch* b, uint32_t job, uint32_t kind, void* dst, size_t bytes);
 int sppm_batch_get_frame_info(sppm_batch* b, uint32_t job, sppm_frame_info* info);
 int sppm_batch_get_info(sppm_batch* b, sppm_batch_info* info);
+/* Checkpoints of one job (the layout of sppm_save_checkpoint): a job can move between a batch
+   and a single-job context, or be preempted and resumed. */
+size_t sppm_batch_checkpoint_bytes(const sppm_batch* b, uint32_t job);
+int sppm_batch_save_checkpoint(sppm_batch* b, uint32_t job, void* dst, size_t bytes);
+int sppm_batch_load_checkpoint(sppm_batch* b, uint32_t job, const void* src, size_t bytes);
 
 int sppm_batch_set_stage_timing_mask(sppm_batch* b, uint32_t mask);
 int sppm_batch_read_stage_times(sppm_batch* b, float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]);
