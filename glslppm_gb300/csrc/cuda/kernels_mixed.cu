@@ -32,20 +32,19 @@ constexpr int kTraceBlock = 128;
 constexpr int kSmemStack = 16;  // top of each thread's stack, in shared memory (16 KB per block)
 constexpr int kLocalStack = kStack - kSmemStack;  // deeper entries, in local memory (rarely touched)
 
+// slab distances of child K's box: plane = origin + byte * 2^e, so its distance along the ray is
+// byte * (2^e / d) + (origin - o) / d = fmaf(byte, A, B) with the per-node A = 2^e * (1/d) (exact:
+// a power-of-two scale) and B = fmaf(origin, 1/d, -o/d)
 template <int K>
-__device__ __forceinline__ void child_box(const float4& w0, const float4& w2, const float4& w3, float sx, float sy,
-                                          float sz, float rx, float ry, float rz, float nx, float ny, float nz,
-                                          float tbest, float& tn, bool& hit) {
+__device__ __forceinline__ void child_box(const float4& w2, const float4& w3, float Ax, float Ay, float Az, float Bx,
+                                          float By, float Bz, float tbest, float& tn, bool& hit) {
     constexpr uint32_t sel = 0x7650u | (uint32_t)K;  // byte K of the word into byte 0, 0x4B into byte 3
-    const float lx = fmaf(byte_f(__float_as_uint(w2.x), sel), sx, w0.x);
-    const float ly = fmaf(byte_f(__float_as_uint(w2.y), sel), sy, w0.y);
-    const float lz = fmaf(byte_f(__float_as_uint(w2.z), sel), sz, w0.z);
-    const float hx = fmaf(byte_f(__float_as_uint(w2.w), sel), sx, w0.x);
-    const float hy = fmaf(byte_f(__float_as_uint(w3.x), sel), sy, w0.y);
-    const float hz = fmaf(byte_f(__float_as_uint(w3.y), sel), sz, w0.z);
-    const float ax = fmaf(lx, rx, nx), bx = fmaf(hx, rx, nx);
-    const float ay = fmaf(ly, ry, ny), by = fmaf(hy, ry, ny);
-    const float az = fmaf(lz, rz, nz), bz = fmaf(hz, rz, nz);
+    const float ax = fmaf(byte_f(__float_as_uint(w2.x), sel), Ax, Bx);
+    const float ay = fmaf(byte_f(__float_as_uint(w2.y), sel), Ay, By);
+    const float az = fmaf(byte_f(__float_as_uint(w2.z), sel), Az, Bz);
+    const float bx = fmaf(byte_f(__float_as_uint(w2.w), sel), Ax, Bx);
+    const float by = fmaf(byte_f(__float_as_uint(w3.x), sel), Ay, By);
+    const float bz = fmaf(byte_f(__float_as_uint(w3.y), sel), Az, Bz);
     const float t0 = fmaxf(fmax3(fminf(ax, bx), fminf(ay, by), fminf(az, bz)), 0.0f);
     // the far bound widened by a few ulps so that rounding never rejects a grazing hit
     const float t1 = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fmaxf(az, bz)) * 1.00000036f;
@@ -141,10 +140,12 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
             const int cnt = (int)(eb >> 24);
             float t[4];
             bool hit[4];
-            child_box<0>(w0, w2, w3, sx, sy, sz, rx, ry, rz, nx, ny, nz, ht, t[0], hit[0]);
-            child_box<1>(w0, w2, w3, sx, sy, sz, rx, ry, rz, nx, ny, nz, ht, t[1], hit[1]);
-            child_box<2>(w0, w2, w3, sx, sy, sz, rx, ry, rz, nx, ny, nz, ht, t[2], hit[2]);
-            child_box<3>(w0, w2, w3, sx, sy, sz, rx, ry, rz, nx, ny, nz, ht, t[3], hit[3]);
+            const float Ax = sx * rx, Ay = sy * ry, Az = sz * rz;
+            const float Bx = fmaf(w0.x, rx, nx), By = fmaf(w0.y, ry, ny), Bz = fmaf(w0.z, rz, nz);
+            child_box<0>(w2, w3, Ax, Ay, Az, Bx, By, Bz, ht, t[0], hit[0]);
+            child_box<1>(w2, w3, Ax, Ay, Az, Bx, By, Bz, ht, t[1], hit[1]);
+            child_box<2>(w2, w3, Ax, Ay, Az, Bx, By, Bz, ht, t[2], hit[2]);
+            child_box<3>(w2, w3, Ax, Ay, Az, Bx, By, Bz, ht, t[3], hit[3]);
             int32_t c[4] = {__float_as_int(w1.x), __float_as_int(w1.y), __float_as_int(w1.z), __float_as_int(w1.w)};
 #pragma unroll
             for (int k = 0; k < 4; k++) {
