@@ -126,16 +126,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def profile_traffic(kernel: str):
-    """Per-launch DRAM traffic of `kernel` on this workload, from its committed ncu summary."""
-    p = REPO / "profiles" / f"{kernel}_cornell1024.md"
+def profile_traffic(kernel: str, workload: str = "cornell1024"):
+    """Per-launch DRAM traffic of `kernel` on a workload, from the committed ncu summary
+    (profiles/<kernel>_<workload>.md; the large-mesh summary covers both traversal kernels)."""
+    name = f"{kernel}_{workload}.md" if workload == "cornell1024" else f"k_trace_photons_{workload}.md"
+    p = REPO / "profiles" / name
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
         if line.startswith("traffic_bytes_per_launch:"):
             try:
+                if kernel == "k_trace_photons4" and workload != "cornell1024":
+                    return float(line.split("k_trace_photons4:", 1)[1].split(")")[0])
                 return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
+            except (ValueError, IndexError):
                 return None
     return None
 
@@ -600,9 +604,10 @@ def run_large_line(args, rank, world, local):
     if cnt and tr_n:
         bpl = cnt["photon_segments"] / cnt["passes"] * (64 + 32 * cnt["nodes_per_segment"] + 36 * cnt["tris_per_segment"])
         achieved = bpl / (tr_ms / tr_n / 1000.0) / 1e9
+        kname = "k_trace_photons4" if prec == N.PRECISION_MIXED else "k_trace_photons"
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None,
-                "kernel": "k_trace_photons4" if prec == N.PRECISION_MIXED else "k_trace_photons",
+                "frac": round(achieved / peak, 4), "traffic": profile_traffic(kname, "largemesh"),
+                "kernel": kname,
                 "peak_kind": peak_kind, "nodes_per_segment": round(cnt["nodes_per_segment"], 2),
                 "tris_per_segment": round(cnt["tris_per_segment"], 2), "algorithmic_bytes_per_launch": round(bpl)}
     if rank == 0:
