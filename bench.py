@@ -340,6 +340,8 @@ def run_gpu(args, rank, world, local):
                            parallelism=f"replicas x{world}"),
             "mrays_per_s": round(mrays, 3),
             "stage_ms_per_launch": {k: round(v[0] / v[1], 4) for k, v in stages.items() if v[1]},
+            "stage_bandwidth": stage_bandwidth(stages, npix, P, (fi1.photon_segments - fi0.photon_segments) / K,
+                                               peak),
             "gpu_launches": int(launches),
             "e2e": {"value": round(e2e, 3), "unit": "Mphotons/s", "h2d_bytes_per_step": 64,
                     "d2h_bytes_per_step": int(npix * 3 * 4), "steps": E},
@@ -698,6 +700,24 @@ def run_batched_line(args, rank, world, local):
             "clocks": clocks.summary(), "setup_seconds": res["setup_seconds"],
         }
         print(json.dumps(line), flush=True)
+
+
+def stage_bandwidth(stages: dict, npix: int, photon_slots: int, segments_per_pass: float, peak: float) -> dict:
+    """Algorithmic bytes over event-timed launch duration for the memory-bound stages:
+    gather + update 472 B per pixel (40 B hit point, 8 x (8 B slot + 36 B photon), 80 B of
+    statistics read and written), photon store + hash insert 28 B per stored segment (16 B position
+    and validity, 4 B key, 8 B atomics) plus the 48-byte photon record written, ray binning 12 B
+    per queued ray."""
+    out = {}
+    units = {"gather": (npix, 472.0), "photon_store": (segments_per_pass, 28.0 + 48.0),
+             "ray_bins": (segments_per_pass, 12.0)}
+    for name, (n, per) in units.items():
+        ms, cnt = stages.get(name, (0.0, 0))
+        if cnt and ms > 0:
+            gbs = n * per / (ms / cnt / 1000.0) / 1e9
+            out[name] = {"bytes_per_unit": per, "units": int(n), "achieved_gbs": round(gbs, 1),
+                         "frac": round(gbs / peak, 4)}
+    return out
 
 
 def traversal_counters(r):
