@@ -600,6 +600,12 @@ Runner::~Runner() {
     for (auto e : event_pool) cudaEventDestroy(e);
     for (auto e : placeholder)
         if (e) cudaEventDestroy(e);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
+    if (side) {
+        cudaStreamSynchronize(side);
+        cudaStreamDestroy(side);
+    }
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -611,6 +617,9 @@ int Runner::init(int dev, uint32_t prec, uint32_t fl, uint32_t interval, uint32_
     max_jobs = jobs_max;
     SPPM_CK(cudaSetDevice(device));
     SPPM_CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    SPPM_CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    SPPM_CK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    SPPM_CK(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
     int st = desc_mem.reserve(Arena::align(sizeof(JobDesc) * std::max<uint32_t>(max_jobs, 1)));
     if (st) return st;
     d_jobs = desc_mem.take<JobDesc>(std::max<uint32_t>(max_jobs, 1));
@@ -734,18 +743,20 @@ cudaEvent_t Runner::get_event() {
 
 // start or end of a timed stage: while a frame graph is being captured, an event record node
 // with a placeholder event; otherwise a pooled event recorded on the stream
-void Runner::timed(int stage, bool start) {
+void Runner::timed(int stage, bool start, cudaStream_t s) {
     if (!((timing_mask >> stage) & 1u)) return;
+    if (!s) s = stream;
     if (capturing) {
-        cudaEventRecordWithFlags(placeholder[2 * stage + (start ? 0 : 1)], stream, cudaEventRecordExternal);
+        cudaEventRecordWithFlags(placeholder[2 * stage + (start ? 0 : 1)], s, cudaEventRecordExternal);
         return;
     }
     if (start) {
         StageEvent e{stage, get_event(), get_event()};
-        cudaEventRecord(e.a, stream);
+        cudaEventRecord(e.a, s);
+        open_stage[stage] = pending.size();
         pending.push_back(e);
     } else {
-        cudaEventRecord(pending.back().b, stream);
+        cudaEventRecord(pending[open_stage[stage]].b, s);
     }
 }
 
@@ -754,16 +765,23 @@ int Runner::enqueue_frame(uint32_t phase) {
     timed(SPPM_STAGE_FRAME_BEGIN, true);
     launch_frame_begin(hsh, queue, stream);
     timed(SPPM_STAGE_FRAME_BEGIN, false);
-    if (phase_has_eye(phase)) {
-        timed(SPPM_STAGE_EYE, true);
-        launch_eye(eye_pix[phase], precision == SPPM_PRECISION_MIXED, stream);
-        timed(SPPM_STAGE_EYE, false);
-        timed(SPPM_STAGE_GRID, true);
-        launch_grid(d_jobs, eye_ids[phase], eye_pix[phase].njobs, stream);
-        timed(SPPM_STAGE_GRID, false);
+    // the eye pass and the grid it sets run beside the photon generation and traversal (which do
+    // not read them); the photon store (hash insertion) waits for the grid
+    const bool eye = phase_has_eye(phase);
+    if (eye) {
+        SPPM_CK(cudaEventRecord(fork_ev, stream));
+        SPPM_CK(cudaStreamWaitEvent(side, fork_ev, 0));
+        timed(SPPM_STAGE_EYE, true, side);
+        launch_eye(eye_pix[phase], precision == SPPM_PRECISION_MIXED, side);
+        timed(SPPM_STAGE_EYE, false, side);
+        timed(SPPM_STAGE_GRID, true, side);
+        launch_grid(d_jobs, eye_ids[phase], eye_pix[phase].njobs, side);
+        timed(SPPM_STAGE_GRID, false, side);
+        SPPM_CK(cudaEventRecord(join_ev, side));
     }
     const bool mixed = precision == SPPM_PRECISION_MIXED;
     if ((flags & SPPM_FLAG_FUSED_PHOTON) && !mixed) {
+        if (eye) SPPM_CK(cudaStreamWaitEvent(stream, join_ev, 0));
         timed(SPPM_STAGE_PHOTON, true);
         launch_photon_fp32(pho, count_traversal, stream);
         timed(SPPM_STAGE_PHOTON, false);
@@ -780,6 +798,7 @@ int Runner::enqueue_frame(uint32_t phase) {
         if (mixed) launch_trace_photons4(pho, queue, trace_blocks, stream);
         else launch_trace_photons_fp32(pho, queue, count_traversal, trace_blocks, stream);
         timed(SPPM_STAGE_PHOTON_TRACE, false);
+        if (eye) SPPM_CK(cudaStreamWaitEvent(stream, join_ev, 0));
         timed(SPPM_STAGE_PHOTON_STORE, true);
         launch_photon_store_fp32(pho, queue, stream);
         if (mixed) launch_slot_fill(pho, queue, stream);

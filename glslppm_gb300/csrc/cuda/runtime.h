@@ -123,6 +123,8 @@ struct FrameGraph {
 struct Runner {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;             // the eye pass's branch, forked from and joined to stream
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     uint32_t precision = SPPM_PRECISION_FP32, flags = 0, eye_interval = 10, max_jobs = 0;
     Arena desc_mem;                // JobDesc[max_jobs]
     JobDesc* d_jobs = nullptr;
@@ -140,6 +142,7 @@ struct Runner {
     uint32_t timing_mask = 0;  // bit k: time stage k
     bool count_traversal = false;
     std::vector<StageEvent> pending;
+    size_t open_stage[SPPM_STAGE_COUNT] = {0};  // pending entry of each stage's last start
     std::vector<cudaEvent_t> event_pool;
     float stage_ms[SPPM_STAGE_COUNT] = {0};
     uint32_t stage_launches[SPPM_STAGE_COUNT] = {0};
@@ -161,7 +164,7 @@ struct Runner {
     int read_stage_times(float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]);
     int resolve(Job& j, uint32_t kind);
     cudaEvent_t get_event();
-    void timed(int stage, bool start);
+    void timed(int stage, bool start, cudaStream_t s = nullptr);
 
   private:
     int enqueue_frame(uint32_t phase);
