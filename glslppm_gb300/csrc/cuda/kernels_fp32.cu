@@ -810,7 +810,10 @@ __global__ void k_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t nj
 // ----------------------------------------------------------------------------------------------
 // k_photon: photontrace.fs main (:464-720), sum.fs, hash.fs + scatter.vs + correction.vs
 // ----------------------------------------------------------------------------------------------
-__device__ __forceinline__ void light_sample(const JobDesc& J, float4& rndv, f3& flux, f3& dir, f3& org, uint32_t& err) {
+// GenerateLightSourceSample (photontrace.fs:345-440) up to its cosine lobe: the origin, the flux and
+// the lobe's normal (the lobe itself is cosine_lobe, drawn right after, shared with the bounces)
+__device__ __forceinline__ void light_sample(const JobDesc& J, float4& rndv, f3& flux, f3& lobe_n, f3& org,
+                                             uint32_t& err) {
     const DevScene& S = J.scene;
     const float rnd = gpu_rnd(rndv);
     int low = 0;
@@ -846,12 +849,15 @@ __device__ __forceinline__ void light_sample(const JobDesc& J, float4& rndv, f3&
     const f3 nrm = normalize(add(add(scl(N0, a), scl(N1, b)), scl(N2, c)));
     const f3 gnrm = mk(r0.x, r0.y, r0.z);
     o = add(o, scl(gnrm, 1.0e-5f));
-    float rx = gpu_rnd(rndv);
-    float ry = gpu_rnd(rndv);
-    rx = xmul(6.283184f, rx);
-    ry = xsqrt(ry);
-    dir = onb(mk(xmul(sppm_fsin(rx), ry), xsqrt(xsub(1.0f, xmul(ry, ry))), xmul(sppm_fcos(rx), ry)), nrm);
+    lobe_n = nrm;
     org = o;
+}
+
+// cosine lobe around n (photontrace.fs:432-439 for emission, :567-578 for matte bounces): two draws
+__device__ __forceinline__ f3 cosine_lobe(float4& rndv, f3 n) {
+    const float r0 = xmul(6.283184f, gpu_rnd(rndv));
+    const float r1 = xsqrt(gpu_rnd(rndv));
+    return onb(mk(xmul(sppm_fsin(r0), r1), xsqrt(xsub(1.0f, xmul(r1, r1))), xmul(sppm_fcos(r0), r1)), n);
 }
 
 __device__ __forceinline__ void ibl_sample(const JobDesc& J, float4& rndv, f3& flux, f3& dir, f3& org) {
@@ -878,15 +884,6 @@ __device__ __forceinline__ void ibl_sample(const JobDesc& J, float4& rndv, f3& f
     dir = neg(d);
 }
 
-__device__ __forceinline__ void matte_bounce(float4& rndv, f3 ipos, f3 gnrm, f3 inrm, float eps, f3& rorg, f3& rdir) {
-    const float r0 = xmul(6.283184f, gpu_rnd(rndv));
-    const float r1 = xsqrt(gpu_rnd(rndv));
-    const f3 v = mk(xmul(sppm_fsin(r0), r1), xsqrt(xsub(1.0f, xmul(r1, r1))), xmul(sppm_fcos(r0), r1));
-    rorg = add(ipos, scl(gnrm, eps));
-    rdir = onb(v, inrm);
-    if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
-}
-
 // emit a photon or bounce the stored one (photontrace.fs main :464-686): the ray of this pass
 struct PhotonRay {
     f3 org, dir, flux;
@@ -897,6 +894,9 @@ struct PhotonRay {
 
 __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t sidx, uint32_t frame, float4& rndv,
                                                      uint32_t& err) {
+    // Emission and the diffuse bounces end in the same cosine lobe: each path sets up its lobe
+    // (normal, origin; the draws before the lobe stay in the path) and the lanes draw the lobe
+    // together, then finish their path (the flip against the geometric normal, Russian roulette).
     const DevScene& S = J.scene;
     const float eps = 1e-6f;
     PhotonRay R;
@@ -906,35 +906,65 @@ __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t 
     // the previous segment's record, loaded with the hit (a bounce needs it; an emission does not)
     const float4 PP = J.ph.pos[sidx], PF = J.ph.flux[sidx], PD = J.ph.dir[sidx];
     R.depth = xadd((float)hitin.y, 1.0f);
-    if (hitin.x < 0 || R.depth >= (float)J.max_path) {
-        if (S.light_area != 0.0f) light_sample(J, rndv, R.flux, R.dir, R.org, err);
-        else ibl_sample(J, rndv, R.flux, R.dir, R.org);
-        R.emitted = 1;
-        R.depth = 0.0f;
-        R.cont = true;
-        return R;
-    }
-    f3 flux = mk(fabsf(PF.x), fabsf(PF.y), fabsf(PF.z));
-    const f3 ipos = xyz(PP);
-    f3 inrm = mk(PP.w, PF.w, PD.w);
-    const f3 pd = xyz(PD);
-    const float4 r0 = __ldg(S.tri_shade + (size_t)hitin.x * 6);
-    const f3 gnrm = mk(r0.x, r0.y, r0.z);
-    const DevMaterial& m = S.mats[__float_as_int(r0.w)];
-    f3 icol = mk(m.color[0], m.color[1], m.color[2]);
-    const int brdf = m.brdf;
+    const bool emit = hitin.x < 0 || R.depth >= (float)J.max_path;
+    bool lobe = false, flip = false;
+    f3 lobe_n = mk(0, 0, 0), gnrm = mk(0, 0, 0), icol = mk(0, 0, 0), flux = mk(0, 0, 0);
     f3 rorg = mk(0, 0, 0), rdir = mk(0, 0, 0);
-    if (brdf == 0) {
-        matte_bounce(rndv, ipos, gnrm, inrm, eps, rorg, rdir);
-    } else if (brdf == 1 || brdf == 4) {
-        rorg = add(ipos, scl(gnrm, eps));
-        if (brdf == 4) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
-        rdir = reflect(pd, inrm);
-        if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
-    } else if (brdf == 2 || brdf == 5) {
-        if (brdf == 5) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
-        const float ln = dot(inrm, pd);
-        if (ln < 0.0f) {
+    if (emit) {
+        if (S.light_area != 0.0f) {
+            light_sample(J, rndv, R.flux, lobe_n, rorg, err);
+            lobe = true;
+        } else {
+            ibl_sample(J, rndv, R.flux, rdir, rorg);
+        }
+    } else {
+        flux = mk(fabsf(PF.x), fabsf(PF.y), fabsf(PF.z));
+        const f3 ipos = xyz(PP);
+        f3 inrm = mk(PP.w, PF.w, PD.w);
+        const f3 pd = xyz(PD);
+        const float4 r0 = __ldg(S.tri_shade + (size_t)hitin.x * 6);
+        gnrm = mk(r0.x, r0.y, r0.z);
+        const DevMaterial& m = S.mats[__float_as_int(r0.w)];
+        icol = mk(m.color[0], m.color[1], m.color[2]);
+        const int brdf = m.brdf;
+        if (brdf == 0) {
+            rorg = add(ipos, scl(gnrm, eps));  // matte_bounce
+            lobe_n = inrm;
+            lobe = flip = true;
+        } else if (brdf == 1 || brdf == 4) {
+            rorg = add(ipos, scl(gnrm, eps));
+            if (brdf == 4) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
+            rdir = reflect(pd, inrm);
+            if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
+        } else if (brdf == 2 || brdf == 5) {
+            if (brdf == 5) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
+            const float ln = dot(inrm, pd);
+            if (ln < 0.0f) {
+                const float re = fresnel(neg(pd), inrm, 1.0f, m.eta);
+                if (gpu_rnd(rndv) < re) {
+                    rorg = add(ipos, scl(gnrm, eps));
+                    rdir = reflect(pd, inrm);
+                    icol = mk(1.0f, 1.0f, 1.0f);
+                    if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
+                } else {
+                    rorg = sub(ipos, scl(gnrm, eps));
+                    rdir = refract(pd, inrm, xdiv(1.0f, m.eta));
+                    if (dot(rdir, gnrm) > 0.0f) rdir = neg(rdir);
+                }
+            } else {
+                const float re = fresnel(neg(pd), neg(inrm), m.eta, 1.0f);
+                if (gpu_rnd(rndv) < re) {
+                    rorg = sub(ipos, scl(gnrm, eps));
+                    rdir = reflect(pd, neg(inrm));
+                    if (dot(rdir, neg(gnrm)) < 0.0f) rdir = neg(rdir);
+                } else {
+                    rorg = add(ipos, scl(gnrm, eps));
+                    rdir = refract(pd, neg(inrm), m.eta);
+                    if (dot(rdir, neg(gnrm)) > 0.0f) rdir = neg(rdir);
+                }
+            }
+        } else if (brdf == 3 || brdf == 6) {
+            if (brdf == 6) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
             const float re = fresnel(neg(pd), inrm, 1.0f, m.eta);
             if (gpu_rnd(rndv) < re) {
                 rorg = add(ipos, scl(gnrm, eps));
@@ -942,33 +972,23 @@ __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t 
                 icol = mk(1.0f, 1.0f, 1.0f);
                 if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
             } else {
-                rorg = sub(ipos, scl(gnrm, eps));
-                rdir = refract(pd, inrm, xdiv(1.0f, m.eta));
-                if (dot(rdir, gnrm) > 0.0f) rdir = neg(rdir);
-            }
-        } else {
-            const float re = fresnel(neg(pd), neg(inrm), m.eta, 1.0f);
-            if (gpu_rnd(rndv) < re) {
-                rorg = sub(ipos, scl(gnrm, eps));
-                rdir = reflect(pd, neg(inrm));
-                if (dot(rdir, neg(gnrm)) < 0.0f) rdir = neg(rdir);
-            } else {
-                rorg = add(ipos, scl(gnrm, eps));
-                rdir = refract(pd, neg(inrm), m.eta);
-                if (dot(rdir, neg(gnrm)) > 0.0f) rdir = neg(rdir);
+                rorg = add(ipos, scl(gnrm, eps));  // matte_bounce
+                lobe_n = inrm;
+                lobe = flip = true;
             }
         }
-    } else if (brdf == 3 || brdf == 6) {
-        if (brdf == 6) inrm = glossy_reflect(inrm, inrm, m.g, rndv);
-        const float re = fresnel(neg(pd), inrm, 1.0f, m.eta);
-        if (gpu_rnd(rndv) < re) {
-            rorg = add(ipos, scl(gnrm, eps));
-            rdir = reflect(pd, inrm);
-            icol = mk(1.0f, 1.0f, 1.0f);
-            if (dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
-        } else {
-            matte_bounce(rndv, ipos, gnrm, inrm, eps, rorg, rdir);
-        }
+    }
+    if (lobe) {
+        rdir = cosine_lobe(rndv, lobe_n);
+        if (flip && dot(rdir, gnrm) < 0.0f) rdir = neg(rdir);
+    }
+    R.org = rorg;
+    R.dir = rdir;
+    if (emit) {
+        R.emitted = 1;
+        R.depth = 0.0f;
+        R.cont = true;
+        return R;
     }
     // Russian roulette (:671-685)
     const float pmax = fmaxf(fmaxf(icol.x, icol.y), icol.z);
@@ -980,8 +1000,6 @@ __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t 
         flux = mul(flux, icol);
     }
     R.emitted = 0;
-    R.org = rorg;
-    R.dir = rdir;
     R.flux = flux;
     return R;
 }
