@@ -312,9 +312,26 @@ int Job::init(const sppm_config& c, JobDesc* dd, uint32_t sl, cudaStream_t s) {
     return reset(s);
 }
 
+Job::~Job() {
+    for (int k = 0; k < 4; k++) {
+        if (stage_used[k]) cudaEventSynchronize(stage_ev[k]);
+        if (stage_ev[k]) cudaEventDestroy(stage_ev[k]);
+    }
+    if (stage) cudaFreeHost(stage);
+}
+
+// queues the upload of the host descriptor on s through a pinned staging slot (no stream sync)
 int Job::write_desc(cudaStream_t s) {
-    SPPM_CK(cudaMemcpyAsync(d_desc, &desc, sizeof(JobDesc), cudaMemcpyHostToDevice, s));
-    SPPM_CK(cudaStreamSynchronize(s));  // the host copy may change right after this call
+    if (!stage) {
+        SPPM_CK(cudaMallocHost(&stage, 4 * sizeof(JobDesc)));
+        for (auto& e : stage_ev) SPPM_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const uint32_t k = stage_next++ & 3u;
+    if (stage_used[k]) SPPM_CK(cudaEventSynchronize(stage_ev[k]));
+    stage[k] = desc;
+    SPPM_CK(cudaMemcpyAsync(d_desc, &stage[k], sizeof(JobDesc), cudaMemcpyHostToDevice, s));
+    SPPM_CK(cudaEventRecord(stage_ev[k], s));
+    stage_used[k] = true;
     return SPPM_OK;
 }
 
@@ -439,7 +456,6 @@ int Job::set_camera(const sppm_camera* cam, cudaStream_t s) {
     J.cam_cy = (float)cam->height * 0.5f;
     J.cam_dist = cam->distance;
     have_camera = true;
-    SPPM_CK(cudaStreamSynchronize(s));
     return write_desc(s);
 }
 

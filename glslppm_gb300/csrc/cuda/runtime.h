@@ -72,6 +72,16 @@ struct Job {
     uint32_t slot = 0;
     bool have_scene = false, have_camera = false;
     float fixed_radius = 0.0f;
+    // pinned staging slots for descriptor uploads, so that a camera change is queued without
+    // waiting for the frames already queued (slot k is reused once its copy has run)
+    JobDesc* stage = nullptr;
+    cudaEvent_t stage_ev[4] = {};
+    bool stage_used[4] = {};
+    uint32_t stage_next = 0;
+    Job() = default;
+    Job(const Job&) = delete;
+    Job& operator=(const Job&) = delete;
+    ~Job();
     int64_t start_frame = 0;       // runner frame at which the job's frame 0 is (or was) queued;
                                    // negative for a job resumed with more frames than the runner
     // the runner phase (frame mod interval) at which this job's eye passes fall
