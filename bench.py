@@ -14,6 +14,15 @@ geometry); the reference publishes no number for this workload.
   roofline  the photon-trace kernel against the measured HBM copy bandwidth.
   cpu_baseline  the CPU oracle (C restatement of the shaders, OpenMP) on the host cores.
 
+The same line carries the other configurations' summaries (each can be skipped, and each is the
+headline of its own --workload run):
+  batched  64 seeded Cornell variants advanced as one batch, against the plain FP32 single-job
+           path looped over the same jobs (--no-batched; --workload batched)
+  large    the 4.1M-triangle displaced sphere + heightfield at 1920x1080, 2^21 photons per pass,
+           BVH built on the GPU (--no-large; --workload large)
+  serving  Poisson arrivals of requests into the continuous-batching server, p50/p99 time to
+           target per arrival rate (--no-serving; --workload serving)
+
 --impl reference: the reference's GLSL pipeline cannot run on this machine (no OpenGL stack), so the
 reference arm times the CPU restatement of the reference's shader path (the oracle) on all host
 cores, on the same workload, a bounded number of passes.
@@ -354,6 +363,17 @@ def run_gpu(args, rank, world, local):
         res = run_batched(args, dev, args.batch_steps, W, prec)
         if rank == 0:
             out["batched"] = {k: v for k, v in res.items() if not k.startswith("_")}
+    if not args.no_large:
+        ln = run_large(args, world, dev, args.large_steps, W)
+        if rank == 0:
+            out["large"] = {k: ln[k] for k in ("value", "unit", "steps", "ms_per_step", "mrays_per_s", "config",
+                                                "stage_ms_per_launch", "setup_seconds", "e2e", "roofline")}
+    if not args.no_serving:
+        rows = run_serving(args, dev)
+        if rank == 0:
+            out["serving"] = {"config": dict(SERVING, precision=args.precision, rates=args.serve_rates,
+                                             requests_per_rate=args.serve_requests,
+                                             passes_per_request=args.serve_passes), "by_rate": rows}
     if rank == 0:
         print(json.dumps(out), flush=True)
     return out
@@ -532,6 +552,13 @@ LARGE = {"workload": "large-mesh", "triangles": "4.1M (displaced geodesic sphere
 
 def run_large_line(args, rank, world, local):
     """--workload large: the large-mesh scene at 1920x1080 with 2^21 photons per pass."""
+    line = run_large(args, world, local, args.steps, args.warmup)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_large(args, world, local, K, W):
+    """The large-mesh workload's JSON line (every rank measures; rank 0 prints)."""
     import glslppm_gb300 as g
     from glslppm_gb300 import native as N, scenes
     prec = N.PRECISION_MIXED if args.precision == "mixed" else N.PRECISION_FP32
@@ -550,7 +577,6 @@ def run_large_line(args, rank, world, local):
     r.upload_scene(mesh)
     t_up = time.perf_counter() - t2
     r.set_camera(cam)
-    K, W = args.steps, args.warmup
     clocks = ClockSampler(local).__enter__()
     r.run_passes(W)
     fi0 = r.frame_info()
@@ -612,7 +638,8 @@ def run_large_line(args, rank, world, local):
                 "kernel": kname,
                 "peak_kind": peak_kind, "nodes_per_segment": round(cnt["nodes_per_segment"], 2),
                 "tris_per_segment": round(cnt["tris_per_segment"], 2), "algorithmic_bytes_per_launch": round(bpl)}
-    if rank == 0:
+    r.close()
+    if True:
         line = {
             "metric": "SPPM Mphotons/s + Mrays/s at fixed RMSE vs FP64 oracle, plain vs batched",
             "value": round(value, 3), "unit": "Mphotons/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -628,7 +655,7 @@ def run_large_line(args, rank, world, local):
                     "d2h_bytes_per_step": int(cfg.width * cfg.height * 12), "steps": E},
             "roofline": roof, "cpu_baseline": None, "clocks": clocks.summary(),
         }
-        print(json.dumps(line), flush=True)
+    return line
 
 
 def run_serving_line(args, rank, world, local):
@@ -741,10 +768,13 @@ def main():
                     help="the JSON line's headline workload; the default line also carries the batched "
                          "workload's summary under 'batched' unless --no-batched")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--large-steps", type=int, default=20)
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=100)
-    ap.add_argument("--serve-rates", default="1,10,50,200")
-    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-rates", default="10,200")
+    ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-pool", type=int, default=32)
     ap.add_argument("--serve-passes", type=int, default=256)
     args = ap.parse_args()
