@@ -127,19 +127,24 @@ struct JobDesc {
 constexpr uint32_t kRayDirClasses = 24;
 constexpr uint32_t kRayCellBits = 3;
 constexpr uint32_t kRayBins = kRayDirClasses << (3 * kRayCellBits);
+// eye pixels whose path the exact eye pass defers to its block-wide pass per frame (beyond it
+// the per-thread walk traces them)
+constexpr uint32_t kEyeDeferred = 4096;
 
 // ray queue of the wavefront photon pass: org.w holds the photon's global item index
 struct RayQueue {
     float4* org;
     float4* dir;
     float4* hit;          // (triangle or -1 as int bits, barycentrics v, w, u)
-    uint32_t* counters;   // [0] rays queued, [1] fetch head of the trace kernel, [2] rays set aside
+    uint32_t* counters;   // [0] rays queued, [1] fetch head of the trace kernel, [2] rays set aside,
+                          // [3] eye pixels deferred
     uint32_t capacity;
     uint32_t* slow;       // [capacity] queue indices of the rays traced one per warp
     // binning (all null when the rays are traced in queue order)
     uint2* key;           // [capacity] (bin, rank within the bin)
     uint32_t* bins;       // [kRayBins] counts, then exclusive offsets
     uint32_t* perm;       // [capacity] queue index of the i-th ray in bin order
+    uint32_t* eye_deferred;  // [kEyeDeferred] launch indices of the deferred eye pixels
 };
 
 // the work of one launch: items [prefix[k], prefix[k+1]) belong to jobs[job_ids[k]]

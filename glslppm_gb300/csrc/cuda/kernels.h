@@ -9,7 +9,7 @@ namespace sppm_dev {
 
 // plain FP32 path (kernels_fp32.cu)
 void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
-void launch_eye(const LaunchSet& ls, bool mixed, cudaStream_t s);  // mixed: 4-wide BVH traversal
+void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, cudaStream_t s);  // mixed: 4-wide BVH traversal
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s);
 void launch_photon_fp32(const LaunchSet& ls, bool count_traversal, cudaStream_t s);
 void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);

@@ -585,6 +585,7 @@ __global__ void k_frame_begin(LaunchSet ls, RayQueue q) {
         q.counters[0] = 0;
         q.counters[1] = 0;
         q.counters[2] = 0;
+        q.counters[3] = 0;
     }
     if (q.bins && g < kRayBins) q.bins[g] = 0u;
     if (g >= ls.total) return;
@@ -649,17 +650,20 @@ __device__ __forceinline__ Hit trace_eye4(const DevScene& s, f3 org, f3 dir, boo
     return h;
 }
 
-template <bool MIXED>
-__global__ void __launch_bounds__(128) k_eye(LaunchSet ls) {
-    const uint32_t g = grid_tid();
-    if (g >= ls.total) return;
-    const int k = find_job(ls, g);
-    const JobDesc& J = ls.jobs[ls.job_ids[k]];
-    JobState* st = J.state;
-    const uint32_t p = g - ls.prefix[k];
+// the eye path of one pixel (eyeraytrace.fs main :396-554) up to its outputs; `trace(org, dir,
+// cull, hit)` finds the closest hit and may decline (returns false), which abandons the path
+// without side effects so that it can be rerun from its stored state
+struct EyeOut {
+    f3 pos, col, nrm, rdir, emi;
+    float4 rndv;
+    Hit last;
+    uint32_t segs;
+};
+
+template <class Trace>
+__device__ __forceinline__ bool eye_path(const JobDesc& J, const JobState* st, uint32_t p, Trace&& trace, EyeOut& out) {
     const uint32_t px = p % J.W, py = p / J.W;
     const DevScene& S = J.scene;
-    uint32_t err = 0;
     float4 rndv = J.px.rng[p];
     const float eps = 1e-5f;
     const f3 U = mk(J.cam_u[0], J.cam_u[1], J.cam_u[2]);
@@ -687,7 +691,8 @@ __global__ void __launch_bounds__(128) k_eye(LaunchSet ls) {
     last.t = 1.0e20f;
     uint32_t segs = 0;
     for (uint32_t j = 0; j < J.max_path; j++) {
-        const Hit h = MIXED ? trace_eye4(S, rorg, rdir, j == 0, err) : trace_exact<false>(S, rorg, rdir, j == 0, err);
+        Hit h;
+        if (!trace(rorg, rdir, j == 0, h)) return false;  // deferred to the block-wide pass
         last = h;
         segs++;
         if (h.tri < 0) {
@@ -752,27 +757,108 @@ __global__ void __launch_bounds__(128) k_eye(LaunchSet ls) {
             }
         }
     }
+    out.pos = pos;
+    out.col = col;
+    out.nrm = nrm;
+    out.rdir = rdir;
+    out.emi = emi;
+    out.rndv = rndv;
+    out.last = last;
+    out.segs = segs;
+    return true;
+}
+
+// the pixel outputs of a finished eye path (the running emission mean of :543-545)
+__device__ __forceinline__ void eye_write(const JobDesc& J, const JobState* st, uint32_t p, const EyeOut& o) {
     float4 qe = J.px.emi_n[p];
     const float a = xdiv(1.0f, (float)st->eye_samples);
     const float oma = xsub(1.0f, a);
-    qe.x = xadd(xmul(qe.x, oma), xmul(emi.x, a));
-    qe.y = xadd(xmul(qe.y, oma), xmul(emi.y, a));
-    qe.z = xadd(xmul(qe.z, oma), xmul(emi.z, a));
-    J.px.pos[p] = f4(pos, rdir.x);
-    J.px.refl[p] = f4(col, rdir.y);
-    J.px.nrm[p] = f4(nrm, rdir.z);
-    J.px.rng[p] = rndv;
-    J.px.tri[p] = last.tri;
-    J.px.t[p] = last.t;
+    qe.x = xadd(xmul(qe.x, oma), xmul(o.emi.x, a));
+    qe.y = xadd(xmul(qe.y, oma), xmul(o.emi.y, a));
+    qe.z = xadd(xmul(qe.z, oma), xmul(o.emi.z, a));
+    J.px.pos[p] = f4(o.pos, o.rdir.x);
+    J.px.refl[p] = f4(o.col, o.rdir.y);
+    J.px.nrm[p] = f4(o.nrm, o.rdir.z);
+    J.px.rng[p] = o.rndv;
+    J.px.tri[p] = o.last.tri;
+    J.px.t[p] = o.last.t;
     J.px.emi_n[p] = qe;
-    warp_bbox_atomics(st, pos, k);
+}
+
+// eye pass, one thread per pixel.  A ray with a zero direction component (slab_degenerate)
+// would walk most of the tree in one lane: the exact path defers such pixels to k_eye_coop
+// (their whole path is rerun there with block-wide walks); the mixed path's slab tests do not
+// degenerate.
+template <bool MIXED>
+__global__ void __launch_bounds__(128) k_eye(LaunchSet ls, uint32_t* deferred_n, uint32_t* deferred,
+                                                uint32_t deferred_cap) {
+    const uint32_t g = grid_tid();
+    if (g >= ls.total) return;
+    const int k = find_job(ls, g);
+    const JobDesc& J = ls.jobs[ls.job_ids[k]];
+    JobState* st = J.state;
+    const uint32_t p = g - ls.prefix[k];
+    uint32_t err = 0;
+    EyeOut o;
+    const bool done = eye_path(J, st, p, [&](f3 org, f3 dir, bool cull, Hit& h) {
+        if (MIXED) {
+            h = trace_eye4(J.scene, org, dir, cull, err);
+            return true;
+        }
+        if (slab_degenerate(dir)) {
+            const uint32_t slot = atomicAdd(deferred_n, 1u);
+            if (slot < deferred_cap) {
+                deferred[slot] = g;
+                return false;
+            }
+        }
+        h = trace_exact<false>(J.scene, org, dir, cull, err);
+        return true;
+    }, o);
+    if (done) eye_write(J, st, p, o);
+    const f3 bpos = done ? o.pos : mk(__int_as_float(0x7FC00000), __int_as_float(0x7FC00000), __int_as_float(0x7FC00000));
+    warp_bbox_atomics(st, bpos, k);  // a deferred pixel contributes nothing (NaN is ignored)
     // segment count and errors: one atomic per warp and job
     const unsigned mask = __match_any_sync(__activemask(), k);
-    const uint32_t wsegs = __reduce_add_sync(mask, segs);
+    const uint32_t wsegs = __reduce_add_sync(mask, done ? o.segs : 0u);
     const uint32_t werr = __reduce_or_sync(mask, err);
     if ((threadIdx.x & 31) == (__ffs(mask) - 1)) {
         atomicAdd(&st->eye_segments, (unsigned long long)wsegs);
         if (werr) atomicOr(&st->err, werr);
+    }
+}
+
+// the deferred pixels of k_eye<false>, one block of 1024 threads per pixel: every thread runs
+// the same path (identical values), each trace is block_trace_exact, thread 0 writes
+__global__ void __launch_bounds__(kBlockWalk) k_eye_coop(LaunchSet ls, const uint32_t* deferred_n,
+                                                         const uint32_t* deferred, uint32_t deferred_cap) {
+    __shared__ BlockWalkShared sh;
+    const uint32_t n = min(*deferred_n, deferred_cap);
+    for (uint32_t w = blockIdx.x; w < n; w += gridDim.x) {
+        const uint32_t g = deferred[w];
+        const int k = find_job(ls, g);
+        const JobDesc& J = ls.jobs[ls.job_ids[k]];
+        JobState* st = J.state;
+        const uint32_t p = g - ls.prefix[k];
+        uint32_t err = 0;
+        EyeOut o;
+        eye_path(J, st, p, [&](f3 org, f3 dir, bool cull, Hit& h) {
+            TraversalCount ct;
+            h = block_trace_exact<false, false>(J.scene, org, dir, cull, err, &ct, sh);
+            return true;
+        }, o);
+        if (threadIdx.x == 0) {
+            eye_write(J, st, p, o);
+            const float v[3] = {o.pos.x, o.pos.y, o.pos.z};
+            for (int c = 0; c < 3; c++) {
+                if (!(v[c] == v[c])) continue;
+                atomicMax(&st->bbmax_key[c], float_key(v[c]));
+                atomicMin(&st->bbmin_key[c], float_key(v[c]));
+            }
+            atomicAdd(&st->eye_segments, (unsigned long long)o.segs);
+            if (err) atomicOr(&st->err, err);
+        }
+        __syncthreads();
     }
 }
 
@@ -1599,10 +1685,15 @@ void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) 
     const uint32_t n = q.bins && ls.total < kRayBins ? kRayBins : ls.total;
     if (ls.total) k_frame_begin<<<blocks_for(n, 256), 256, 0, s>>>(ls, q);
 }
-void launch_eye(const LaunchSet& ls, bool mixed, cudaStream_t s) {
+void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, cudaStream_t s) {
     if (!ls.total) return;
-    if (mixed) k_eye<true><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
-    else k_eye<false><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
+    if (mixed) {
+        k_eye<true><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, nullptr, nullptr, 0);
+        return;
+    }
+    k_eye<false><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q.counters + 3, q.eye_deferred, kEyeDeferred);
+    // a fixed grid (the count is on the device): blocks beyond the deferred pixels exit at once
+    k_eye_coop<<<32, kBlockWalk, 0, s>>>(ls, q.counters + 3, q.eye_deferred, kEyeDeferred);
 }
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s) {
     if (njobs) k_grid<<<blocks_for(njobs, 64), 64, 0, s>>>(jobs, job_ids, njobs);

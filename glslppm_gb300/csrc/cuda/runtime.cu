@@ -724,7 +724,8 @@ int Runner::rebuild() {
     if (cap > queue.capacity || !queue.org) {
         const bool binned = !(flags & SPPM_FLAG_UNBINNED_RAYS);
         const size_t c = std::max<uint32_t>(cap, 1);
-        size_t bytes = 3 * Arena::align(c * 16) + Arena::align(64) + Arena::align(c * 4);
+        size_t bytes = 3 * Arena::align(c * 16) + Arena::align(64) + Arena::align(c * 4) +
+                       Arena::align(kEyeDeferred * 4);
         if (binned) bytes += Arena::align(c * 8) + Arena::align(c * 4) + Arena::align(kRayBins * 4);
         if ((st = queue_mem.reserve(bytes))) return st;
         Arena& a = queue_mem;
@@ -734,6 +735,7 @@ int Runner::rebuild() {
         queue.hit = a.take<float4>(c);
         queue.counters = a.take<uint32_t>(16);
         queue.slow = a.take<uint32_t>(c);
+        queue.eye_deferred = a.take<uint32_t>(kEyeDeferred);
         if (binned) {
             queue.key = a.take<uint2>(c);
             queue.perm = a.take<uint32_t>(c);
@@ -788,7 +790,7 @@ int Runner::enqueue_frame(uint32_t phase) {
         SPPM_CK(cudaEventRecord(fork_ev, stream));
         SPPM_CK(cudaStreamWaitEvent(side, fork_ev, 0));
         timed(SPPM_STAGE_EYE, true, side);
-        launch_eye(eye_pix[phase], precision == SPPM_PRECISION_MIXED, side);
+        launch_eye(eye_pix[phase], queue, precision == SPPM_PRECISION_MIXED, side);
         timed(SPPM_STAGE_EYE, false, side);
         timed(SPPM_STAGE_GRID, true, side);
         launch_grid(d_jobs, eye_ids[phase], eye_pix[phase].njobs, side);

@@ -99,6 +99,27 @@ def test_unbinned_photon_rays_bit_exact(cornell_c1_mesh):
     run_pair(cfg, mesh.scene(), cam, [1, 11])
 
 
+def flat_camera(sc, w, h):
+    """A camera whose basis vectors have no x component: every primary eye ray lies in the plane
+    x = origin.x, so each has an exact zero direction component (a degenerate slab test)."""
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, w, h, sc.fov)
+    cam.u[0], cam.u[1], cam.u[2] = 0.0, 0.0, -0.5
+    cam.v[0], cam.v[1], cam.v[2] = 0.0, 1.0, 0.0
+    cam.w[0], cam.w[1], cam.w[2] = 0.0, 0.0, -1.0
+    return cam
+
+
+@pytest.mark.parametrize("w,h", [(32, 32), (80, 64)])
+def test_eye_rays_with_zero_direction_components_bit_exact(cornell_c1_mesh, w, h):
+    """Eye rays with a zero direction component are deferred to the block-wide eye pass (at most
+    4096 pixels a frame; the 80x64 image has more, and the rest are walked one per thread): the
+    state equals the oracle's either way."""
+    sc, mesh = cornell_c1_mesh
+    cfg = g.default_config(w, height=h, photon_width=64, photon_height=32, radius_rule=N.RADIUS_DIAGONAL,
+                           radius_fraction=0.01)
+    run_pair(cfg, mesh.scene(), flat_camera(sc, w, h), [1, 10, 11, 21])
+
+
 def test_state_bit_exact_non_square_and_hash_seed(cornell_c1_mesh):
     sc, mesh = cornell_c1_mesh
     cfg = g.default_config(40, height=24, photon_width=48, photon_height=20, hash_slots=1500,
