@@ -6,7 +6,7 @@ import ctypes as C
 import numpy as np
 
 from . import native as N
-from .renderer import Mesh, SceneArrays, _state_array, scene_from_arrays
+from .renderer import Mesh, SceneArrays, _check_image_buffer, _release_tickets, _state_array, scene_from_arrays
 
 
 def _scene(scene):
@@ -31,6 +31,7 @@ class Batch:
         self._h = out
         self.config = cfg
         self._sizes: dict[int, tuple[int, int]] = {}
+        self._inflight: dict[int, np.ndarray] = {}  # host images of copies not yet waited for
 
     def job_bytes(self, config: N.Config, scene) -> int:
         n = C.c_uint64()
@@ -64,6 +65,7 @@ class Batch:
 
     def synchronize(self) -> None:
         N.check(N.lib.sppm_batch_synchronize(self._h))
+        self._inflight.clear()
 
     def read_image(self, job: int, kind: int = N.IMAGE_RADIANCE, out: np.ndarray | None = None) -> np.ndarray:
         w, h = self._sizes[job]
@@ -71,6 +73,26 @@ class Batch:
             out = np.empty((h, w, 3), dtype=np.float32)
         N.check(N.lib.sppm_batch_read_image(self._h, job, kind, out.ctypes.data, w * h * 3))
         return out
+
+    def read_image_async(self, job: int, out: np.ndarray, kind: int = N.IMAGE_RADIANCE) -> int:
+        """Renderer.read_image_async for one job; the ticket is the batch's."""
+        w, h = self._sizes[job]
+        _check_image_buffer(out, w, h)
+        t = C.c_uint64()
+        N.check(N.lib.sppm_batch_read_image_async(self._h, job, kind, out.ctypes.data, out.size, C.byref(t)))
+        self._inflight[int(t.value)] = out
+        return int(t.value)
+
+    def image_wait(self, ticket: int) -> None:
+        N.check(N.lib.sppm_batch_image_wait(self._h, ticket))
+        _release_tickets(self._inflight, ticket)
+
+    def image_done(self, ticket: int) -> bool:
+        done = C.c_int()
+        N.check(N.lib.sppm_batch_image_query(self._h, ticket, C.byref(done)))
+        if done.value:
+            _release_tickets(self._inflight, ticket)
+        return bool(done.value)
 
     def read_state(self, job: int, kind: str) -> np.ndarray:
         k = N.STATE[kind]

@@ -124,6 +124,24 @@ int sppm_read_image(sppm_ctx* c, uint32_t kind, float* rgb, size_t num_floats) {
     return c->rt.synchronize();
 }
 
+int sppm_read_image_async(sppm_ctx* c, uint32_t kind, float* rgb, size_t num_floats, uint64_t* ticket) {
+    if (!c || !rgb || !ticket) return fail(SPPM_ERR_ARG, "null argument");
+    if (kind > SPPM_IMAGE_DISPLAY) return fail(SPPM_ERR_ARG, "unknown image kind %u", kind);
+    if (num_floats != (size_t)c->job.npix * 3)
+        return fail(SPPM_ERR_ARG, "image needs %zu floats", (size_t)c->job.npix * 3);
+    return c->rt.read_image_async(c->job, kind, rgb, num_floats * 4, ticket);
+}
+
+int sppm_image_wait(sppm_ctx* c, uint64_t ticket) {
+    if (!c) return fail(SPPM_ERR_ARG, "null argument");
+    return c->rt.image_wait(ticket, true, nullptr);
+}
+
+int sppm_image_query(sppm_ctx* c, uint64_t ticket, int* done) {
+    if (!c || !done) return fail(SPPM_ERR_ARG, "null argument");
+    return c->rt.image_wait(ticket, false, done);
+}
+
 size_t sppm_state_bytes(const sppm_ctx* c, uint32_t kind) {
     if (!c) return 0;
     size_t b = 0;

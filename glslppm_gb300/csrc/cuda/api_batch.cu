@@ -198,6 +198,25 @@ int sppm_batch_read_image(sppm_batch* b, uint32_t id, uint32_t kind, float* rgb,
     return b->rt.synchronize();
 }
 
+int sppm_batch_read_image_async(sppm_batch* b, uint32_t id, uint32_t kind, float* rgb, size_t num_floats,
+                                uint64_t* ticket) {
+    Job* j = job_of(b, id);
+    if (!j || !rgb || !ticket) return fail(SPPM_ERR_ARG, "no job %u or null argument", id);
+    if (kind > SPPM_IMAGE_DISPLAY) return fail(SPPM_ERR_ARG, "unknown image kind %u", kind);
+    if (num_floats != (size_t)j->npix * 3) return fail(SPPM_ERR_ARG, "image needs %zu floats", (size_t)j->npix * 3);
+    return b->rt.read_image_async(*j, kind, rgb, num_floats * 4, ticket);
+}
+
+int sppm_batch_image_wait(sppm_batch* b, uint64_t ticket) {
+    if (!b) return fail(SPPM_ERR_ARG, "null argument");
+    return b->rt.image_wait(ticket, true, nullptr);
+}
+
+int sppm_batch_image_query(sppm_batch* b, uint64_t ticket, int* done) {
+    if (!b || !done) return fail(SPPM_ERR_ARG, "null argument");
+    return b->rt.image_wait(ticket, false, done);
+}
+
 size_t sppm_batch_state_bytes(const sppm_batch* b, uint32_t id, uint32_t kind) {
     const Job* j = job_of(b, id);
     if (!j) return 0;

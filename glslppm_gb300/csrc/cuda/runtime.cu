@@ -313,6 +313,10 @@ int Job::init(const sppm_config& c, JobDesc* dd, uint32_t sl, cudaStream_t s) {
 }
 
 Job::~Job() {
+    if (copy_ev) {
+        if (copy_pending) cudaEventSynchronize(copy_ev);  // the copy reads this job's image
+        cudaEventDestroy(copy_ev);
+    }
     for (int k = 0; k < 4; k++) {
         if (stage_used[k]) cudaEventSynchronize(stage_ev[k]);
         if (stage_ev[k]) cudaEventDestroy(stage_ev[k]);
@@ -618,6 +622,13 @@ Runner::~Runner() {
         if (e) cudaEventDestroy(e);
     if (fork_ev) cudaEventDestroy(fork_ev);
     if (join_ev) cudaEventDestroy(join_ev);
+    if (copy) {
+        cudaStreamSynchronize(copy);
+        cudaStreamDestroy(copy);
+    }
+    if (resolved_ev) cudaEventDestroy(resolved_ev);
+    for (auto& t : tickets) cudaEventDestroy(t.ev);
+    for (auto e : ticket_pool) cudaEventDestroy(e);
     if (side) {
         cudaStreamSynchronize(side);
         cudaStreamDestroy(side);
@@ -636,6 +647,8 @@ int Runner::init(int dev, uint32_t prec, uint32_t fl, uint32_t interval, uint32_
     SPPM_CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     SPPM_CK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
     SPPM_CK(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
+    SPPM_CK(cudaStreamCreateWithFlags(&copy, cudaStreamNonBlocking));
+    SPPM_CK(cudaEventCreateWithFlags(&resolved_ev, cudaEventDisableTiming));
     int st = desc_mem.reserve(Arena::align(sizeof(JobDesc) * std::max<uint32_t>(max_jobs, 1)));
     if (st) return st;
     d_jobs = desc_mem.take<JobDesc>(std::max<uint32_t>(max_jobs, 1));
@@ -901,6 +914,9 @@ int Runner::run(uint32_t n) {
 int Runner::synchronize() {
     SPPM_CK(cudaSetDevice(device));
     SPPM_CK(cudaStreamSynchronize(stream));
+    SPPM_CK(cudaStreamSynchronize(copy));
+    for (auto& t : tickets) ticket_pool.push_back(t.ev);
+    tickets.clear();
     std::vector<uint32_t> errs(active.size(), 0);
     for (size_t i = 0; i < active.size(); i++)
         SPPM_CK(cudaMemcpyAsync(&errs[i], &active[i]->d_state->err, 4, cudaMemcpyDeviceToHost, stream));
@@ -952,11 +968,68 @@ int Runner::read_stage_times(float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_
 
 int Runner::resolve(Job& j, uint32_t kind) {
     SPPM_CK(cudaSetDevice(device));
+    if (j.copy_pending) SPPM_CK(cudaStreamWaitEvent(stream, j.copy_ev, 0));
     timed(SPPM_STAGE_RESOLVE, true);
     if (precision == SPPM_PRECISION_MIXED) launch_resolve_mixed(j.self_set(d_jobs, 0), kind, stream);
     else launch_resolve_fp32(j.self_set(d_jobs, 0), kind, stream);
     timed(SPPM_STAGE_RESOLVE, false);
     return launch_check("resolve");
+}
+
+// at most this many copies in flight: one more waits for the oldest
+constexpr size_t kMaxTickets = 16;
+
+int Runner::read_image_async(Job& j, uint32_t kind, float* rgb, size_t bytes, uint64_t* ticket) {
+    int st = resolve(j, kind);
+    if (st) return st;
+    if (!j.copy_ev) SPPM_CK(cudaEventCreateWithFlags(&j.copy_ev, cudaEventDisableTiming));
+    if (tickets.size() >= kMaxTickets) {
+        SPPM_CK(cudaEventSynchronize(tickets.front().ev));
+        ticket_pool.push_back(tickets.front().ev);
+        tickets.pop_front();
+    }
+    cudaEvent_t ev = nullptr;
+    if (!ticket_pool.empty()) {
+        ev = ticket_pool.back();
+        ticket_pool.pop_back();
+    } else {
+        SPPM_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    SPPM_CK(cudaEventRecord(resolved_ev, stream));
+    SPPM_CK(cudaStreamWaitEvent(copy, resolved_ev, 0));
+    SPPM_CK(cudaMemcpyAsync(rgb, j.d_image, bytes, cudaMemcpyDeviceToHost, copy));
+    SPPM_CK(cudaEventRecord(j.copy_ev, copy));
+    j.copy_pending = true;
+    SPPM_CK(cudaEventRecord(ev, copy));
+    tickets.push_back(Ticket{next_ticket, ev});
+    if (ticket) *ticket = next_ticket;
+    next_ticket++;
+    return SPPM_OK;
+}
+
+int Runner::image_wait(uint64_t ticket, bool block, int* done) {
+    if (ticket == 0 || ticket >= next_ticket) return fail(SPPM_ERR_ARG, "unknown image ticket %llu",
+                                                          (unsigned long long)ticket);
+    SPPM_CK(cudaSetDevice(device));
+    // copies run in ticket order on one stream: once a ticket's event has fired, so have all
+    // older ones
+    while (!tickets.empty() && tickets.front().id <= ticket) {
+        Ticket& t = tickets.front();
+        if (block) {
+            SPPM_CK(cudaEventSynchronize(t.ev));
+        } else {
+            const cudaError_t q = cudaEventQuery(t.ev);
+            if (q == cudaErrorNotReady) {
+                if (done) *done = 0;
+                return SPPM_OK;
+            }
+            if (q != cudaSuccess) return fail(SPPM_ERR_CUDA, "image copy failed: %s", cudaGetErrorString(q));
+        }
+        ticket_pool.push_back(t.ev);
+        tickets.pop_front();
+    }
+    if (done) *done = 1;
+    return SPPM_OK;
 }
 
 }  // namespace sppm_rt

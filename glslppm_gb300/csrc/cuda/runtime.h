@@ -10,6 +10,7 @@
 #pragma once
 
 #include <cstdint>
+#include <deque>
 #include <memory>
 #include <vector>
 
@@ -78,6 +79,10 @@ struct Job {
     cudaEvent_t stage_ev[4] = {};
     bool stage_used[4] = {};
     uint32_t stage_next = 0;
+    // the last image copy queued on the runner's copy stream (it reads d_image, which the next
+    // resolve overwrites)
+    cudaEvent_t copy_ev = nullptr;
+    bool copy_pending = false;
     Job() = default;
     Job(const Job&) = delete;
     Job& operator=(const Job&) = delete;
@@ -135,6 +140,17 @@ struct Runner {
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;             // the eye pass's branch, forked from and joined to stream
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    // image copies to host memory run on `copy` beside the passes queued after them; each has a
+    // ticket (numbered from 1) whose event marks its end
+    cudaStream_t copy = nullptr;
+    cudaEvent_t resolved_ev = nullptr;
+    struct Ticket {
+        uint64_t id;
+        cudaEvent_t ev;
+    };
+    std::deque<Ticket> tickets;   // copies whose end has not been observed, oldest first
+    std::vector<cudaEvent_t> ticket_pool;
+    uint64_t next_ticket = 1;
     uint32_t precision = SPPM_PRECISION_FP32, flags = 0, eye_interval = 10, max_jobs = 0;
     Arena desc_mem;                // JobDesc[max_jobs]
     JobDesc* d_jobs = nullptr;
@@ -173,6 +189,10 @@ struct Runner {
     int time(uint32_t n, float* ms);
     int read_stage_times(float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]);
     int resolve(Job& j, uint32_t kind);
+    // resolve + copy of the image into host memory without waiting; *ticket names the copy
+    int read_image_async(Job& j, uint32_t kind, float* rgb, size_t bytes, uint64_t* ticket);
+    // waits for the copy of `ticket` (block) or reports whether it has ended (*done)
+    int image_wait(uint64_t ticket, bool block, int* done);
     cudaEvent_t get_event();
     void timed(int stage, bool start, cudaStream_t s = nullptr);
 

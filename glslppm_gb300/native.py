@@ -143,6 +143,9 @@ SIGNATURES = {
     "sppm_run_passes": (C.c_int, [P, C.c_uint32]),
     "sppm_synchronize": (C.c_int, [P]),
     "sppm_read_image": (C.c_int, [P, C.c_uint32, P, C.c_size_t]),
+    "sppm_read_image_async": (C.c_int, [P, C.c_uint32, P, C.c_size_t, C.POINTER(C.c_uint64)]),
+    "sppm_image_wait": (C.c_int, [P, C.c_uint64]),
+    "sppm_image_query": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_int)]),
     "sppm_read_state": (C.c_int, [P, C.c_uint32, P, C.c_size_t]),
     "sppm_state_bytes": (C.c_size_t, [P, C.c_uint32]),
     "sppm_checkpoint_bytes": (C.c_size_t, [P]),
@@ -180,6 +183,9 @@ SIGNATURES = {
     "sppm_batch_time_passes": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_float)]),
     "sppm_batch_synchronize": (C.c_int, [P]),
     "sppm_batch_read_image": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.c_size_t]),
+    "sppm_batch_read_image_async": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.c_size_t, C.POINTER(C.c_uint64)]),
+    "sppm_batch_image_wait": (C.c_int, [P, C.c_uint64]),
+    "sppm_batch_image_query": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_int)]),
     "sppm_batch_state_bytes": (C.c_size_t, [P, C.c_uint32, C.c_uint32]),
     "sppm_batch_read_state": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.c_size_t]),
     "sppm_batch_get_frame_info": (C.c_int, [P, C.c_uint32, C.POINTER(FrameInfo)]),

@@ -201,6 +201,17 @@ def _state_array(kind: str, nbytes: int) -> np.ndarray:
     return np.empty((nbytes // 16, 4), dtype=np.float32)
 
 
+def _check_image_buffer(out: np.ndarray, width: int, height: int) -> None:
+    if (not isinstance(out, np.ndarray) or out.dtype != np.float32 or not out.flags.c_contiguous
+            or out.size != width * height * 3):
+        raise N.SppmError(N.ERR_ARG, f"image buffer must be C-contiguous float32 with {width * height * 3} elements")
+
+
+def _release_tickets(inflight: dict, ticket: int) -> None:
+    for t in [t for t in inflight if t <= ticket]:
+        del inflight[t]
+
+
 class Renderer:
     """One SPPM render job on one GPU (CGPURT + m_display)."""
 
@@ -210,6 +221,7 @@ class Renderer:
         N.check(N.lib.sppm_create(C.byref(config), device, C.byref(out)))
         self._h = out
         self.width, self.height = config.width, config.height
+        self._inflight: dict[int, np.ndarray] = {}  # host images of copies not yet waited for
 
     # CGPURT::PrecalculateMeshData + CreateTextures
     def upload_scene(self, scene) -> None:
@@ -236,6 +248,7 @@ class Renderer:
 
     def synchronize(self) -> None:
         N.check(N.lib.sppm_synchronize(self._h))
+        self._inflight.clear()
 
     def read_image(self, kind: int = N.IMAGE_RADIANCE, out: np.ndarray | None = None) -> np.ndarray:
         n = self.width * self.height * 3
@@ -243,6 +256,27 @@ class Renderer:
             out = np.empty((self.height, self.width, 3), dtype=np.float32)
         N.check(N.lib.sppm_read_image(self._h, kind, out.ctypes.data, n))
         return out
+
+    def read_image_async(self, out: np.ndarray, kind: int = N.IMAGE_RADIANCE) -> int:
+        """Queues the resolve and the copy into `out` (page-locked, e.g. pinned_empty, for the
+        copy to overlap the next passes) and returns its ticket; `out` holds the image once
+        image_wait(ticket) or synchronize() has returned."""
+        _check_image_buffer(out, self.width, self.height)
+        t = C.c_uint64()
+        N.check(N.lib.sppm_read_image_async(self._h, kind, out.ctypes.data, out.size, C.byref(t)))
+        self._inflight[int(t.value)] = out
+        return int(t.value)
+
+    def image_wait(self, ticket: int) -> None:
+        N.check(N.lib.sppm_image_wait(self._h, ticket))
+        _release_tickets(self._inflight, ticket)
+
+    def image_done(self, ticket: int) -> bool:
+        done = C.c_int()
+        N.check(N.lib.sppm_image_query(self._h, ticket, C.byref(done)))
+        if done.value:
+            _release_tickets(self._inflight, ticket)
+        return bool(done.value)
 
     def state_bytes(self, kind: str) -> int:
         return int(N.lib.sppm_state_bytes(self._h, N.STATE[kind]))

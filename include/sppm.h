@@ -193,6 +193,18 @@ typedef enum sppm_image_kind {
 } sppm_image_kind;
 /* Resolves the image and copies width*height*3 floats (row 0 = bottom row, as GL) to rgb. */
 int sppm_read_image(sppm_ctx* ctx, uint32_t kind, float* rgb, size_t num_floats);
+/* The same without waiting (no counterpart in the reference, which displays every frame from
+   the GPU): the resolve is queued behind the passes already queued, and the copy into rgb runs
+   on a second stream beside the passes queued after it.  *ticket (numbered from 1) names the
+   copy; rgb must stay valid and unread until sppm_image_wait(ctx, ticket) (or sppm_synchronize)
+   returns.  Page-locked rgb (sppm_host_alloc) lets the copy overlap; with pageable memory the
+   call waits for the copy.  At most 16 copies are in flight: a further call waits for the
+   oldest. */
+int sppm_read_image_async(sppm_ctx* ctx, uint32_t kind, float* rgb, size_t num_floats, uint64_t* ticket);
+/* Waits until the copy named by ticket (and every older one) has ended. */
+int sppm_image_wait(sppm_ctx* ctx, uint64_t ticket);
+/* Sets *done to 1 when the copy named by ticket has ended, else 0; never waits. */
+int sppm_image_query(sppm_ctx* ctx, uint64_t ticket, int* done);
 
 /* Writes an image as sppm_read_image returns it to a file (no counterpart in the reference,
    which only displays):  SPPM_FILE_PFM keeps the linear floats (little-endian, bottom row first,

@@ -64,6 +64,12 @@ int sppm_batch_time_passes(sppm_batch* b, uint32_t n, float* ms);
 int sppm_batch_synchronize(sppm_batch* b);
 
 int sppm_batch_read_image(sppm_batch* b, uint32_t job, uint32_t kind, float* rgb, size_t num_floats);
+/* sppm_read_image_async / sppm_image_wait / sppm_image_query for one job of the batch (the
+   tickets are the batch's; a removed job's copy is waited for before its memory is freed). */
+int sppm_batch_read_image_async(sppm_batch* b, uint32_t job, uint32_t kind, float* rgb, size_t num_floats,
+                                uint64_t* ticket);
+int sppm_batch_image_wait(sppm_batch* b, uint64_t ticket);
+int sppm_batch_image_query(sppm_batch* b, uint64_t ticket, int* done);
 size_t sppm_batch_state_bytes(const sppm_batch* b, uint32_t job, uint32_t kind);
 int sppm_batch_read_state(sppm_batch* b, uint32_t job, uint32_t kind, void* dst, size_t bytes);
 int sppm_batch_get_frame_info(sppm_batch* b, uint32_t job, sppm_frame_info* info);
