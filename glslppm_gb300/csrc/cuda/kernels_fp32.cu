@@ -978,8 +978,10 @@ struct PhotonRay {
     uint32_t emitted;
 };
 
-__device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t sidx, uint32_t frame, float4& rndv,
-                                                     uint32_t& err) {
+// hitin: the previous segment's (triangle, depth), (-1, 0) before the first; PP, PF, PD: its
+// record (position, flux, direction, with the normal in the w components)
+__device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, int2 hitin, float4 PP, float4 PF, float4 PD,
+                                                     float4& rndv, uint32_t& err) {
     // Emission and the diffuse bounces end in the same cosine lobe: each path sets up its lobe
     // (normal, origin; the draws before the lobe stay in the path) and the lanes draw the lobe
     // together, then finish their path (the flip against the geometric normal, Russian roulette).
@@ -988,9 +990,6 @@ __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t 
     PhotonRay R;
     R.org = mk(0, 0, 0);
     R.dir = mk(0, 0, 0);
-    const int2 hitin = frame == 0 ? make_int2(-1, 0) : J.ph.hit[sidx];
-    // the previous segment's record, loaded with the hit (a bounce needs it; an emission does not)
-    const float4 PP = J.ph.pos[sidx], PF = J.ph.flux[sidx], PD = J.ph.dir[sidx];
     R.depth = xadd((float)hitin.y, 1.0f);
     const bool emit = hitin.x < 0 || R.depth >= (float)J.max_path;
     bool lobe = false, flip = false;
@@ -1088,6 +1087,12 @@ __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t 
     R.emitted = 0;
     R.flux = flux;
     return R;
+}
+
+__device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t sidx, uint32_t frame, float4& rndv,
+                                                     uint32_t& err) {
+    const int2 hitin = frame == 0 ? make_int2(-1, 0) : J.ph.hit[sidx];
+    return photon_generate(J, hitin, J.ph.pos[sidx], J.ph.flux[sidx], J.ph.dir[sidx], rndv, err);
 }
 
 __device__ __forceinline__ void photon_terminate(const JobDesc& J, uint32_t sidx) {
@@ -1199,16 +1204,74 @@ __global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
 // ----------------------------------------------------------------------------------------------
 // generate: emit/bounce every slot; RR-terminated photons are finished here, the others append
 // their ray to the queue (warp-aggregated append)
+//
+// The block's slots are first reordered so that the emissions (a photon with no previous hit or
+// at the bounce limit) come before the bounces: each warp then runs one of the two paths (the
+// state written is per slot, so the order of work changes nothing).
 __global__ void __launch_bounds__(128) k_photon_gen(LaunchSet ls, RayQueue q) {
-    const uint32_t g = grid_tid();
-    if (g >= ls.total) return;
+    // the slot and its record in processing order (the loads of every slot's record are issued
+    // together, before the reorder)
+    __shared__ uint32_t order[128];
+    __shared__ int2 rec_hit[128];
+    __shared__ float4 rec_pos[128], rec_flux[128], rec_dir[128], rec_rng[128];
+    __shared__ uint32_t warp_emit[4], warp_valid[4];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    {
+        const uint32_t g0 = grid_tid();
+        const bool valid = g0 < ls.total;
+        bool emit = false;
+        int2 h = make_int2(-1, 0);
+        float4 pp, pf, pd, rn;
+        if (valid) {
+            const int k0 = find_job(ls, g0);
+            const JobDesc& J0 = ls.jobs[ls.job_ids[k0]];
+            const JobState* st0 = J0.state;
+            const uint32_t s0 = g0 - ls.prefix[k0];
+            if (st0->frame != 0) h = J0.ph.hit[s0];
+            pp = J0.ph.pos[s0];
+            pf = J0.ph.flux[s0];
+            pd = J0.ph.dir[s0];
+            rn = J0.ph.rng[s0];
+            emit = h.x < 0 || xadd((float)h.y, 1.0f) >= (float)J0.max_path;
+        }
+        const unsigned em = __ballot_sync(0xFFFFFFFFu, emit), vm = __ballot_sync(0xFFFFFFFFu, valid);
+        if (lane == 0) {
+            warp_emit[warp] = __popc(em);
+            warp_valid[warp] = __popc(vm);
+        }
+        __syncthreads();
+        uint32_t e_before = 0, v_before = 0, e_total = 0;
+        for (uint32_t w = 0; w < 4; w++) {
+            if (w < warp) {
+                e_before += warp_emit[w];
+                v_before += warp_valid[w];
+            }
+            e_total += warp_emit[w];
+        }
+        const unsigned below = (1u << lane) - 1u;
+        if (valid) {
+            // emissions at [0, e_total), bounces after them
+            const uint32_t dst = emit ? e_before + __popc(em & below)
+                                      : e_total + (v_before - e_before) + __popc(vm & ~em & below);
+            order[dst] = g0;
+            rec_hit[dst] = h;
+            rec_pos[dst] = pp;
+            rec_flux[dst] = pf;
+            rec_dir[dst] = pd;
+            rec_rng[dst] = rn;
+        }
+        __syncthreads();
+        if (threadIdx.x >= warp_valid[0] + warp_valid[1] + warp_valid[2] + warp_valid[3]) return;
+    }
+    const uint32_t g = order[threadIdx.x];
     const int k = find_job(ls, g);
     const JobDesc& J = ls.jobs[ls.job_ids[k]];
     JobState* st = J.state;
     const uint32_t sidx = g - ls.prefix[k];
     uint32_t err = 0;
-    float4 rndv = J.ph.rng[sidx];
-    const PhotonRay R = photon_generate(J, sidx, st->frame, rndv, err);
+    const uint32_t t = threadIdx.x;
+    float4 rndv = rec_rng[t];
+    const PhotonRay R = photon_generate(J, rec_hit[t], rec_pos[t], rec_flux[t], rec_dir[t], rndv, err);
     J.ph.rng[sidx] = rndv;
     if (R.cont) {
         J.ph.flux[sidx] = f4(R.flux, 0.0f);  // flux before the segment, read back by k_photon_store
