@@ -156,7 +156,9 @@ int sppm_read_state(sppm_ctx* c, uint32_t kind, void* dst, size_t bytes) {
     if (bytes != need) return fail(SPPM_ERR_ARG, "state kind %u has %zu bytes, %zu requested", kind, need, bytes);
     SPPM_CK(cudaSetDevice(c->rt.device));
     SPPM_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->rt.stream));
-    return c->rt.synchronize();
+    const int st = c->rt.synchronize();
+    if (st == SPPM_OK) state_to_host_layout(kind, dst, bytes);
+    return st;
 }
 
 size_t sppm_checkpoint_bytes(const sppm_ctx* c) { return c ? c->job.checkpoint_bytes() : 0; }

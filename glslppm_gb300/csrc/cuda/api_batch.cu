@@ -233,7 +233,9 @@ int sppm_batch_read_state(sppm_batch* b, uint32_t id, uint32_t kind, void* dst, 
     if (bytes != need) return fail(SPPM_ERR_ARG, "state kind %u has %zu bytes, %zu requested", kind, need, bytes);
     SPPM_CK(cudaSetDevice(b->rt.device));
     SPPM_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, b->rt.stream));
-    return b->rt.synchronize();
+    const int st = b->rt.synchronize();
+    if (st == SPPM_OK) state_to_host_layout(kind, dst, bytes);
+    return st;
 }
 
 size_t sppm_batch_checkpoint_bytes(const sppm_batch* b, uint32_t id) {

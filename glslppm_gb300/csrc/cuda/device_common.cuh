@@ -76,7 +76,9 @@ struct DevPixels {
     float4 *pos, *refl, *nrm, *rng, *emi_n, *flux_r;
     int32_t* tri;
     float* t;
-    double *stat_n, *stat_r2, *stat_tau;  // mixed precision statistics (tau: 3 per pixel)
+    // mixed precision statistics as double-float pairs (value = x + y, |y| <= ulp(x) / 2): N, R^2
+    // and tau (3 per pixel), kept in FP32 arithmetic (GB300's FP64 rate is a small fraction of FP32)
+    float2 *stat_n, *stat_r2, *stat_tau;
 };
 
 struct DevPhotons {

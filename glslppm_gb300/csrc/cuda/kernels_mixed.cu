@@ -249,7 +249,36 @@ __global__ void __launch_bounds__(256) k_slot_fill(LaunchSet ls, RayQueue q) {
     J.slots[slot] = r;
 }
 
-// progressive.fs with the slot records, FP32 flux gathering and FP64 statistics
+// double-float arithmetic (Dekker 1971; Knuth, TAOCP vol. 2, 4.2.2): a value is the unevaluated sum
+// hi + lo of two floats with |lo| <= ulp(hi) / 2, about 48 significant bits.  The operations are
+// error-free transformations built from IEEE FP32 adds, multiplies and fmaf; the intrinsics keep
+// the compiler from contracting or reassociating them.
+__device__ __forceinline__ float2 df_fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ float2 df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return make_float2(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ float2 df_two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return make_float2(p, __fmaf_rn(a, b, -p));
+}
+// x * f
+__device__ __forceinline__ float2 df_mul_f(float2 x, float f) {
+    const float p = __fmul_rn(x.x, f);
+    const float e = __fmaf_rn(x.y, f, __fmaf_rn(x.x, f, -p));
+    return df_fast_two_sum(p, e);
+}
+// x + y
+__device__ __forceinline__ float2 df_add(float2 x, float2 y) {
+    const float2 s = df_two_sum(x.x, y.x);
+    return df_fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(x.y, y.y)));
+}
+
+// progressive.fs with the slot records, FP32 flux gathering and double-float statistics
 __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
     const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
     if (gi >= ls.total) return;
@@ -264,11 +293,12 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
         st->num_photons += e;
         st->photon_segments += st->segments_frame;
     }
-    double N = J.px.stat_n[p];
-    double R2 = frame == 0 ? (double)st->r0 * (double)st->r0 : J.px.stat_r2[p];
-    double tx = frame == 0 ? 0.0 : J.px.stat_tau[3 * (size_t)p + 0];
-    double ty = frame == 0 ? 0.0 : J.px.stat_tau[3 * (size_t)p + 1];
-    double tz = frame == 0 ? 0.0 : J.px.stat_tau[3 * (size_t)p + 2];
+    const float2 zero = make_float2(0.0f, 0.0f);
+    float2 N = J.px.stat_n[p];
+    float2 R2 = frame == 0 ? df_two_prod(st->r0, st->r0) : J.px.stat_r2[p];
+    float2 tx = frame == 0 ? zero : J.px.stat_tau[3 * (size_t)p + 0];
+    float2 ty = frame == 0 ? zero : J.px.stat_tau[3 * (size_t)p + 1];
+    float2 tz = frame == 0 ? zero : J.px.stat_tau[3 * (size_t)p + 2];
     if (J.px.tri[p] >= 0) {
         const float G = st->grid_scale;
         const float hs1 = st->hash_scale1;
@@ -277,7 +307,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
         const float gx = fabsf(qp4.x - st->bbmin[0]) * G, gy = fabsf(qp4.y - st->bbmin[1]) * G,
                     gz = fabsf(qp4.z - st->bbmin[2]) * G;
         const float ix = floorf(gx - 0.5f), iy = floorf(gy - 0.5f), iz = floorf(gz - 0.5f);
-        const float R2f = (float)R2;  // the in-radius test in FP32 (no FP64 square root)
+        const float R2f = R2.x + R2.y;  // the in-radius test in FP32
         const float invG = 1.0f / G;
         float fx = 0.0f, fy = 0.0f, fz = 0.0f, M = 0.0f;
 #pragma unroll
@@ -307,17 +337,15 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
             M += cf;
         }
         // shrink ratio (N + alpha M) / (N + M) = 1 - (1 - alpha) M / (N + M), computed in FP32 (its
-        // relative error ~1e-7 per pass); the statistics themselves accumulate in FP64 with fused
-        // multiply-adds, so GB300's slow FP64 units see no division and no square root
-        const float denom = (float)(N + (double)M);
+        // relative error ~1e-7 per pass); the statistics accumulate in double-float
+        const float denom = (N.x + N.y) + M;
         const float ggf = M > 0.0f ? fminf(1.0f - (1.0f - J.alpha) * (M / denom), 1.0f) : 1.0f;
-        const double gg = (double)ggf;
-        R2 *= gg;
-        N = fma((double)J.alpha, (double)M, N);
+        R2 = df_mul_f(R2, ggf);
+        N = df_add(N, df_two_prod(J.alpha, M));
         const float s = J.scene.flux_unscale * 0.318309886f;
-        tx = fma(tx, gg, (double)(fx * s * qr4.x * ggf));
-        ty = fma(ty, gg, (double)(fy * s * qr4.y * ggf));
-        tz = fma(tz, gg, (double)(fz * s * qr4.z * ggf));
+        tx = df_add(df_mul_f(tx, ggf), make_float2(fx * s * qr4.x * ggf, 0.0f));
+        ty = df_add(df_mul_f(ty, ggf), make_float2(fy * s * qr4.y * ggf, 0.0f));
+        tz = df_add(df_mul_f(tz, ggf), make_float2(fz * s * qr4.z * ggf, 0.0f));
         J.px.stat_n[p] = N;
     }
     J.px.stat_r2[p] = R2;
@@ -326,18 +354,20 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
     J.px.stat_tau[3 * (size_t)p + 2] = tz;
 }
 
-// re.fs from the FP64 statistics
+// re.fs from the double-float statistics (the image is FP32: the pairs' high parts carry it)
 __global__ void k_resolve_mixed(LaunchSet ls, uint32_t display) {
     const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
     if (gi >= ls.total) return;
     const int k = find_job(ls, gi);
     const JobDesc& J = ls.jobs[ls.job_ids[k]];
     const uint32_t p = gi - ls.prefix[k];
-    const double den = J.px.stat_r2[p] * 3.141592653589793 * (double)J.state->num_photons;
+    const float2 r2 = J.px.stat_r2[p];
+    const float den = (r2.x + r2.y) * 3.14159265f * (float)J.state->num_photons;
     const float4 qe = J.px.emi_n[p];
     const float e[3] = {qe.x, qe.y, qe.z};
     for (int c = 0; c < 3; c++) {
-        float v = (float)(J.px.stat_tau[3 * (size_t)p + c] / den) + e[c];
+        const float2 t = J.px.stat_tau[3 * (size_t)p + c];
+        float v = (t.x + t.y) / den + e[c];
         if (display) {
             v = 1.0f - sppm_fexp(-v * 60000.0f);
             v = v < 0.0031308f ? 12.92f * v : 1.055f * sppm_fpow(v, 0.416666666667f) - 0.055f;

@@ -33,6 +33,17 @@ int launch_check(const char* what) {
     return SPPM_OK;
 }
 
+void state_to_host_layout(uint32_t kind, void* buf, size_t bytes) {
+    if (kind < SPPM_STATE_STATS_N || kind > SPPM_STATE_STATS_TAU) return;
+    char* b = static_cast<char*>(buf);
+    for (size_t i = 0; i + 8 <= bytes; i += 8) {
+        float pair[2];
+        memcpy(pair, b + i, 8);
+        const double v = (double)pair[0] + (double)pair[1];  // exact: the pair spans < 53 bits
+        memcpy(b + i, &v, 8);
+    }
+}
+
 int validate_config(const sppm_config* c) {
     if (!c) return fail(SPPM_ERR_ARG, "null config");
     if (c->width == 0 || c->height == 0 || c->photon_width == 0 || c->photon_height == 0)
@@ -284,9 +295,9 @@ int Job::init(const sppm_config& c, JobDesc* dd, uint32_t sl, cudaStream_t s) {
     J.count = a.take<uint32_t>(hn);
     if (c.precision == SPPM_PRECISION_MIXED) {
         J.slots = a.take<SlotRec>(hn);
-        J.px.stat_n = a.take<double>(np);
-        J.px.stat_r2 = a.take<double>(np);
-        J.px.stat_tau = a.take<double>(np * 3);
+        J.px.stat_n = a.take<float2>(np);
+        J.px.stat_r2 = a.take<float2>(np);
+        J.px.stat_tau = a.take<float2>(np * 3);
         if (!J.px.stat_tau) return fail(SPPM_ERR_OOM, "state arena sizing error (mixed)");
     }
     if (!J.count) return fail(SPPM_ERR_OOM, "state arena sizing error");
@@ -520,7 +531,7 @@ struct CheckpointHeader {
     char magic[8];
     uint32_t version, W, H, PW, PH, hash_num, precision, state_bytes;
 };
-constexpr char kCheckpointMagic[8] = {'S', 'P', 'P', 'M', 'C', 'K', 'P', '1'};
+constexpr char kCheckpointMagic[8] = {'S', 'P', 'P', 'M', 'C', 'K', 'P', '2'};
 constexpr uint32_t kCheckpointKinds = SPPM_STATE_STATS_TAU + 1;
 }  // namespace
 

@@ -58,6 +58,9 @@ struct Arena {
 };
 
 int validate_config(const sppm_config* c);
+// state kinds whose device layout differs from what readers get: the mixed-precision statistics
+// are double-float pairs on the device and doubles for the reader (converted in place)
+void state_to_host_layout(uint32_t kind, void* buf, size_t bytes);
 int launch_check(const char* what);
 
 // one render job (scene + camera + progressive state)

@@ -234,7 +234,9 @@ typedef enum sppm_state_kind {
     SPPM_STATE_STATS_R2 = 16,       /* double/pixel  R^2                                        */
     SPPM_STATE_STATS_TAU = 17       /* double3/pixel tau                                        */
 } sppm_state_kind;
-/* Copies one state array to host memory; `bytes` must equal the array's size. */
+/* Copies one state array to host memory; `bytes` must equal the array's size.  The statistics
+   (kinds 15-17) are held on the device as double-float pairs (two floats whose sum is the value)
+   and arrive as doubles. */
 int sppm_read_state(sppm_ctx* ctx, uint32_t kind, void* dst, size_t bytes);
 /* Size in bytes of a state array (0 if the kind is not kept by this precision). */
 size_t sppm_state_bytes(const sppm_ctx* ctx, uint32_t kind);
