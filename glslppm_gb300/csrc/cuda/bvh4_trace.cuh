@@ -48,7 +48,9 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
             break;
         }
         const float4* np = reinterpret_cast<const float4*>(nodes + cur);
-        const float4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3);
+        float4 w0, w1, w2, w3;
+        ldg32(np, w0, w1);
+        ldg32(np + 2, w2, w3);
         const uint32_t eb = __float_as_uint(w0.w);
         const float sx = node_scale(eb & 0xFF), sy = node_scale((eb >> 8) & 0xFF), sz = node_scale((eb >> 16) & 0xFF);
         const int cnt = (int)(eb >> 24);

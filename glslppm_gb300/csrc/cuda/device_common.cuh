@@ -28,13 +28,20 @@ constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
 constexpr uint32_t kErrWatchdogTraverse = 1u;
 constexpr uint32_t kErrWatchdogLight = 2u;
 
-struct __align__(16) NodeX {
+struct __align__(32) NodeX {
     float bmin[3];
     int32_t miss;  // position in the same ordering, -1 = end
     float bmax[3];
     int32_t tri;   // -1 internal; leaf: triangle id, | kEmitterBit for lights
 };
 static_assert(sizeof(NodeX) == 32, "NodeX is one 32-byte sector");
+
+// 32 bytes of read-only data in one 256-bit global load (sm_100 and later); p 32-byte aligned
+__device__ __forceinline__ void ldg32(const void* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
 
 struct __align__(16) DevMaterial {
     float color[3];
@@ -47,7 +54,7 @@ struct __align__(16) DevMaterial {
 // 4-wide quantised BVH node of the mixed path (host layout: csrc/host/scene_bvh4.h, 64 bytes):
 // w[0] = origin xyz, exponent bytes x|y|z|count; w[1] = children; w[2] = qlo x,y,z, qhi x;
 // w[3] = qhi y,z
-struct __align__(16) Node4Dev {
+struct __align__(32) Node4Dev {
     float4 w[4];
 };
 

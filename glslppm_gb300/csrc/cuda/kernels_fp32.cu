@@ -87,8 +87,8 @@ __device__ __forceinline__ Hit trace_exact(const DevScene& s, f3 org, f3 dir, bo
             err |= kErrWatchdogTraverse;
             break;
         }
-        const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + i));
-        const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + i) + 1);
+        float4 A, B;
+        ldg32(nodes + i, A, B);
         if (COUNT) cnt->nodes++;
         const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
         const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
@@ -170,8 +170,8 @@ __device__ __noinline__ Hit coop_trace_exact(const DevScene& s, f3 org, f3 dir, 
         float tmin = 0.0f, tt = 0.0f, bu = 0.0f, bv = 0.0f, bw = 0.0f;
         int32_t miss = -1, tri = -1, mat = -1;
         if (j < nn) {
-            const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + j));
-            const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + j) + 1);
+            float4 A, B;
+            ldg32(nodes + j, A, B);
             const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
             const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
             tmin = fmax3(fminf(lx, hx), fminf(ly, hy), fminf(lz, hz));
@@ -328,8 +328,10 @@ __device__ __noinline__ Hit block_trace_exact(const DevScene& s, f3 org, f3 dir,
             float tmin = 0.0f, tt = 0.0f, bu = 0.0f, bv = 0.0f, bw = 0.0f;
             int32_t miss = -1, tri = -1, mat = -1;
             if (j < nn) {
-                const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + j));
-                const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + j) + 1);
+                float4 A, B;
+                // two 16-byte loads: this toolkit's ptxas fails on the 256-bit form in this function
+                A = __ldg(reinterpret_cast<const float4*>(nodes + j));
+                B = __ldg(reinterpret_cast<const float4*>(nodes + j) + 1);
                 const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
                 const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
                 tmin = fmax3(fminf(lx, hx), fminf(ly, hy), fminf(lz, hz));
@@ -1440,8 +1442,8 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
                 finished = true;
                 break;
             }
-            const float4 A = __ldg(reinterpret_cast<const float4*>(nodes + node));
-            const float4 B = __ldg(reinterpret_cast<const float4*>(nodes + node) + 1);
+            float4 A, B;
+            ldg32(nodes + node, A, B);
             if (COUNT) tc.nodes++;
             const float lx = xadd(xmul(rcp.x, A.x), t0.x), ly = xadd(xmul(rcp.y, A.y), t0.y), lz = xadd(xmul(rcp.z, A.z), t0.z);
             const float hx = xadd(xmul(rcp.x, B.x), t0.x), hy = xadd(xmul(rcp.y, B.y), t0.y), hz = xadd(xmul(rcp.z, B.z), t0.z);
