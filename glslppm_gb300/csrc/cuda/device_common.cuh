@@ -236,11 +236,27 @@ __device__ __forceinline__ float fractf(float x) { return xsub(x, floorf(x)); }
         v[i] = xmul(s[i], minv);                                                                 \
     }
 
+// one lane of the step: the new state in s[L], the lane's value in v[L]
+template <int L>
+__device__ __forceinline__ void schrage_lane(float s[4], float v[4]) {
+    if (L == 0) SPPM_RND_LANE(0, 1225.0f, 1112.0f, 3423.0f, 4194287.0f, 8.163265302e-04f, 2.384195454e-07f)
+    if (L == 1) SPPM_RND_LANE(1, 1585.0f, 367.0f, 2646.0f, 4194277.0f, 6.309148157e-04f, 2.384201139e-07f)
+    if (L == 2) SPPM_RND_LANE(2, 2457.0f, 92.0f, 1707.0f, 4194191.0f, 4.070004215e-04f, 2.384250024e-07f)
+    if (L == 3) SPPM_RND_LANE(3, 2098.0f, 265.0f, 1999.0f, 4194167.0f, 4.766444326e-04f, 2.384263666e-07f)
+}
+// the value of lane L for state x (the new state is not kept)
+template <int L>
+__device__ __forceinline__ float schrage_value(float x) {
+    float s[4] = {x, x, x, x}, v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    schrage_lane<L>(s, v);
+    return v[L];
+}
+
 __device__ __forceinline__ void schrage4(float s[4], float v[4]) {
-    SPPM_RND_LANE(0, 1225.0f, 1112.0f, 3423.0f, 4194287.0f, 8.163265302e-04f, 2.384195454e-07f)
-    SPPM_RND_LANE(1, 1585.0f, 367.0f, 2646.0f, 4194277.0f, 6.309148157e-04f, 2.384201139e-07f)
-    SPPM_RND_LANE(2, 2457.0f, 92.0f, 1707.0f, 4194191.0f, 4.070004215e-04f, 2.384250024e-07f)
-    SPPM_RND_LANE(3, 2098.0f, 265.0f, 1999.0f, 4194167.0f, 4.766444326e-04f, 2.384263666e-07f)
+    schrage_lane<0>(s, v);
+    schrage_lane<1>(s, v);
+    schrage_lane<2>(s, v);
+    schrage_lane<3>(s, v);
 }
 
 __device__ __forceinline__ float gpu_rnd(float4& n) {
@@ -260,6 +276,29 @@ __device__ __forceinline__ uint32_t hash_cell(f3 cell, float grid_scale, float h
     const float hmax = xsub(hash_num, 1.0f);
     if (h > hmax) h = hmax;
     return (uint32_t)h;
+}
+
+// the slots of the 2x2x2 cells from `base` (cell c = base + (c & 1, c >> 1 & 1, c >> 2)): each hash
+// lane depends on one coordinate (lane 3 on the grid scale alone), so the 32 lane steps of eight
+// hash_cell calls reduce to seven; the combination per cell is hash_cell's
+__device__ __forceinline__ void hash_cells8(f3 base, float grid_scale, float hash_scale1, float hash_num,
+                                            uint32_t slot[8]) {
+    // the coordinates as the callers form them (base + 0 turns -0 into +0)
+    const float x0 = __fadd_rn(base.x, 0.0f), y0 = __fadd_rn(base.y, 0.0f), z0 = __fadd_rn(base.z, 0.0f);
+    const float x1 = __fadd_rn(base.x, 1.0f), y1 = __fadd_rn(base.y, 1.0f), z1 = __fadd_rn(base.z, 1.0f);
+    const float vx[2] = {schrage_value<0>(__fmul_rn(x0, hash_scale1)), schrage_value<0>(__fmul_rn(x1, hash_scale1))};
+    const float vy[2] = {schrage_value<1>(__fmul_rn(y0, hash_scale1)), schrage_value<1>(__fmul_rn(y1, hash_scale1))};
+    const float vz[2] = {schrage_value<2>(__fmul_rn(z0, hash_scale1)), schrage_value<2>(__fmul_rn(z1, hash_scale1))};
+    const float vw = schrage_value<3>(__fmul_rn(__fmul_rn(grid_scale, 0.5f), hash_scale1));
+    const float hmax = __fsub_rn(hash_num, 1.0f);
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const float u = __fsub_rn(__fadd_rn(__fsub_rn(vx[c & 1], vy[(c >> 1) & 1]), vz[c >> 2]), vw);
+        float h = floorf(__fmul_rn(__fsub_rn(u, floorf(u)), hash_num));
+        if (!(h >= 0.0f)) h = 0.0f;
+        if (h > hmax) h = hmax;
+        slot[c] = (uint32_t)h;
+    }
 }
 
 // order-preserving float <-> uint32 encoding (for atomicMin/atomicMax on floats)

@@ -1580,11 +1580,7 @@ __global__ void __launch_bounds__(256, 4) k_gather(LaunchSet ls) {
         // the candidate photons' positions, then the accumulation in cell order (the sum's order
         // is progressive.fs's)
         uint32_t slot[8], win[8];
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-            const f3 cell = mk(xadd(ii.x, (float)(c & 1)), xadd(ii.y, (float)((c >> 1) & 1)), xadd(ii.z, (float)(c >> 2)));
-            slot[c] = hash_cell(cell, G, hs1, hn);
-        }
+        hash_cells8(ii, G, hs1, hn, slot);
 #pragma unroll
         for (int c = 0; c < 8; c++) win[c] = __ldg(&J.winner[slot[c]]);
         uint32_t inside = 0;

@@ -312,10 +312,12 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
         const float R2f = R2.x + R2.y;  // the in-radius test in FP32
         const float invG = 1.0f / G;
         float fx = 0.0f, fy = 0.0f, fz = 0.0f, M = 0.0f;
+        uint32_t slots[8];
+        hash_cells8(mk(ix, iy, iz), G, hs1, hn, slots);
 #pragma unroll
         for (int c = 0; c < 8; c++) {
             const float cx = ix + (float)(c & 1), cy = iy + (float)((c >> 1) & 1), cz = iz + (float)(c >> 2);
-            const uint32_t slot = hash_cell(mk(cx, cy, cz), G, hs1, hn);
+            const uint32_t slot = slots[c];
             const SlotRec r = J.slots[slot];
             const uint32_t cnt = r.w0.y >> 16;
             if (cnt == 0 || J.winner[slot] == kEmptySlot) continue;
