@@ -413,11 +413,11 @@ def pinned_empty(shape, dtype=np.float32) -> np.ndarray:
 
 
 def write_image(path, rgb: np.ndarray, fmt: str = "pfm") -> None:
-    """Writes an [h, w, 3] image as read_image returns it (row 0 = bottom): 'pfm' keeps the linear
-    floats, 'ppm' writes 8-bit values (for display images)."""
+    """Writes an [h, w, 3] image as read_image returns it (row 0 = bottom): 'pfm' and 'exr' keep the
+    linear floats, 'ppm' writes 8-bit values (for display images)."""
     rgb = np.ascontiguousarray(rgb, dtype=np.float32)
     h, w = rgb.shape[:2]
-    N.check(N.lib.sppm_write_image_file(str(path).encode(), rgb.ctypes.data, w, h, {"pfm": 0, "ppm": 1}[fmt]))
+    N.check(N.lib.sppm_write_image_file(str(path).encode(), rgb.ctypes.data, w, h, {"pfm": 0, "ppm": 1, "exr": 2}[fmt]))
 
 
 def debug_fpmath(fn: int, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:

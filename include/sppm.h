@@ -209,8 +209,10 @@ int sppm_image_query(sppm_ctx* ctx, uint64_t ticket, int* done);
 /* Writes an image as sppm_read_image returns it to a file (no counterpart in the reference,
    which only displays):  SPPM_FILE_PFM keeps the linear floats (little-endian, bottom row first,
    as the format stores rows); SPPM_FILE_PPM writes binary 8-bit P6, top row first, with
-   clamp(v, 0, 1) * 255 rounded -- meant for SPPM_IMAGE_DISPLAY images. */
-typedef enum sppm_file_format { SPPM_FILE_PFM = 0, SPPM_FILE_PPM = 1 } sppm_file_format;
+   clamp(v, 0, 1) * 255 rounded -- meant for SPPM_IMAGE_DISPLAY images; SPPM_FILE_EXR writes an
+   OpenEXR 2 single-part scanline file, uncompressed, channels B G R as 32-bit floats, top row
+   first. */
+typedef enum sppm_file_format { SPPM_FILE_PFM = 0, SPPM_FILE_PPM = 1, SPPM_FILE_EXR = 2 } sppm_file_format;
 int sppm_write_image_file(const char* path, const float* rgb, uint32_t width, uint32_t height, uint32_t format);
 
 /* Per-pixel / per-photon / per-slot state, for parity checks and checkpointing. */

@@ -163,3 +163,50 @@ def test_image_files(tmp_path):
     assert np.array_equal(px, ref)
     with pytest.raises(g.SppmError):
         g.write_image(tmp_path / "missing" / "x.pfm", img)
+
+
+def _read_exr(raw: bytes):
+    """Parses an uncompressed single-part scanline OpenEXR file by the format's published layout."""
+    import struct
+    assert struct.unpack_from("<II", raw, 0) == (20000630, 2)
+    pos, attrs = 8, {}
+    while raw[pos] != 0:
+        name_end = raw.index(b"\0", pos)
+        name = raw[pos:name_end].decode()
+        type_end = raw.index(b"\0", name_end + 1)
+        typ = raw[name_end + 1:type_end].decode()
+        (size,) = struct.unpack_from("<I", raw, type_end + 1)
+        attrs[name] = (typ, raw[type_end + 5:type_end + 5 + size])
+        pos = type_end + 5 + size
+    pos += 1
+    chans, cl = [], attrs["channels"][1]
+    q = 0
+    while cl[q] != 0:
+        e = cl.index(b"\0", q)
+        ptype, plin, xs, ys = struct.unpack_from("<iB3xii", cl, e + 1)
+        chans.append((cl[q:e].decode(), ptype, xs, ys))
+        q = e + 17
+    x0, y0, x1, y1 = struct.unpack("<iiii", attrs["dataWindow"][1])
+    w, h = x1 - x0 + 1, y1 - y0 + 1
+    assert attrs["compression"] == ("compression", b"\0") and attrs["lineOrder"] == ("lineOrder", b"\0")
+    offsets = struct.unpack_from(f"<{h}Q", raw, pos)
+    out = {c[0]: np.zeros((h, w), np.float32) for c in chans}
+    for off in offsets:
+        y, n = struct.unpack_from("<iI", raw, off)
+        assert n == 4 * w * len(chans)
+        data = np.frombuffer(raw, dtype="<f4", count=w * len(chans), offset=off + 8).reshape(len(chans), w)
+        for k, c in enumerate(chans):
+            out[c[0]][y - y0] = data[k]
+    return chans, w, h, out
+
+
+def test_exr_file(tmp_path):
+    img = np.random.default_rng(1).random((6, 9, 3)).astype(np.float32) * 3.0
+    img[2, 4] = (np.inf, -0.5, 1e-30)
+    g.write_image(tmp_path / "a.exr", img, "exr")
+    chans, w, h, planes = _read_exr((tmp_path / "a.exr").read_bytes())
+    assert (w, h) == (9, 6)
+    assert [c[0] for c in chans] == ["B", "G", "R"] and all(c[1:] == (2, 1, 1) for c in chans)
+    top_first = img[::-1]
+    for k, name in enumerate("RGB"):
+        assert np.array_equal(planes[name].view(np.uint32), np.ascontiguousarray(top_first[..., k]).view(np.uint32))
