@@ -369,7 +369,8 @@ def run_gpu(args, rank, world, local):
             "stage_bandwidth": stage_bandwidth(stages, npix, P, (fi1.photon_segments - fi0.photon_segments) / K,
                                                peak),
             "gpu_launches": int(launches),
-            "e2e": {"value": round(e2e, 3), "unit": "Mphotons/s", "h2d_bytes_per_step": 64,
+            "e2e": {"value": round(e2e, 3), "unit": "Mphotons/s",
+                    "h2d_bytes_per_step": int(N.lib.sppm_camera_upload_bytes()),
                     "d2h_bytes_per_step": int(npix * 3 * 4), "steps": E},
             "roofline": roof,
             "cpu_baseline": cpu,
@@ -450,13 +451,13 @@ def run_batched(args, device: int, K: int, W: int, precision: int):
     # end to end: every step sets each job's camera (host->device), runs one pass and reads each
     # job's progress counters back (device->host)
     E = max(5, min(K, 30))
-    fe0 = [b.frame_info(j) for j in ids]
+    fe0 = b.frame_infos(ids)
     t0 = time.perf_counter()
     for _ in range(E):
         for j, (_, _, _, cam) in zip(ids, jobs):
             b.set_camera(j, cam)
         b.run_passes(1)
-        fe = [b.frame_info(j) for j in ids]
+        fe = b.frame_infos(ids)
     te = time.perf_counter() - t0
     e2e = sum(y.photons_emitted - x.photons_emitted for x, y in zip(fe0, fe)) / te / 1e6
     # per-stage breakdown over a further 10-pass cycle (every stage timed, outside the timed region)
@@ -499,8 +500,9 @@ def run_batched(args, device: int, K: int, W: int, precision: int):
         "plain_loop": {"value": round(loop, 3), "unit": "Mphotons/s", "ms_per_pass_all_jobs": round(loop_ms, 4),
                        "note": "plain FP32 single-job contexts run one after another, device time per pass summed"},
         "speedup_vs_plain_loop": round(batched / loop, 3),
-        "e2e": {"value": round(e2e, 3), "unit": "Mphotons/s", "h2d_bytes_per_step": 64 * len(ids),
-                "d2h_bytes_per_step": 128 * len(ids), "steps": E},
+        "e2e": {"value": round(e2e, 3), "unit": "Mphotons/s",
+                "h2d_bytes_per_step": int(N.lib.sppm_camera_upload_bytes()) * len(ids),
+                "d2h_bytes_per_step": int(N.lib.sppm_batch_frame_record_bytes()) * len(ids), "steps": E},
         "setup_seconds": round(setup_s, 2),
         "_launches": int(launches), "_trace": tr, "_counters": cnt, "_photons": photons, "_ms": ms,
     }
@@ -665,7 +667,8 @@ def run_large(args, world, local, K, W):
             "stage_ms_per_launch": {k: round(v[0] / v[1], 4) for k, v in stages.items() if v[1]},
             "setup_seconds": {"generate": round(t_gen, 2), "gpu_bvh_build": round(t_bvh, 3), "upload": round(t_up, 2)},
             "gpu_launches": int(launches),
-            "e2e": {"value": round(e2e, 3), "unit": "Mphotons/s", "h2d_bytes_per_step": 64,
+            "e2e": {"value": round(e2e, 3), "unit": "Mphotons/s",
+                    "h2d_bytes_per_step": int(N.lib.sppm_camera_upload_bytes()),
                     "d2h_bytes_per_step": int(cfg.width * cfg.height * 12), "steps": E},
             "roofline": roof, "cpu_baseline": None, "clocks": clocks.summary(),
         }

@@ -108,6 +108,14 @@ class Batch:
         N.check(N.lib.sppm_batch_get_frame_info(self._h, job, C.byref(fi)))
         return fi
 
+    def frame_infos(self, jobs) -> list:
+        """frame_info of several jobs with one device-to-host copy."""
+        jobs = list(jobs)
+        ids = (C.c_uint32 * len(jobs))(*jobs)
+        out = (N.FrameInfo * len(jobs))()
+        N.check(N.lib.sppm_batch_get_frame_infos(self._h, ids, len(jobs), out))
+        return list(out)
+
     def save_checkpoint(self, job: int) -> bytes:
         n = int(N.lib.sppm_batch_checkpoint_bytes(self._h, job))
         buf = C.create_string_buffer(n)

@@ -113,6 +113,8 @@ int sppm_synchronize(sppm_ctx* c) {
     return c->rt.synchronize();
 }
 
+size_t sppm_camera_upload_bytes(void) { return sizeof(JobDesc); }
+
 int sppm_read_image(sppm_ctx* c, uint32_t kind, float* rgb, size_t num_floats) {
     if (!c || !rgb) return fail(SPPM_ERR_ARG, "null argument");
     if (kind > SPPM_IMAGE_DISPLAY) return fail(SPPM_ERR_ARG, "unknown image kind %u", kind);

@@ -273,6 +273,18 @@ int sppm_batch_get_frame_info(sppm_batch* b, uint32_t id, sppm_frame_info* fi) {
     return SPPM_OK;
 }
 
+int sppm_batch_get_frame_infos(sppm_batch* b, const uint32_t* ids, uint32_t n, sppm_frame_info* fi) {
+    if (!b || (n && (!ids || !fi))) return fail(SPPM_ERR_ARG, "null argument");
+    std::vector<Job*> jobs(n);
+    for (uint32_t k = 0; k < n; k++) {
+        jobs[k] = job_of(b, ids[k]);
+        if (!jobs[k]) return fail(SPPM_ERR_ARG, "no job %u", ids[k]);
+    }
+    return b->rt.frame_infos(jobs.data(), n, fi);
+}
+
+size_t sppm_batch_frame_record_bytes(void) { return sizeof(JobState); }
+
 int sppm_batch_get_info(sppm_batch* b, sppm_batch_info* info) {
     if (!b || !info) return fail(SPPM_ERR_ARG, "null argument");
     memset(info, 0, sizeof(*info));

@@ -7,6 +7,14 @@
 
 namespace sppm_dev {
 
+// the JobStates of up to kStateGatherMax job slots copied into out[0..n) (kernel parameter)
+constexpr uint32_t kStateGatherMax = 256;
+struct StateGather {
+    uint32_t n;
+    uint32_t slot[kStateGatherMax];
+};
+void launch_gather_states(const JobDesc* jobs, const StateGather& list, JobState* out, cudaStream_t s);
+
 // plain FP32 path (kernels_fp32.cu)
 void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
 void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, cudaStream_t s);  // mixed: 4-wide BVH traversal

@@ -1737,11 +1737,23 @@ __global__ void __launch_bounds__(1024) k_debug_trace(DevScene s, const float* o
     if (e) atomicOr(err, e);
 }
 
+// one block per listed job: its JobState word by word
+__global__ void k_gather_states(const JobDesc* jobs, StateGather list, JobState* out) {
+    static_assert(sizeof(JobState) % 4 == 0, "JobState is copied in 32-bit words");
+    if (blockIdx.x >= list.n) return;
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs[list.slot[blockIdx.x]].state);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(out + blockIdx.x);
+    for (uint32_t w = threadIdx.x; w < sizeof(JobState) / 4; w += blockDim.x) dst[w] = src[w];
+}
+
 // ----------------------------------------------------------------------------------------------
 // launchers
 // ----------------------------------------------------------------------------------------------
 static inline uint32_t blocks_for(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
 
+void launch_gather_states(const JobDesc* jobs, const StateGather& list, JobState* out, cudaStream_t s) {
+    if (list.n) k_gather_states<<<list.n, 64, 0, s>>>(jobs, list, out);
+}
 void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
     const uint32_t n = q.bins && ls.total < kRayBins ? kRayBins : ls.total;
     if (ls.total) k_frame_begin<<<blocks_for(n, 256), 256, 0, s>>>(ls, q);

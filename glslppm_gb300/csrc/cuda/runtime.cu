@@ -504,6 +504,11 @@ int Job::frame_info(sppm_frame_info* fi, cudaStream_t s) const {
     JobState st;
     SPPM_CK(cudaMemcpyAsync(&st, d_state, sizeof(st), cudaMemcpyDeviceToHost, s));
     SPPM_CK(cudaStreamSynchronize(s));
+    fill_frame_info(st, fi);
+    return SPPM_OK;
+}
+
+void fill_frame_info(const JobState& st, sppm_frame_info* fi) {
     memset(fi, 0, sizeof(*fi));
     fi->frames = st.frames_started;
     fi->eye_samples = st.eye_samples;
@@ -523,7 +528,6 @@ int Job::frame_info(sppm_frame_info* fi, cudaStream_t s) const {
     fi->counted_nodes = st.count_nodes;
     fi->counted_triangles = st.count_tris;
     fi->coop_segments = st.coop_segments;
-    return SPPM_OK;
 }
 
 namespace {
@@ -640,6 +644,7 @@ Runner::~Runner() {
     if (resolved_ev) cudaEventDestroy(resolved_ev);
     for (auto& t : tickets) cudaEventDestroy(t.ev);
     for (auto e : ticket_pool) cudaEventDestroy(e);
+    if (info_host) cudaFreeHost(info_host);
     if (side) {
         cudaStreamSynchronize(side);
         cudaStreamDestroy(side);
@@ -1016,6 +1021,34 @@ int Runner::read_image_async(Job& j, uint32_t kind, float* rgb, size_t bytes, ui
     if (ticket) *ticket = next_ticket;
     next_ticket++;
     return SPPM_OK;
+}
+
+int Runner::frame_infos(Job* const* jobs, uint32_t n, sppm_frame_info* out) {
+    if (n == 0) return SPPM_OK;
+    SPPM_CK(cudaSetDevice(device));
+    const uint32_t cap = std::max<uint32_t>(max_jobs, 1);
+    if (!info_host) {
+        int st = info_mem.reserve(Arena::align(sizeof(JobState) * cap));
+        if (st) return st;
+        SPPM_CK(cudaMallocHost(&info_host, sizeof(JobState) * cap));
+    }
+    JobState* d_out = reinterpret_cast<JobState*>(info_mem.base);
+    for (uint32_t i0 = 0; i0 < n; i0 += cap) {
+        const uint32_t m = std::min(cap, n - i0);
+        for (uint32_t c0 = 0; c0 < m; c0 += kStateGatherMax) {
+            StateGather list{};
+            list.n = std::min<uint32_t>(kStateGatherMax, m - c0);
+            for (uint32_t k = 0; k < list.n; k++) list.slot[k] = jobs[i0 + c0 + k]->slot;
+            launch_gather_states(d_jobs, list, d_out + c0, stream);
+        }
+        SPPM_CK(cudaMemcpyAsync(info_host, d_out, sizeof(JobState) * m, cudaMemcpyDeviceToHost, stream));
+        SPPM_CK(cudaStreamSynchronize(stream));
+        for (uint32_t k = 0; k < m; k++) {
+            fill_frame_info(info_host[k], out + i0 + k);
+            out[i0 + k].kernel_launches = kernel_launches;
+        }
+    }
+    return launch_check("frame counters");
 }
 
 int Runner::image_wait(uint64_t ticket, bool block, int* done) {

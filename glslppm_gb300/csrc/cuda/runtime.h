@@ -63,6 +63,9 @@ int validate_config(const sppm_config* c);
 void state_to_host_layout(uint32_t kind, void* buf, size_t bytes);
 int launch_check(const char* what);
 
+// the caller's view of a job's frame counters
+void fill_frame_info(const JobState& st, sppm_frame_info* fi);
+
 // one render job (scene + camera + progressive state)
 struct Job {
     sppm_config cfg{};
@@ -154,6 +157,8 @@ struct Runner {
     std::deque<Ticket> tickets;   // copies whose end has not been observed, oldest first
     std::vector<cudaEvent_t> ticket_pool;
     uint64_t next_ticket = 1;
+    Arena info_mem;                 // JobState[max_jobs] gathered by frame_infos
+    JobState* info_host = nullptr;  // page-locked copy
     uint32_t precision = SPPM_PRECISION_FP32, flags = 0, eye_interval = 10, max_jobs = 0;
     Arena desc_mem;                // JobDesc[max_jobs]
     JobDesc* d_jobs = nullptr;
@@ -196,6 +201,8 @@ struct Runner {
     int read_image_async(Job& j, uint32_t kind, float* rgb, size_t bytes, uint64_t* ticket);
     // waits for the copy of `ticket` (block) or reports whether it has ended (*done)
     int image_wait(uint64_t ticket, bool block, int* done);
+    // the frame counters of several jobs: one gather kernel and one copy
+    int frame_infos(Job* const* jobs, uint32_t n, sppm_frame_info* out);
     cudaEvent_t get_event();
     void timed(int stage, bool start, cudaStream_t s = nullptr);
 

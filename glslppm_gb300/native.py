@@ -143,6 +143,7 @@ SIGNATURES = {
     "sppm_run_passes": (C.c_int, [P, C.c_uint32]),
     "sppm_synchronize": (C.c_int, [P]),
     "sppm_read_image": (C.c_int, [P, C.c_uint32, P, C.c_size_t]),
+    "sppm_camera_upload_bytes": (C.c_size_t, []),
     "sppm_read_image_async": (C.c_int, [P, C.c_uint32, P, C.c_size_t, C.POINTER(C.c_uint64)]),
     "sppm_image_wait": (C.c_int, [P, C.c_uint64]),
     "sppm_image_query": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_int)]),
@@ -183,6 +184,8 @@ SIGNATURES = {
     "sppm_batch_time_passes": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_float)]),
     "sppm_batch_synchronize": (C.c_int, [P]),
     "sppm_batch_read_image": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.c_size_t]),
+    "sppm_batch_get_frame_infos": (C.c_int, [P, C.POINTER(C.c_uint32), C.c_uint32, P]),
+    "sppm_batch_frame_record_bytes": (C.c_size_t, []),
     "sppm_batch_read_image_async": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.c_size_t, C.POINTER(C.c_uint64)]),
     "sppm_batch_image_wait": (C.c_int, [P, C.c_uint64]),
     "sppm_batch_image_query": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_int)]),

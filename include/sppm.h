@@ -179,7 +179,10 @@ int sppm_create(const sppm_config* cfg, int device, sppm_ctx** out);
 /* Copies the scene to the device in the traversal layout (CGPURT::PrecalculateMeshData +
    CreateTextures, gpurt.cpp:8-16, 47-552). The caller's arrays are not retained. */
 int sppm_upload_scene(sppm_ctx* ctx, const sppm_scene* scene);
+/* Queues the camera's upload (the job descriptor, sppm_camera_upload_bytes() bytes, through a
+   page-locked staging slot; the frames already queued keep the previous camera). */
 int sppm_set_camera(sppm_ctx* ctx, const sppm_camera* cam);
+size_t sppm_camera_upload_bytes(void);
 /* Back to frame 0: re-seeds the random state (RandomizeTextures, glslppm.cpp:113-140). */
 int sppm_reset(sppm_ctx* ctx);
 /* Queues n SPPM frames (m_display, glslppm.cpp:214-536) on the context's stream. */

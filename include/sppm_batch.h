@@ -73,6 +73,10 @@ int sppm_batch_image_query(sppm_batch* b, uint64_t ticket, int* done);
 size_t sppm_batch_state_bytes(const sppm_batch* b, uint32_t job, uint32_t kind);
 int sppm_batch_read_state(sppm_batch* b, uint32_t job, uint32_t kind, void* dst, size_t bytes);
 int sppm_batch_get_frame_info(sppm_batch* b, uint32_t job, sppm_frame_info* info);
+/* sppm_batch_get_frame_info for n jobs at once (one device-to-host copy for all of them, of
+   sppm_batch_frame_record_bytes() bytes per job). */
+int sppm_batch_get_frame_infos(sppm_batch* b, const uint32_t* jobs, uint32_t n, sppm_frame_info* infos);
+size_t sppm_batch_frame_record_bytes(void);
 int sppm_batch_get_info(sppm_batch* b, sppm_batch_info* info);
 /* Checkpoints of one job (the layout of sppm_save_checkpoint): a job can move between a batch
    and a single-job context, or be preempted and resumed. */

@@ -96,6 +96,14 @@ def test_jobs_joining_and_leaving_keep_their_own_schedule():
         assert_same(b.read_state(a, k), ref_a[k], f"job a {k}")
         assert_same(b.read_state(j, k), ref_j[k], f"joined job {k}")
     assert b.frame_info(j).frames == 15 and b.frame_info(j).eye_samples == 2
+    # all jobs' counters in one call equal the one-job calls, field by field
+    many = b.frame_infos([j, a, a])
+    for got, want in zip(many, [b.frame_info(j), b.frame_info(a), b.frame_info(a)]):
+        for name, _ in N.FrameInfo._fields_:
+            assert getattr(got, name) == getattr(want, name) or name in ("bbox_min", "bbox_max", "aa_offset"), name
+        assert list(got.bbox_min) == list(want.bbox_min) and list(got.aa_offset) == list(want.aa_offset)
+    with pytest.raises(N.SppmError):
+        b.frame_infos([a, c])  # c has left
     with pytest.raises(N.SppmError):
         b.read_state(c, "hit_position")
     # the freed slot is reused
