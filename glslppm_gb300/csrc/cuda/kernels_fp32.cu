@@ -1405,7 +1405,12 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
                     if (q.perm) idx = q.perm[idx];
                     const float4 o = q.org[idx], d = q.dir[idx];
                     const uint32_t g = __float_as_uint(o.w);
-                    job_k = find_job(ls, g);
+                    const int nk = find_job(ls, g);
+                    if (err && nk != job_k) {  // an error belongs to the job whose ray raised it
+                        atomicOr(&ls.jobs[ls.job_ids[job_k]].state->err, err);
+                        err = 0;
+                    }
+                    job_k = nk;
                     if (COUNT && job_k != tc_job) {
                         flush_counts();
                         tc_job = job_k;

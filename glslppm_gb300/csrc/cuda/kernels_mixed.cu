@@ -107,7 +107,12 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
                 } else {
                     if (q.perm) idx = q.perm[idx];
                     const float4 o = q.org[idx], d = q.dir[idx];
-                    job_k = find_job(ls, __float_as_uint(o.w));
+                    const int nk = find_job(ls, __float_as_uint(o.w));
+                    if (err && nk != job_k) {  // an error belongs to the job whose ray raised it
+                        atomicOr(&ls.jobs[ls.job_ids[job_k]].state->err, err);
+                        err = 0;
+                    }
+                    job_k = nk;
                     const DevScene& S = ls.jobs[ls.job_ids[job_k]].scene;
                     nodes = S.nodes4;
                     tri_isect = S.tri_isect;

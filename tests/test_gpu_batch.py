@@ -136,3 +136,31 @@ def test_batch_rejects_mismatched_jobs():
     cfg.eye_pass_interval = 5
     with pytest.raises(N.SppmError):
         b.add_job(cfg, sc.to_mesh(), camera_for(sc, w, h))
+
+
+def test_watchdog_error_names_the_job_whose_rays_raised_it(cornell_metal):
+    """One job's BVH links form a cycle: its traversals hit their step bound and the batch reports
+    that job (not another job whose rays the same warps traced next); once it is removed the
+    other job runs on without an error.  (The mixed path's 4-wide tree is built from the links at
+    upload, which rejects such a scene.)"""
+    precision = N.PRECISION_FP32
+    arrays, d = cornell_metal
+    from tests.golden.fixtures import camera_from
+    bad = g.renderer.SceneArrays(**{k: (v.copy() if isinstance(v, np.ndarray) else v)
+                                    for k, v in arrays.__dict__.items()})
+    internal = bad.node_triangle[bad.order_base] < 0
+    bad.order_miss[internal] = 0  # back to the root
+    cam = camera_from(d, 16, 16)
+    b = g.Batch(precision=precision, max_jobs=4)
+    cfg = g.default_config(16, precision=precision)
+    good = b.add_job(cfg, arrays, cam)
+    broken = b.add_job(cfg, bad, cam)
+    b.run_passes(2)
+    with pytest.raises(N.SppmError) as e:
+        b.synchronize()
+    assert e.value.status == N.ERR_WATCHDOG
+    assert f"job {broken}:" in str(e.value), str(e.value)
+    b.remove_job(broken)
+    b.run_passes(2)
+    b.synchronize()
+    assert b.frame_info(good).frames == 4
