@@ -26,6 +26,42 @@ __device__ __forceinline__ float node_scale(uint8_t e) { return __uint_as_float(
 // ignored by fminf/fmaxf and the ray would enter every box the other axes allow)
 __device__ __forceinline__ float slab_dir(float d) { return fabsf(d) < 1e-30f ? copysignf(1e-30f, d) : d; }
 
+// byte k of w as an exact float: the byte placed in the low mantissa of 2^23, minus 2^23
+__device__ __forceinline__ float byte_f(uint32_t w, uint32_t sel) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f;
+}
+
+// slab distances of child K's box: plane = origin + byte * 2^e, so its distance along the ray is
+// byte * (2^e / d) + (origin - o) / d = fmaf(byte, A, B) with the per-node A = 2^e * (1/d) (exact:
+// a power-of-two scale) and B = fmaf(origin, 1/d, -o/d)
+template <int K>
+__device__ __forceinline__ void child_box(const float4& w2, const float4& w3, float Ax, float Ay, float Az, float Bx,
+                                          float By, float Bz, float tbest, float& tn, bool& hit) {
+    constexpr uint32_t sel = 0x7650u | (uint32_t)K;  // byte K of the word into byte 0, 0x4B into byte 3
+    const float ax = fmaf(byte_f(__float_as_uint(w2.x), sel), Ax, Bx);
+    const float ay = fmaf(byte_f(__float_as_uint(w2.y), sel), Ay, By);
+    const float az = fmaf(byte_f(__float_as_uint(w2.z), sel), Az, Bz);
+    const float bx = fmaf(byte_f(__float_as_uint(w2.w), sel), Ax, Bx);
+    const float by = fmaf(byte_f(__float_as_uint(w3.x), sel), Ay, By);
+    const float bz = fmaf(byte_f(__float_as_uint(w3.y), sel), Az, Bz);
+    const float t0 = fmaxf(fmax3(fminf(ax, bx), fminf(ay, by), fminf(az, bz)), 0.0f);
+    // the far bound widened by a few ulps so that rounding never rejects a grazing hit
+    const float t1 = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fmaxf(az, bz)) * 1.00000036f;
+    tn = t0;
+    hit = t0 <= t1 && t0 <= tbest;
+}
+
+__device__ __forceinline__ void cswap(float& ta, int32_t& ca, float& tb, int32_t& cb) {
+    if (tb < ta) {
+        const float t = ta;
+        ta = tb;
+        tb = t;
+        const int32_t c = ca;
+        ca = cb;
+        cb = c;
+    }
+}
+
 // closest hit through the 4-wide BVH; PHOTON rays skip emitters, eye rays of the first bounce
 // cull back faces (eyeraytrace.fs:130)
 template <bool PHOTON>
@@ -54,37 +90,31 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
         const uint32_t eb = __float_as_uint(w0.w);
         const float sx = node_scale(eb & 0xFF), sy = node_scale((eb >> 8) & 0xFF), sz = node_scale((eb >> 16) & 0xFF);
         const int cnt = (int)(eb >> 24);
-        const int32_t ch[4] = {__float_as_int(w1.x), __float_as_int(w1.y), __float_as_int(w1.z), __float_as_int(w1.w)};
-        const uint32_t qlx = __float_as_uint(w2.x), qly = __float_as_uint(w2.y), qlz = __float_as_uint(w2.z);
-        const uint32_t qhx = __float_as_uint(w2.w), qhy = __float_as_uint(w3.x), qhz = __float_as_uint(w3.y);
+        int32_t ch[4] = {__float_as_int(w1.x), __float_as_int(w1.y), __float_as_int(w1.z), __float_as_int(w1.w)};
         // slab test of the (up to) four children
         float tnear[4];
         bool hit[4];
+        const float Ax = sx * rx, Ay = sy * ry, Az = sz * rz;
+        const float Bx = fmaf(w0.x, rx, nx), By = fmaf(w0.y, ry, ny), Bz = fmaf(w0.z, rz, nz);
+        child_box<0>(w2, w3, Ax, Ay, Az, Bx, By, Bz, h.t, tnear[0], hit[0]);
+        child_box<1>(w2, w3, Ax, Ay, Az, Bx, By, Bz, h.t, tnear[1], hit[1]);
+        child_box<2>(w2, w3, Ax, Ay, Az, Bx, By, Bz, h.t, tnear[2], hit[2]);
+        child_box<3>(w2, w3, Ax, Ay, Az, Bx, By, Bz, h.t, tnear[3], hit[3]);
+        // leaf children: their triangles in child order (a closer hit shrinks the search), one copy
+        // of the test in a loop over the leaves
+        uint32_t leaves = 0;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            const float lx = fmaf((float)((qlx >> (8 * k)) & 0xFF), sx, w0.x);
-            const float ly = fmaf((float)((qly >> (8 * k)) & 0xFF), sy, w0.y);
-            const float lz = fmaf((float)((qlz >> (8 * k)) & 0xFF), sz, w0.z);
-            const float hx = fmaf((float)((qhx >> (8 * k)) & 0xFF), sx, w0.x);
-            const float hy = fmaf((float)((qhy >> (8 * k)) & 0xFF), sy, w0.y);
-            const float hz = fmaf((float)((qhz >> (8 * k)) & 0xFF), sz, w0.z);
-            const float ax = fmaf(lx, rx, nx), bx = fmaf(hx, rx, nx);
-            const float ay = fmaf(ly, ry, ny), by = fmaf(hy, ry, ny);
-            const float az = fmaf(lz, rz, nz), bz = fmaf(hz, rz, nz);
-            const float t0 = fmaxf(fmax3(fminf(ax, bx), fminf(ay, by), fminf(az, bz)), 0.0f);
-            // widen the far bound by a few ulps so that rounding never rejects a grazing hit
-            const float t1 = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fmaxf(az, bz)) * 1.00000036f;
-            tnear[k] = t0;
-            hit[k] = k < cnt && t0 <= t1 && t0 <= h.t;
-        }
-        // leaf children: test their triangle now (a closer hit shrinks the search)
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
+            hit[k] = hit[k] && k < cnt;
             if (!hit[k] || ch[k] >= 0) continue;
             hit[k] = false;
-            const int32_t code = ~ch[k];
-            if (PHOTON && (code & kEmitterBit)) continue;
-            const int32_t tri = code & kTriMask;
+            if (!(PHOTON && (~ch[k] & kEmitterBit))) leaves |= 1u << k;
+        }
+        while (leaves) {
+            const int k = __ffs(leaves) - 1;
+            leaves &= leaves - 1;
+            const int32_t ck = k == 0 ? ch[0] : (k == 1 ? ch[1] : (k == 2 ? ch[2] : ch[3]));
+            const int32_t tri = ~ck & kTriMask;
             const float4 a = __ldg(&tri_isect[(size_t)tri * 3 + 0]);
             const float4 b = __ldg(&tri_isect[(size_t)tri * 3 + 1]);
             const float4 c = __ldg(&tri_isect[(size_t)tri * 3 + 2]);
@@ -109,34 +139,27 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
                 h.bw = u;
             }
         }
-        // internal children: nearest next, the others on the stack (farthest first)
-        int32_t order[4];
-        float ot[4];
-        int n = 0;
+        // internal children hit before the closest hit so far, sorted near to far: the nearest
+        // is next, the others go on the stack farthest first
+        const float inf = __int_as_float(0x7f800000);
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            if (hit[k] && tnear[k] <= h.t) {
-                int j = n++;
-                while (j > 0 && ot[j - 1] < tnear[k]) {  // descending distance
-                    ot[j] = ot[j - 1];
-                    order[j] = order[j - 1];
-                    j--;
-                }
-                ot[j] = tnear[k];
-                order[j] = ch[k];
-            }
-        }
-        if (n > 0) {
-            if (sp + n - 1 > kStack) {
+        for (int k = 0; k < 4; k++)
+            if (!(hit[k] && tnear[k] <= h.t)) tnear[k] = inf;
+        cswap(tnear[0], ch[0], tnear[1], ch[1]);
+        cswap(tnear[2], ch[2], tnear[3], ch[3]);
+        cswap(tnear[0], ch[0], tnear[2], ch[2]);
+        cswap(tnear[1], ch[1], tnear[3], ch[3]);
+        cswap(tnear[1], ch[1], tnear[2], ch[2]);
+        if (tnear[0] < inf) {
+            const int pushes = (tnear[1] < inf) + (tnear[2] < inf) + (tnear[3] < inf);
+            if (sp + pushes > kStack) {
                 err |= kErrWatchdogTraverse;
                 break;
             }
-            for (int j = 0; j < n - 1; j++) {
-                stack_node[sp] = order[j];
-                stack_t[sp] = ot[j];
-                sp++;
-            }
-            cur = order[n - 1];
+            if (tnear[3] < inf) stack_node[sp] = ch[3], stack_t[sp++] = tnear[3];
+            if (tnear[2] < inf) stack_node[sp] = ch[2], stack_t[sp++] = tnear[2];
+            if (tnear[1] < inf) stack_node[sp] = ch[1], stack_t[sp++] = tnear[1];
+            cur = ch[0];
             continue;
         }
         bool found = false;

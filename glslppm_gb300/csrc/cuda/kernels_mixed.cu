@@ -23,45 +23,9 @@
 
 namespace sppm_dev {
 
-// byte k of w as an exact float: the byte placed in the low mantissa of 2^23, minus 2^23
-__device__ __forceinline__ float byte_f(uint32_t w, uint32_t sel) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f;
-}
-
 constexpr int kTraceBlock = 128;
 constexpr int kSmemStack = 16;  // top of each thread's stack, in shared memory (16 KB per block)
 constexpr int kLocalStack = kStack - kSmemStack;  // deeper entries, in local memory (rarely touched)
-
-// slab distances of child K's box: plane = origin + byte * 2^e, so its distance along the ray is
-// byte * (2^e / d) + (origin - o) / d = fmaf(byte, A, B) with the per-node A = 2^e * (1/d) (exact:
-// a power-of-two scale) and B = fmaf(origin, 1/d, -o/d)
-template <int K>
-__device__ __forceinline__ void child_box(const float4& w2, const float4& w3, float Ax, float Ay, float Az, float Bx,
-                                          float By, float Bz, float tbest, float& tn, bool& hit) {
-    constexpr uint32_t sel = 0x7650u | (uint32_t)K;  // byte K of the word into byte 0, 0x4B into byte 3
-    const float ax = fmaf(byte_f(__float_as_uint(w2.x), sel), Ax, Bx);
-    const float ay = fmaf(byte_f(__float_as_uint(w2.y), sel), Ay, By);
-    const float az = fmaf(byte_f(__float_as_uint(w2.z), sel), Az, Bz);
-    const float bx = fmaf(byte_f(__float_as_uint(w2.w), sel), Ax, Bx);
-    const float by = fmaf(byte_f(__float_as_uint(w3.x), sel), Ay, By);
-    const float bz = fmaf(byte_f(__float_as_uint(w3.y), sel), Az, Bz);
-    const float t0 = fmaxf(fmax3(fminf(ax, bx), fminf(ay, by), fminf(az, bz)), 0.0f);
-    // the far bound widened by a few ulps so that rounding never rejects a grazing hit
-    const float t1 = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fmaxf(az, bz)) * 1.00000036f;
-    tn = t0;
-    hit = t0 <= t1 && t0 <= tbest;
-}
-
-__device__ __forceinline__ void cswap(float& ta, int32_t& ca, float& tb, int32_t& cb) {
-    if (tb < ta) {
-        const float t = ta;
-        ta = tb;
-        tb = t;
-        const int32_t c = ca;
-        ca = cb;
-        cb = c;
-    }
-}
 
 // photon segments through the 4-wide BVH: persistent warps with dynamic ray fetch (a lane whose
 // ray finished takes the next queued ray), one node per lane per step, closest child first, the
@@ -154,14 +118,22 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
             child_box<2>(w2, w3, Ax, Ay, Az, Bx, By, Bz, ht, t[2], hit[2]);
             child_box<3>(w2, w3, Ax, Ay, Az, Bx, By, Bz, ht, t[3], hit[3]);
             int32_t c[4] = {__float_as_int(w1.x), __float_as_int(w1.y), __float_as_int(w1.z), __float_as_int(w1.w)};
+            // leaf children hit: their triangles, in child order (photons pass through emitters);
+            // one copy of the test in a loop over the leaves, so a warp runs it as many times as
+            // its lane with the most leaves needs
+            uint32_t leaves = 0;
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 hit[k] = hit[k] && k < cnt;
                 if (!hit[k] || c[k] >= 0) continue;
-                // a leaf child: its triangle (photons pass through emitters)
                 hit[k] = false;
-                const int32_t code = ~c[k];
-                if (code & kEmitterBit) continue;
+                if (!(~c[k] & kEmitterBit)) leaves |= 1u << k;
+            }
+            while (leaves) {
+                const int k = __ffs(leaves) - 1;
+                leaves &= leaves - 1;
+                const int32_t ck = k == 0 ? c[0] : (k == 1 ? c[1] : (k == 2 ? c[2] : c[3]));
+                const int32_t code = ~ck;
                 const float4 a = __ldg(&tri_isect[(size_t)code * 3 + 0]);
                 const float4 b = __ldg(&tri_isect[(size_t)code * 3 + 1]);
                 const float4 cc = __ldg(&tri_isect[(size_t)code * 3 + 2]);
