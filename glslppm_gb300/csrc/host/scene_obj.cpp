@@ -5,6 +5,9 @@
 // shader path and the parity tests compare it word for word:
 //  * lines are read in chunks of at most 79 characters (fgets with an 80-byte buffer,
 //    mesh.cpp:137,139 and :209,262); a longer line continues as a new "line";
+//  * every mtllib line's MTL file is read before any usemtl line is matched (the reference reads
+//    them in a first pass over the file, mesh.cpp:138-149), so a usemtl may name a material of
+//    an MTL file listed further down;
 //  * an MTL material is appended when its "Ns" line is read (mesh.cpp:178-186); Ka/Kd/Ks carry
 //    over from the previous material when a block omits them; "Ke" is read as Ka (:155);
 //  * material and usemtl names keep their trailing characters (newline) and must match exactly
@@ -14,6 +17,8 @@
 //  * normals are normalised when read (:272-276); positions are p*scale+offset (:632-634);
 //  * the material classifier of mesh.cpp:520-611 (mirror/plastic/glossy/glass/light, diffuse
 //    albedo x0.9, glass albedo square-rooted) and the packed glossiness of gpurt.cpp:126.
+// The file is read once and its lines are parsed in parallel ranges (cut at line ends, each cut
+// into the same 79-character chunks); materials and errors are resolved afterwards in file order.
 // Deliberate differences, reported as errors instead of undefined behaviour: unreadable files,
 // malformed faces and out-of-range indices (SPPM_ERR_IO), textured (map_Kd) and "sss" materials
 // (SPPM_ERR_UNSUPPORTED).  The MTL file is opened relative to the OBJ file's directory.
@@ -22,8 +27,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "scene_internal.h"
@@ -154,83 +161,170 @@ void sppm_mesh::prepare_lights() {
     for (size_t i = 0; i < light_cdf.size(); i++) light_cdf[i] = light_cdf[i] / light_area;
 }
 
+namespace {
+
+// what one range of the file's lines holds, in file order
+struct ObjPart {
+    std::vector<float> v, n;
+    std::vector<int> vind, nind;  // per face vertex (0-based; -1 for a missing normal)
+    uint32_t faces = 0;
+    bool no_normals = false;
+    // mtllib and usemtl lines (resolved in file order afterwards: reading an MTL file appends
+    // materials that later usemtl lines match) and the first malformed face
+    struct Event {
+        uint32_t face;  // faces of this part before the line
+        int kind;       // 0 mtllib, 1 usemtl, 2 malformed face
+        std::string name;
+    };
+    std::vector<Event> events;
+};
+
+// one fgets chunk of the reference's loop (mesh.cpp:209-345); false after a malformed face
+bool parse_obj_line(const char* line, ObjPart& P) {
+    if (starts_with(line, "mtllib")) {
+        std::string name = tail(line, 7);
+        if (!name.empty()) name.erase(name.size() - 1, 1);  // the reference drops the last character
+        P.events.push_back({P.faces, 0, name});
+    }
+    if (line[0] == 'v') {
+        if (line[1] == 'n') {
+            float x = 0, y = 0, z = 0;
+            sscanf(&line[2], "%f %f %f", &x, &y, &z);
+            const float l = sppm::sqrt_f32(x * x + y * y + z * z);
+            P.n.push_back(x / l);
+            P.n.push_back(y / l);
+            P.n.push_back(z / l);
+        } else if (line[1] == 't') {
+            // texture coordinates are only used by textured materials, which are rejected
+        } else {
+            float x = 0, y = 0, z = 0;
+            sscanf(&line[1], "%f %f %f", &x, &y, &z);
+            P.v.push_back(x);
+            P.v.push_back(y);
+            P.v.push_back(z);
+        }
+    }
+    if (starts_with(line, "usemtl")) {
+        P.events.push_back({P.faces, 1, tail(line, 7)});
+    } else if (line[0] == 'f') {
+        char w[3][32];
+        if (sscanf(&line[1], "%31s %31s %31s", w[0], w[1], w[2]) != 3) {
+            P.events.push_back({P.faces, 2, std::string()});
+            return false;
+        }
+        for (int k = 0; k < 3; k++) {
+            int vi, ti, ni;
+            split_face_vertex(w[k], &vi, &ti, &ni);
+            P.vind.push_back(vi - 1);
+            if (ni) P.nind.push_back(ni - 1);
+            else {
+                P.nind.push_back(-1);
+                P.no_normals = true;
+            }
+        }
+        P.faces++;
+    }
+    return true;
+}
+
+// the lines of buf[begin, end) (begin at a line start), cut into chunks of at most 79 characters
+// the way fgets(line, 80, fp) cuts them
+void parse_obj_range(const char* buf, size_t begin, size_t end, ObjPart& P) {
+    char line[81];
+    size_t p = begin;
+    while (p < end) {
+        const char* nl = static_cast<const char*>(memchr(buf + p, '\n', end - p));
+        const size_t stop = nl ? (size_t)(nl - buf) + 1 : end;  // past the newline
+        while (p < stop) {
+            const size_t len = std::min<size_t>(79, stop - p);
+            memcpy(line, buf + p, len);
+            line[len] = '\0';
+            p += len;
+            if (!parse_obj_line(line, P)) return;
+        }
+    }
+}
+
+}  // namespace
+
 extern "C" int sppm_mesh_load_obj(const char* path, const float offset[3], float scale, sppm_mesh** out) {
     if (!path || !offset || !out) return fail(SPPM_ERR_ARG, "sppm_mesh_load_obj: null argument");
     *out = nullptr;
-    FILE* fp = fopen(path, "r");
+    FILE* fp = fopen(path, "rb");
     if (!fp) return fail(SPPM_ERR_IO, "cannot open OBJ file '%s'", path);
-
-    std::vector<MtlEntry> mtls;
-    std::vector<float> v, n, t;
-    std::vector<int> vind, nind, tind, mind;
-    bool no_normals = false, no_texcoords = false, no_materials = true;
-    int cmaterial = 0;
-    char line[81];
-    while (fgets(line, 80, fp) != nullptr) {
-        if (starts_with(line, "mtllib")) {
-            std::string name = tail(line, 7);
-            if (!name.empty()) name.erase(name.size() - 1, 1);  // the reference drops the last character
-            const int st = read_mtl(dir_of(path) + name, mtls);
-            if (st != SPPM_OK) {
-                fclose(fp);
-                return st;
-            }
-        }
-        if (line[0] == 'v') {
-            if (line[1] == 'n') {
-                float x = 0, y = 0, z = 0;
-                sscanf(&line[2], "%f %f %f", &x, &y, &z);
-                const float l = sppm::sqrt_f32(x * x + y * y + z * z);
-                n.push_back(x / l);
-                n.push_back(y / l);
-                n.push_back(z / l);
-            } else if (line[1] == 't') {
-                float a = 0, b = 0;
-                sscanf(&line[2], "%f %f", &a, &b);
-                t.push_back(a);
-                t.push_back(b);
-            } else {
-                float x = 0, y = 0, z = 0;
-                sscanf(&line[1], "%f %f %f", &x, &y, &z);
-                v.push_back(x);
-                v.push_back(y);
-                v.push_back(z);
-            }
-        }
-        if (starts_with(line, "usemtl")) {
-            const std::string name = tail(line, 7);
-            for (size_t i = 0; i < mtls.size(); i++) {
-                if (name == mtls[i].name) {
-                    cmaterial = (int)i;
-                    no_materials = false;
-                    break;
-                }
-            }
-        } else if (line[0] == 'f') {
-            char s[3][32];
-            if (sscanf(&line[1], "%31s %31s %31s", s[0], s[1], s[2]) != 3) {
-                fclose(fp);
-                return fail(SPPM_ERR_IO, "'%s': face line with fewer than three vertices", path);
-            }
-            mind.push_back(cmaterial);
-            for (int k = 0; k < 3; k++) {
-                int vi, ti, ni;
-                split_face_vertex(s[k], &vi, &ti, &ni);
-                vind.push_back(vi - 1);
-                if (ni) nind.push_back(ni - 1);
-                else {
-                    nind.push_back(-1);
-                    no_normals = true;
-                }
-                if (ti) tind.push_back(ti - 1);
-                else {
-                    tind.push_back(-1);
-                    no_texcoords = true;
-                }
-            }
-        }
+    std::vector<char> buf;
+    {
+        char block[1 << 16];
+        size_t got;
+        while ((got = fread(block, 1, sizeof block, fp)) > 0) buf.insert(buf.end(), block, block + got);
     }
     fclose(fp);
+    // fgets stops at a NUL byte's line as text functions see it: keep the text before the first
+    const size_t size = std::find(buf.begin(), buf.end(), '\0') - buf.begin();
+
+    // ranges of whole lines, parsed in parallel
+    unsigned threads = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    if (size < (4u << 20)) threads = 1;
+    std::vector<size_t> cut(threads + 1, size);
+    cut[0] = 0;
+    for (unsigned k = 1; k < threads; k++) {
+        size_t c = std::max(cut[k - 1], size * k / threads);
+        const char* nl = c < size ? static_cast<const char*>(memchr(buf.data() + c, '\n', size - c)) : nullptr;
+        cut[k] = nl ? (size_t)(nl - buf.data()) + 1 : size;
+    }
+    std::vector<ObjPart> parts(threads);
+    {
+        std::vector<std::thread> pool;
+        for (unsigned k = 1; k < threads; k++)
+            pool.emplace_back(parse_obj_range, buf.data(), cut[k], cut[k + 1], std::ref(parts[k]));
+        parse_obj_range(buf.data(), cut[0], cut[1], parts[0]);
+        for (auto& th : pool) th.join();
+    }
+    buf.clear();
+    buf.shrink_to_fit();
+
+    // every MTL file first, in file order (the reference's first pass, mesh.cpp:138-149, reads
+    // them all before its second pass matches any usemtl line)
+    std::vector<MtlEntry> mtls;
+    for (const ObjPart& P : parts)
+        for (const ObjPart::Event& e : P.events)
+            if (e.kind == 0) {
+                const int st = read_mtl(dir_of(path) + e.name, mtls);
+                if (st != SPPM_OK) return st;
+            }
+    // then, in file order, the material switches and the first malformed face
+    std::vector<int> mind;
+    bool no_normals = false, no_materials = true;
+    int cmaterial = 0;
+    std::vector<float> v, n;
+    std::vector<int> vind, nind;
+    for (ObjPart& P : parts) {
+        uint32_t done = 0;  // faces of this part given a material so far
+        for (const ObjPart::Event& e : P.events) {
+            mind.insert(mind.end(), e.face - done, cmaterial);
+            done = e.face;
+            if (e.kind == 0) {
+                continue;
+            } else if (e.kind == 1) {
+                for (size_t i = 0; i < mtls.size(); i++) {
+                    if (e.name == mtls[i].name) {
+                        cmaterial = (int)i;
+                        no_materials = false;
+                        break;
+                    }
+                }
+            } else {
+                return fail(SPPM_ERR_IO, "'%s': face line with fewer than three vertices", path);
+            }
+        }
+        mind.insert(mind.end(), P.faces - done, cmaterial);
+        no_normals = no_normals || P.no_normals;
+        v.insert(v.end(), P.v.begin(), P.v.end());
+        n.insert(n.end(), P.n.begin(), P.n.end());
+        vind.insert(vind.end(), P.vind.begin(), P.vind.end());
+        nind.insert(nind.end(), P.nind.begin(), P.nind.end());
+        P = ObjPart();
+    }
 
     std::unique_ptr<sppm_mesh> m(new sppm_mesh());
     const uint32_t nt = (uint32_t)mind.size();
@@ -266,7 +360,6 @@ extern "C" int sppm_mesh_load_obj(const char* path, const float offset[3], float
             }
         }
     }
-    (void)no_texcoords;  // texcoords are only read for textured materials, which are rejected
 
     bool have_light = false;
     if (!no_materials) {

@@ -104,6 +104,65 @@ def test_loader_quirks_equal_reference(tmp_path):
     assert_scene_equal(ref, mine)
 
 
+def _quirky_obj(tmp_path, name, pad_lines):
+    """An OBJ with material switches, a second mtllib half way, missing normals, quads and long
+    lines, padded with `pad_lines` long comment lines between its lines (the padding changes no
+    data: a comment chunk starts with '#' or 'x')."""
+    (tmp_path / "q.mtl").write_text("newmtl a\nKd 0.5 0.25 0.125\nNs 10\nnewmtl b\nKs 0.5 0.5 0.5\nNs 100\n")
+    (tmp_path / "r.mtl").write_text("newmtl lamp\nKe 2 2 2\nNs 0\nnewmtl gloss\nKs 1 1 1\nNs 40\n")
+    rng = np.random.default_rng(5)
+    lines = ["mtllib q.mtl\n"]
+    pts = rng.random((600, 3)).astype(np.float32)
+    lines += ["v %.9g %.9g %.9g\n" % tuple(map(float, p)) for p in pts]
+    lines += ["vn 0 0 2\n", "vn 0 1 0\n", "vn 1 0 0\n"]
+    mats = ["a\n", "b\n", "lamp\n", "gloss\n", "none\n"]
+    for t in range(3000):
+        if t == 1500:
+            lines.append("mtllib r.mtl\n")
+        if t % 97 == 0:
+            lines.append("usemtl " + mats[(t // 97) % len(mats)])
+        a, b, c, d4 = rng.integers(1, 601, size=4)
+        if t % 7 == 3:
+            lines.append(f"f {a}//3 {b}//1 {c}//2 {d4}//1\n")
+        elif t == 2222:
+            lines.append(f"f {a}//1 {b} {c}//2\n")  # one missing normal: face normals everywhere
+        else:
+            lines.append(f"f {a}//1 {b}//2 {c}//3\n")
+    pad = "# " + "x" * 300 + "\n"
+    per_line = -(-pad_lines // len(lines))  # padding lines after each line (rounded up)
+    out = []
+    for line in lines:
+        out.append(line)
+        out.extend([pad] * per_line)
+    (tmp_path / name).write_text("".join(out))
+    return tmp_path / name
+
+
+def test_obj_reader_threads_give_the_sequential_result(tmp_path):
+    """A file above the size at which the reader splits its lines across threads gives the same
+    arrays as the same lines read in one range (materials switch and an mtllib sits across the
+    ranges' boundaries)."""
+    small = _quirky_obj(tmp_path, "small.obj", 0)
+    big = _quirky_obj(tmp_path, "big.obj", 16000)
+    assert small.stat().st_size < (4 << 20) < big.stat().st_size
+    a = g.Mesh.load_obj(str(small), (0, 0, 0), 1.5).arrays()
+    b = g.Mesh.load_obj(str(big), (0, 0, 0), 1.5).arrays()
+    for k in ("positions", "normals", "material_ids", "materials", "light_cdf", "light_triangles"):
+        x, y = getattr(a, k), getattr(b, k)
+        assert np.array_equal(np.asarray(x).view(np.uint8), np.asarray(y).view(np.uint8)), k
+
+
+@pytest.mark.reference
+def test_threaded_obj_reader_equals_reference(tmp_path):
+    from oracle.build import build_ref
+    from oracle.refdump import run_ref_host_dump
+    build_ref()
+    big = _quirky_obj(tmp_path, "big.obj", 16000)
+    ref = run_ref_host_dump(big, 1.5)
+    mine = g.Mesh.load_obj(str(big), (0, 0, 0), 1.5).build_bvh().arrays()
+    assert_scene_equal(ref, mine)
+
+
 @pytest.mark.reference
 def test_drop_in_gpurt_header_with_reference_host_code(tmp_path):
     """include/sppm_gpurt.hpp compiled into the reference's own mesh.cpp/bvh.cpp/camera.cpp flattens
