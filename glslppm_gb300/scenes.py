@@ -21,6 +21,14 @@ import numpy as np
 from .renderer import MATERIAL_DTYPE
 
 BRDF_LIGHT, BRDF_MATTE, BRDF_MIRROR = -1, 0, 1
+# the other classes of the reference's material classifier (mesh.cpp:520-611)
+BRDF_GLASS, BRDF_PLASTIC, BRDF_GLOSSY, BRDF_GLOSSY_GLASS, BRDF_GLOSSY_PLASTIC = 2, 3, 4, 5, 6
+
+
+def packed_glossiness(specularity: float) -> float:
+    """g = 1 / ((2 / (1 - specularity))^2.71828 + 1) (gpurt.cpp:126), in single precision."""
+    f = np.float32
+    return float(f(1.0) / (f(f(2.0) / (f(1.0) - f(specularity))) ** f(2.71828) + f(1.0)))
 
 
 @dataclass
@@ -30,15 +38,32 @@ class MaterialSpec:
     color: tuple  # final albedo / emission as the renderer uses it
     eta: float = 1.7
     glossiness: float = 0.0
+    specularity: float = 1.0  # Ns / 100 of the glossy classes (>= 0.5), for the MTL block
 
     def mtl(self) -> str:
-        """MTL block that the reference loader classifies into this material (mesh.cpp:520-611)."""
+        """MTL block that the reference loader classifies into this material (mesh.cpp:520-611):
+        Ka > 0 makes a light; Ns = 100 with Ks = (1,1,1) a mirror, with 0 < |Ks|^2 < 3 plastic;
+        Ns < 100 the glossy classes; a name starting with "glass" glass, eta = |Ks|^2 / 3 + 1; the
+        loader scales matte and plastic albedo by 0.9 and takes the square root of glass albedo."""
+        zero = (0.0, 0.0, 0.0)
+        ks_eta = (math.sqrt(max(self.eta - 1.0, 0.0)),) * 3  # |Ks|^2 / 3 + 1 = eta
+        ns = 100.0 if self.brdf in (BRDF_MIRROR, BRDF_GLASS, BRDF_PLASTIC, BRDF_MATTE) else 100.0 * self.specularity
         if self.brdf == BRDF_LIGHT:
-            ka, kd, ks, ns = (1.0, 1.0, 1.0), self.color, (0.0, 0.0, 0.0), 0.0
+            ka, kd, ks, ns = (1.0, 1.0, 1.0), self.color, zero, 0.0
         elif self.brdf == BRDF_MIRROR:
-            ka, kd, ks, ns = (0.0, 0.0, 0.0), self.color, (1.0, 1.0, 1.0), 100.0
-        else:  # the loader scales Lambertian albedo by 0.9
-            ka, kd, ks, ns = (0.0, 0.0, 0.0), tuple(c / 0.9 for c in self.color), (0.0, 0.0, 0.0), 100.0
+            ka, kd, ks = zero, self.color, (1.0, 1.0, 1.0)
+        elif self.brdf == BRDF_GLOSSY:
+            ka, kd, ks = zero, self.color, (1.0, 1.0, 1.0)
+        elif self.brdf in (BRDF_GLASS, BRDF_GLOSSY_GLASS):
+            if not self.name.startswith("glass"):
+                raise ValueError("the reference loader makes glass of materials named glass*")
+            ka, kd, ks = zero, tuple(c * c for c in self.color), ks_eta
+        elif self.brdf == BRDF_PLASTIC:
+            ka, kd, ks = zero, tuple(c / 0.9 for c in self.color), (0.5, 0.5, 0.5)
+        elif self.brdf == BRDF_GLOSSY_PLASTIC:
+            ka, kd, ks = zero, self.color, (0.5, 0.5, 0.5)
+        else:  # matte: the loader scales Lambertian albedo by 0.9
+            ka, kd, ks = zero, tuple(c / 0.9 for c in self.color), zero
         f = lambda v: " ".join("%.9g" % x for x in v)
         return f"newmtl {self.name}\nKa {f(ka)}\nKd {f(kd)}\nKs {f(ks)}\nNs {ns:.1f}\n"
 
@@ -178,6 +203,32 @@ def cornell_box(segments: int = 64, rings: int = 32) -> SceneSpec:
     nrm = np.concatenate([p[1] for p in parts]).astype(np.float32)
     mid = np.concatenate([np.full(len(p[0]), p[2], dtype=np.int32) for p in parts])
     return SceneSpec(pos, nrm, mid, mats)
+
+
+def materials_box(segments: int = 16, rings: int = 8, light: bool = True) -> SceneSpec:
+    """The Cornell box with a material of every class the reference's classifier makes: the two
+    spheres are half glass / half glossy glass and half plastic / half glossy plastic, the left
+    wall glossy metal.  light=False turns the ceiling light into a white wall: with no emitting
+    triangle the photons come from the environment (GenerateIBLSample, photontrace.fs:283-341)
+    and eye rays that leave the scene see the sky colour."""
+    sc = cornell_box(segments, rings)
+    mats = list(sc.materials) + [
+        MaterialSpec("glass", BRDF_GLASS, (0.95, 0.95, 0.95), eta=1.5),
+        MaterialSpec("plastic", BRDF_PLASTIC, (0.6, 0.3, 0.2)),
+        MaterialSpec("glossy", BRDF_GLOSSY, (0.8, 0.8, 0.8), glossiness=packed_glossiness(0.5), specularity=0.5),
+        MaterialSpec("glass_glossy", BRDF_GLOSSY_GLASS, (0.9, 0.9, 0.95), eta=1.5,
+                     glossiness=packed_glossiness(0.6), specularity=0.6),
+        MaterialSpec("plastic_glossy", BRDF_GLOSSY_PLASTIC, (0.2, 0.5, 0.7), glossiness=packed_glossiness(0.7),
+                     specularity=0.7),
+    ]
+    ids = sc.material_ids.copy()
+    s1, s2 = np.nonzero(ids == 4)[0], np.nonzero(ids == 5)[0]
+    ids[s1[: len(s1) // 2]], ids[s1[len(s1) // 2:]] = 6, 9
+    ids[s2[: len(s2) // 2]], ids[s2[len(s2) // 2:]] = 7, 10
+    ids[ids == 1] = 8
+    if not light:
+        ids[ids == 3] = 0
+    return SceneSpec(sc.positions, sc.normals, ids, mats, sc.camera_origin, sc.camera_lookat, sc.fov)
 
 
 @dataclass

@@ -120,6 +120,18 @@ def test_eye_rays_with_zero_direction_components_bit_exact(cornell_c1_mesh, w, h
     run_pair(cfg, mesh.scene(), flat_camera(sc, w, h), [1, 10, 11, 21])
 
 
+@pytest.mark.parametrize("light", [True, False])
+def test_state_bit_exact_every_material_class(light):
+    """Glass, plastic, glossy metal, glossy glass and glossy plastic surfaces; without the light,
+    photons from the environment (GenerateIBLSample) and the sky seen by escaping eye rays."""
+    from glslppm_gb300 import scenes
+    sc = scenes.materials_box(light=light)
+    cfg = g.default_config(40, height=32, photon_width=64, photon_height=32, radius_rule=N.RADIUS_DIAGONAL,
+                           radius_fraction=0.01)
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 40, 32, sc.fov)
+    run_pair(cfg, sc.to_mesh().scene(), cam, [1, 10, 11, 21])
+
+
 def test_state_bit_exact_non_square_and_hash_seed(cornell_c1_mesh):
     sc, mesh = cornell_c1_mesh
     cfg = g.default_config(40, height=24, photon_width=48, photon_height=20, hash_slots=1500,

@@ -104,6 +104,23 @@ def test_loader_quirks_equal_reference(tmp_path):
     assert_scene_equal(ref, mine)
 
 
+@pytest.mark.reference
+@pytest.mark.parametrize("light", [True, False])
+def test_every_material_class_round_trips_through_the_reference_loader(tmp_path, light):
+    """The MTL dialect of scenes.MaterialSpec.mtl makes the reference's classifier produce every
+    BRDF class of materials_box; our loader gives the same arrays."""
+    from oracle.build import build_ref
+    from oracle.refdump import run_ref_host_dump
+    build_ref()
+    spec = scenes.materials_box(light=light)
+    obj = spec.write_obj(tmp_path / "m.obj")
+    ref = run_ref_host_dump(obj, 1.0)
+    mine = g.Mesh.load_obj(str(obj)).build_bvh().arrays()
+    assert_scene_equal(ref, mine)
+    assert [int(b) for b in mine.materials["brdf"]] == [m.brdf for m in spec.materials]
+    assert (len(mine.light_cdf) > 0) == light
+
+
 def _quirky_obj(tmp_path, name, pad_lines):
     """An OBJ with material switches, a second mtllib half way, missing normals, quads and long
     lines, padded with `pad_lines` long comment lines between its lines (the padding changes no

@@ -67,3 +67,14 @@ def test_oracle_equals_reference_shaders_cornell_box(cornell_c1_mesh):
     sc, mesh = cornell_c1_mesh
     cam = g.look_at(sc.camera_origin, sc.camera_lookat, 32, 32, sc.fov)
     run(mesh.scene(), cam, 32, [1, 3, 12])
+
+
+@pytest.mark.parametrize("light", [True, False])
+def test_oracle_equals_reference_shaders_every_material_class(light):
+    """Glass, plastic, glossy metal, glossy glass and glossy plastic (and, without the light, the
+    environment emission and sky of GenerateIBLSample)."""
+    from glslppm_gb300 import scenes
+    sc = scenes.materials_box(light=light)
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 32, 32, sc.fov)  # power of two: ReduceTexture
+    run(sc.to_mesh().scene(), cam, 32, [1, 2, 11, 21])
+
