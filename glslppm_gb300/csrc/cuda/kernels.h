@@ -15,6 +15,10 @@ struct StateGather {
 };
 void launch_gather_states(const JobDesc* jobs, const StateGather& list, JobState* out, cudaStream_t s);
 
+// bytes (a multiple of 8) from page-locked host memory mapped into the device's address space to
+// device memory, by one block (a small upload without a copy-engine transfer)
+void launch_copy_from_host(void* dst, const void* src_mapped, size_t bytes, cudaStream_t s);
+
 // plain FP32 path (kernels_fp32.cu)
 void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
 void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, cudaStream_t s);  // mixed: 4-wide BVH traversal

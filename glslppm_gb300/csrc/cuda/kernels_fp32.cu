@@ -1742,6 +1742,10 @@ __global__ void __launch_bounds__(1024) k_debug_trace(DevScene s, const float* o
     if (e) atomicOr(err, e);
 }
 
+__global__ void k_copy_from_host(unsigned long long* dst, const unsigned long long* src, uint32_t words) {
+    for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+}
+
 // one block per listed job: its JobState word by word
 __global__ void k_gather_states(const JobDesc* jobs, StateGather list, JobState* out) {
     static_assert(sizeof(JobState) % 4 == 0, "JobState is copied in 32-bit words");
@@ -1756,6 +1760,10 @@ __global__ void k_gather_states(const JobDesc* jobs, StateGather list, JobState*
 // ----------------------------------------------------------------------------------------------
 static inline uint32_t blocks_for(uint32_t n, uint32_t b) { return (n + b - 1) / b; }
 
+void launch_copy_from_host(void* dst, const void* src_mapped, size_t bytes, cudaStream_t s) {
+    k_copy_from_host<<<1, 64, 0, s>>>(static_cast<unsigned long long*>(dst),
+                                       static_cast<const unsigned long long*>(src_mapped), (uint32_t)(bytes / 8));
+}
 void launch_gather_states(const JobDesc* jobs, const StateGather& list, JobState* out, cudaStream_t s) {
     if (list.n) k_gather_states<<<list.n, 64, 0, s>>>(jobs, list, out);
 }

@@ -337,14 +337,18 @@ Job::~Job() {
 
 // queues the upload of the host descriptor on s through a pinned staging slot (no stream sync)
 int Job::write_desc(cudaStream_t s) {
+    static_assert(sizeof(JobDesc) % 8 == 0, "JobDesc is uploaded in 8-byte words");
     if (!stage) {
-        SPPM_CK(cudaMallocHost(&stage, 4 * sizeof(JobDesc)));
+        SPPM_CK(cudaHostAlloc(&stage, 4 * sizeof(JobDesc), cudaHostAllocMapped));
+        SPPM_CK(cudaHostGetDevicePointer(&stage_dev, stage, 0));
         for (auto& e : stage_ev) SPPM_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     const uint32_t k = stage_next++ & 3u;
     if (stage_used[k]) SPPM_CK(cudaEventSynchronize(stage_ev[k]));
     stage[k] = desc;
-    SPPM_CK(cudaMemcpyAsync(d_desc, &stage[k], sizeof(JobDesc), cudaMemcpyHostToDevice, s));
+    // read by a kernel straight from the mapped slot: no copy-engine round trip on the stream
+    launch_copy_from_host(d_desc, stage_dev + k, sizeof(JobDesc), s);
+    SPPM_CK(cudaGetLastError());
     SPPM_CK(cudaEventRecord(stage_ev[k], s));
     stage_used[k] = true;
     return SPPM_OK;

@@ -82,6 +82,7 @@ struct Job {
     // pinned staging slots for descriptor uploads, so that a camera change is queued without
     // waiting for the frames already queued (slot k is reused once its copy has run)
     JobDesc* stage = nullptr;
+    JobDesc* stage_dev = nullptr;  // the slots' address on the device (mapped host memory)
     cudaEvent_t stage_ev[4] = {};
     bool stage_used[4] = {};
     uint32_t stage_next = 0;
