@@ -10,19 +10,22 @@ from glslppm_gb300 import native as N
 pytestmark = pytest.mark.gpu
 
 
-def _renderer(sc, mesh, w, h):
+def _renderer(sc, mesh, w, h, precision=N.PRECISION_FP32):
     cfg = g.default_config(w, height=h, photon_width=64, photon_height=64, radius_rule=N.RADIUS_DIAGONAL,
-                           radius_fraction=0.01)
+                           radius_fraction=0.01, precision=precision)
     r = g.Renderer(cfg)
     r.upload_scene(mesh.scene())
     r.set_camera(g.look_at(sc.camera_origin, sc.camera_lookat, w, h, sc.fov))
     return r
 
 
-@pytest.mark.parametrize("pinned", [True, False])
-def test_streamed_images_equal_synchronous_reads(cornell_c1_mesh, pinned):
+@pytest.mark.parametrize("pinned,precision", [(True, N.PRECISION_FP32), (False, N.PRECISION_FP32),
+                                              (True, N.PRECISION_MIXED)])
+def test_streamed_images_equal_synchronous_reads(cornell_c1_mesh, pinned, precision):
+    """Images read without waiting, radiance and display alternately, with several copies in
+    flight: each equals the synchronous read of a second context after the same passes."""
     sc, mesh = cornell_c1_mesh
-    a, b = _renderer(sc, mesh, 48, 40), _renderer(sc, mesh, 48, 40)
+    a, b = _renderer(sc, mesh, 48, 40, precision), _renderer(sc, mesh, 48, 40, precision)
     steps, depth = 12, 3
     make = (lambda: g.pinned_empty((40, 48, 3), np.float32)) if pinned else (lambda: np.empty((40, 48, 3), np.float32))
     bufs = [make() for _ in range(steps)]
