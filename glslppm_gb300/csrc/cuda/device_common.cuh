@@ -18,6 +18,7 @@
 
 #include "sppm.h"
 #include "sppm_fpmath.h"
+#include "sppm_texture.h"
 
 namespace sppm_dev {
 
@@ -77,6 +78,12 @@ struct DevScene {
     uint32_t num_nodes, num_tris, num_lights, num_mats;
     float light_area, light_stride;
     float bsphere[4];
+    // material textures: null tri_tex when no texture coordinate of the scene is below 1e10 (no
+    // lookups can happen); tex [layers][512][512] RGBA8, mat_layer [num_mats] (-1: magenta)
+    const float2* tri_tex;     // [num_tris][3] texture coordinates T0, T1, T2
+    const uint8_t* tex;
+    const int32_t* mat_layer;
+    float mat_rcp;             // MaterialNumRcp = 1 / num_mats
 };
 
 struct DevPixels {

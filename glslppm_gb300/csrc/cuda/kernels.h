@@ -21,10 +21,12 @@ void launch_copy_from_host(void* dst, const void* src_mapped, size_t bytes, cuda
 
 // plain FP32 path (kernels_fp32.cu)
 void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
-void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, cudaStream_t s);  // mixed: 4-wide BVH traversal
+// mixed: 4-wide BVH traversal; textured: some job of the launch has texture coordinates (the
+// kernel variants with texture lookups)
+void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, bool textured, cudaStream_t s);
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s);
-void launch_photon_fp32(const LaunchSet& ls, bool count_traversal, cudaStream_t s);
-void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
+void launch_photon_fp32(const LaunchSet& ls, bool count_traversal, bool textured, cudaStream_t s);
+void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, bool textured, cudaStream_t s);
 void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool count_traversal,
                                uint32_t persistent_blocks, cudaStream_t s);
 void launch_ray_bins(const RayQueue& q, cudaStream_t s);

@@ -531,6 +531,34 @@ __device__ __forceinline__ Shade shade_hit(const DevScene& s, const Hit& h) {
     return o;
 }
 
+// col *= texture3D(VolumeTextureTextures, vec3(tex, r)).rgb when |tex.x| < 1e10 (eyeraytrace.fs:
+// 443-446, photontrace.fs:418-422, 562-565), tex = T2 * b0 + T0 * b1 + T1 * b2 of the triangle's
+// texture coordinates (eyeraytrace.fs:280); sampling as include/sppm_texture.h pins it
+__device__ __forceinline__ f3 textured(const DevScene& S, int32_t tri, float b0, float b1, float b2, float r, f3 col) {
+    const float2 T0 = __ldg(&S.tri_tex[(size_t)tri * 3]), T1 = __ldg(&S.tri_tex[(size_t)tri * 3 + 1]),
+                 T2 = __ldg(&S.tri_tex[(size_t)tri * 3 + 2]);
+    const float tu = xadd(xadd(xmul(T2.x, b0), xmul(T0.x, b1)), xmul(T1.x, b2));
+    const float tv = xadd(xadd(xmul(T2.y, b0), xmul(T0.y, b1)), xmul(T1.y, b2));
+    if (!(fabsf(tu) < 1e+10f)) return col;
+    float t[3];
+    sppm_tex_sample(S.tex, S.mat_layer, S.num_mats, tu, tv, r, t);
+    return mk(xmul(col.x, t[0]), xmul(col.y, t[1]), xmul(col.z, t[2]));
+}
+
+// a photon bounce's colour: the hit's barycentrics from the stored position (photontrace.fs:
+// 521-545), then the texture at layer (material + 0.5 + 0.25) / materials (:562-565)
+__device__ __forceinline__ f3 textured_bounce(const DevScene& S, int32_t tri, f3 ipos, int32_t mat, f3 icol) {
+    const float4* ts = S.tri_shade + (size_t)tri * 6;
+    const float4 r1 = __ldg(ts + 1), r2 = __ldg(ts + 2), r3 = __ldg(ts + 3);
+    const f3 V0 = mk(r1.x, r1.y, r1.z), V1 = mk(r1.w, r2.x, r2.y), V2 = mk(r2.z, r2.w, r3.x);
+    const float bx = length(cross(sub(V1, V0), sub(ipos, V0)));
+    const float by = length(cross(sub(V2, V1), sub(ipos, V1)));
+    const float bz = length(cross(sub(V0, V2), sub(ipos, V2)));
+    const float bs = xadd(xadd(bx, by), bz);
+    return textured(S, tri, xdiv(bx, bs), xdiv(by, bs), xdiv(bz, bs),
+                    xmul(S.mat_rcp, xadd(xadd((float)mat, 0.5f), 0.25f)), icol);
+}
+
 // ----------------------------------------------------------------------------------------------
 // BRDF helpers (eyeraytrace.fs:293-392, photontrace.fs:60-89, 258-280, 443-461)
 // ----------------------------------------------------------------------------------------------
@@ -662,7 +690,8 @@ struct EyeOut {
     uint32_t segs;
 };
 
-template <class Trace>
+// TEX: the launch may hold a job whose scene has texture coordinates (texture lookups compiled in)
+template <bool TEX, class Trace>
 __device__ __forceinline__ bool eye_path(const JobDesc& J, const JobState* st, uint32_t p, Trace&& trace, EyeOut& out) {
     const uint32_t px = p % J.W, py = p / J.W;
     const DevScene& S = J.scene;
@@ -702,9 +731,11 @@ __device__ __forceinline__ bool eye_path(const JobDesc& J, const JobState* st, u
             if (S.light_area == 0.0f) emi = mul(mk(0.7f, 0.7f, 1.0f), col);
             break;
         }
-        const Shade i = shade_hit(S, h);
+        Shade i = shade_hit(S, h);
         pos = i.pos;
         nrm = i.nrm;
+        if (TEX && S.tri_tex)
+            i.col = textured(S, h.tri, h.bu, h.bv, h.bw, xmul(S.mat_rcp, xadd((float)h.mat, 0.5f)), i.col);
         if (i.brdf == -1) {
             nrm = mk(0, 0, 0);
             emi = mul(col, i.col);
@@ -791,7 +822,7 @@ __device__ __forceinline__ void eye_write(const JobDesc& J, const JobState* st, 
 // would walk most of the tree in one lane: the exact path defers such pixels to k_eye_coop
 // (their whole path is rerun there with block-wide walks); the mixed path's slab tests do not
 // degenerate.
-template <bool MIXED>
+template <bool MIXED, bool TEX>
 __global__ void __launch_bounds__(128) k_eye(LaunchSet ls, uint32_t* deferred_n, uint32_t* deferred,
                                                 uint32_t deferred_cap) {
     const uint32_t g = grid_tid();
@@ -802,7 +833,7 @@ __global__ void __launch_bounds__(128) k_eye(LaunchSet ls, uint32_t* deferred_n,
     const uint32_t p = g - ls.prefix[k];
     uint32_t err = 0;
     EyeOut o;
-    const bool done = eye_path(J, st, p, [&](f3 org, f3 dir, bool cull, Hit& h) {
+    const bool done = eye_path<TEX>(J, st, p, [&](f3 org, f3 dir, bool cull, Hit& h) {
         if (MIXED) {
             h = trace_eye4(J.scene, org, dir, cull, err);
             return true;
@@ -832,6 +863,7 @@ __global__ void __launch_bounds__(128) k_eye(LaunchSet ls, uint32_t* deferred_n,
 
 // the deferred pixels of k_eye<false>, one block of 1024 threads per pixel: every thread runs
 // the same path (identical values), each trace is block_trace_exact, thread 0 writes
+template <bool TEX>
 __global__ void __launch_bounds__(kBlockWalk) k_eye_coop(LaunchSet ls, const uint32_t* deferred_n,
                                                          const uint32_t* deferred, uint32_t deferred_cap) {
     __shared__ BlockWalkShared sh;
@@ -844,7 +876,7 @@ __global__ void __launch_bounds__(kBlockWalk) k_eye_coop(LaunchSet ls, const uin
         const uint32_t p = g - ls.prefix[k];
         uint32_t err = 0;
         EyeOut o;
-        eye_path(J, st, p, [&](f3 org, f3 dir, bool cull, Hit& h) {
+        eye_path<TEX>(J, st, p, [&](f3 org, f3 dir, bool cull, Hit& h) {
             TraversalCount ct;
             h = block_trace_exact<false, false>(J.scene, org, dir, cull, err, &ct, sh);
             return true;
@@ -900,6 +932,7 @@ __global__ void k_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t nj
 // ----------------------------------------------------------------------------------------------
 // GenerateLightSourceSample (photontrace.fs:345-440) up to its cosine lobe: the origin, the flux and
 // the lobe's normal (the lobe itself is cosine_lobe, drawn right after, shared with the bounces)
+template <bool TEX>
 __device__ __forceinline__ void light_sample(const JobDesc& J, float4& rndv, f3& flux, f3& lobe_n, f3& org,
                                              uint32_t& err) {
     const DevScene& S = J.scene;
@@ -933,6 +966,8 @@ __device__ __forceinline__ void light_sample(const JobDesc& J, float4& rndv, f3&
     const f3 N0 = mk(r3.y, r3.z, r3.w), N1 = mk(r4.x, r4.y, r4.z), N2 = mk(r4.w, r5.x, r5.y);
     const DevMaterial& m = S.mats[__float_as_int(r0.w)];
     flux = scl(mk(m.color[0], m.color[1], m.color[2]), xmul(S.light_area, 3.141592f));
+    if (TEX && S.tri_tex)  // T = T2 * c + T0 * a + T1 * b (photontrace.fs:413-422)
+        flux = textured(S, lt, c, a, b, xmul(S.mat_rcp, xadd((float)__float_as_int(r0.w), 0.75f)), flux);
     f3 o = add(add(scl(V0, a), scl(V1, b)), scl(V2, c));
     const f3 nrm = normalize(add(add(scl(N0, a), scl(N1, b)), scl(N2, c)));
     const f3 gnrm = mk(r0.x, r0.y, r0.z);
@@ -982,6 +1017,7 @@ struct PhotonRay {
 
 // hitin: the previous segment's (triangle, depth), (-1, 0) before the first; PP, PF, PD: its
 // record (position, flux, direction, with the normal in the w components)
+template <bool TEX>
 __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, int2 hitin, float4 PP, float4 PF, float4 PD,
                                                      float4& rndv, uint32_t& err) {
     // Emission and the diffuse bounces end in the same cosine lobe: each path sets up its lobe
@@ -999,7 +1035,7 @@ __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, int2 hiti
     f3 rorg = mk(0, 0, 0), rdir = mk(0, 0, 0);
     if (emit) {
         if (S.light_area != 0.0f) {
-            light_sample(J, rndv, R.flux, lobe_n, rorg, err);
+            light_sample<TEX>(J, rndv, R.flux, lobe_n, rorg, err);
             lobe = true;
         } else {
             ibl_sample(J, rndv, R.flux, rdir, rorg);
@@ -1013,6 +1049,7 @@ __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, int2 hiti
         gnrm = mk(r0.x, r0.y, r0.z);
         const DevMaterial& m = S.mats[__float_as_int(r0.w)];
         icol = mk(m.color[0], m.color[1], m.color[2]);
+        if (TEX && S.tri_tex) icol = textured_bounce(S, hitin.x, ipos, __float_as_int(r0.w), icol);
         const int brdf = m.brdf;
         if (brdf == 0) {
             rorg = add(ipos, scl(gnrm, eps));  // matte_bounce
@@ -1091,10 +1128,11 @@ __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, int2 hiti
     return R;
 }
 
+template <bool TEX>
 __device__ __forceinline__ PhotonRay photon_generate(const JobDesc& J, uint32_t sidx, uint32_t frame, float4& rndv,
                                                      uint32_t& err) {
     const int2 hitin = frame == 0 ? make_int2(-1, 0) : J.ph.hit[sidx];
-    return photon_generate(J, hitin, J.ph.pos[sidx], J.ph.flux[sidx], J.ph.dir[sidx], rndv, err);
+    return photon_generate<TEX>(J, hitin, J.ph.pos[sidx], J.ph.flux[sidx], J.ph.dir[sidx], rndv, err);
 }
 
 __device__ __forceinline__ void photon_terminate(const JobDesc& J, uint32_t sidx) {
@@ -1165,7 +1203,7 @@ __device__ __forceinline__ void photon_counters(JobState* st, int k, unsigned ac
 }
 
 // fused photon pass: one thread per photon slot, generate + trace + store + hash insert
-template <bool COUNT>
+template <bool COUNT, bool TEX>
 __global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
     const uint32_t g = grid_tid();
     if (g >= ls.total) return;
@@ -1175,7 +1213,7 @@ __global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
     const uint32_t sidx = g - ls.prefix[k];
     uint32_t err = 0;
     float4 rndv = J.ph.rng[sidx];
-    const PhotonRay R = photon_generate(J, sidx, st->frame, rndv, err);
+    const PhotonRay R = photon_generate<TEX>(J, sidx, st->frame, rndv, err);
     uint32_t slot = 0xFFFFFFFFu;
     TraversalCount tc;
     if (R.cont) {
@@ -1210,6 +1248,7 @@ __global__ void __launch_bounds__(128) k_photon(LaunchSet ls) {
 // The block's slots are first reordered so that the emissions (a photon with no previous hit or
 // at the bounce limit) come before the bounces: each warp then runs one of the two paths (the
 // state written is per slot, so the order of work changes nothing).
+template <bool TEX>
 __global__ void __launch_bounds__(128) k_photon_gen(LaunchSet ls, RayQueue q) {
     // the slot and its record in processing order (the loads of every slot's record are issued
     // together, before the reorder)
@@ -1273,7 +1312,7 @@ __global__ void __launch_bounds__(128) k_photon_gen(LaunchSet ls, RayQueue q) {
     uint32_t err = 0;
     const uint32_t t = threadIdx.x;
     float4 rndv = rec_rng[t];
-    const PhotonRay R = photon_generate(J, rec_hit[t], rec_pos[t], rec_flux[t], rec_dir[t], rndv, err);
+    const PhotonRay R = photon_generate<TEX>(J, rec_hit[t], rec_pos[t], rec_flux[t], rec_dir[t], rndv, err);
     J.ph.rng[sidx] = rndv;
     if (R.cont) {
         J.ph.flux[sidx] = f4(R.flux, 0.0f);  // flux before the segment, read back by k_photon_store
@@ -1771,27 +1810,37 @@ void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) 
     const uint32_t n = q.bins && ls.total < kRayBins ? kRayBins : ls.total;
     if (ls.total) k_frame_begin<<<blocks_for(n, 256), 256, 0, s>>>(ls, q);
 }
-void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, cudaStream_t s) {
-    if (!ls.total) return;
+template <bool TEX>
+static void launch_eye_t(const LaunchSet& ls, const RayQueue& q, bool mixed, cudaStream_t s) {
     if (mixed) {
-        k_eye<true><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, nullptr, nullptr, 0);
+        k_eye<true, TEX><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, nullptr, nullptr, 0);
         return;
     }
-    k_eye<false><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q.counters + 3, q.eye_deferred, kEyeDeferred);
+    k_eye<false, TEX><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q.counters + 3, q.eye_deferred, kEyeDeferred);
     // a fixed grid (the count is on the device): blocks beyond the deferred pixels exit at once
-    k_eye_coop<<<32, kBlockWalk, 0, s>>>(ls, q.counters + 3, q.eye_deferred, kEyeDeferred);
+    k_eye_coop<TEX><<<32, kBlockWalk, 0, s>>>(ls, q.counters + 3, q.eye_deferred, kEyeDeferred);
+}
+void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, bool textured, cudaStream_t s) {
+    if (!ls.total) return;
+    if (textured) launch_eye_t<true>(ls, q, mixed, s);
+    else launch_eye_t<false>(ls, q, mixed, s);
 }
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s) {
     if (njobs) k_grid<<<blocks_for(njobs, 64), 64, 0, s>>>(jobs, job_ids, njobs);
 }
-void launch_photon_fp32(const LaunchSet& ls, bool count, cudaStream_t s) {
+void launch_photon_fp32(const LaunchSet& ls, bool count, bool textured, cudaStream_t s) {
     if (!ls.total) return;
-    if (count) k_photon<true><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
-    else k_photon<false><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls);
+    const uint32_t b = blocks_for(ls.total, 128);
+    if (count && textured) k_photon<true, true><<<b, 128, 0, s>>>(ls);
+    else if (count) k_photon<true, false><<<b, 128, 0, s>>>(ls);
+    else if (textured) k_photon<false, true><<<b, 128, 0, s>>>(ls);
+    else k_photon<false, false><<<b, 128, 0, s>>>(ls);
 }
 
-void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
-    if (ls.total) k_photon_gen<<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q);
+void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, bool textured, cudaStream_t s) {
+    if (!ls.total) return;
+    if (textured) k_photon_gen<true><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q);
+    else k_photon_gen<false><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q);
 }
 void launch_ray_bins(const RayQueue& q, cudaStream_t s) {
     if (!q.key || !q.capacity) return;

@@ -120,6 +120,8 @@ struct Packed {
     std::vector<DevMaterial> mats;
     std::vector<float> light_cdf;
     std::vector<int32_t> light_tri;
+    std::vector<float2> tri_tex;     // empty when no texture coordinate is below 1e10
+    std::vector<int32_t> mat_layer;  // [num_materials]
 };
 
 int check_scene(const sppm_scene* s) {
@@ -216,6 +218,26 @@ int pack_scene(const sppm_scene* s, Packed& out) {
     for (uint32_t l = 0; l < nl; l++)
         if (out.light_tri[l] < 0 || (uint32_t)out.light_tri[l] >= nt)
             return fail(SPPM_ERR_ARG, "light %u: triangle %d out of range", l, out.light_tri[l]);
+    // textures: each material's layer (or -1) and, when any texture coordinate can be used,
+    // the triangles' coordinates
+    out.mat_layer.assign(nm, -1);
+    if (s->num_textures) {
+        if (!s->textures || !s->material_texture) return fail(SPPM_ERR_ARG, "texture arrays missing");
+        for (uint32_t m = 0; m < nm; m++) {
+            const int32_t l = s->material_texture[m];
+            if (l < -1 || l >= (int32_t)s->num_textures)
+                return fail(SPPM_ERR_ARG, "material %u: texture %d out of range", m, l);
+            out.mat_layer[m] = l;
+        }
+    }
+    bool any_tex = false;
+    if (s->texcoords)
+        for (size_t k = 0; k < (size_t)nt * 6 && !any_tex; k++) any_tex = std::fabs(s->texcoords[k]) < 1e10f;
+    if (any_tex) {
+        out.tri_tex.resize((size_t)nt * 3);
+        for (size_t k = 0; k < (size_t)nt * 3; k++)
+            out.tri_tex[k] = make_float2(s->texcoords[k * 2], s->texcoords[k * 2 + 1]);
+    }
     return SPPM_OK;
 }
 
@@ -250,7 +272,9 @@ uint64_t Job::scene_bytes(const sppm_scene& s, uint32_t precision) {
     const uint64_t nt = s.num_triangles, nn = s.num_nodes;
     uint64_t b = Arena::align(6 * nn * sizeof(NodeX)) + Arena::align(nt * 48) + Arena::align(nt * 96) +
                  Arena::align(std::max<uint64_t>(s.num_materials, 1) * sizeof(DevMaterial)) +
-                 2 * Arena::align(std::max<uint64_t>(s.num_lights, 1) * 4) + 1024;
+                 2 * Arena::align(std::max<uint64_t>(s.num_lights, 1) * 4) + 1024 +
+                 Arena::align((uint64_t)s.num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4) +
+                 Arena::align(std::max<uint64_t>(s.num_materials, 1) * 4) + (s.texcoords ? Arena::align(nt * 24) : 0);
     // the 4-wide tree has at most one node per internal binary node
     if (precision == SPPM_PRECISION_MIXED) b += Arena::align(std::max<uint64_t>(nn, 1) * sizeof(sppm::Node4));
     else b += Arena::align(sizeof(sppm::Node4));
@@ -413,7 +437,9 @@ int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
                          Arena::align(pk.shade.size() * 16) + Arena::align(pk.mats.size() * sizeof(DevMaterial)) +
                          Arena::align(std::max<size_t>(pk.light_cdf.size(), 1) * 4) +
                          Arena::align(std::max<size_t>(pk.light_tri.size(), 1) * 4) +
-                         Arena::align(std::max<size_t>(nodes4.size(), 1) * sizeof(sppm::Node4)) + 1024;
+                         Arena::align(std::max<size_t>(nodes4.size(), 1) * sizeof(sppm::Node4)) + 1024 +
+                         Arena::align(pk.tri_tex.size() * sizeof(float2)) + Arena::align(pk.mat_layer.size() * 4) +
+                         Arena::align((size_t)scene->num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4);
     SPPM_CK(cudaStreamSynchronize(s));
     if ((st = scene_mem.reserve(bytes))) return st;
     scene_bytes_used = bytes;
@@ -432,6 +458,21 @@ int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
     sppm::Node4* n4 = nullptr;
     if ((st = put(scene_mem, nodes4, &n4, s))) return st;
     S.nodes4 = nodes4.empty() ? nullptr : reinterpret_cast<const Node4Dev*>(n4);
+    float2* ttex = nullptr;
+    int32_t* mlayer = nullptr;
+    if ((st = put(scene_mem, pk.tri_tex, &ttex, s))) return st;
+    if ((st = put(scene_mem, pk.mat_layer, &mlayer, s))) return st;
+    uint8_t* tex = nullptr;
+    if (scene->num_textures) {
+        const size_t tb = (size_t)scene->num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4;
+        tex = scene_mem.take<uint8_t>(tb);
+        if (!tex) return fail(SPPM_ERR_OOM, "scene arena sizing error (textures)");
+        SPPM_CK(cudaMemcpyAsync(tex, scene->textures, tb, cudaMemcpyHostToDevice, s));
+    }
+    S.tri_tex = pk.tri_tex.empty() ? nullptr : ttex;
+    S.mat_layer = mlayer;
+    S.tex = tex;
+    S.mat_rcp = 1.0f / (float)scene->num_materials;
     S.flux_unscale = scene->light_area != 0.0f ? scene->light_area * 3.141592f : 1.0f;
     S.flux_unscale_inv = 1.0f / S.flux_unscale;
     S.nodes = nodes;
@@ -823,7 +864,7 @@ int Runner::enqueue_frame(uint32_t phase) {
         SPPM_CK(cudaEventRecord(fork_ev, stream));
         SPPM_CK(cudaStreamWaitEvent(side, fork_ev, 0));
         timed(SPPM_STAGE_EYE, true, side);
-        launch_eye(eye_pix[phase], queue, precision == SPPM_PRECISION_MIXED, side);
+        launch_eye(eye_pix[phase], queue, precision == SPPM_PRECISION_MIXED, textured, side);
         timed(SPPM_STAGE_EYE, false, side);
         timed(SPPM_STAGE_GRID, true, side);
         launch_grid(d_jobs, eye_ids[phase], eye_pix[phase].njobs, side);
@@ -834,11 +875,11 @@ int Runner::enqueue_frame(uint32_t phase) {
     if ((flags & SPPM_FLAG_FUSED_PHOTON) && !mixed) {
         if (eye) SPPM_CK(cudaStreamWaitEvent(stream, join_ev, 0));
         timed(SPPM_STAGE_PHOTON, true);
-        launch_photon_fp32(pho, count_traversal, stream);
+        launch_photon_fp32(pho, count_traversal, textured, stream);
         timed(SPPM_STAGE_PHOTON, false);
     } else {
         timed(SPPM_STAGE_PHOTON, true);
-        launch_photon_gen_fp32(pho, queue, stream);
+        launch_photon_gen_fp32(pho, queue, textured, stream);
         timed(SPPM_STAGE_PHOTON, false);
         if (queue.key) {
             timed(SPPM_STAGE_RAY_BINS, true);
@@ -879,6 +920,7 @@ int Runner::build_graph(uint32_t phase, FrameGraph& g) {
     g.graph = graph;
     g.mask = timing_mask;
     g.counting = count_traversal;
+    g.textured = textured;
     size_t n = 0;
     SPPM_CK(cudaGraphGetNodes(graph, nullptr, &n));
     std::vector<cudaGraphNode_t> nodes(n);
@@ -904,12 +946,15 @@ int Runner::run(uint32_t n) {
     int st;
     if (dirty && (st = rebuild())) return st;
     if (active.empty()) return SPPM_OK;
+    // the kernel variants with texture lookups when some job's scene has texture coordinates
+    textured = false;
+    for (const Job* j : active) textured = textured || j->desc.scene.tri_tex != nullptr;
     // the traversal-counting kernels run eagerly (they are a measurement pass)
     const bool use_graphs = !(flags & SPPM_FLAG_EAGER_LAUNCH) && !count_traversal;
     for (uint32_t k = 0; k < n; k++) {
         const uint32_t phase = (uint32_t)(frames % eye_interval);
         FrameGraph& g = graphs[phase_has_eye(phase) ? phase : eye_interval];
-        if (!g.exec || g.mask != timing_mask || g.counting != count_traversal) {
+        if (!g.exec || g.mask != timing_mask || g.counting != count_traversal || g.textured != textured) {
             // captured, and launched only in graph mode; eager mode keeps it to count kernels
             if ((st = build_graph(phase, g))) return st;
         }

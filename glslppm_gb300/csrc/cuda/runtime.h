@@ -137,6 +137,7 @@ struct FrameGraph {
     uint32_t mask = 0;
     uint32_t kernels = 0;   // kernel nodes (launches per replay)
     bool counting = false;  // captured with the traversal-counting kernels
+    bool textured = false;  // captured with the kernel variants that look up textures
     cudaGraphNode_t ev_a[SPPM_STAGE_COUNT] = {}, ev_b[SPPM_STAGE_COUNT] = {};
     void drop();
 };
@@ -176,6 +177,7 @@ struct Runner {
     // stage timing
     uint32_t timing_mask = 0;  // bit k: time stage k
     bool count_traversal = false;
+    bool textured = false;         // some active job's scene has texture coordinates
     std::vector<StageEvent> pending;
     size_t open_stage[SPPM_STAGE_COUNT] = {0};  // pending entry of each stage's last start
     std::vector<cudaEvent_t> event_pool;

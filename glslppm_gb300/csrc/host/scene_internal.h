@@ -66,6 +66,10 @@ struct sppm_mesh {
     std::vector<int32_t> node_triangle; // [num_nodes]
     std::vector<int32_t> order_base;    // [6][num_nodes]
     std::vector<int32_t> order_miss;    // [6][num_nodes]
+    // material textures (map_Kd) resampled to 512x512 RGBA8; material_texture[m] = layer or -1
+    std::vector<uint8_t> textures;
+    std::vector<int32_t> material_texture;
+    uint32_t num_textures = 0;
 
     sppm::V3 pos(uint32_t t, int v) const {
         const float* p = &positions[(size_t)t * 9 + v * 3];

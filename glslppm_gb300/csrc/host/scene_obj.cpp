@@ -20,8 +20,8 @@
 // The file is read once and its lines are parsed in parallel ranges (cut at line ends, each cut
 // into the same 79-character chunks); materials and errors are resolved afterwards in file order.
 // Deliberate differences, reported as errors instead of undefined behaviour: unreadable files,
-// malformed faces and out-of-range indices (SPPM_ERR_IO), textured (map_Kd) and "sss" materials
-// (SPPM_ERR_UNSUPPORTED).  The MTL file is opened relative to the OBJ file's directory.
+// malformed faces and out-of-range indices (SPPM_ERR_IO), "sss" materials (SPPM_ERR_UNSUPPORTED).
+// map_Kd textures are binary 8-bit PPM files (LoadPPM, mesh.cpp:37-54).  The MTL file is opened relative to the OBJ file's directory.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -34,6 +34,7 @@
 #include <vector>
 
 #include "scene_internal.h"
+#include "sppm_texture.h"
 
 using sppm::fail;
 using sppm::V3;
@@ -46,7 +47,34 @@ struct MtlEntry {
     V3 ka{0, 0, 0}, kd{0, 0, 0}, ks{0, 0, 0};
     float ns = 0.0f;
     bool textured = false;
+    int tex_w = 0, tex_h = 0;
+    std::vector<uint8_t> texture;  // RGB8, rows top to bottom as the P6 file stores them
 };
+
+std::string dir_of(const char* path) {
+    const char* slash = strrchr(path, '/');
+    return slash ? std::string(path, slash - path + 1) : std::string();
+}
+
+// LoadPPM (mesh.cpp:37-54): binary P6, maximum value 255
+int load_ppm(const std::string& path, MtlEntry& m) {
+    FILE* fp = fopen(path.c_str(), "rb");
+    if (!fp) return fail(SPPM_ERR_IO, "cannot open texture '%s'", path.c_str());
+    int w = 0, h = 0, maxv = 0;
+    const bool ok = fscanf(fp, "P6 %d %d %d", &w, &h, &maxv) == 3 && w > 0 && h > 0 && maxv == 255 &&
+                    (long long)w * h <= (1ll << 28) && fgetc(fp) != EOF;
+    if (!ok) {
+        fclose(fp);
+        return fail(SPPM_ERR_IO, "'%s' is not a binary 8-bit PPM (P6, 255)", path.c_str());
+    }
+    m.tex_w = w;
+    m.tex_h = h;
+    m.texture.resize((size_t)w * h * 3);
+    const size_t got = fread(m.texture.data(), 1, m.texture.size(), fp);
+    fclose(fp);
+    if (got != m.texture.size()) return fail(SPPM_ERR_IO, "texture '%s' is truncated", path.c_str());
+    return SPPM_OK;
+}
 
 bool starts_with(const char* line, const char* prefix) {
     return strncmp(line, prefix, strlen(prefix)) == 0;
@@ -82,9 +110,20 @@ int read_mtl(const std::string& path, std::vector<MtlEntry>& out) {
             cur.ns = s;
             out.push_back(cur);
         } else if (starts_with(line, "map_Kd")) {
-            fclose(fp);
-            return fail(SPPM_ERR_UNSUPPORTED, "textured materials (map_Kd in '%s') are not supported",
-                        path.c_str());
+            // the texture goes to the material last appended (mesh.cpp:117-123): a map_Kd line
+            // belongs after the block's Ns line
+            std::string name = tail(line, 7);
+            if (!name.empty()) name.erase(name.size() - 1, 1);
+            if (out.empty()) {
+                fclose(fp);
+                return fail(SPPM_ERR_IO, "'%s': map_Kd before any complete material", path.c_str());
+            }
+            out.back().textured = true;
+            const int st = load_ppm(dir_of(path.c_str()) + name, out.back());
+            if (st != SPPM_OK) {
+                fclose(fp);
+                return st;
+            }
         }
     }
     fclose(fp);
@@ -110,10 +149,6 @@ void split_face_vertex(const char* word, int* vi, int* ti, int* ni) {
     *ni = atoi(sn.c_str());
 }
 
-std::string dir_of(const char* path) {
-    const char* slash = strrchr(path, '/');
-    return slash ? std::string(path, slash - path + 1) : std::string();
-}
 
 // CGPURT::CreateTextures packs g = 1 / ((2 / (1 - specularity))^2.71828 + 1) (gpurt.cpp:126)
 float packed_glossiness(float specularity) {
@@ -165,10 +200,10 @@ namespace {
 
 // what one range of the file's lines holds, in file order
 struct ObjPart {
-    std::vector<float> v, n;
-    std::vector<int> vind, nind;  // per face vertex (0-based; -1 for a missing normal)
+    std::vector<float> v, n, t;
+    std::vector<int> vind, nind, tind;  // per face vertex (0-based; -1 for a missing index)
     uint32_t faces = 0;
-    bool no_normals = false;
+    bool no_normals = false, no_texcoords = false;
     // mtllib and usemtl lines (resolved in file order afterwards: reading an MTL file appends
     // materials that later usemtl lines match) and the first malformed face
     struct Event {
@@ -195,7 +230,10 @@ bool parse_obj_line(const char* line, ObjPart& P) {
             P.n.push_back(y / l);
             P.n.push_back(z / l);
         } else if (line[1] == 't') {
-            // texture coordinates are only used by textured materials, which are rejected
+            float a = 0, b = 0;
+            sscanf(&line[2], "%f %f", &a, &b);
+            P.t.push_back(a);
+            P.t.push_back(b);
         } else {
             float x = 0, y = 0, z = 0;
             sscanf(&line[1], "%f %f %f", &x, &y, &z);
@@ -220,6 +258,11 @@ bool parse_obj_line(const char* line, ObjPart& P) {
             else {
                 P.nind.push_back(-1);
                 P.no_normals = true;
+            }
+            if (ti) P.tind.push_back(ti - 1);
+            else {
+                P.tind.push_back(-1);
+                P.no_texcoords = true;
             }
         }
         P.faces++;
@@ -294,10 +337,10 @@ extern "C" int sppm_mesh_load_obj(const char* path, const float offset[3], float
             }
     // then, in file order, the material switches and the first malformed face
     std::vector<int> mind;
-    bool no_normals = false, no_materials = true;
+    bool no_normals = false, no_texcoords = false, no_materials = true;
     int cmaterial = 0;
-    std::vector<float> v, n;
-    std::vector<int> vind, nind;
+    std::vector<float> v, n, t;
+    std::vector<int> vind, nind, tind;
     for (ObjPart& P : parts) {
         uint32_t done = 0;  // faces of this part given a material so far
         for (const ObjPart::Event& e : P.events) {
@@ -319,10 +362,13 @@ extern "C" int sppm_mesh_load_obj(const char* path, const float offset[3], float
         }
         mind.insert(mind.end(), P.faces - done, cmaterial);
         no_normals = no_normals || P.no_normals;
+        no_texcoords = no_texcoords || P.no_texcoords;
         v.insert(v.end(), P.v.begin(), P.v.end());
         n.insert(n.end(), P.n.begin(), P.n.end());
+        t.insert(t.end(), P.t.begin(), P.t.end());
         vind.insert(vind.end(), P.vind.begin(), P.vind.end());
         nind.insert(nind.end(), P.nind.begin(), P.nind.end());
+        tind.insert(tind.end(), P.tind.begin(), P.tind.end());
         P = ObjPart();
     }
 
@@ -339,6 +385,8 @@ extern "C" int sppm_mesh_load_obj(const char* path, const float offset[3], float
             return fail(SPPM_ERR_IO, "'%s': vertex index %d out of range", path, vind[k] + 1);
         if (!no_normals && (nind[k] < 0 || (size_t)nind[k] >= nn))
             return fail(SPPM_ERR_IO, "'%s': normal index %d out of range", path, nind[k] + 1);
+        if (!no_texcoords && (tind[k] < 0 || (size_t)tind[k] >= t.size() / 2))
+            return fail(SPPM_ERR_IO, "'%s': texture coordinate index %d out of range", path, tind[k] + 1);
     }
     for (uint32_t i = 0; i < nt; i++) {
         for (int k = 0; k < 3; k++) {
@@ -404,6 +452,26 @@ extern "C" int sppm_mesh_load_obj(const char* path, const float offset[3], float
             m->materials.push_back(mat);
         }
         for (uint32_t i = 0; i < nt; i++) m->material_ids[i] = mind[i];
+        // textures: each textured material's map_Kd resampled to a 512x512 layer
+        // (gpurt.cpp:176-196); a triangle of a textured material keeps its texture coordinates
+        // when every face vertex of the file has one (mesh.cpp:342-349, 657-666)
+        m->material_texture.assign(mtls.size(), -1);
+        const size_t layer_bytes = (size_t)SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4;
+        for (size_t i = 0; i < mtls.size(); i++) {
+            if (!mtls[i].textured) continue;
+            m->material_texture[i] = (int32_t)m->num_textures++;
+            m->textures.resize(m->num_textures * layer_bytes);
+            sppm_tex_resample(mtls[i].texture.data(), mtls[i].tex_w, mtls[i].tex_h,
+                              m->textures.data() + (m->num_textures - 1) * layer_bytes);
+        }
+        if (!no_texcoords)
+            for (uint32_t i = 0; i < nt; i++) {
+                if (!mtls[mind[i]].textured) continue;
+                for (int k = 0; k < 3; k++) {
+                    m->texcoords[(size_t)i * 6 + k * 2] = t[(size_t)tind[i * 3 + k] * 2];
+                    m->texcoords[(size_t)i * 6 + k * 2 + 1] = t[(size_t)tind[i * 3 + k] * 2 + 1];
+                }
+            }
     } else {
         // default material (mesh.cpp:615-620): brdf 0; its colour is never assigned in the
         // reference, so it keeps TVector3's zero default
@@ -413,6 +481,7 @@ extern "C" int sppm_mesh_load_obj(const char* path, const float offset[3], float
         mat.brdf = 0;
         mat.glossiness = 0.0f;
         m->materials.push_back(mat);
+        m->material_texture.assign(1, -1);
     }
     m->finish_geometry();
     if (have_light) m->prepare_lights();
@@ -484,6 +553,9 @@ extern "C" int sppm_mesh_get_scene(const sppm_mesh* m, sppm_scene* s) {
     s->node_triangle = m->node_triangle.data();
     s->order_base = m->order_base.data();
     s->order_miss = m->order_miss.data();
+    s->num_textures = m->num_textures;
+    s->textures = m->num_textures ? m->textures.data() : nullptr;
+    s->material_texture = m->material_texture.empty() ? nullptr : m->material_texture.data();
     return SPPM_OK;
 }
 

@@ -73,6 +73,8 @@ class Scene(C.Structure):
         ("num_nodes", C.c_uint32), ("node_bounds", C.POINTER(C.c_float)),
         ("node_triangle", C.POINTER(C.c_int32)), ("order_base", C.POINTER(C.c_int32)),
         ("order_miss", C.POINTER(C.c_int32)),
+        ("num_textures", C.c_uint32), ("textures", C.POINTER(C.c_uint8)),
+        ("material_texture", C.POINTER(C.c_int32)),
     ]
 
 

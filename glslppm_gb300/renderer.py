@@ -9,7 +9,7 @@ scene (``precalculate_mesh_data``), set the camera, run SPPM frames (``display``
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 
@@ -58,6 +58,9 @@ class SceneArrays:
     node_triangle: np.ndarray
     order_base: np.ndarray
     order_miss: np.ndarray
+    # material textures: [num_textures, 512, 512, 4] uint8 and [num_materials] layer or -1
+    textures: np.ndarray = field(default_factory=lambda: np.zeros((0, 512, 512, 4), np.uint8))
+    material_texture: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
 
 
 MATERIAL_DTYPE = np.dtype([("color", "<f4", 3), ("eta", "<f4"), ("brdf", "<i4"), ("glossiness", "<f4")])
@@ -131,6 +134,8 @@ class Mesh:
             node_triangle=grab(s.node_triangle, nn, np.int32),
             order_base=grab(s.order_base, nn * 6, np.int32).reshape(6, nn),
             order_miss=grab(s.order_miss, nn * 6, np.int32).reshape(6, nn),
+            textures=grab(s.textures, s.num_textures * 512 * 512 * 4, np.uint8).reshape(-1, 512, 512, 4),
+            material_texture=grab(s.material_texture, nm if s.material_texture else 0, np.int32),
         )
 
     @property
@@ -182,6 +187,11 @@ def scene_from_arrays(a: SceneArrays) -> N.Scene:
     s.node_triangle = _fptr(arr(a.node_triangle, np.int32), C.c_int32)
     s.order_base = _fptr(arr(a.order_base, np.int32), C.c_int32)
     s.order_miss = _fptr(arr(a.order_miss, np.int32), C.c_int32)
+    tex = arr(getattr(a, "textures", np.zeros((0, 512, 512, 4), np.uint8)), np.uint8)
+    s.num_textures = tex.shape[0] if tex.size else 0
+    if s.num_textures:
+        s.textures = C.cast(tex.ctypes.data, C.POINTER(C.c_uint8))
+        s.material_texture = _fptr(arr(a.material_texture, np.int32), C.c_int32)
     s._keep = keep
     return s
 

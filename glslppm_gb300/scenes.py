@@ -39,8 +39,9 @@ class MaterialSpec:
     eta: float = 1.7
     glossiness: float = 0.0
     specularity: float = 1.0  # Ns / 100 of the glossy classes (>= 0.5), for the MTL block
+    texture: np.ndarray | None = None  # map_Kd image, uint8 [h, w, 3], rows top to bottom
 
-    def mtl(self) -> str:
+    def mtl(self, texture_file: str | None = None) -> str:
         """MTL block that the reference loader classifies into this material (mesh.cpp:520-611):
         Ka > 0 makes a light; Ns = 100 with Ks = (1,1,1) a mirror, with 0 < |Ks|^2 < 3 plastic;
         Ns < 100 the glossy classes; a name starting with "glass" glass, eta = |Ks|^2 / 3 + 1; the
@@ -65,7 +66,9 @@ class MaterialSpec:
         else:  # matte: the loader scales Lambertian albedo by 0.9
             ka, kd, ks = zero, tuple(c / 0.9 for c in self.color), zero
         f = lambda v: " ".join("%.9g" % x for x in v)
-        return f"newmtl {self.name}\nKa {f(ka)}\nKd {f(kd)}\nKs {f(ks)}\nNs {ns:.1f}\n"
+        block = f"newmtl {self.name}\nKa {f(ka)}\nKd {f(kd)}\nKs {f(ks)}\nNs {ns:.1f}\n"
+        # the reference gives a map_Kd texture to the material its Ns line completed (mesh.cpp:117-123)
+        return block + (f"map_Kd {texture_file}\n" if texture_file else "")
 
 
 @dataclass
@@ -77,6 +80,7 @@ class SceneSpec:
     camera_origin: tuple = (0.5, 0.5, 2.15)
     camera_lookat: tuple = (0.5, 0.5, 0.0)
     fov: float = 45.0
+    texcoords: np.ndarray | None = None  # [n, 3, 2] float32 (used by textured materials)
 
     @property
     def num_triangles(self) -> int:
@@ -96,16 +100,27 @@ class SceneSpec:
         return Mesh.from_arrays(self.positions, self.material_ids, self.material_array(), self.normals).build_bvh()
 
     def write_obj(self, path: str | Path) -> Path:
-        """OBJ + MTL (same stem) in the dialect of the reference loader."""
+        """OBJ + MTL (same stem) in the dialect of the reference loader; textures as binary PPM
+        files beside them (<stem>_<material index>.ppm)."""
         path = Path(path)
         mtl = path.with_suffix(".mtl")
-        mtl.write_text("".join(m.mtl() + "\n" for m in self.materials))
+        blocks = []
+        for k, m in enumerate(self.materials):
+            tex_name = None
+            if m.texture is not None:
+                tex_name = f"{path.stem}_{k}.ppm"
+                img = np.ascontiguousarray(m.texture, dtype=np.uint8)
+                (path.parent / tex_name).write_bytes(b"P6\n%d %d\n255\n" % (img.shape[1], img.shape[0]) + img.tobytes())
+            blocks.append(m.mtl(tex_name) + "\n")
+        mtl.write_text("".join(blocks))
         lines = [f"mtllib {mtl.name}\n"]
         n = self.num_triangles
         p = self.positions.reshape(-1, 3)
         nr = self.normals.reshape(-1, 3)
         lines += ["v %.9g %.9g %.9g\n" % tuple(map(float, v)) for v in p]
         lines += ["vn %.9g %.9g %.9g\n" % tuple(map(float, v)) for v in nr]
+        if self.texcoords is not None:
+            lines += ["vt %.9g %.9g\n" % tuple(map(float, v)) for v in self.texcoords.reshape(-1, 2)]
         cur = None
         for t in range(n):
             m = int(self.material_ids[t])
@@ -113,7 +128,10 @@ class SceneSpec:
                 lines.append(f"usemtl {self.materials[m].name}\n")
                 cur = m
             a, b, c = 3 * t + 1, 3 * t + 2, 3 * t + 3
-            lines.append(f"f {a}//{a} {b}//{b} {c}//{c}\n")
+            if self.texcoords is not None:
+                lines.append(f"f {a}/{a}/{a} {b}/{b}/{b} {c}/{c}/{c}\n")
+            else:
+                lines.append(f"f {a}//{a} {b}//{b} {c}//{c}\n")
         for ln in lines:
             if len(ln) > 79:
                 raise ValueError(f"OBJ line longer than the reference loader's 79-character chunks: {ln!r}")
@@ -229,6 +247,32 @@ def materials_box(segments: int = 16, rings: int = 8, light: bool = True) -> Sce
     if not light:
         ids[ids == 3] = 0
     return SceneSpec(sc.positions, sc.normals, ids, mats, sc.camera_origin, sc.camera_lookat, sc.fov)
+
+
+def textured_box(segments: int = 16, rings: int = 8) -> SceneSpec:
+    """The Cornell box with map_Kd textures (the reference's VolumeTextureTextures): a checker on
+    the white walls, a 53x37 gradient on the green wall (not a power of two: the reference's
+    nearest resampling to 512x512), a textured light and striped diffuse sphere; planar texture
+    coordinates that run past 1 (GL_REPEAT).  Load it through write_obj + Mesh.load_obj (the
+    from-arrays path carries no textures)."""
+    import dataclasses
+    sc = cornell_box(segments, rings)
+    yy, xx = np.mgrid[0:64, 0:64]
+    on = ((xx // 8) + (yy // 8)) % 2 == 0
+    checker = np.stack([np.where(on, 230, 40), np.full_like(xx, 180), np.where(on, 30, 220)], -1).astype(np.uint8)
+    gy, gx = np.mgrid[0:37, 0:53]
+    gradient = np.stack([gx * 255 // 52, gy * 255 // 36, np.full_like(gx, 128)], -1).astype(np.uint8)
+    glow = np.random.default_rng(11).integers(150, 256, size=(16, 16, 3)).astype(np.uint8)
+    sy, sx = np.mgrid[0:32, 0:128]
+    stripes = np.stack([np.where((sx // 16) % 2 == 0, 250, 60), np.full_like(sx, 90), np.full_like(sx, 200)],
+                       -1).astype(np.uint8)
+    mats = [dataclasses.replace(m) for m in sc.materials]
+    for k, tex in ((0, checker), (2, gradient), (3, glow), (5, stripes)):
+        mats[k] = dataclasses.replace(mats[k], texture=tex)
+    p = sc.positions.astype(np.float64)
+    uv = np.stack([2.0 * p[..., 0] + 0.37 * p[..., 1], 2.0 * p[..., 2] - 0.53 * p[..., 1]], -1).astype(np.float32)
+    return SceneSpec(sc.positions, sc.normals, sc.material_ids, mats, sc.camera_origin, sc.camera_lookat, sc.fov,
+                     texcoords=uv)
 
 
 @dataclass

@@ -133,6 +133,11 @@ typedef struct sppm_scene {
     /* ... and for each of the 6 orderings o (+x,-x,+y,-y,+z,-z), the traversal sequence:      */
     const int32_t* order_base;     /* [6][num_nodes] nodes[o][i].idBase (canonical id)           */
     const int32_t* order_miss;     /* [6][num_nodes] nodes[o][i].idMiss (index in ordering o)    */
+    /* material textures (map_Kd), resampled to 512x512 as gpurt.cpp:158-198 does; sampled as the
+       shaders sample VolumeTextureTextures (include/sppm_texture.h).  num_textures = 0: none.   */
+    uint32_t num_textures;
+    const uint8_t* textures;           /* [num_textures][512][512][4] RGBA8 (A unused)           */
+    const int32_t* material_texture;   /* [num_materials] the material's texture or -1           */
 } sppm_scene;
 
 /* Camera as the eye pass consumes it (glslppm.cpp:259-273): TCamera after TCamera::Set. */

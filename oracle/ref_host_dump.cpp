@@ -14,7 +14,8 @@
 // materials {f32 r,g,b,eta; i32 brdf; f32 glossiness}[m], light_triangles i32[l], light_cdf f32[l],
 // light_area f32, bbox f32[6], node_bounds f32[nodes*6], node_triangle i32[nodes],
 // order_base i32[6*nodes], order_miss i32[6*nodes], camera {f32 origin[3],u[3],v[3],w[3],distance;
-// u32 width,height} (zeros when no camera arguments are given).
+// u32 width,height} (zeros when no camera arguments are given), then per material {u32 textured,
+// width, height; u8 rgb[width*height*3] when textured} as LoadPPM read it.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -117,6 +118,13 @@ int main(int argc, char** argv) {
     }
     put(f, camrec, sizeof(camrec));
     put(f, camwh, sizeof(camwh));
+    // material textures as LoadPPM read them: per material u32 textured, width, height, RGB8 bytes
+    for (size_t i = 0; i < mesh.materials.size(); i++) {
+        const TMaterial& m = mesh.materials[i];
+        const unsigned rec[3] = {m.isTextured ? 1u : 0u, (unsigned)m.textureWidth, (unsigned)m.textureHeight};
+        put(f, rec, sizeof(rec));
+        if (m.isTextured) put(f, m.texture.data(), m.texture.size());
+    }
     fclose(f);
     return 0;
 }

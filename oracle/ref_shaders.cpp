@@ -27,6 +27,7 @@
 
 #include "glsl_compat.hpp"
 #include "sppm.h"
+#include "sppm_texture.h"
 
 namespace glsl {
 struct InOut {
@@ -34,10 +35,17 @@ struct InOut {
     typedef ::glsl::vec3& vec3;
     typedef ::glsl::vec4& vec4;
 };
+// VolumeTextureTextures of the scene being run (set by ref_gl_run_frames): GL_LINEAR + GL_REPEAT
+// as include/sppm_texture.h pins them
 static int g_texture3d_calls = 0;
-vec4 texture3D(const sampler3D&, const vec3&) {
+static const uint8_t* g_tex = nullptr;
+static const int32_t* g_layer = nullptr;
+static uint32_t g_layers_nm = 0;
+vec4 texture3D(const sampler3D&, const vec3& c) {
     g_texture3d_calls++;
-    return vec4(1.0f);
+    float t[3];
+    sppm_tex_sample(g_tex, g_layer, g_layers_nm, c.x, c.y, c.z, t);
+    return vec4(t[0], t[1], t[2], 1.0f);
 }
 }  // namespace glsl
 
@@ -148,6 +156,9 @@ struct RefGL {
     float poly_stride[2] = {0, 0}, material_stride = 0, light_stride = 0, light_area = 0, material_num_rcp = 0;
     int num_lights = 0;
     vec4 scene_bsphere;
+    // VolumeTextureTextures: the textured materials' 512x512 layers, the others magenta
+    std::vector<uint8_t> tex;
+    std::vector<int32_t> mat_layer;
     // state textures
     Tex q_pos, q_refl, q_nrm, rnd_eye, q_isect, q_emi, q_flux;
     Tex p_pos, p_flux, p_dir, rnd_photon, p_isect, p_emitted, p_index, p_hash, p_corr, minmax_q, minmax_p;
@@ -518,6 +529,12 @@ EXPORT void* ref_gl_create(const sppm_scene* scene, const sppm_camera* cam, int 
     g->R = resolution;
     g->cam = *cam;
     create_textures(*g, scene);
+    g->mat_layer.assign(scene->num_materials, -1);
+    if (scene->num_textures && scene->textures && scene->material_texture) {
+        g->mat_layer.assign(scene->material_texture, scene->material_texture + scene->num_materials);
+        g->tex.assign(scene->textures, scene->textures + (size_t)scene->num_textures * SPPM_TEXTURE_RES *
+                                                            SPPM_TEXTURE_RES * 4);
+    }
     const int R = resolution;
     for (Tex* t : {&g->q_pos, &g->q_refl, &g->q_nrm, &g->rnd_eye, &g->q_isect, &g->q_emi, &g->q_flux, &g->p_pos,
                    &g->p_flux, &g->p_dir, &g->rnd_photon, &g->p_isect, &g->p_emitted, &g->p_index, &g->p_hash,
@@ -538,8 +555,11 @@ EXPORT void* ref_gl_create(const sppm_scene* scene, const sppm_camera* cam, int 
 
 EXPORT int ref_gl_run_frames(void* h, unsigned n) {
     RefGL* g = (RefGL*)h;
+    glsl::g_tex = g->tex.empty() ? nullptr : g->tex.data();
+    glsl::g_layer = g->mat_layer.data();
+    glsl::g_layers_nm = (uint32_t)g->mat_layer.size();
     for (unsigned k = 0; k < n; k++) run_frame(*g);
-    return g_texture3d_calls;
+    return glsl::g_texture3d_calls;
 }
 
 // texture by name: 0 QueryPosition, 1 QueryReflectance, 2 QueryNormal, 3 RandomEye, 4 QueryIntersection,

@@ -51,6 +51,13 @@ def read_dump(path: str | Path) -> dict:
     wh = take("<u4", 2)
     d["camera"] = {"origin": cam[0:3], "u": cam[3:6], "v": cam[6:9], "w": cam[9:12], "distance": float(cam[12]),
                    "width": int(wh[0]), "height": int(wh[1])}
+    # per material: textured flag, width, height and the RGB8 bytes LoadPPM read
+    d["textures_raw"] = []
+    for _ in range(nm):
+        if off >= len(b):
+            break
+        textured, w, h = (int(x) for x in take("<u4", 3))
+        d["textures_raw"].append(take("u1", w * h * 3).reshape(h, w, 3) if textured else None)
     return d
 
 

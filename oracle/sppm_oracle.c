@@ -48,6 +48,7 @@
 
 #include "sppm.h"
 #include "sppm_fpmath.h"
+#include "sppm_texture.h"
 
 #ifdef ORACLE_FP64
 typedef double real;
@@ -98,6 +99,7 @@ static inline vec3 cross3(vec3 a, vec3 b) {
 }
 static inline real length3(vec3 a) { return R_SQRT(dot3(a, a)); }
 static inline vec3 normalize3(vec3 a) { return scl3(a, RC(1.0) / R_SQRT(dot3(a, a))); }
+static inline real len3(vec3 a) { return R_SQRT(dot3(a, a)); }
 static inline vec3 reflect3(vec3 i, vec3 n) {
     const real d = RC(2.0) * dot3(n, i);
     return sub3(i, lscl3(d, n));
@@ -179,6 +181,11 @@ typedef struct {
     int32_t* ntri;                     /* [nn] */
     int32_t* hit_link;                 /* [6][nn] canonical -> canonical or -1 (gpurt.cpp:332-366) */
     int32_t* miss_link;                /* [6][nn] */
+    /* material textures (VolumeTextureTextures, gpurt.cpp:158-198; sampling: sppm_texture.h) */
+    uint8_t* tex;                      /* [layers][512][512][4] or NULL */
+    int32_t* mat_layer;                /* [nm]: layer of the material or -1 (magenta) */
+    float mat_rcp;                     /* MaterialNumRcp = 1 / materials (glslppm.cpp:256, 376) */
+    int any_tex;                       /* some texture coordinate is below 1e10 (else no lookups) */
 } oscene;
 
 typedef struct oracle_ctx {
@@ -225,10 +232,20 @@ static inline int32_t tri_material(const oscene* s, int32_t t) {
 typedef struct {
     real t;
     vec3 pos, nrm, gnrm, col;
+    real texu, texv; /* Result.tex (eyeraytrace.fs:280) */
     int brdf;
     real eta, g;
     int32_t matid;
 } Isect;
+
+/* col *= texture3D(VolumeTextureTextures, vec3(tex, r)).rgb when |tex.x| < 1e10 (eyeraytrace.fs:443-446,
+   photontrace.fs:418-422, 562-565) */
+static vec3 tex_modulate(const oscene* s, real tu, real tv, float r, vec3 col) {
+    if (!(R_FABS(tu) < RC(1e+10))) return col;
+    float t[3];
+    sppm_tex_sample(s->tex, s->mat_layer, s->nm, (float)tu, (float)tv, r, t);
+    return v3(col.x * (real)t[0], col.y * (real)t[1], col.z * (real)t[2]);
+}
 
 typedef struct {
     int32_t tri;
@@ -251,6 +268,7 @@ static Isect raytrace(oracle_ctx* c, vec3 org, vec3 dir, int photon, int cull, L
     memset(&r, 0, sizeof(r));
     r.t = RC(1.0e+30);
     r.matid = -1;
+    r.texu = r.texv = RC(1.0e+30);
     LastIsect is = {-1, -1, photon ? RC(1.0e30) : RC(1.0e20)};
     real bu = 0, bv = 0, bw = 0; /* Barycentric = uvt.ywx -> (v, w, u) */
     const int face = cube_face(dir);
@@ -306,6 +324,8 @@ static Isect raytrace(oracle_ctx* c, vec3 org, vec3 dir, int photon, int cull, L
         r.t = is.t;
         r.pos = add3(add3(scl3(V2, bu), scl3(V0, bv)), scl3(V1, bw));
         r.nrm = normalize3(add3(add3(scl3(N2, bu), scl3(N0, bv)), scl3(N1, bw)));
+        r.texu = (s->tv[is.tri * 3 + 2].w * bu + s->tv[is.tri * 3].w * bv) + s->tv[is.tri * 3 + 1].w * bw;
+        r.texv = (s->tn[is.tri * 3 + 2].w * bu + s->tn[is.tri * 3].w * bv) + s->tn[is.tri * 3 + 1].w * bw;
         r.gnrm = normalize3(cross3(sub3(V1, V0), sub3(V2, V0)));
         const vec4 m0 = s->mat[is.mat * 2], m1 = s->mat[is.mat * 2 + 1];
         r.col = xyz(m0);
@@ -393,7 +413,7 @@ static void eye_pixel(oracle_ctx* c, uint32_t px, uint32_t py) {
     LastIsect last = {-1, -1, RC(1.0e20)};
     uint64_t segs = 0;
     for (uint32_t j = 0; j < c->cfg.max_path_length; j++) {
-        const Isect i = raytrace(c, rorg, rdir, 0, j == 0, &last);
+        Isect i = raytrace(c, rorg, rdir, 0, j == 0, &last);
         segs++;
         if (i.t == RC(1.0e+30)) {
             nrm = v3(0, 0, 0);
@@ -402,6 +422,8 @@ static void eye_pixel(oracle_ctx* c, uint32_t px, uint32_t py) {
         }
         pos = i.pos;
         nrm = i.nrm;
+        if (c->sc.any_tex)
+            i.col = tex_modulate(&c->sc, i.texu, i.texv, c->sc.mat_rcp * ((float)i.matid + 0.5f), i.col);
         if (i.brdf == -1) {
             nrm = v3(0, 0, 0);
             emi = mul3(col, i.col);
@@ -513,6 +535,12 @@ static void light_sample(oracle_ctx* c, vec4* rndv, vec3* flux, vec3* dir, vec3*
     const vec3 N0 = tri_normal(s, lt, 0), N1 = tri_normal(s, lt, 1), N2 = tri_normal(s, lt, 2);
     const int32_t mi = tri_material(s, lt);
     *flux = scl3(xyz(s->mat[mi * 2]), s->light_area * RC(3.141592));
+    if (s->any_tex) {
+        /* T = T2 * c + T0 * a + T1 * b (photontrace.fs:413-422) */
+        const real tu = (s->tv[lt * 3 + 2].w * cc + s->tv[lt * 3].w * a) + s->tv[lt * 3 + 1].w * b;
+        const real tw = (s->tn[lt * 3 + 2].w * cc + s->tn[lt * 3].w * a) + s->tn[lt * 3 + 1].w * b;
+        *flux = tex_modulate(s, tu, tw, s->mat_rcp * ((float)mi + 0.75f), *flux);
+    }
     vec3 o = add3(add3(scl3(V0, a), scl3(V1, b)), scl3(V2, cc));
     const vec3 nrm = normalize3(add3(add3(scl3(N0, a), scl3(N1, b)), scl3(N2, cc)));
     const vec3 gnrm = normalize3(cross3(sub3(V1, V0), sub3(V2, V0)));
@@ -575,6 +603,17 @@ static int photon_slot(oracle_ctx* c, uint32_t sidx) {
         vec3 inrm = pnrm;
         const int32_t mi = tri_material(s, ptri);
         vec3 icol = xyz(s->mat[mi * 2]);
+        if (s->any_tex) {
+            /* the hit's barycentrics from the stored position (photontrace.fs:521-545) */
+            const real bx = len3(cross3(sub3(V1, V0), sub3(ipos, V0)));
+            const real by = len3(cross3(sub3(V2, V1), sub3(ipos, V1)));
+            const real bz = len3(cross3(sub3(V0, V2), sub3(ipos, V2)));
+            const real bw_ = (bx + by) + bz;
+            const real nx = bx / bw_, ny = by / bw_, nz = bz / bw_;
+            const real tu = (s->tv[ptri * 3 + 2].w * nx + s->tv[ptri * 3].w * ny) + s->tv[ptri * 3 + 1].w * nz;
+            const real tw = (s->tn[ptri * 3 + 2].w * nx + s->tn[ptri * 3].w * ny) + s->tn[ptri * 3 + 1].w * nz;
+            icol = tex_modulate(s, tu, tw, s->mat_rcp * (((float)mi + 0.5f) + 0.25f), icol);
+        }
         const int brdf = (int)s->mat[mi * 2 + 1].x;
         const real ieta = s->mat[mi * 2].w;
         const real ig = s->mat[mi * 2 + 1].y;
@@ -979,6 +1018,20 @@ EXPORT oracle_ctx* ORACLE_API(create)(const sppm_config* cfg, const sppm_scene* 
     }
     s->light_area = scene->light_area;
     s->light_stride = s->nl ? (real)(1.0f / (float)s->nl) : RC(0.0);
+    s->mat_rcp = 1.0f / (float)s->nm;
+    s->mat_layer = (int32_t*)malloc(sizeof(int32_t) * s->nm);
+    for (uint32_t m = 0; m < s->nm; m++)
+        s->mat_layer[m] = (scene->num_textures && scene->material_texture) ? scene->material_texture[m] : -1;
+    s->any_tex = 0;
+    if (scene->texcoords)
+        for (size_t k = 0; k < (size_t)nt * 6; k++)
+            if (fabsf(scene->texcoords[k]) < 1e10f) s->any_tex = 1;
+    s->tex = NULL;
+    if (scene->num_textures && scene->textures && scene->material_texture) {
+        const size_t bytes = (size_t)scene->num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4;
+        s->tex = (uint8_t*)malloc(bytes);
+        memcpy(s->tex, scene->textures, bytes);
+    }
     {
         /* SceneBSphere (glslppm.cpp:388-393) in single precision on the host */
         const float* mn = scene->bbox_min;
@@ -1263,6 +1316,8 @@ EXPORT void ORACLE_API(destroy)(oracle_ctx* c) {
     free(s->tv);
     free(s->tn);
     free(s->mat);
+    free(s->mat_layer);
+    free(s->tex);
     free(s->light_tri);
     free(s->light_cdf);
     free(s->nb);

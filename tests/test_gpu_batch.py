@@ -164,3 +164,29 @@ def test_watchdog_error_names_the_job_whose_rays_raised_it(cornell_metal):
     b.run_passes(2)
     b.synchronize()
     assert b.frame_info(good).frames == 4
+
+
+@pytest.mark.parametrize("precision", [N.PRECISION_FP32, N.PRECISION_MIXED])
+def test_textured_and_untextured_jobs_in_one_batch(tmp_path, precision):
+    """A textured job makes the batch launch the kernel variants with texture lookups for every
+    job: each job still has the state of its own single-job context."""
+    tex = scenes.textured_box()
+    tex_mesh = g.Mesh.load_obj(str(tex.write_obj(tmp_path / "t.obj"))).build_bvh()
+    plain = scenes.cornell_box(16, 8)
+    plain_mesh = plain.to_mesh()
+    w, h = 32, 24
+    cfg = config_for(w, h, 32, 32, precision)
+    b = g.Batch(precision=precision, max_jobs=4)
+    jt = b.add_job(cfg, tex_mesh, camera_for(tex, w, h))
+    jp = b.add_job(cfg, plain_mesh, camera_for(plain, w, h))
+    b.run_passes(12)
+    b.synchronize()
+    for j, mesh, spec in ((jt, tex_mesh, tex), (jp, plain_mesh, plain)):
+        r = g.Renderer(cfg)
+        r.upload_scene(mesh)
+        r.set_camera(camera_for(spec, w, h))
+        r.run_passes(12)
+        r.synchronize()
+        for k in KINDS:
+            assert_same(b.read_state(j, k), r.read_state(k), f"job {j} {k}")
+

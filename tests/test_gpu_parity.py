@@ -132,6 +132,21 @@ def test_state_bit_exact_every_material_class(light):
     run_pair(cfg, sc.to_mesh().scene(), cam, [1, 10, 11, 21])
 
 
+@pytest.mark.parametrize("fused", [False, True])
+def test_state_bit_exact_textured(tmp_path, fused):
+    """map_Kd textures read through the OBJ loader: the eye path, emission from a textured light
+    and photon bounces look them up (GL_LINEAR / GL_REPEAT as include/sppm_texture.h pins it)."""
+    from glslppm_gb300 import scenes
+    sc = scenes.textured_box()
+    mesh = g.Mesh.load_obj(str(sc.write_obj(tmp_path / "t.obj"))).build_bvh()
+    cfg = g.default_config(40, height=32, photon_width=64, photon_height=32, radius_rule=N.RADIUS_DIAGONAL,
+                           radius_fraction=0.01)
+    if fused:
+        cfg.flags |= N.FLAG_FUSED_PHOTON
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 40, 32, sc.fov)
+    run_pair(cfg, mesh.scene(), cam, [1, 10, 11, 21])
+
+
 def test_state_bit_exact_non_square_and_hash_seed(cornell_c1_mesh):
     sc, mesh = cornell_c1_mesh
     cfg = g.default_config(40, height=24, photon_width=48, photon_height=20, hash_slots=1500,

@@ -121,6 +121,37 @@ def test_every_material_class_round_trips_through_the_reference_loader(tmp_path,
     assert (len(mine.light_cdf) > 0) == light
 
 
+def _resample_like_reference(img):
+    """gpurt.cpp:176-196: layer texel (x, y) = source texel (x * w / 512, y * h / 512)."""
+    h, w = img.shape[:2]
+    xs = np.arange(512) * w // 512
+    ys = np.arange(512) * h // 512
+    out = np.full((512, 512, 4), 255, np.uint8)
+    out[..., :3] = img[ys][:, xs]
+    return out
+
+
+@pytest.mark.reference
+def test_textured_scene_equals_reference_loader(tmp_path):
+    """map_Kd PPM textures, vt coordinates on every face vertex (kept for textured materials
+    only), the textures resampled to 512x512 as the reference's packing does."""
+    from oracle.build import build_ref
+    from oracle.refdump import run_ref_host_dump
+    build_ref()
+    spec = scenes.textured_box()
+    obj = spec.write_obj(tmp_path / "t.obj")
+    ref = run_ref_host_dump(obj, 1.0)
+    mine = g.Mesh.load_obj(str(obj)).build_bvh().arrays()
+    assert_scene_equal(ref, mine)
+    assert np.array_equal(ref["texcoords"].view(np.uint32), mine.texcoords.view(np.uint32))
+    raw = ref["textures_raw"]
+    layers = [k for k, t in enumerate(raw) if t is not None]
+    assert layers == [k for k, m in enumerate(spec.materials) if m.texture is not None]
+    assert [int(x) for x in mine.material_texture] == [layers.index(k) if k in layers else -1 for k in range(len(raw))]
+    for k in layers:
+        assert np.array_equal(mine.textures[layers.index(k)], _resample_like_reference(raw[k])), k
+
+
 def _quirky_obj(tmp_path, name, pad_lines):
     """An OBJ with material switches, a second mtllib half way, missing normals, quads and long
     lines, padded with `pad_lines` long comment lines between its lines (the padding changes no

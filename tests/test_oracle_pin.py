@@ -33,7 +33,7 @@ def compare(o, r, label):
     assert not bad, f"{label}: oracle differs from the reference shaders: {bad}"
 
 
-def run(scene, cam, R, checkpoints):
+def run(scene, cam, R, checkpoints, textured=False):
     from oracle.binding import Oracle
     from oracle.build import build_ref
     from oracle.refdump import RefShaders
@@ -44,7 +44,8 @@ def run(scene, cam, R, checkpoints):
     done = 0
     for k in checkpoints:
         o.run_frames(k - done)
-        assert r.run_frames(k - done) == 0  # no texture lookups on untextured scenes
+        lookups = r.run_frames(k - done)  # texture3D calls so far
+        assert (lookups > 0) == textured
         done = k
         compare(o, r, f"after {k} frames")
         s, fi = r.scalars(), o.frame_info()
@@ -77,4 +78,15 @@ def test_oracle_equals_reference_shaders_every_material_class(light):
     sc = scenes.materials_box(light=light)
     cam = g.look_at(sc.camera_origin, sc.camera_lookat, 32, 32, sc.fov)  # power of two: ReduceTexture
     run(sc.to_mesh().scene(), cam, 32, [1, 2, 11, 21])
+
+
+def test_oracle_equals_reference_shaders_textured(tmp_path):
+    """map_Kd textures sampled on the eye path, by photon emission from a textured light and by
+    photon bounces (barycentrics from the stored position), GL_LINEAR / GL_REPEAT as
+    include/sppm_texture.h pins them."""
+    from glslppm_gb300 import scenes
+    sc = scenes.textured_box()
+    mesh = g.Mesh.load_obj(str(sc.write_obj(tmp_path / "t.obj"))).build_bvh()
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 32, 32, sc.fov)
+    run(mesh.scene(), cam, 32, [1, 2, 11, 21], textured=True)
 
