@@ -19,6 +19,7 @@
 #include "camera.h"  // the reference's TCamera
 #include "mesh.h"    // the reference's TMesh
 #include "sppm.h"
+#include "sppm_texture.h"
 
 class CGPURT {
 public:
@@ -90,6 +91,19 @@ public:
             mats[m].brdf = tm.brdf;
             mats[m].glossiness = 1.0f / (std::pow(2.0f / (1.0f - tm.specularity), 2.71828f) + 1.0f);  // gpurt.cpp:126
         }
+        // map_Kd textures resampled to the 512x512 layers of VolumeTextureTextures (gpurt.cpp:158-198)
+        mtex.assign(mesh.materials.size(), -1);
+        layers.clear();
+        unsigned nlayers = 0;
+        const size_t layer_bytes = (size_t)SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4;
+        for (size_t m = 0; m < mesh.materials.size(); m++) {
+            const TMaterial& tm = mesh.materials[m];
+            if (!tm.isTextured || tm.texture.size() < (size_t)tm.textureWidth * tm.textureHeight * 3) continue;
+            mtex[m] = (int32_t)nlayers++;
+            layers.resize(nlayers * layer_bytes);
+            sppm_tex_resample(tm.texture.data(), tm.textureWidth, tm.textureHeight,
+                              layers.data() + (nlayers - 1) * layer_bytes);
+        }
         const int nn = bvh.nodesNum;
         bounds.resize((size_t)nn * 6);
         tri.resize(nn);
@@ -129,6 +143,9 @@ public:
         s.node_triangle = tri.data();
         s.order_base = base.data();
         s.order_miss = miss.data();
+        s.num_textures = nlayers;
+        s.textures = nlayers ? layers.data() : nullptr;
+        s.material_texture = mtex.data();
         *out = s;
     }
 
@@ -152,4 +169,6 @@ private:
     std::vector<float> pos, nrm, tex, bounds;
     std::vector<int> mat, tri, base, miss;
     std::vector<sppm_material> mats;
+    std::vector<uint8_t> layers;  // [textures][512][512][4]
+    std::vector<int32_t> mtex;    // texture of each material or -1
 };

@@ -44,6 +44,18 @@ int main(int argc, char** argv) {
     const unsigned wh[2] = {0, 0};
     put(f, cam, sizeof(cam));
     put(f, wh, sizeof(wh));
+    // per material: the flattened texture layer as a 512x512 RGB8 record (textured flag, 512, 512)
+    for (unsigned m = 0; m < s.num_materials; m++) {
+        const int layer = s.material_texture ? s.material_texture[m] : -1;
+        const unsigned rec[3] = {layer >= 0 ? 1u : 0u, 512u, 512u};
+        put(f, rec, sizeof(rec));
+        if (layer < 0) continue;
+        std::vector<unsigned char> rgb((size_t)512 * 512 * 3);
+        const unsigned char* src = s.textures + (size_t)layer * 512 * 512 * 4;
+        for (size_t i = 0; i < (size_t)512 * 512; i++)
+            for (int c = 0; c < 3; c++) rgb[i * 3 + c] = src[i * 4 + c];
+        put(f, rgb.data(), rgb.size());
+    }
     fclose(f);
     const int frames = atoi(argv[4]);
     if (frames > 0) {

@@ -235,6 +235,28 @@ def test_drop_in_gpurt_header_with_reference_host_code(tmp_path):
         assert np.array_equal(np.asarray(a[k]).view(np.uint8), np.asarray(b[k]).view(np.uint8)), k
 
 
+@pytest.mark.reference
+def test_drop_in_gpurt_header_passes_textures(tmp_path):
+    """The CGPURT shim hands the reference TMesh's map_Kd textures over as 512x512 layers, equal
+    to the reference's resampling and to our own loader's."""
+    import subprocess
+    from oracle.build import build_ref
+    from oracle.refdump import read_dump, run_ref_host_dump
+    exe = build_ref().get("gpurt_shim")
+    obj = scenes.textured_box().write_obj(tmp_path / "t.obj")
+    out = tmp_path / "shim.bin"
+    subprocess.run([str(exe), obj.name, "1.0", str(out), "0"], cwd=str(tmp_path), check=True, capture_output=True)
+    a, ref = read_dump(out), run_ref_host_dump(obj, 1.0)
+    for k in FIELDS:
+        assert np.array_equal(np.asarray(a[k]).view(np.uint8), np.asarray(ref[k]).view(np.uint8)), k
+    mine = g.Mesh.load_obj(str(obj)).arrays()
+    for m, (layer, raw) in enumerate(zip(a["textures_raw"], ref["textures_raw"])):
+        assert (layer is None) == (raw is None), m
+        if raw is not None:
+            assert np.array_equal(layer, _resample_like_reference(raw)[..., :3]), m
+            assert np.array_equal(layer, mine.textures[mine.material_texture[m]][..., :3]), m
+
+
 def test_cornell_variants_are_seeded_and_in_range():
     from glslppm_gb300 import scenes
     a, b = scenes.cornell_variant(7), scenes.cornell_variant(7)
