@@ -526,6 +526,7 @@ void run_frame(RefGL& g) {
 
 EXPORT void* ref_gl_create(const sppm_scene* scene, const sppm_camera* cam, int resolution) {
     RefGL* g = new RefGL();
+    glsl::g_texture3d_calls = 0;  // lookups are counted per harness
     g->R = resolution;
     g->cam = *cam;
     create_textures(*g, scene);
@@ -551,6 +552,13 @@ EXPORT void* ref_gl_create(const sppm_scene* scene, const sppm_camera* cam, int 
             v = vec4(x, y, z, w);
         }
     return g;
+}
+
+// FocalLength / ApertureSize (glslppm.cpp:31-32, keyboard-adjustable in the reference)
+EXPORT void ref_gl_set_lens(void* h, float focal, float aperture) {
+    RefGL* g = (RefGL*)h;
+    g->focal = focal;
+    g->aperture = aperture;
 }
 
 EXPORT int ref_gl_run_frames(void* h, unsigned n) {

@@ -89,6 +89,7 @@ class RefShaders:
         self.lib = C.CDLL(str(lib_path))
         P = C.c_void_p
         for name, res, args in (("ref_gl_create", P, [P, P, C.c_int]), ("ref_gl_run_frames", C.c_int, [P, C.c_uint]),
+                                ("ref_gl_set_lens", None, [P, C.c_float, C.c_float]),
                                 ("ref_gl_read", C.c_int, [P, C.c_int, P]), ("ref_gl_scalars", None, [P, P]),
                                 ("ref_gl_display", None, [P, P]), ("ref_gl_destroy", None, [P])):
             fn = getattr(self.lib, name)
@@ -97,6 +98,9 @@ class RefShaders:
         self._scene = scene
         self.R = resolution
         self._h = self.lib.ref_gl_create(C.addressof(scene), C.addressof(camera), resolution)
+
+    def set_lens(self, focal: float, aperture: float) -> None:
+        self.lib.ref_gl_set_lens(self._h, focal, aperture)
 
     def run_frames(self, n: int) -> int:
         return self.lib.ref_gl_run_frames(self._h, n)  # texture3D calls (0 for untextured scenes)

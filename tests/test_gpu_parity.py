@@ -147,6 +147,16 @@ def test_state_bit_exact_textured(tmp_path, fused):
     run_pair(cfg, mesh.scene(), cam, [1, 10, 11, 21])
 
 
+def test_state_bit_exact_depth_of_field(cornell_c1_mesh):
+    """A thin lens with a non-zero aperture focused inside the box."""
+    sc, mesh = cornell_c1_mesh
+    cfg = g.default_config(40, height=32, photon_width=64, photon_height=32, radius_rule=N.RADIUS_DIAGONAL,
+                           radius_fraction=0.01)
+    cfg.focal_length, cfg.aperture = 1.8, 0.06
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 40, 32, sc.fov)
+    run_pair(cfg, mesh.scene(), cam, [1, 11, 21])
+
+
 def test_state_bit_exact_non_square_and_hash_seed(cornell_c1_mesh):
     sc, mesh = cornell_c1_mesh
     cfg = g.default_config(40, height=24, photon_width=48, photon_height=20, hash_slots=1500,

@@ -33,14 +33,17 @@ def compare(o, r, label):
     assert not bad, f"{label}: oracle differs from the reference shaders: {bad}"
 
 
-def run(scene, cam, R, checkpoints, textured=False):
+def run(scene, cam, R, checkpoints, textured=False, lens=None):
     from oracle.binding import Oracle
     from oracle.build import build_ref
     from oracle.refdump import RefShaders
     build_ref()
     cfg = g.default_config(R)
-    o = Oracle(cfg, scene, cam)
     r = RefShaders(scene, cam, R)
+    if lens is not None:
+        cfg.focal_length, cfg.aperture = lens
+        r.set_lens(*lens)
+    o = Oracle(cfg, scene, cam)
     done = 0
     for k in checkpoints:
         o.run_frames(k - done)
@@ -89,4 +92,11 @@ def test_oracle_equals_reference_shaders_textured(tmp_path):
     mesh = g.Mesh.load_obj(str(sc.write_obj(tmp_path / "t.obj"))).build_bvh()
     cam = g.look_at(sc.camera_origin, sc.camera_lookat, 32, 32, sc.fov)
     run(mesh.scene(), cam, 32, [1, 2, 11, 21], textured=True)
+
+
+def test_oracle_equals_reference_shaders_depth_of_field(cornell_c1_mesh):
+    """A thin lens with a non-zero aperture (eyeraytrace.fs:404-421)."""
+    sc, mesh = cornell_c1_mesh
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 32, 32, sc.fov)
+    run(mesh.scene(), cam, 32, [1, 11, 21], lens=(1.8, 0.06))
 
