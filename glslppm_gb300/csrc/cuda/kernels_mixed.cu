@@ -11,7 +11,9 @@
 //    direction (snorm16 x3) and the slot's photon count -- so the gather reads one sector per cell
 //    instead of the winner index, three photon arrays and the count; the in-cell test becomes an
 //    integer compare;
-//  * flux is gathered in FP32 and the per-pixel statistics N, R^2 and tau are kept in FP64.
+//  * flux is gathered in FP32 and the per-pixel statistics N, R^2 and tau are kept as double-float
+//    pairs (about 48 significant bits from FP32 arithmetic: GB300's FP64 rate is a small fraction
+//    of its FP32 rate).
 // Emission/bounce (photon generation), photon records and hashing stay the plain FP32 kernels.
 #include <cstdint>
 

@@ -51,7 +51,8 @@ typedef enum sppm_precision {
        restatement of the shaders. */
     SPPM_PRECISION_FP32 = 0,
     /* Mixed: FMA-contracted traversal over outward-rounded quantised child boxes, photon flux
-       and direction stored in FP16, flux gathered in FP32, per-pixel N, R^2 and tau in FP64. */
+       and direction stored in FP16, flux gathered in FP32, per-pixel N, R^2 and tau as double-float
+       pairs (read as doubles). */
     SPPM_PRECISION_MIXED = 1
 } sppm_precision;
 
