@@ -459,14 +459,14 @@ def run_batched(args, device: int, K: int, W: int, precision: int):
     segs = sum((y.photon_segments + y.eye_segments) - (x.photon_segments + x.eye_segments) for x, y in zip(f0, f1))
     info = b.info()
     batched = photons / (ms / 1000.0) / 1e6
-    # end to end: every step sets each job's camera (host->device), runs one pass and reads each
-    # job's progress counters back (device->host)
+    # end to end: every step sets each job's camera (host->device, one upload launch for all
+    # jobs), runs one pass and reads each job's progress counters back (device->host)
     E = max(5, min(K, 30))
+    cams = [cam for (_, _, _, cam) in jobs]
     fe0 = b.frame_infos(ids)
     t0 = time.perf_counter()
     for _ in range(E):
-        for j, (_, _, _, cam) in zip(ids, jobs):
-            b.set_camera(j, cam)
+        b.set_cameras(ids, cams)
         b.run_passes(1)
         fe = b.frame_infos(ids)
     te = time.perf_counter() - t0

@@ -55,6 +55,15 @@ class Batch:
     def set_camera(self, job: int, camera: N.Camera) -> None:
         N.check(N.lib.sppm_batch_set_camera(self._h, job, C.byref(camera)))
 
+    def set_cameras(self, jobs, cameras) -> None:
+        """set_camera for every (job, camera) pair, the descriptor uploads queued as one launch."""
+        jobs, cameras = list(jobs), list(cameras)
+        if len(jobs) != len(cameras):
+            raise ValueError(f"{len(jobs)} jobs but {len(cameras)} cameras")
+        ids = (C.c_uint32 * len(jobs))(*jobs)
+        cams = (N.Camera * len(cameras))(*cameras)
+        N.check(N.lib.sppm_batch_set_cameras(self._h, len(jobs), ids, cams))
+
     def run_passes(self, n: int = 1) -> None:
         N.check(N.lib.sppm_batch_run_passes(self._h, n))
 

@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include "kernels.h"
 #include "runtime.h"
 #include "sppm_batch.h"
 
@@ -170,6 +171,35 @@ int sppm_batch_set_camera(sppm_batch* b, uint32_t id, const sppm_camera* cam) {
     if (!j || !cam) return fail(SPPM_ERR_ARG, "no job %u or null camera", id);
     SPPM_CK(cudaSetDevice(b->rt.device));
     return j->set_camera(cam, b->rt.stream);
+}
+
+int sppm_batch_set_cameras(sppm_batch* b, uint32_t n, const uint32_t* ids, const sppm_camera* cams) {
+    if (!b || (n && (!ids || !cams))) return fail(SPPM_ERR_ARG, "null batch, job list or camera list");
+    std::vector<Job*> js(n);
+    for (uint32_t i = 0; i < n; i++) {
+        js[i] = job_of(b, ids[i]);
+        if (!js[i]) return fail(SPPM_ERR_ARG, "no job %u", ids[i]);
+        for (uint32_t p = 0; p < i; p++)
+            if (js[p] == js[i]) return fail(SPPM_ERR_ARG, "job %u listed twice", ids[i]);
+    }
+    SPPM_CK(cudaSetDevice(b->rt.device));
+    int st = SPPM_OK;
+    for (uint32_t i0 = 0; i0 < n; i0 += kDescCopyMax) {
+        const uint32_t m = std::min(n - i0, kDescCopyMax);
+        DescCopy list;
+        list.n = m;
+        for (uint32_t i = 0; i < m; i++) {
+            Job* j = js[i0 + i];
+            j->set_camera_desc(&cams[i0 + i]);
+            if ((st = j->stage_desc(&list.src[i]))) return st;
+            list.dst[i] = j->d_desc;
+        }
+        launch_copy_descs(list, b->rt.stream);
+        SPPM_CK(cudaGetLastError());
+        for (uint32_t i = 0; i < m; i++)
+            if ((st = js[i0 + i]->staged(b->rt.stream))) return st;
+    }
+    return SPPM_OK;
 }
 
 int sppm_batch_run_passes(sppm_batch* b, uint32_t n) {

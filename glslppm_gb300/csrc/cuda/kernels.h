@@ -19,6 +19,16 @@ void launch_gather_states(const JobDesc* jobs, const StateGather& list, JobState
 // device memory, by one block (a small upload without a copy-engine transfer)
 void launch_copy_from_host(void* dst, const void* src_mapped, size_t bytes, cudaStream_t s);
 
+// up to kDescCopyMax job descriptors from mapped staging slots to the runner's table, one block
+// per descriptor, in one launch (kernel parameter)
+constexpr uint32_t kDescCopyMax = 128;
+struct DescCopy {
+    uint32_t n;
+    JobDesc* dst[kDescCopyMax];
+    const JobDesc* src[kDescCopyMax];
+};
+void launch_copy_descs(const DescCopy& list, cudaStream_t s);
+
 // plain FP32 path (kernels_fp32.cu)
 void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
 // mixed: 4-wide BVH traversal; textured: some job of the launch has texture coordinates (the

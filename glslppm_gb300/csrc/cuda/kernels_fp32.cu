@@ -1785,6 +1785,14 @@ __global__ void k_copy_from_host(unsigned long long* dst, const unsigned long lo
     for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
 }
 
+__global__ void k_copy_descs(DescCopy list) {
+    static_assert(sizeof(JobDesc) % 8 == 0, "JobDesc is copied in 8-byte words");
+    if (blockIdx.x >= list.n) return;
+    auto* dst = reinterpret_cast<unsigned long long*>(list.dst[blockIdx.x]);
+    const auto* src = reinterpret_cast<const unsigned long long*>(list.src[blockIdx.x]);
+    for (uint32_t w = threadIdx.x; w < sizeof(JobDesc) / 8; w += blockDim.x) dst[w] = src[w];
+}
+
 // one block per listed job: its JobState word by word
 __global__ void k_gather_states(const JobDesc* jobs, StateGather list, JobState* out) {
     static_assert(sizeof(JobState) % 4 == 0, "JobState is copied in 32-bit words");
@@ -1802,6 +1810,9 @@ static inline uint32_t blocks_for(uint32_t n, uint32_t b) { return (n + b - 1) /
 void launch_copy_from_host(void* dst, const void* src_mapped, size_t bytes, cudaStream_t s) {
     k_copy_from_host<<<1, 64, 0, s>>>(static_cast<unsigned long long*>(dst),
                                        static_cast<const unsigned long long*>(src_mapped), (uint32_t)(bytes / 8));
+}
+void launch_copy_descs(const DescCopy& list, cudaStream_t s) {
+    if (list.n) k_copy_descs<<<list.n, 64, 0, s>>>(list);
 }
 void launch_gather_states(const JobDesc* jobs, const StateGather& list, JobState* out, cudaStream_t s) {
     if (list.n) k_gather_states<<<list.n, 64, 0, s>>>(jobs, list, out);

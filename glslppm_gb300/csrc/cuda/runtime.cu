@@ -359,22 +359,53 @@ Job::~Job() {
     if (stage) cudaFreeHost(stage);
 }
 
-// queues the upload of the host descriptor on s through a pinned staging slot (no stream sync)
-int Job::write_desc(cudaStream_t s) {
+// copies the host descriptor into the next of four pinned, mapped staging slots (waiting for the
+// slot's previous upload to finish) and returns the slot's device address in *src
+int Job::stage_desc(const JobDesc** src) {
     static_assert(sizeof(JobDesc) % 8 == 0, "JobDesc is uploaded in 8-byte words");
     if (!stage) {
         SPPM_CK(cudaHostAlloc(&stage, 4 * sizeof(JobDesc), cudaHostAllocMapped));
         SPPM_CK(cudaHostGetDevicePointer(&stage_dev, stage, 0));
         for (auto& e : stage_ev) SPPM_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
-    const uint32_t k = stage_next++ & 3u;
+    const uint32_t k = stage_next & 3u;
     if (stage_used[k]) SPPM_CK(cudaEventSynchronize(stage_ev[k]));
     stage[k] = desc;
-    // read by a kernel straight from the mapped slot: no copy-engine round trip on the stream
-    launch_copy_from_host(d_desc, stage_dev + k, sizeof(JobDesc), s);
-    SPPM_CK(cudaGetLastError());
+    *src = stage_dev + k;
+    return SPPM_OK;
+}
+
+// marks the slot filled by the last stage_desc as in use until the work queued on s so far is done
+int Job::staged(cudaStream_t s) {
+    const uint32_t k = stage_next++ & 3u;
     SPPM_CK(cudaEventRecord(stage_ev[k], s));
     stage_used[k] = true;
+    return SPPM_OK;
+}
+
+// queues the upload of the host descriptor on s through a pinned staging slot (no stream sync)
+int Job::write_desc(cudaStream_t s) {
+    const JobDesc* src = nullptr;
+    int st = stage_desc(&src);
+    if (st) return st;
+    // read by a kernel straight from the mapped slot: no copy-engine round trip on the stream
+    launch_copy_from_host(d_desc, src, sizeof(JobDesc), s);
+    SPPM_CK(cudaGetLastError());
+    return staged(s);
+}
+
+int Job::set_camera_desc(const sppm_camera* cam) {
+    JobDesc& J = desc;
+    for (int k = 0; k < 3; k++) {
+        J.cam_pos[k] = cam->origin[k];
+        J.cam_u[k] = cam->u[k];
+        J.cam_v[k] = cam->v[k];
+        J.cam_w[k] = cam->w[k];
+    }
+    J.cam_cx = (float)cam->width * 0.5f;
+    J.cam_cy = (float)cam->height * 0.5f;
+    J.cam_dist = cam->distance;
+    have_camera = true;
     return SPPM_OK;
 }
 
@@ -505,17 +536,7 @@ int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
 }
 
 int Job::set_camera(const sppm_camera* cam, cudaStream_t s) {
-    JobDesc& J = desc;
-    for (int k = 0; k < 3; k++) {
-        J.cam_pos[k] = cam->origin[k];
-        J.cam_u[k] = cam->u[k];
-        J.cam_v[k] = cam->v[k];
-        J.cam_w[k] = cam->w[k];
-    }
-    J.cam_cx = (float)cam->width * 0.5f;
-    J.cam_cy = (float)cam->height * 0.5f;
-    J.cam_dist = cam->distance;
-    have_camera = true;
+    set_camera_desc(cam);
     return write_desc(s);
 }
 

@@ -112,8 +112,11 @@ struct Job {
     int init(const sppm_config& cfg, JobDesc* d_desc, uint32_t slot, cudaStream_t s);
     int upload_scene(const sppm_scene* scene, cudaStream_t s);
     int set_camera(const sppm_camera* cam, cudaStream_t s);
+    int set_camera_desc(const sppm_camera* cam);  // host descriptor only; uploaded by the caller
     int reset(cudaStream_t s);
     int write_desc(cudaStream_t s);
+    int stage_desc(const JobDesc** src);  // write_desc in two halves, for uploads of many jobs
+    int staged(cudaStream_t s);           // in one launch (launch_copy_descs)
     void* state_ptr(uint32_t kind, size_t* bytes) const;
     int frame_info(sppm_frame_info* fi, cudaStream_t s) const;
     // checkpoint: header + JobState + every state array (flat binary, this build's layout)

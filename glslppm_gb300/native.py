@@ -182,6 +182,7 @@ SIGNATURES = {
     "sppm_batch_remove_job": (C.c_int, [P, C.c_uint32]),
     "sppm_batch_reset_job": (C.c_int, [P, C.c_uint32]),
     "sppm_batch_set_camera": (C.c_int, [P, C.c_uint32, C.POINTER(Camera)]),
+    "sppm_batch_set_cameras": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(Camera)]),
     "sppm_batch_run_passes": (C.c_int, [P, C.c_uint32]),
     "sppm_batch_time_passes": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_float)]),
     "sppm_batch_synchronize": (C.c_int, [P]),

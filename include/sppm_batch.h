@@ -57,6 +57,10 @@ int sppm_batch_add_job(sppm_batch* b, const sppm_config* cfg, const sppm_scene* 
 int sppm_batch_remove_job(sppm_batch* b, uint32_t job);
 int sppm_batch_reset_job(sppm_batch* b, uint32_t job);
 int sppm_batch_set_camera(sppm_batch* b, uint32_t job, const sppm_camera* cam);
+/* The same as sppm_batch_set_camera(b, jobs[i], &cams[i]) for i in [0, n), with the n descriptor
+   uploads queued as one launch (per 128 jobs) instead of n.  Every id is checked before any
+   camera changes: an unknown or repeated id fails the whole call with SPPM_ERR_ARG. */
+int sppm_batch_set_cameras(sppm_batch* b, uint32_t n, const uint32_t* jobs, const sppm_camera* cams);
 
 /* Queues n passes of every resident job. */
 int sppm_batch_run_passes(sppm_batch* b, uint32_t n);

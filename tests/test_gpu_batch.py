@@ -190,3 +190,39 @@ def test_textured_and_untextured_jobs_in_one_batch(tmp_path, precision):
         for k in KINDS:
             assert_same(b.read_state(j, k), r.read_state(k), f"job {j} {k}")
 
+
+
+def test_cameras_set_in_one_call_equal_one_by_one():
+    """sppm_batch_set_cameras between passes gives, bit for bit, what sppm_batch_set_camera per
+    job gives; a list with an unknown or repeated id fails whole and changes no camera."""
+    specs = small_jobs()
+    meshes = [s[0].to_mesh() for s in specs]
+
+    def moved(sc, w, h, step):
+        o = tuple(c + 0.01 * step * (i + 1) for i, c in enumerate(sc.camera_origin))
+        return g.look_at(o, sc.camera_lookat, w, h, sc.fov)
+
+    batches = []
+    for _ in range(2):
+        b = g.Batch(max_jobs=8)
+        ids = [b.add_job(config_for(w, h, pw, ph), m, camera_for(sc, w, h))
+               for (sc, w, h, pw, ph), m in zip(specs, meshes)]
+        batches.append((b, ids))
+    (a, ia), (c, ic) = batches
+    for step in range(1, 4):
+        cams = [moved(sc, w, h, step) for (sc, w, h, pw, ph) in specs]
+        a.set_cameras(ia, cams)
+        for j, cam in zip(ic, cams):
+            c.set_camera(j, cam)
+        a.run_passes(4)
+        c.run_passes(4)
+    bad = [moved(sc, w, h, 9) for (sc, w, h, pw, ph) in specs]
+    for ids in ([ia[0], 7, ia[2]], [ia[0], ia[1], ia[0]]):
+        with pytest.raises(N.SppmError) as e:
+            a.set_cameras(ids, bad)
+        assert e.value.status == N.ERR_ARG
+    a.run_passes(11)
+    c.run_passes(11)
+    for ja, jc in zip(ia, ic):
+        assert_same(a.read_image(ja), c.read_image(jc), f"job {ja} image")
+        assert_same(a.read_state(ja, "hit_position"), c.read_state(jc, "hit_position"), f"job {ja} hits")
