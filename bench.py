@@ -188,6 +188,15 @@ def make_renderer(device: int, precision: int = 0, eye_pass_interval: int = 10):
     return r, mesh, cfg, cam
 
 
+def autotune(ctx, args, cycles: int):
+    """The library's launch-shape autotuner (Renderer/Batch.autotune) on the job's first passes,
+    before the warm-up; the shapes chosen go into the line's config (None with --no-autotune)."""
+    if args.no_autotune:
+        return None
+    best, _ = ctx.autotune(cycles)
+    return best.as_dict()
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -281,8 +290,10 @@ def run_gpu(args, rank, world, local):
     P = cfg.photon_width * cfg.photon_height
     npix = cfg.width * cfg.height
     clocks = ClockSampler(dev).__enter__()
-    # warm-up passes (include at least one eye pass), then align to an eye-pass boundary so the
-    # timed region holds exactly one eye pass per 10 passes
+    # launch shapes chosen by the library's autotuner on the job's first passes (results do not
+    # depend on them), then the warm-up passes (at least one eye pass) and an alignment to an
+    # eye-pass boundary so the timed region holds exactly one eye pass per 10 passes
+    tuning = autotune(r, args, cycles=2)
     r.run_passes(W)
     fi0 = r.frame_info()
     L = args.eye_pass_interval
@@ -374,7 +385,7 @@ def run_gpu(args, rank, world, local):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(WORKLOAD, precision=args.precision, l2="working set > 129 MB L2 (no flush)",
                            eye_pass_every=args.eye_pass_interval,
-                           parallelism=f"replicas x{world}"),
+                           parallelism=f"replicas x{world}", tuning=tuning),
             "mrays_per_s": round(mrays, 3),
             "stage_ms_per_launch": {k: round(v[0] / v[1], 4) for k, v in stages.items() if v[1]},
             "stage_bandwidth": stage_bandwidth(stages, npix, P, (fi1.photon_segments - fi0.photon_segments) / K,
@@ -444,6 +455,7 @@ def run_batched(args, device: int, K: int, W: int, precision: int):
     b = g.Batch(precision=precision, max_jobs=len(jobs), device=device)
     ids = [b.add_job(cfg, m, cam) for (_, m, cfg, cam) in jobs]
     setup_s = time.perf_counter() - t_setup
+    tuning = autotune(b, args, cycles=1)
     b.run_passes(W)
     b.synchronize()
     f0 = [b.frame_info(j) for j in ids]
@@ -501,7 +513,7 @@ def run_batched(args, device: int, K: int, W: int, precision: int):
         "config": dict(BATCHED, precision="mixed" if precision == N.PRECISION_MIXED else "fp32",
                        triangles_total=int(sum(s.scene.num_triangles for (s, _, _, _) in jobs)),
                        photon_slots_per_pass=int(info.photon_slots), pixels=int(info.pixels),
-                       device_bytes=int(info.bytes_used)),
+                       device_bytes=int(info.bytes_used), tuning=tuning),
         "value": round(batched, 3), "unit": "Mphotons/s", "mrays_per_s": round(segs / (ms / 1000.0) / 1e6, 3),
         "steps": K, "warmup": W, "ms_per_step": round(ms / K, 4),
         "photon_trace_ms_per_launch": round(tr[0] / max(tr[1], 1), 4),
@@ -608,6 +620,7 @@ def run_large(args, world, local, K, W):
     t_up = time.perf_counter() - t2
     r.set_camera(cam)
     clocks = ClockSampler(local).__enter__()
+    tuning = autotune(r, args, cycles=1)
     r.run_passes(W)
     fi0 = r.frame_info()
     align = (10 - fi0.frames % 10) % 10
@@ -673,7 +686,8 @@ def run_large(args, world, local, K, W):
             "ms_per_step": round(1000.0 * t / K, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(LARGE, precision=args.precision, triangles_exact=sc.num_triangles,
-                           l2="BVH + triangles 2.2 GB > 129 MB L2 (no flush)", parallelism=f"replicas x{world}"),
+                           l2="BVH + triangles 2.2 GB > 129 MB L2 (no flush)", parallelism=f"replicas x{world}",
+                           tuning=tuning),
             "mrays_per_s": round(segs / t / 1e6, 3),
             "stage_ms_per_launch": {k: round(v[0] / v[1], 4) for k, v in stages.items() if v[1]},
             "setup_seconds": {"generate": round(t_gen, 2), "gpu_bvh_build": round(t_bvh, 3), "upload": round(t_up, 2)},
@@ -795,6 +809,8 @@ def main():
                          "value measures what the eye pass costs)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch shapes instead of autotuning them before the warm-up")
     ap.add_argument("--workload", default="cornell-1024", choices=["cornell-1024", "batched", "serving", "large"],
                     help="the JSON line's headline workload; the default line also carries the batched "
                          "workload's summary under 'batched' unless --no-batched")

@@ -6,9 +6,9 @@ ABI of ``include/sppm.h``); this package is its host-side mirror.  Importing the
 """
 from .native import NativeLibraryMissing, SppmError, device_count  # noqa: F401
 from .renderer import (Mesh, Renderer, default_config, look_at, pinned_empty, scene_from_arrays,  # noqa: F401
-                       write_image)
+                       tune_hash_slots, write_image)
 from . import native, scenes  # noqa: F401
 from .batch import Batch, Server  # noqa: F401
 
-__all__ = ["Batch", "Server", "Mesh", "Renderer", "default_config", "look_at", "pinned_empty", "scene_from_arrays", "write_image", "SppmError",
+__all__ = ["Batch", "Server", "Mesh", "Renderer", "default_config", "look_at", "pinned_empty", "scene_from_arrays", "tune_hash_slots", "write_image", "SppmError",
            "NativeLibraryMissing", "device_count", "native", "scenes"]

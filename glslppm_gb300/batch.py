@@ -72,6 +72,23 @@ class Batch:
         N.check(N.lib.sppm_batch_time_passes(self._h, n, C.byref(ms)))
         return float(ms.value)
 
+    def set_tuning(self, tuning=None, **fields) -> None:
+        """Launch shapes (sppm_tuning): an N.Tuning, or its fields by name (others 0 = default)."""
+        t = tuning if tuning is not None else N.Tuning(**fields)
+        N.check(N.lib.sppm_batch_set_tuning(self._h, C.byref(t)))
+
+    def get_tuning(self) -> N.Tuning:
+        t = N.Tuning()
+        N.check(N.lib.sppm_batch_get_tuning(self._h, C.byref(t)))
+        return t
+
+    def autotune(self, cycles: int = 1) -> tuple[N.Tuning, float]:
+        """Runs the next passes under candidate launch shapes and keeps the fastest; returns the
+        shapes chosen and their device time per pass (ms)."""
+        t, ms = N.Tuning(), C.c_float()
+        N.check(N.lib.sppm_batch_autotune(self._h, cycles, C.byref(t), C.byref(ms)))
+        return t, float(ms.value)
+
     def synchronize(self) -> None:
         N.check(N.lib.sppm_batch_synchronize(self._h))
         self._inflight.clear()

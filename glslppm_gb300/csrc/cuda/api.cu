@@ -223,6 +223,57 @@ int sppm_time_passes(sppm_ctx* c, uint32_t n, float* ms) {
     return c->rt.time(n, ms);
 }
 
+int sppm_set_tuning(sppm_ctx* c, const sppm_tuning* t) {
+    if (!c) return fail(SPPM_ERR_ARG, "null context");
+    return c->rt.set_tuning(t);
+}
+
+int sppm_get_tuning(sppm_ctx* c, sppm_tuning* t) {
+    if (!c || !t) return fail(SPPM_ERR_ARG, "null argument");
+    c->rt.get_tuning(t);
+    return SPPM_OK;
+}
+
+int sppm_autotune(sppm_ctx* c, uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
+    if (!c) return fail(SPPM_ERR_ARG, "null context");
+    if (!c->job.have_scene || !c->job.have_camera)
+        return fail(SPPM_ERR_STATE, "upload a scene and set a camera before tuning");
+    return c->rt.autotune(cycles, best, ms_per_pass);
+}
+
+int sppm_tune_hash_slots(const sppm_config* cfg, const sppm_scene* scene, const sppm_camera* cam, int device,
+                         uint32_t passes, uint32_t* hash_slots, float ms_out[3]) {
+    if (!cfg || !scene || !cam || !hash_slots || !passes) return fail(SPPM_ERR_ARG, "null argument or zero passes");
+    int st = validate_config(cfg);
+    if (st) return st;
+    const uint64_t P = (uint64_t)cfg->photon_width * cfg->photon_height;
+    float best = 0.0f;
+    for (uint32_t k = 0; k < 3; k++) {
+        const uint64_t slots = P << k;
+        if (slots > (1ull << 28)) {
+            if (ms_out) ms_out[k] = -1.0f;  // beyond the largest table a configuration may ask for
+            continue;
+        }
+        sppm_config c = *cfg;
+        c.hash_slots = (uint32_t)slots;
+        sppm_ctx* ctx = nullptr;
+        float ms = 0.0f;
+        if ((st = sppm_create(&c, device, &ctx)) || (st = sppm_upload_scene(ctx, scene)) ||
+            (st = sppm_set_camera(ctx, cam)) || (st = sppm_run_passes(ctx, passes)) ||
+            (st = sppm_time_passes(ctx, passes, &ms))) {
+            sppm_destroy(ctx);
+            return st;
+        }
+        sppm_destroy(ctx);
+        if (ms_out) ms_out[k] = ms / (float)passes;
+        if (k == 0 || ms < 0.99f * best) {
+            best = ms;
+            *hash_slots = (uint32_t)slots;
+        }
+    }
+    return SPPM_OK;
+}
+
 void sppm_destroy(sppm_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->rt.device);

@@ -207,6 +207,22 @@ int sppm_batch_run_passes(sppm_batch* b, uint32_t n) {
     return b->rt.run(n);
 }
 
+int sppm_batch_set_tuning(sppm_batch* b, const sppm_tuning* t) {
+    if (!b) return fail(SPPM_ERR_ARG, "null batch");
+    return b->rt.set_tuning(t);
+}
+
+int sppm_batch_get_tuning(sppm_batch* b, sppm_tuning* t) {
+    if (!b || !t) return fail(SPPM_ERR_ARG, "null argument");
+    b->rt.get_tuning(t);
+    return SPPM_OK;
+}
+
+int sppm_batch_autotune(sppm_batch* b, uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
+    if (!b) return fail(SPPM_ERR_ARG, "null batch");
+    return b->rt.autotune(cycles, best, ms_per_pass);
+}
+
 int sppm_batch_time_passes(sppm_batch* b, uint32_t n, float* ms) {
     if (!b || !ms) return fail(SPPM_ERR_ARG, "null argument");
     return b->rt.time(n, ms);

@@ -33,7 +33,8 @@ void launch_copy_descs(const DescCopy& list, cudaStream_t s);
 void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
 // mixed: 4-wide BVH traversal; textured: some job of the launch has texture coordinates (the
 // kernel variants with texture lookups)
-void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, bool textured, cudaStream_t s);
+// block: threads per block (a multiple of 32 up to the kernel's launch bound; 0 = the bound)
+void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, bool textured, uint32_t block, cudaStream_t s);
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s);
 void launch_photon_fp32(const LaunchSet& ls, bool count_traversal, bool textured, cudaStream_t s);
 void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, bool textured, cudaStream_t s);
@@ -41,16 +42,16 @@ void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool coun
                                uint32_t persistent_blocks, cudaStream_t s);
 void launch_ray_bins(const RayQueue& q, cudaStream_t s);
 void launch_trace_photons_coop(const LaunchSet& ls, const RayQueue& q, bool count_traversal, cudaStream_t s);
-void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
+void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, uint32_t block, cudaStream_t s);
 uint32_t trace_photons_blocks_per_sm();
 
 // mixed-precision path (kernels_mixed.cu)
 void launch_trace_photons4(const LaunchSet& ls, const RayQueue& q, uint32_t persistent_blocks, cudaStream_t s);
 uint32_t trace_photons4_blocks_per_sm();
 void launch_slot_fill(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
-void launch_gather_mixed(const LaunchSet& ls, cudaStream_t s);
+void launch_gather_mixed(const LaunchSet& ls, uint32_t block, cudaStream_t s);
 void launch_resolve_mixed(const LaunchSet& ls, uint32_t display, cudaStream_t s);
-void launch_gather_fp32(const LaunchSet& ls, cudaStream_t s);
+void launch_gather_fp32(const LaunchSet& ls, uint32_t block, cudaStream_t s);
 void launch_resolve_fp32(const LaunchSet& ls, uint32_t display, cudaStream_t s);
 void launch_hash_build(const float4* pos, const float4* flux, uint32_t pw, uint32_t ph, uint32_t hash_num,
                        const float bbmin[3], float grid_scale, uint32_t flags, uint32_t* winner, uint32_t* count,

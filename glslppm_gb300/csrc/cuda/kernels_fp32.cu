@@ -1402,6 +1402,7 @@ __global__ void __launch_bounds__(256) k_ray_bins_scatter(RayQueue q) {
 template <bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q) {
     const uint32_t total = q.counters[0];
+    const int refill = q.refill_steps ? (int)q.refill_steps : 32;
     const unsigned lane = threadIdx.x & 31;
     const uint32_t kNeed = 0xFFFFFFFFu, kDone = 0xFFFFFFFEu;
     uint32_t idx = kNeed;
@@ -1480,7 +1481,7 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
         if (idx >= kDone) continue;
         bool finished = false;
 #pragma unroll 1
-        for (int it = 0; it < 32; it++) {
+        for (int it = 0; it < refill; it++) {
             if (steps++ > nn) {
                 err |= kErrWatchdogTraverse;
                 finished = true;
@@ -1821,20 +1822,26 @@ void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) 
     const uint32_t n = q.bins && ls.total < kRayBins ? kRayBins : ls.total;
     if (ls.total) k_frame_begin<<<blocks_for(n, 256), 256, 0, s>>>(ls, q);
 }
+// block sizes: a multiple of 32 up to the kernel's launch bound (0 or anything else: the bound)
+static uint32_t block_or(uint32_t block, uint32_t bound) {
+    return block >= 32 && block <= bound && block % 32 == 0 ? block : bound;
+}
+
 template <bool TEX>
-static void launch_eye_t(const LaunchSet& ls, const RayQueue& q, bool mixed, cudaStream_t s) {
+static void launch_eye_t(const LaunchSet& ls, const RayQueue& q, bool mixed, uint32_t block, cudaStream_t s) {
+    const uint32_t b = block_or(block, 128);
     if (mixed) {
-        k_eye<true, TEX><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, nullptr, nullptr, 0);
+        k_eye<true, TEX><<<blocks_for(ls.total, b), b, 0, s>>>(ls, nullptr, nullptr, 0);
         return;
     }
-    k_eye<false, TEX><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q.counters + 3, q.eye_deferred, kEyeDeferred);
+    k_eye<false, TEX><<<blocks_for(ls.total, b), b, 0, s>>>(ls, q.counters + 3, q.eye_deferred, kEyeDeferred);
     // a fixed grid (the count is on the device): blocks beyond the deferred pixels exit at once
     k_eye_coop<TEX><<<32, kBlockWalk, 0, s>>>(ls, q.counters + 3, q.eye_deferred, kEyeDeferred);
 }
-void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, bool textured, cudaStream_t s) {
+void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, bool textured, uint32_t block, cudaStream_t s) {
     if (!ls.total) return;
-    if (textured) launch_eye_t<true>(ls, q, mixed, s);
-    else launch_eye_t<false>(ls, q, mixed, s);
+    if (textured) launch_eye_t<true>(ls, q, mixed, block, s);
+    else launch_eye_t<false>(ls, q, mixed, block, s);
 }
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s) {
     if (njobs) k_grid<<<blocks_for(njobs, 64), 64, 0, s>>>(jobs, job_ids, njobs);
@@ -1872,8 +1879,9 @@ void launch_trace_photons_coop(const LaunchSet& ls, const RayQueue& q, bool coun
     else k_trace_photons_coop<false><<<64, kBlockWalk, 0, s>>>(ls, q);
 }
 
-void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
-    if (ls.total) k_photon_store<<<blocks_for(q.capacity, 128), 128, 0, s>>>(ls, q);
+void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, uint32_t block, cudaStream_t s) {
+    const uint32_t b = block_or(block, 128);
+    if (ls.total) k_photon_store<<<blocks_for(q.capacity, b), b, 0, s>>>(ls, q);
 }
 
 uint32_t trace_photons_blocks_per_sm() {
@@ -1881,8 +1889,9 @@ uint32_t trace_photons_blocks_per_sm() {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_photons<false>, 128, 0) != cudaSuccess) n = 4;
     return n > 0 ? (uint32_t)n : 1u;
 }
-void launch_gather_fp32(const LaunchSet& ls, cudaStream_t s) {
-    if (ls.total) k_gather<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls);
+void launch_gather_fp32(const LaunchSet& ls, uint32_t block, cudaStream_t s) {
+    const uint32_t b = block_or(block, 256);
+    if (ls.total) k_gather<<<blocks_for(ls.total, b), b, 0, s>>>(ls);
 }
 void launch_resolve_fp32(const LaunchSet& ls, uint32_t display, cudaStream_t s) {
     if (ls.total) k_resolve<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls, display);

@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
         }
     };
     const uint32_t total = q.counters[0];
+    const int refill = q.refill_steps ? (int)q.refill_steps : 16;
     const unsigned lane = threadIdx.x & 31, tid = threadIdx.x;
     const uint32_t kNeed = 0xFFFFFFFFu, kDone = 0xFFFFFFFEu;
     uint32_t idx = kNeed;
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
         if (idx == kDone) continue;
         bool finished = false;
 #pragma unroll 1
-        for (int it = 0; it < 16 && !finished; it++) {
+        for (int it = 0; it < refill && !finished; it++) {
             if (++visits > (1u << 22)) {
                 err |= kErrWatchdogTraverse;
                 finished = true;
@@ -372,8 +373,9 @@ uint32_t trace_photons4_blocks_per_sm() {
 void launch_slot_fill(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
     if (q.capacity) k_slot_fill<<<blocks_for(q.capacity, 256), 256, 0, s>>>(ls, q);
 }
-void launch_gather_mixed(const LaunchSet& ls, cudaStream_t s) {
-    if (ls.total) k_gather_mixed<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls);
+void launch_gather_mixed(const LaunchSet& ls, uint32_t block, cudaStream_t s) {
+    const uint32_t b = block >= 32 && block <= 256 && block % 32 == 0 ? block : 256;
+    if (ls.total) k_gather_mixed<<<blocks_for(ls.total, b), b, 0, s>>>(ls);
 }
 void launch_resolve_mixed(const LaunchSet& ls, uint32_t display, cudaStream_t s) {
     if (ls.total) k_resolve_mixed<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls, display);

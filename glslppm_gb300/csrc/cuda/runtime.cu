@@ -734,10 +734,11 @@ int Runner::init(int dev, uint32_t prec, uint32_t fl, uint32_t interval, uint32_
     int st = desc_mem.reserve(Arena::align(sizeof(JobDesc) * std::max<uint32_t>(max_jobs, 1)));
     if (st) return st;
     d_jobs = desc_mem.take<JobDesc>(std::max<uint32_t>(max_jobs, 1));
-    int sms = 0;
-    SPPM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    trace_blocks = (uint32_t)sms * (precision == SPPM_PRECISION_MIXED ? trace_photons4_blocks_per_sm()
-                                                                      : trace_photons_blocks_per_sm());
+    int nsm = 0;
+    SPPM_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+    sms = (uint32_t)nsm;
+    trace_fit = precision == SPPM_PRECISION_MIXED ? trace_photons4_blocks_per_sm() : trace_photons_blocks_per_sm();
+    trace_blocks = sms * trace_fit;
     graphs.resize(eye_interval + 1);
     dirty = true;
     return SPPM_OK;
@@ -875,8 +876,17 @@ void Runner::timed(int stage, bool start, cudaStream_t s) {
 
 // the launches of one frame (m_display, glslppm.cpp:214-536) for every active job
 int Runner::enqueue_frame(uint32_t phase) {
+    // the queue as the launches see it: the tuned refill interval, and no bins when the rays are
+    // traced in queue order
+    RayQueue q = queue;
+    q.refill_steps = tune.trace_refill_steps;
+    if (tune.unbinned_rays) {
+        q.key = nullptr;
+        q.perm = nullptr;
+        q.bins = nullptr;
+    }
     timed(SPPM_STAGE_FRAME_BEGIN, true);
-    launch_frame_begin(hsh, queue, stream);
+    launch_frame_begin(hsh, q, stream);
     timed(SPPM_STAGE_FRAME_BEGIN, false);
     // the eye pass and the grid it sets run beside the photon generation and traversal (which do
     // not read them); the photon store (hash insertion) waits for the grid
@@ -885,7 +895,7 @@ int Runner::enqueue_frame(uint32_t phase) {
         SPPM_CK(cudaEventRecord(fork_ev, stream));
         SPPM_CK(cudaStreamWaitEvent(side, fork_ev, 0));
         timed(SPPM_STAGE_EYE, true, side);
-        launch_eye(eye_pix[phase], queue, precision == SPPM_PRECISION_MIXED, textured, side);
+        launch_eye(eye_pix[phase], q, precision == SPPM_PRECISION_MIXED, textured, tune.eye_block, side);
         timed(SPPM_STAGE_EYE, false, side);
         timed(SPPM_STAGE_GRID, true, side);
         launch_grid(d_jobs, eye_ids[phase], eye_pix[phase].njobs, side);
@@ -900,26 +910,26 @@ int Runner::enqueue_frame(uint32_t phase) {
         timed(SPPM_STAGE_PHOTON, false);
     } else {
         timed(SPPM_STAGE_PHOTON, true);
-        launch_photon_gen_fp32(pho, queue, textured, stream);
+        launch_photon_gen_fp32(pho, q, textured, stream);
         timed(SPPM_STAGE_PHOTON, false);
-        if (queue.key) {
+        if (q.key) {
             timed(SPPM_STAGE_RAY_BINS, true);
-            launch_ray_bins(queue, stream);
+            launch_ray_bins(q, stream);
             timed(SPPM_STAGE_RAY_BINS, false);
         }
         timed(SPPM_STAGE_PHOTON_TRACE, true);
-        if (mixed) launch_trace_photons4(pho, queue, trace_blocks, stream);
-        else launch_trace_photons_fp32(pho, queue, count_traversal, trace_blocks, stream);
+        if (mixed) launch_trace_photons4(pho, q, trace_blocks, stream);
+        else launch_trace_photons_fp32(pho, q, count_traversal, trace_blocks, stream);
         timed(SPPM_STAGE_PHOTON_TRACE, false);
         if (eye) SPPM_CK(cudaStreamWaitEvent(stream, join_ev, 0));
         timed(SPPM_STAGE_PHOTON_STORE, true);
-        launch_photon_store_fp32(pho, queue, stream);
-        if (mixed) launch_slot_fill(pho, queue, stream);
+        launch_photon_store_fp32(pho, q, tune.store_block, stream);
+        if (mixed) launch_slot_fill(pho, q, stream);
         timed(SPPM_STAGE_PHOTON_STORE, false);
     }
     timed(SPPM_STAGE_GATHER, true);
-    if (mixed) launch_gather_mixed(pix, stream);
-    else launch_gather_fp32(pix, stream);
+    if (mixed) launch_gather_mixed(pix, tune.gather_block, stream);
+    else launch_gather_fp32(pix, tune.gather_block, stream);
     timed(SPPM_STAGE_GATHER, false);
     return launch_check("SPPM frame");
 }
@@ -1029,6 +1039,84 @@ int Runner::time(uint32_t n, float* ms) {
     event_pool.push_back(a);
     event_pool.push_back(b);
     return synchronize();
+}
+
+static bool block_ok(uint32_t b, uint32_t bound) { return b == 0 || (b >= 32 && b <= bound && b % 32 == 0); }
+
+int Runner::set_tuning(const sppm_tuning* t) {
+    if (!t) return fail(SPPM_ERR_ARG, "null tuning");
+    if (t->trace_blocks_per_sm > trace_fit)
+        return fail(SPPM_ERR_ARG, "trace_blocks_per_sm %u: at most %u traversal blocks fit on an SM",
+                    t->trace_blocks_per_sm, trace_fit);
+    if (t->trace_refill_steps > 4096) return fail(SPPM_ERR_ARG, "trace_refill_steps %u > 4096", t->trace_refill_steps);
+    if (!block_ok(t->eye_block, 128) || !block_ok(t->store_block, 128) || !block_ok(t->gather_block, 256))
+        return fail(SPPM_ERR_ARG, "block sizes are 0 or multiples of 32 up to 128 (eye, store) and 256 (gather)");
+    if (t->unbinned_rays > 1) return fail(SPPM_ERR_ARG, "unbinned_rays is 0 or 1");
+    SPPM_CK(cudaSetDevice(device));
+    SPPM_CK(cudaStreamSynchronize(stream));
+    tune = *t;
+    trace_blocks = sms * (tune.trace_blocks_per_sm ? tune.trace_blocks_per_sm : trace_fit);
+    drop_graphs();
+    return SPPM_OK;
+}
+
+void Runner::get_tuning(sppm_tuning* t) const {
+    *t = tune;
+    if (!t->trace_blocks_per_sm) t->trace_blocks_per_sm = trace_fit;
+    if (!t->trace_refill_steps) t->trace_refill_steps = precision == SPPM_PRECISION_MIXED ? 16u : 32u;
+    if (!t->eye_block) t->eye_block = 128;
+    if (!t->store_block) t->store_block = 128;
+    if (!t->gather_block) t->gather_block = 256;
+    if (flags & SPPM_FLAG_UNBINNED_RAYS) t->unbinned_rays = 1;  // created without ray bins
+}
+
+int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
+    if (!cycles) return fail(SPPM_ERR_ARG, "autotune needs at least one eye-pass cycle per candidate");
+    int st;
+    SPPM_CK(cudaSetDevice(device));
+    if (dirty && (st = rebuild())) return st;
+    if (active.empty()) return fail(SPPM_ERR_STATE, "no job to tune on");
+    // a window of whole eye-pass cycles holds every phase equally often, wherever it starts
+    const uint32_t L = eye_interval, window = cycles * L;
+    sppm_tuning cur;
+    get_tuning(&cur);
+    auto measure = [&](const sppm_tuning& t, float* ms) -> int {
+        int e = set_tuning(&t);
+        if (e) return e;
+        if ((e = run(L))) return e;  // captures the graphs untimed
+        return time(window, ms);
+    };
+    float cur_ms = 0.0f;
+    if ((st = measure(cur, &cur_ms))) return st;
+    // one sweep of coordinate descent; a candidate must beat the current shapes by 1 %
+    auto knob = [&](uint32_t sppm_tuning::*field, std::vector<uint32_t> values) -> int {
+        for (uint32_t v : values) {
+            if (v == cur.*field) continue;
+            sppm_tuning t = cur;
+            t.*field = v;
+            float ms = 0.0f;
+            const int e = measure(t, &ms);
+            if (e) return e;
+            if (ms < 0.99f * cur_ms) {
+                cur = t;
+                cur_ms = ms;
+            }
+        }
+        return SPPM_OK;
+    };
+    std::vector<uint32_t> blocks;
+    for (uint32_t b : {trace_fit, (3 * trace_fit + 3) / 4, (trace_fit + 1) / 2})
+        if (b >= 1 && std::find(blocks.begin(), blocks.end(), b) == blocks.end()) blocks.push_back(b);
+    if ((st = knob(&sppm_tuning::trace_blocks_per_sm, blocks))) return st;
+    if ((st = knob(&sppm_tuning::trace_refill_steps, {8u, 16u, 32u, 64u}))) return st;
+    if (queue.key && (st = knob(&sppm_tuning::unbinned_rays, {0u, 1u}))) return st;
+    if ((st = knob(&sppm_tuning::gather_block, {256u, 128u, 64u}))) return st;
+    if ((st = knob(&sppm_tuning::store_block, {128u, 64u}))) return st;
+    if ((st = knob(&sppm_tuning::eye_block, {128u, 64u}))) return st;
+    if ((st = set_tuning(&cur))) return st;
+    if (best) *best = cur;
+    if (ms_per_pass) *ms_per_pass = cur_ms / (float)window;
+    return SPPM_OK;
 }
 
 int Runner::read_stage_times(float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]) {

@@ -176,6 +176,8 @@ struct Runner {
     uint64_t frames = 0;                     // frames queued
     uint64_t kernel_launches = 0;
     uint32_t trace_blocks = 0;
+    uint32_t sms = 0, trace_fit = 0;  // SMs; traversal blocks of 128 threads that fit on one SM
+    sppm_tuning tune{};               // launch shapes (zero fields: the defaults)
     bool dirty = true;
     // stage timing
     uint32_t timing_mask = 0;  // bit k: time stage k
@@ -201,6 +203,13 @@ struct Runner {
     int run(uint32_t n);           // queue n frames of every active job
     int synchronize();             // waits and reports device-side watchdog errors of every job
     int time(uint32_t n, float* ms);
+    // launch shapes: checked, then every frame graph is captured again with them (results do not
+    // depend on them); get_tuning reports the shapes in effect
+    int set_tuning(const sppm_tuning* t);
+    void get_tuning(sppm_tuning* t) const;
+    // times the next passes under candidate shapes (coordinate descent, each candidate over
+    // `cycles` eye-pass cycles after one untimed cycle) and keeps the fastest
+    int autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass);
     int read_stage_times(float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]);
     int resolve(Job& j, uint32_t kind);
     // resolve + copy of the image into host memory without waiting; *ticket names the copy

@@ -123,6 +123,14 @@ class ServerStats(C.Structure):
                 ("photons", C.c_uint64), ("busy_seconds", C.c_double)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("trace_refill_steps", C.c_uint32), ("eye_block", C.c_uint32),
+                ("store_block", C.c_uint32), ("gather_block", C.c_uint32), ("unbinned_rays", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+
 REQUEST_QUEUED, REQUEST_RUNNING, REQUEST_DONE, REQUEST_FAILED = 0, 1, 2, 3
 
 
@@ -160,6 +168,11 @@ SIGNATURES = {
     "sppm_enable_traversal_counters": (C.c_int, [P, C.c_int]),
     "sppm_read_stage_times": (C.c_int, [P, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     "sppm_time_passes": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_float)]),
+    "sppm_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "sppm_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "sppm_autotune": (C.c_int, [P, C.c_uint32, C.POINTER(Tuning), C.POINTER(C.c_float)]),
+    "sppm_tune_hash_slots": (C.c_int, [C.POINTER(Config), C.POINTER(Scene), C.POINTER(Camera), C.c_int, C.c_uint32,
+                                       C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
     "sppm_destroy": (None, [P]),
     "sppm_hash_build": (C.c_int, [P, P, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), C.c_float,
                                   C.c_uint32, P, P, P]),
@@ -184,6 +197,9 @@ SIGNATURES = {
     "sppm_batch_set_camera": (C.c_int, [P, C.c_uint32, C.POINTER(Camera)]),
     "sppm_batch_set_cameras": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(Camera)]),
     "sppm_batch_run_passes": (C.c_int, [P, C.c_uint32]),
+    "sppm_batch_set_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "sppm_batch_get_tuning": (C.c_int, [P, C.POINTER(Tuning)]),
+    "sppm_batch_autotune": (C.c_int, [P, C.c_uint32, C.POINTER(Tuning), C.POINTER(C.c_float)]),
     "sppm_batch_time_passes": (C.c_int, [P, C.c_uint32, C.POINTER(C.c_float)]),
     "sppm_batch_synchronize": (C.c_int, [P]),
     "sppm_batch_read_image": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.c_size_t]),

@@ -365,6 +365,23 @@ class Renderer:
         N.check(N.lib.sppm_time_passes(self._h, n, C.byref(ms)))
         return float(ms.value)
 
+    def set_tuning(self, tuning=None, **fields) -> None:
+        """Launch shapes (sppm_tuning): an N.Tuning, or its fields by name (others 0 = default)."""
+        t = tuning if tuning is not None else N.Tuning(**fields)
+        N.check(N.lib.sppm_set_tuning(self._h, C.byref(t)))
+
+    def get_tuning(self) -> N.Tuning:
+        t = N.Tuning()
+        N.check(N.lib.sppm_get_tuning(self._h, C.byref(t)))
+        return t
+
+    def autotune(self, cycles: int = 1) -> tuple[N.Tuning, float]:
+        """Runs the next passes under candidate launch shapes and keeps the fastest; returns the
+        shapes chosen and their device time per pass (ms)."""
+        t, ms = N.Tuning(), C.c_float()
+        N.check(N.lib.sppm_autotune(self._h, cycles, C.byref(t), C.byref(ms)))
+        return t, float(ms.value)
+
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
             N.lib.sppm_destroy(self._h)
@@ -392,6 +409,21 @@ def hash_build(d_pos: int, d_flux: int, photon_width: int, photon_height: int, h
 
 
 REDUCE_MIN, REDUCE_MAX, REDUCE_SUM = 0, 1, 2
+
+
+def tune_hash_slots(cfg: N.Config, scene, camera: N.Camera, passes: int = 20, device: int = 0) -> tuple[int, list]:
+    """The hash-table size by measurement (sppm_tune_hash_slots): hash_slots of P, 2P and 4P
+    photon slots timed in scratch contexts; returns the fastest and the three times per pass (ms;
+    -1 for a size that was not a candidate)."""
+    if isinstance(scene, Mesh):
+        scene = scene.scene()
+    elif isinstance(scene, SceneArrays):
+        keep = scene
+        scene = scene_from_arrays(keep)
+    slots, ms = C.c_uint32(), (C.c_float * 3)()
+    N.check(N.lib.sppm_tune_hash_slots(C.byref(cfg), C.byref(scene), C.byref(camera), device, passes,
+                                       C.byref(slots), ms))
+    return int(slots.value), [float(x) for x in ms]
 
 
 def reduce_texture(d_texture: int, resolution: int, op: int, stream: int = 0) -> np.ndarray:

@@ -306,6 +306,39 @@ int sppm_read_stage_times(sppm_ctx* ctx, float ms[SPPM_STAGE_COUNT], uint32_t la
 /* Device time (ms) of `n` frames measured with CUDA events on the context's stream. */
 int sppm_time_passes(sppm_ctx* ctx, uint32_t n, float* ms);
 
+/* ---- launch shapes and their autotuner ------------------------------------------------------
+   No counterpart in the reference (its shader passes are fixed draw calls).  The shapes change
+   how a pass is launched, never what it computes: images and state are the same bit for bit under
+   every tuning. */
+typedef struct sppm_tuning {
+    uint32_t trace_blocks_per_sm; /* resident blocks of the persistent photon traversal per SM
+                                     (0 = as many as fit)                                       */
+    uint32_t trace_refill_steps;  /* traversal steps a warp takes before it refills its idle
+                                     lanes from the ray queue (0 = 32; 4-wide traversal 16)     */
+    uint32_t eye_block;           /* threads per block of the eye pass (0 = 128; 32..128)       */
+    uint32_t store_block;         /* of the photon store + hash insertion (0 = 128; 32..128)    */
+    uint32_t gather_block;        /* of the gather + progressive update (0 = 256; 32..256)      */
+    uint32_t unbinned_rays;       /* 1: photon rays traced in queue order instead of binned     */
+} sppm_tuning;
+/* Block sizes are multiples of 32.  The frame graphs are captured again with the new shapes. */
+int sppm_set_tuning(sppm_ctx* ctx, const sppm_tuning* tuning);
+/* The shapes in effect (defaults filled in). */
+int sppm_get_tuning(sppm_ctx* ctx, sppm_tuning* tuning);
+/* Runs the context's next passes under candidate shapes and leaves the fastest in effect: one
+   sweep of coordinate descent over the fields above, each candidate run for one untimed and
+   `cycles` timed eye-pass cycles (eye_pass_interval passes each), a candidate kept when it is at
+   least 1 % faster than the best so far.  These are ordinary passes of the job (its frame count
+   advances).  *best and *ms_per_pass (either may be NULL) receive the chosen shapes and their
+   time per pass. */
+int sppm_autotune(sppm_ctx* ctx, uint32_t cycles, sppm_tuning* best, float* ms_per_pass);
+/* The hash-table size (hash load factor) by measurement: scratch contexts of this configuration,
+   scene and camera with hash_slots = P, 2P and 4P (P = photon slots; load factors 1, 1/2, 1/4)
+   each run `passes` untimed and `passes` timed passes; *hash_slots receives the fastest and
+   ms_per_pass (may be NULL) the three times (-1 for a size above the 2^28-slot limit).  A table larger than P makes fewer grid cells share a
+   slot, which changes the image: this is a configuration value chosen before a job starts. */
+int sppm_tune_hash_slots(const sppm_config* cfg, const sppm_scene* scene, const sppm_camera* cam, int device,
+                         uint32_t passes, uint32_t* hash_slots, float ms_per_pass[3]);
+
 void sppm_destroy(sppm_ctx* ctx);
 
 /* ---- stage-level entry points (device pointers) --------------------------------------------- */

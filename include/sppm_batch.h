@@ -64,6 +64,11 @@ int sppm_batch_set_cameras(sppm_batch* b, uint32_t n, const uint32_t* jobs, cons
 
 /* Queues n passes of every resident job. */
 int sppm_batch_run_passes(sppm_batch* b, uint32_t n);
+/* Launch shapes of the batch's passes (sppm_tuning in sppm.h; one set for all jobs) and their
+   autotuner, which runs the batch's next passes as sppm_autotune does a context's. */
+int sppm_batch_set_tuning(sppm_batch* b, const sppm_tuning* tuning);
+int sppm_batch_get_tuning(sppm_batch* b, sppm_tuning* tuning);
+int sppm_batch_autotune(sppm_batch* b, uint32_t cycles, sppm_tuning* best, float* ms_per_pass);
 int sppm_batch_time_passes(sppm_batch* b, uint32_t n, float* ms);
 int sppm_batch_synchronize(sppm_batch* b);
 

@@ -48,7 +48,7 @@ def test_struct_layouts_match_the_header(native_lib, tmp_path):
     structs = {"sppm_config": N.Config, "sppm_material": N.Material, "sppm_scene": N.Scene,
                "sppm_camera": N.Camera, "sppm_frame_info": N.FrameInfo, "sppm_batch_config": N.BatchConfig,
                "sppm_batch_info": N.BatchInfo, "sppm_server_config": N.ServerConfig,
-               "sppm_request_info": N.RequestInfo, "sppm_server_stats": N.ServerStats}
+               "sppm_request_info": N.RequestInfo, "sppm_server_stats": N.ServerStats, "sppm_tuning": N.Tuning}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sppm.h"', '#include "sppm_batch.h"',
              '#include "sppm_server.h"', "int main(void) {"]
     for cname, cls in structs.items():
