@@ -398,9 +398,11 @@ def run_gpu(args, rank, world, local):
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
         }
+    batch_tuning = None
     if not args.no_batched:
         prec = N.PRECISION_MIXED if args.precision == "mixed" else N.PRECISION_FP32
         res = run_batched(args, dev, args.batch_steps, W, prec)
+        batch_tuning = res["config"]["tuning"]
         if rank == 0:
             out["batched"] = {k: v for k, v in res.items() if not k.startswith("_")}
     if not args.no_large:
@@ -409,11 +411,12 @@ def run_gpu(args, rank, world, local):
             out["large"] = {k: ln[k] for k in ("value", "unit", "steps", "ms_per_step", "mrays_per_s", "config",
                                                 "stage_ms_per_launch", "setup_seconds", "e2e", "roofline")}
     if not args.no_serving:
-        rows = run_serving(args, dev)
+        rows = run_serving(args, dev, batch_tuning)
         if rank == 0:
             out["serving"] = {"config": dict(SERVING, precision=args.precision, rates=args.serve_rates,
                                              requests_per_rate=args.serve_requests,
-                                             passes_per_request=args.serve_passes), "by_rate": rows}
+                                             passes_per_request=args.serve_passes, tuning=batch_tuning),
+                              "by_rate": rows}
     if rank == 0:
         print(json.dumps(out), flush=True)
     return out
@@ -538,7 +541,7 @@ SERVING = {"workload": "serving-poisson", "scene_pool": "seeded Cornell variants
            "memory_budget_gb": 180, "eye_pass_every": 10}
 
 
-def run_serving(args, device: int):
+def run_serving(args, device: int, tuning: dict | None = None):
     """Poisson arrivals of render requests into the continuous-batching server; per arrival rate,
     p50/p99 time to target and aggregate Mphotons/s."""
     import glslppm_gb300 as g
@@ -549,7 +552,10 @@ def run_serving(args, device: int):
     rates = [float(x) for x in args.serve_rates.split(",")]
     out = []
     for lam in rates:
-        srv = g.Server(precision=prec, max_jobs=256, memory_budget=180 << 30, passes_per_step=1, device=device)
+        # launch shapes: those the batched workload's autotuner chose (same scene distribution), else
+        # the defaults
+        srv = g.Server(precision=prec, max_jobs=256, memory_budget=180 << 30, passes_per_step=1, device=device,
+                       tuning=tuning)
         n = args.serve_requests
         gaps = rng.exponential(1.0 / lam, n)
         reqs = []

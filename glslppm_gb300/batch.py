@@ -208,12 +208,14 @@ class Server:
 
     def __init__(self, precision: int = N.PRECISION_FP32, flags: int = 0, eye_pass_interval: int = 10,
                  max_jobs: int = 256, memory_budget: int = 0, passes_per_step: int = 1, max_queue: int = 4096,
-                 device: int = 0):
+                 device: int = 0, tuning: dict | None = None):
         cfg = N.ServerConfig()
         N.lib.sppm_server_config_defaults(C.byref(cfg))
         cfg.batch.precision, cfg.batch.flags, cfg.batch.eye_pass_interval = precision, flags, eye_pass_interval
         cfg.batch.max_jobs, cfg.batch.memory_budget = max_jobs, memory_budget
         cfg.passes_per_step, cfg.max_queue = passes_per_step, max_queue
+        if tuning:  # launch shapes of the server's batch, e.g. those Batch.autotune chose
+            cfg.tuning = N.Tuning(**tuning)
         out = C.c_void_p()
         N.check(N.lib.sppm_server_create(C.byref(cfg), device, C.byref(out)))
         self._h = out

@@ -1088,7 +1088,9 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
     };
     float cur_ms = 0.0f;
     if ((st = measure(cur, &cur_ms))) return st;
-    // one sweep of coordinate descent; a candidate must beat the current shapes by 1 %
+    // coordinate descent, the knob with the largest effect (ray order) first; a candidate must
+    // beat the best shapes so far by 1 %; a second sweep when the first changed anything
+    bool changed = false;
     auto knob = [&](uint32_t sppm_tuning::*field, std::vector<uint32_t> values) -> int {
         for (uint32_t v : values) {
             if (v == cur.*field) continue;
@@ -1100,6 +1102,7 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
             if (ms < 0.99f * cur_ms) {
                 cur = t;
                 cur_ms = ms;
+                changed = true;
             }
         }
         return SPPM_OK;
@@ -1107,12 +1110,16 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
     std::vector<uint32_t> blocks;
     for (uint32_t b : {trace_fit, (3 * trace_fit + 3) / 4, (trace_fit + 1) / 2})
         if (b >= 1 && std::find(blocks.begin(), blocks.end(), b) == blocks.end()) blocks.push_back(b);
-    if ((st = knob(&sppm_tuning::trace_blocks_per_sm, blocks))) return st;
-    if ((st = knob(&sppm_tuning::trace_refill_steps, {8u, 16u, 32u, 64u}))) return st;
-    if (queue.key && (st = knob(&sppm_tuning::unbinned_rays, {0u, 1u}))) return st;
-    if ((st = knob(&sppm_tuning::gather_block, {256u, 128u, 64u}))) return st;
-    if ((st = knob(&sppm_tuning::store_block, {128u, 64u}))) return st;
-    if ((st = knob(&sppm_tuning::eye_block, {128u, 64u}))) return st;
+    for (int sweep = 0; sweep < 2; sweep++) {
+        changed = false;
+        if (queue.key && (st = knob(&sppm_tuning::unbinned_rays, {0u, 1u}))) return st;
+        if ((st = knob(&sppm_tuning::trace_refill_steps, {8u, 16u, 32u, 64u}))) return st;
+        if ((st = knob(&sppm_tuning::trace_blocks_per_sm, blocks))) return st;
+        if ((st = knob(&sppm_tuning::gather_block, {256u, 128u, 64u}))) return st;
+        if ((st = knob(&sppm_tuning::store_block, {128u, 64u}))) return st;
+        if ((st = knob(&sppm_tuning::eye_block, {128u, 64u}))) return st;
+        if (!changed) break;
+    }
     if ((st = set_tuning(&cur))) return st;
     if (best) *best = cur;
     if (ms_per_pass) *ms_per_pass = cur_ms / (float)window;

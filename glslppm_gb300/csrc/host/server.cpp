@@ -227,6 +227,10 @@ int sppm_server_create(const sppm_server_config* cfg, int device, sppm_server** 
     s->cfg = *cfg;
     int st = sppm_batch_create(&cfg->batch, device, &s->batch);
     if (st) return st;
+    if ((st = sppm_batch_set_tuning(s->batch, &cfg->tuning))) {
+        sppm_batch_destroy(s->batch);
+        return st;
+    }
     sppm_batch_info bi;
     sppm_batch_get_info(s->batch, &bi);
     s->budget = bi.memory_budget;

@@ -105,8 +105,17 @@ class BatchInfo(C.Structure):
                 ("photon_slots", C.c_uint64), ("pixels", C.c_uint64)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("trace_refill_steps", C.c_uint32), ("eye_block", C.c_uint32),
+                ("store_block", C.c_uint32), ("gather_block", C.c_uint32), ("unbinned_rays", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+
 class ServerConfig(C.Structure):
-    _fields_ = [("batch", BatchConfig), ("passes_per_step", C.c_uint32), ("max_queue", C.c_uint32)]
+    _fields_ = [("batch", BatchConfig), ("passes_per_step", C.c_uint32), ("max_queue", C.c_uint32),
+                ("tuning", Tuning)]
 
 
 class RequestInfo(C.Structure):
@@ -121,14 +130,6 @@ class ServerStats(C.Structure):
                 ("failed", C.c_uint64), ("resident", C.c_uint32), ("queued", C.c_uint32),
                 ("bytes_used", C.c_uint64), ("memory_budget", C.c_uint64), ("passes", C.c_uint64),
                 ("photons", C.c_uint64), ("busy_seconds", C.c_double)]
-
-
-class Tuning(C.Structure):
-    _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("trace_refill_steps", C.c_uint32), ("eye_block", C.c_uint32),
-                ("store_block", C.c_uint32), ("gather_block", C.c_uint32), ("unbinned_rays", C.c_uint32)]
-
-    def as_dict(self) -> dict:
-        return {name: int(getattr(self, name)) for name, _ in self._fields_}
 
 
 REQUEST_QUEUED, REQUEST_RUNNING, REQUEST_DONE, REQUEST_FAILED = 0, 1, 2, 3

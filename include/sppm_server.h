@@ -33,6 +33,7 @@ typedef struct sppm_server_config {
     sppm_batch_config batch;   /* precision, flags, eye-pass interval, job slots, memory budget */
     uint32_t passes_per_step;  /* passes queued between admission/retirement rounds (>= 1)     */
     uint32_t max_queue;        /* requests waiting for admission before submit refuses         */
+    sppm_tuning tuning;        /* launch shapes of the server's batch (sppm.h; zeros: defaults) */
 } sppm_server_config;
 
 typedef struct sppm_request_info {

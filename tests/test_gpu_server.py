@@ -98,3 +98,20 @@ def test_submit_from_many_threads_and_poll():
         assert info.state == N.REQUEST_DONE and srv.poll(t).passes_done == passes
         assert np.array_equal(srv.fetch_image(t), alone(cfg, mesh, cam, passes))
     srv.close()
+
+
+def test_server_launch_shapes_keep_results():
+    """A server created with non-default launch shapes (sppm_server_config.tuning) renders every
+    request as a single default context does; an invalid shape fails the creation."""
+    reqs = requests()[:3]
+    srv = g.Server(max_jobs=2, passes_per_step=3,
+                   tuning=dict(unbinned_rays=1, trace_refill_steps=8, gather_block=64, store_block=64))
+    tickets = [srv.submit(cfg, mesh, cam, passes) for (cfg, mesh, cam, passes) in reqs]
+    for t, (cfg, mesh, cam, passes) in zip(tickets, reqs):
+        assert srv.wait(t, timeout=120).state == N.REQUEST_DONE
+        img = srv.fetch_image(t)
+        assert np.array_equal(img.view(np.uint32), alone(cfg, mesh, cam, passes).view(np.uint32)), f"ticket {t}"
+    srv.close()
+    with pytest.raises(N.SppmError) as e:
+        g.Server(max_jobs=2, tuning=dict(gather_block=40))
+    assert e.value.status == N.ERR_ARG
