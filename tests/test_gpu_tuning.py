@@ -144,3 +144,52 @@ def test_hash_slots_tuner(cornell_c1_mesh):
     r.set_camera(cam)
     r.run_passes(3)
     assert r.read_state("slot_count").size == slots
+
+
+def _flat_camera(sc, w, h):
+    """Every primary ray has an exact zero x component (the eye pass defers such pixels)."""
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, w, h, sc.fov)
+    cam.u[0], cam.u[1], cam.u[2] = 0.0, 0.0, -0.5
+    cam.v[0], cam.v[1], cam.v[2] = 0.0, 1.0, 0.0
+    cam.w[0], cam.w[1], cam.w[2] = 0.0, 0.0, -1.0
+    return cam
+
+
+def _pair(cfg, scene, cam, tuning, passes=23):
+    out = []
+    for t in (None, tuning):
+        r = g.Renderer(cfg)
+        r.upload_scene(scene)
+        r.set_camera(cam)
+        if t:
+            r.set_tuning(**t)
+        r.run_passes(passes)
+        out.append(_state(r, cfg.precision))
+        r.close()
+    _same(out[0], out[1], str(tuning))
+
+
+@pytest.mark.parametrize("case", ["textured", "deferred_eye", "environment"])
+def test_tuning_on_textured_deferred_and_environment_paths(tmp_path, cornell_c1_mesh, case):
+    """The kernel variants with texture lookups, the eye pass's deferred-pixel list (80x64 pixels
+    with zero direction components: more than the list holds) and photons from the environment,
+    each under non-default shapes, against a default context."""
+    tuning = dict(eye_block=32, store_block=64, gather_block=96, trace_refill_steps=5, unbinned_rays=1,
+                  trace_blocks_per_sm=1)
+    if case == "textured":
+        sc = scenes.textured_box()
+        scene = g.Mesh.load_obj(str(sc.write_obj(tmp_path / "t.obj"))).build_bvh()
+        w, h = 40, 32
+        cam = g.look_at(sc.camera_origin, sc.camera_lookat, w, h, sc.fov)
+    elif case == "deferred_eye":
+        sc, scene = cornell_c1_mesh
+        w, h = 80, 64
+        cam = _flat_camera(sc, w, h)
+    else:
+        sc = scenes.materials_box(light=False)
+        scene = sc.to_mesh()
+        w, h = 40, 32
+        cam = g.look_at(sc.camera_origin, sc.camera_lookat, w, h, sc.fov)
+    cfg = g.default_config(w, height=h, photon_width=64, photon_height=32, radius_rule=N.RADIUS_DIAGONAL,
+                           radius_fraction=0.01)
+    _pair(cfg, scene, cam, tuning)
