@@ -162,7 +162,7 @@ struct RayQueue {
     uint32_t* perm;       // [capacity] queue index of the i-th ray in bin order
     uint32_t* eye_deferred;  // [kEyeDeferred] launch indices of the deferred eye pixels
     uint32_t refill_steps;   // traversal steps a warp takes between refills of its idle lanes
-                             // (0: 32 for the exact walk, 16 for the 4-wide one)
+                             // (0: 32 for the exact walk, 8 for the 4-wide one)
 };
 
 // the work of one launch: items [prefix[k], prefix[k+1]) belong to jobs[job_ids[k]]

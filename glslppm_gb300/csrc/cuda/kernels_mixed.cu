@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
         }
     };
     const uint32_t total = q.counters[0];
-    const int refill = q.refill_steps ? (int)q.refill_steps : 16;
+    const int refill = q.refill_steps ? (int)q.refill_steps : 8;
     const unsigned lane = threadIdx.x & 31, tid = threadIdx.x;
     const uint32_t kNeed = 0xFFFFFFFFu, kDone = 0xFFFFFFFEu;
     uint32_t idx = kNeed;

@@ -1063,7 +1063,7 @@ int Runner::set_tuning(const sppm_tuning* t) {
 void Runner::get_tuning(sppm_tuning* t) const {
     *t = tune;
     if (!t->trace_blocks_per_sm) t->trace_blocks_per_sm = trace_fit;
-    if (!t->trace_refill_steps) t->trace_refill_steps = precision == SPPM_PRECISION_MIXED ? 16u : 32u;
+    if (!t->trace_refill_steps) t->trace_refill_steps = precision == SPPM_PRECISION_MIXED ? 8u : 32u;
     if (!t->eye_block) t->eye_block = 128;
     if (!t->store_block) t->store_block = 128;
     if (!t->gather_block) t->gather_block = 256;
@@ -1113,7 +1113,7 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
     for (int sweep = 0; sweep < 2; sweep++) {
         changed = false;
         if (queue.key && (st = knob(&sppm_tuning::unbinned_rays, {0u, 1u}))) return st;
-        if ((st = knob(&sppm_tuning::trace_refill_steps, {8u, 16u, 32u, 64u}))) return st;
+        if ((st = knob(&sppm_tuning::trace_refill_steps, {4u, 8u, 16u, 32u, 64u}))) return st;
         if ((st = knob(&sppm_tuning::trace_blocks_per_sm, blocks))) return st;
         if ((st = knob(&sppm_tuning::gather_block, {256u, 128u, 64u}))) return st;
         if ((st = knob(&sppm_tuning::store_block, {128u, 64u}))) return st;

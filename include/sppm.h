@@ -314,7 +314,7 @@ typedef struct sppm_tuning {
     uint32_t trace_blocks_per_sm; /* resident blocks of the persistent photon traversal per SM
                                      (0 = as many as fit)                                       */
     uint32_t trace_refill_steps;  /* traversal steps a warp takes before it refills its idle
-                                     lanes from the ray queue (0 = 32; 4-wide traversal 16)     */
+                                     lanes from the ray queue (0 = 32; 4-wide traversal 8)      */
     uint32_t eye_block;           /* threads per block of the eye pass (0 = 128; 32..128)       */
     uint32_t store_block;         /* of the photon store + hash insertion (0 = 128; 32..128)    */
     uint32_t gather_block;        /* of the gather + progressive update (0 = 256; 32..256)      */
