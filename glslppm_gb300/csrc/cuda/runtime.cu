@@ -1088,8 +1088,9 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
     };
     float cur_ms = 0.0f;
     if ((st = measure(cur, &cur_ms))) return st;
-    // coordinate descent, the knob with the largest effect (ray order) first; a candidate must
-    // beat the best shapes so far by 1 %; a second sweep when the first changed anything
+    // a grid over ray order x refill interval, then coordinate descent over the other knobs (a
+    // second sweep, over all knobs, when the first changed anything); a candidate must beat the
+    // best shapes so far by 1 %
     bool changed = false;
     auto knob = [&](uint32_t sppm_tuning::*field, std::vector<uint32_t> values) -> int {
         for (uint32_t v : values) {
@@ -1110,10 +1111,26 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
     std::vector<uint32_t> blocks;
     for (uint32_t b : {trace_fit, (3 * trace_fit + 3) / 4, (trace_fit + 1) / 2})
         if (b >= 1 && std::find(blocks.begin(), blocks.end(), b) == blocks.end()) blocks.push_back(b);
+    // ray order and refill interval interact: searched together as a grid first
+    for (uint32_t ub : {0u, 1u}) {
+        if (ub && !queue.key) continue;
+        for (uint32_t rs : {4u, 8u, 16u, 32u, 64u}) {
+            if (ub == cur.unbinned_rays && rs == cur.trace_refill_steps) continue;
+            sppm_tuning t = cur;
+            t.unbinned_rays = ub;
+            t.trace_refill_steps = rs;
+            float ms = 0.0f;
+            if ((st = measure(t, &ms))) return st;
+            if (ms < 0.99f * cur_ms) {
+                cur = t;
+                cur_ms = ms;
+            }
+        }
+    }
     for (int sweep = 0; sweep < 2; sweep++) {
         changed = false;
-        if (queue.key && (st = knob(&sppm_tuning::unbinned_rays, {0u, 1u}))) return st;
-        if ((st = knob(&sppm_tuning::trace_refill_steps, {4u, 8u, 16u, 32u, 64u}))) return st;
+        if (sweep && queue.key && (st = knob(&sppm_tuning::unbinned_rays, {0u, 1u}))) return st;
+        if (sweep && (st = knob(&sppm_tuning::trace_refill_steps, {4u, 8u, 16u, 32u, 64u}))) return st;
         if ((st = knob(&sppm_tuning::trace_blocks_per_sm, blocks))) return st;
         if ((st = knob(&sppm_tuning::gather_block, {256u, 128u, 64u}))) return st;
         if ((st = knob(&sppm_tuning::store_block, {128u, 64u}))) return st;

@@ -325,8 +325,9 @@ int sppm_set_tuning(sppm_ctx* ctx, const sppm_tuning* tuning);
 /* The shapes in effect (defaults filled in). */
 int sppm_get_tuning(sppm_ctx* ctx, sppm_tuning* tuning);
 /* Runs the context's next passes under candidate shapes and leaves the fastest in effect:
-   coordinate descent over the fields above (ray order first; a second sweep when the first
-   changed anything), each candidate run for one untimed and `cycles` timed eye-pass cycles
+   a grid over ray order x refill interval, then coordinate descent over the other fields (a
+   second sweep over all of them when the first changed anything), each candidate run for one
+   untimed and `cycles` timed eye-pass cycles
    (eye_pass_interval passes each), a candidate kept when it is at least 1 % faster than the best
    so far.  These are ordinary passes of the job (its frame count
    advances).  *best and *ms_per_pass (either may be NULL) receive the chosen shapes and their
