@@ -191,6 +191,9 @@ def make_renderer(device: int, precision: int = 0, eye_pass_interval: int = 10):
 def autotune(ctx, args, cycles: int):
     """The library's launch-shape autotuner (Renderer/Batch.autotune) on the job's first passes,
     before the warm-up; the shapes chosen go into the line's config (None with --no-autotune)."""
+    if args.tuning:  # fixed shapes (e.g. the ones a tuner chose in an earlier run): no tuner passes
+        ctx.set_tuning(**json.loads(args.tuning))
+        return ctx.get_tuning().as_dict()
     if args.no_autotune:
         return None
     best, _ = ctx.autotune(cycles)
@@ -817,6 +820,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default launch shapes instead of autotuning them before the warm-up")
+    ap.add_argument("--tuning", default=None,
+                    help='fixed launch shapes as JSON, e.g. \'{"trace_refill_steps": 4, "unbinned_rays": 1}\' '
+                         "(sppm_tuning fields; replaces the autotuner)")
     ap.add_argument("--workload", default="cornell-1024", choices=["cornell-1024", "batched", "serving", "large"],
                     help="the JSON line's headline workload; the default line also carries the batched "
                          "workload's summary under 'batched' unless --no-batched")
