@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <mutex>
 
+#include <cuda.h>  // driver types only (CUcontext, CUresult); nothing is linked
 #include <cuda_runtime.h>
 
 #include "../host/scene_internal.h"
@@ -65,28 +66,73 @@ using sppm::fail;
 // Its scratch is this file-scope device array: 512 x 512 float4 = 4 MiB, held by every GPU that
 // loads the library until the process exits.  Host code must not pass `g_reduce_scratch` itself to a
 // kernel (on the host it names a host-side shadow, not device memory): the device address is looked
-// up with cudaGetSymbolAddress once per device, with that device current, and cached.
+// up with cudaGetSymbolAddress once per device and context, with that device current, and cached.
 static __device__ __align__(256) float4 g_reduce_scratch[(SPPM_REDUCE_NOALLOC_MAX_RESOLUTION / 2) *
                                                          (SPPM_REDUCE_NOALLOC_MAX_RESOLUTION / 2)];
 
 namespace {
-std::mutex g_scratch_mutex;
-float4* g_scratch_ptr[64] = {nullptr};  // device address of g_reduce_scratch, per device ordinal
+// The device address of g_reduce_scratch belongs to the CUDA context that loaded the library's
+// device code: a device reset (cudaDeviceReset) destroys that context and the next runtime call
+// creates a new one, in which the array may sit elsewhere.  The cache is therefore keyed on the
+// context's unique id (cuCtxGetId, never reused within a process), read through driver entry
+// points that the runtime hands out, so the library needs no link against the driver library.
+typedef CUresult (*PFN_ctx_get_current)(CUcontext*);
+typedef CUresult (*PFN_ctx_get_id)(CUcontext, unsigned long long*);
 
+struct ScratchEntry {
+    unsigned long long ctx_id;
+    float4* ptr;
+};
+std::mutex g_scratch_mutex;
+ScratchEntry g_scratch_cache[64];  // per device ordinal: the context it was looked up in, address
+PFN_ctx_get_current g_ctx_get_current = nullptr;
+PFN_ctx_get_id g_ctx_get_id = nullptr;
+
+// id of the current context, 0 when none is current (after a reset, before the next runtime call)
+int current_context_id(unsigned long long* id) {
+    *id = 0;
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = cudaDriverEntryPointSymbolNotFound;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e != cudaSuccess || q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return fail(SPPM_ERR_CUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId unavailable: %s",
+                        cudaGetErrorString(e));
+        g_ctx_get_current = reinterpret_cast<PFN_ctx_get_current>(f1);
+        g_ctx_get_id = reinterpret_cast<PFN_ctx_get_id>(f2);
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return fail(SPPM_ERR_CUDA, "cuCtxGetCurrent failed");
+    if (ctx && g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return fail(SPPM_ERR_CUDA, "cuCtxGetId failed");
+    return SPPM_OK;
+}
+
+// Set-up of the entry point: on the first call in a device's current context (and again after a
+// device reset replaced that context), the array's device address is looked up with that device
+// current and cached; later calls in the same context reuse it.
 int scratch_address(float4** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(SPPM_ERR_CUDA, "cudaGetDevice failed: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= 64) return fail(SPPM_ERR_ARG, "device ordinal %d out of range", dev);
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
+    unsigned long long id = 0;
+    int st = current_context_id(&id);
+    if (st) return st;
+    ScratchEntry& c = g_scratch_cache[dev];
+    if (id == 0 || !c.ptr || c.ctx_id != id) {
+        // also makes the device's primary context current when none is
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_reduce_scratch);
         if (e != cudaSuccess || !p)
             return fail(SPPM_ERR_CUDA, "cudaGetSymbolAddress(g_reduce_scratch) failed: %s", cudaGetErrorString(e));
-        g_scratch_ptr[dev] = static_cast<float4*>(p);
+        if (id == 0 && (st = current_context_id(&id)) != SPPM_OK) return st;
+        c.ptr = static_cast<float4*>(p);
+        c.ctx_id = id;
     }
-    *out = g_scratch_ptr[dev];
+    *out = c.ptr;
     return SPPM_OK;
 }
 }  // namespace

@@ -394,6 +394,72 @@ int Job::write_desc(cudaStream_t s) {
     return staged(s);
 }
 
+namespace {
+// 64-bit fingerprint of byte ranges: four independent multiply-xorshift lanes over 8-byte words
+// (a checksum against mix-ups, not a cryptographic hash)
+struct Fingerprint {
+    uint64_t h[4] = {0x243F6A8885A308D3ull, 0x13198A2E03707344ull, 0xA4093822299F31D0ull, 0x082EFA98EC4E6C89ull};
+    static uint64_t mix(uint64_t x) {
+        x ^= x >> 31;
+        x *= 0x7FB5D329728EA185ull;
+        x ^= x >> 27;
+        x *= 0x81DADEF4BC2DD44Dull;
+        return x ^ (x >> 33);
+    }
+    void add(const void* p, size_t bytes) {
+        const uint8_t* b = static_cast<const uint8_t*>(p);
+        size_t i = 0;
+        if (b) {
+            for (; i + 32 <= bytes; i += 32) {
+                uint64_t w[4];
+                memcpy(w, b + i, 32);
+                for (int k = 0; k < 4; k++) h[k] = (h[k] ^ w[k]) * 0x9E3779B97F4A7C15ull + (h[k] >> 29);
+            }
+            uint64_t tail[4] = {0, 0, 0, 0};
+            memcpy(tail, b + i, bytes - i);
+            for (int k = 0; k < 4; k++) h[k] = (h[k] ^ tail[k]) * 0x9E3779B97F4A7C15ull + (h[k] >> 29);
+        }
+        h[0] ^= mix(bytes + 0x51ED27ull);  // lengths and null pointers count too
+    }
+    uint64_t value() const { return mix(h[0] ^ mix(h[1] ^ mix(h[2] ^ mix(h[3])))); }
+};
+
+uint64_t scene_fingerprint(const sppm_scene& sc) {
+    Fingerprint f;
+    const size_t n = sc.num_triangles, nn = sc.num_nodes;
+    f.add(&sc.num_triangles, 4);
+    f.add(sc.positions, n * 36);
+    f.add(sc.normals, n * 36);
+    f.add(sc.texcoords, sc.texcoords ? n * 24 : 0);
+    f.add(sc.material_ids, n * 4);
+    f.add(sc.materials, (size_t)sc.num_materials * sizeof(sppm_material));
+    f.add(sc.light_triangles, (size_t)sc.num_lights * 4);
+    f.add(sc.light_cdf, (size_t)sc.num_lights * 4);
+    f.add(&sc.light_area, 4);
+    f.add(sc.bbox_min, 12);
+    f.add(sc.bbox_max, 12);
+    f.add(sc.node_bounds, nn * 24);
+    f.add(sc.node_triangle, nn * 4);
+    f.add(sc.order_base, nn * 24);
+    f.add(sc.order_miss, nn * 24);
+    f.add(sc.textures, (size_t)sc.num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4);
+    f.add(sc.material_texture, sc.material_texture ? (size_t)sc.num_materials * 4 : 0);
+    return f.value();
+}
+
+uint64_t camera_fingerprint(const sppm_camera& c) {
+    Fingerprint f;
+    f.add(c.origin, 12);
+    f.add(c.u, 12);
+    f.add(c.v, 12);
+    f.add(c.w, 12);
+    f.add(&c.distance, 4);
+    f.add(&c.width, 4);
+    f.add(&c.height, 4);
+    return f.value();
+}
+}  // namespace
+
 int Job::set_camera_desc(const sppm_camera* cam) {
     JobDesc& J = desc;
     for (int k = 0; k < 3; k++) {
@@ -405,6 +471,7 @@ int Job::set_camera_desc(const sppm_camera* cam) {
     J.cam_cx = (float)cam->width * 0.5f;
     J.cam_cy = (float)cam->height * 0.5f;
     J.cam_dist = cam->distance;
+    camera_fp = camera_fingerprint(*cam);
     have_camera = true;
     return SPPM_OK;
 }
@@ -530,6 +597,7 @@ int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
                        ? cfg.radius_fraction * sppm::sqrt_f32(dx * dx + dy * dy + dz * dz)
                        : 0.0f;
     desc.fixed_radius = fixed_radius;
+    scene_fp = scene_fingerprint(*scene);
     have_scene = true;
     if ((st = write_desc(s))) return st;
     return reset(s);
@@ -600,8 +668,10 @@ namespace {
 struct CheckpointHeader {
     char magic[8];
     uint32_t version, W, H, PW, PH, hash_num, precision, state_bytes;
+    uint32_t seed_mode, seed;
+    uint64_t scene_fp, camera_fp;  // what the job rendered (Job::scene_fp, camera_fp)
 };
-constexpr char kCheckpointMagic[8] = {'S', 'P', 'P', 'M', 'C', 'K', 'P', '2'};
+constexpr char kCheckpointMagic[8] = {'S', 'P', 'P', 'M', 'C', 'K', 'P', '3'};
 constexpr uint32_t kCheckpointKinds = SPPM_STATE_STATS_TAU + 1;
 }  // namespace
 
@@ -618,8 +688,9 @@ int Job::save_checkpoint(void* dst, size_t bytes, cudaStream_t s) const {
     if (bytes != checkpoint_bytes()) return fail(SPPM_ERR_ARG, "checkpoint needs %zu bytes", checkpoint_bytes());
     char* p = static_cast<char*>(dst);
     CheckpointHeader h;
+    memset(&h, 0, sizeof(h));
     memcpy(h.magic, kCheckpointMagic, 8);
-    h.version = 1;
+    h.version = 2;
     h.W = W;
     h.H = H;
     h.PW = PW;
@@ -627,6 +698,10 @@ int Job::save_checkpoint(void* dst, size_t bytes, cudaStream_t s) const {
     h.hash_num = hash_num;
     h.precision = cfg.precision;
     h.state_bytes = (uint32_t)sizeof(JobState);
+    h.seed_mode = cfg.seed_mode;
+    h.seed = cfg.seed;
+    h.scene_fp = scene_fp;
+    h.camera_fp = camera_fp;
     memcpy(p, &h, sizeof(h));
     p += sizeof(h);
     SPPM_CK(cudaMemcpyAsync(p, d_state, sizeof(JobState), cudaMemcpyDeviceToHost, s));
@@ -648,11 +723,20 @@ int Job::load_checkpoint(const void* src, size_t bytes, cudaStream_t s, uint32_t
     const char* p = static_cast<const char*>(src);
     CheckpointHeader h;
     memcpy(&h, p, sizeof(h));
-    if (memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != 1 || h.state_bytes != sizeof(JobState))
+    if (memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != 2 || h.state_bytes != sizeof(JobState))
         return fail(SPPM_ERR_ARG, "not a checkpoint of this build");
     if (h.W != W || h.H != H || h.PW != PW || h.PH != PH || h.hash_num != hash_num || h.precision != cfg.precision)
         return fail(SPPM_ERR_ARG, "checkpoint of a %ux%u image with %ux%u photons (%u slots, precision %u) does not "
                     "fit this job", h.W, h.H, h.PW, h.PH, h.hash_num, h.precision);
+    if (h.seed_mode != cfg.seed_mode || h.seed != cfg.seed)
+        return fail(SPPM_ERR_ARG, "checkpoint of a job seeded with mode %u, seed %u; this job has mode %u, seed %u",
+                    h.seed_mode, h.seed, cfg.seed_mode, cfg.seed);
+    if (h.scene_fp != scene_fp)
+        return fail(SPPM_ERR_ARG, "checkpoint of another scene (scene fingerprint %016llx, this job's %016llx)",
+                    (unsigned long long)h.scene_fp, (unsigned long long)scene_fp);
+    if (h.camera_fp != camera_fp)
+        return fail(SPPM_ERR_ARG, "checkpoint of another camera (camera fingerprint %016llx, this job's %016llx)",
+                    (unsigned long long)h.camera_fp, (unsigned long long)camera_fp);
     p += sizeof(h);
     JobState st;
     memcpy(&st, p, sizeof(st));

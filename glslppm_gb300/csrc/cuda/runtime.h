@@ -102,6 +102,9 @@ struct Job {
         return (uint32_t)(((start_frame % L) + L) % L);
     }
     uint64_t scene_bytes_used = 0;
+    // fingerprints of the uploaded scene (every input array) and of the camera, recorded in a
+    // checkpoint so that it only loads into a job that renders the same thing
+    uint64_t scene_fp = 0, camera_fp = 0;
 
     // device bytes of the state arena for a configuration
     static uint64_t state_bytes(const sppm_config& cfg);

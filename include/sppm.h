@@ -275,8 +275,11 @@ int sppm_get_frame_info(sppm_ctx* ctx, sppm_frame_info* info);
 /* Checkpoint / resume of the progressive state (no counterpart in the reference): a flat binary
    image of the frame counters, RNG states, hit points, photon records, hashed grid and
    progressive statistics -- not the scene or camera, which a resuming context uploads itself.
-   Loading it into a context of the same image, photon and hash sizes and precision continues the
-   render exactly where it was saved (the next frames are bit-identical to an uninterrupted run). */
+   The header records fingerprints of the scene (every array of the uploaded sppm_scene), of the
+   camera and of the seed (seed_mode, seed).  Loading it into a context of the same image, photon
+   and hash sizes, precision, seed, scene and camera continues the render exactly where it was
+   saved (the next frames are bit-identical to an uninterrupted run); any other context rejects
+   it with SPPM_ERR_ARG, naming what differs. */
 size_t sppm_checkpoint_bytes(const sppm_ctx* ctx);
 int sppm_save_checkpoint(sppm_ctx* ctx, void* dst, size_t bytes);
 int sppm_load_checkpoint(sppm_ctx* ctx, const void* src, size_t bytes);
@@ -371,8 +374,10 @@ int sppm_reduce_texture(const float* d_texture, uint32_t resolution, uint32_t op
    Its scratch is a fixed 4 MiB array in the library's device memory, which every GPU that loads the
    library keeps until the process exits; resolutions above SPPM_REDUCE_NOALLOC_MAX_RESOLUTION are
    rejected with SPPM_ERR_ARG.  The first call on a device looks up the array's device address
-   (cudaGetSymbolAddress, which may load the library's device code): make that first call before
-   any stream capture.  All calls share the array: calls that overlap on the GPU (on different
+   (cudaGetSymbolAddress, which may load the library's device code) and caches it for the device's
+   current CUDA context; after a device reset (cudaDeviceReset) the next call sees a new context
+   and looks the address up again.  Make the first call on a device, and the first after a reset,
+   before any stream capture.  All calls share the array: calls that overlap on the GPU (on different
    streams, or from several threads) race on it and must be serialised by the caller.  Nothing in
    the array needs to start at zero.  Results equal sppm_reduce_texture's bit for bit. */
 #define SPPM_REDUCE_NOALLOC_MAX_RESOLUTION 1024u

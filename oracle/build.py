@@ -2,9 +2,11 @@
 
 * ``build_oracle()`` compiles the C restatement of the shader path (``sppm_oracle.c``) twice --
   single precision and double precision -- into ``oracle/_build/``.
-* ``build_ref()`` compiles the reference's own sources from the reference checkout into
-  ``oracle/_ref/`` when that checkout is present (``SPPM_REFERENCE_DIR``, default the directory the
-  reference is mounted at on the development machine):
+* ``build_ref(reference_dir)`` compiles the reference's own sources from a reference checkout into
+  ``oracle/_ref/``.  The checkout is the ``reference_dir`` argument, else the ``SPPM_REFERENCE_DIR``
+  environment variable; with neither, nothing is built and a message says why.  The directory a
+  build used is recorded in ``oracle/_ref/REFERENCE_DIR`` so that later test runs find the same
+  sources (``reference_dir()``):
     - ``ref_host_dump``: the reference's ``mesh.cpp``, ``bvh.cpp``, ``bbox.cpp`` and ``camera.cpp``,
       unmodified, linked with ``ref_host_dump.cpp``;
     - ``libref_shaders.so``: the reference's GLSL shaders compiled as C++ through
@@ -27,7 +29,7 @@ REPO = ORACLE_DIR.parent
 BUILD_DIR = ORACLE_DIR / "_build"
 REF_DIR = ORACLE_DIR / "_ref"
 INCLUDE = REPO / "include"
-REFERENCE = Path(os.environ.get("SPPM_REFERENCE_DIR", "/root/reference"))
+_RECORDED = REF_DIR / "REFERENCE_DIR"
 
 STRICT_FP = ["-ffp-contract=off", "-fno-fast-math"]
 
@@ -66,15 +68,38 @@ def build_oracle(force: bool = False) -> dict[str, Path]:
     return out
 
 
+def _is_checkout(d: Path | None) -> bool:
+    return d is not None and (d / "bvh.cpp").is_file() and (d / "photontrace.fs").is_file()
+
+
+def reference_dir() -> Path | None:
+    """The reference checkout: SPPM_REFERENCE_DIR, else the one the last build_ref() used, else None."""
+    env = os.environ.get("SPPM_REFERENCE_DIR")
+    if env:
+        return Path(env)
+    if _RECORDED.is_file():
+        return Path(_RECORDED.read_text().strip())
+    return None
+
+
 def reference_available() -> bool:
-    return (REFERENCE / "bvh.cpp").is_file() and (REFERENCE / "photontrace.fs").is_file()
+    return _is_checkout(reference_dir())
 
 
-def build_ref(force: bool = False) -> dict[str, Path]:
-    """Compile the reference's host code and shaders into oracle/_ref (needs the reference)."""
-    if not reference_available():
+def build_ref(reference_dir_: str | Path | None = None, force: bool = False) -> dict[str, Path]:
+    """Compile the reference's host code and shaders into oracle/_ref (needs a reference checkout)."""
+    src = Path(reference_dir_) if reference_dir_ else (Path(os.environ["SPPM_REFERENCE_DIR"])
+                                                     if os.environ.get("SPPM_REFERENCE_DIR") else None)
+    if src is None:
+        print("oracle/build.py: no reference checkout given (argument or SPPM_REFERENCE_DIR); "
+              "oracle/_ref is not built and the reference-marked tests will skip")
         return {}
+    if not _is_checkout(src):
+        print(f"oracle/build.py: {src} is not a glslppm checkout (bvh.cpp, photontrace.fs); oracle/_ref is not built")
+        return {}
+    REFERENCE = src.resolve()
     REF_DIR.mkdir(parents=True, exist_ok=True)
+    _RECORDED.write_text(str(REFERENCE) + "\n")
     out = {}
     host_srcs = [REFERENCE / f for f in ("mesh.cpp", "bvh.cpp", "bbox.cpp", "camera.cpp")]
     dump = REF_DIR / "ref_host_dump"
@@ -120,5 +145,6 @@ def clean() -> None:
 
 
 if __name__ == "__main__":
+    import sys
     print(build_oracle(force=True))
-    print(build_ref(force=True))
+    print(build_ref(sys.argv[1] if len(sys.argv) > 1 else None, force=True))

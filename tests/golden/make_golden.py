@@ -24,7 +24,7 @@ import numpy as np
 REPO = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(REPO))
 
-from oracle.build import REFERENCE, build_oracle, build_ref  # noqa: E402
+from oracle.build import build_oracle, build_ref, reference_dir  # noqa: E402
 from oracle.refdump import run_ref_host_dump  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
@@ -51,13 +51,13 @@ def scene_dict(d: dict) -> dict:
 
 def main() -> None:
     build_oracle()
-    build_ref()
+    build_ref(reference_dir())
     import glslppm_gb300 as g
     from oracle.binding import Oracle, gpurnd_sequence, hash_build
     from tests.golden.fixtures import camera_from, scene_arrays_from
 
     # 1. the reference's default scene, loaded by the reference's host code
-    cm = run_ref_host_dump(REFERENCE / "cornell_metal.obj", 0.01, ((0, 0, 13), (0, 0, 0), 512, 512, 45))
+    cm = run_ref_host_dump(reference_dir() / "cornell_metal.obj", 0.01, ((0, 0, 13), (0, 0, 0), 512, 512, 45))
     sd = scene_dict(cm)
     save("cornell_metal_scene.npz", **sd)
     arrays = scene_arrays_from(sd)

@@ -80,3 +80,33 @@ def test_checkpoint_of_another_size_is_rejected(cornell_c1_mesh):
     bad[0:8] = b"NOTACKPT"
     with pytest.raises(N.SppmError):
         a.load_checkpoint(bytes(bad))
+
+
+def test_checkpoint_of_another_scene_camera_or_seed_is_rejected(cornell_c1_mesh):
+    """A checkpoint carries fingerprints of the scene, the camera and the seed: loading it into a
+    job of the same sizes that renders something else fails instead of continuing with progressive
+    state that belongs to another image."""
+    sc, mesh = cornell_c1_mesh
+    cfg = g.default_config(16, photon_width=16, photon_height=16)
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 16, 16, sc.fov)
+    a = setup(cfg, mesh, cam)
+    a.run_passes(3)
+    ck = a.save_checkpoint()
+    other = scenes.cornell_variant(4, min_tris=500, max_tris=2000).scene.to_mesh()
+    b = setup(cfg, other, cam)
+    with pytest.raises(N.SppmError, match="another scene"):
+        b.load_checkpoint(ck)
+    moved = g.look_at((sc.camera_origin[0] + 0.01, sc.camera_origin[1], sc.camera_origin[2]), sc.camera_lookat,
+                      16, 16, sc.fov)
+    c = setup(cfg, mesh, moved)
+    with pytest.raises(N.SppmError, match="another camera"):
+        c.load_checkpoint(ck)
+    d = setup(g.default_config(16, photon_width=16, photon_height=16, seed_mode=N.SEED_HASH, seed=7), mesh, cam)
+    with pytest.raises(N.SppmError, match="seeded"):
+        d.load_checkpoint(ck)
+    # the same scene, camera and seed in a fresh context still load and continue
+    e = setup(cfg, mesh, cam)
+    e.load_checkpoint(ck)
+    a.run_passes(2)
+    e.run_passes(2)
+    assert same(a.read_state("flux_radius"), e.read_state("flux_radius"))

@@ -48,19 +48,19 @@ def test_camera_matches_reference_fixture(cornell_metal):
 
 @pytest.mark.reference
 def test_obj_loader_and_bvh_equal_reference_host_code_cornell_metal():
-    from oracle.build import REFERENCE, build_ref
+    from oracle.build import build_ref, reference_dir
     from oracle.refdump import run_ref_host_dump
-    build_ref()
-    ref = run_ref_host_dump(REFERENCE / "cornell_metal.obj", 0.01)
-    mine = g.Mesh.load_obj(str(REFERENCE / "cornell_metal.obj"), (0, 0, 0), 0.01).build_bvh().arrays()
+    build_ref(reference_dir())
+    ref = run_ref_host_dump(reference_dir() / "cornell_metal.obj", 0.01)
+    mine = g.Mesh.load_obj(str(reference_dir() / "cornell_metal.obj"), (0, 0, 0), 0.01).build_bvh().arrays()
     assert_scene_equal(ref, mine)
 
 
 @pytest.mark.reference
 def test_obj_loader_and_bvh_equal_reference_host_code_generated_cornell_box(tmp_path):
-    from oracle.build import build_ref
+    from oracle.build import build_ref, reference_dir
     from oracle.refdump import run_ref_host_dump
-    build_ref()
+    build_ref(reference_dir())
     obj = scenes.cornell_box().write_obj(tmp_path / "cornell.obj")
     ref = run_ref_host_dump(obj, 1.0)
     mine = g.Mesh.load_obj(str(obj)).build_bvh().arrays()
@@ -72,9 +72,9 @@ def test_obj_loader_and_bvh_equal_reference_host_code_generated_cornell_box(tmp_
 def test_loader_quirks_equal_reference(tmp_path):
     """Materials without Ns are dropped, Ka/Kd/Ks carry over, Ke reads as Ka, face normals when an
     index lacks a normal, long lines are chunked at 79 characters, quads use 3 vertices."""
-    from oracle.build import build_ref
+    from oracle.build import build_ref, reference_dir
     from oracle.refdump import run_ref_host_dump
-    build_ref()
+    build_ref(reference_dir())
     (tmp_path / "q.mtl").write_text(
         "newmtl a\nKd 0.5 0.25 0.125\nNs 10\n"
         "newmtl skipped\nKd 0.9 0.9 0.9\n"
@@ -109,9 +109,9 @@ def test_loader_quirks_equal_reference(tmp_path):
 def test_every_material_class_round_trips_through_the_reference_loader(tmp_path, light):
     """The MTL dialect of scenes.MaterialSpec.mtl makes the reference's classifier produce every
     BRDF class of materials_box; our loader gives the same arrays."""
-    from oracle.build import build_ref
+    from oracle.build import build_ref, reference_dir
     from oracle.refdump import run_ref_host_dump
-    build_ref()
+    build_ref(reference_dir())
     spec = scenes.materials_box(light=light)
     obj = spec.write_obj(tmp_path / "m.obj")
     ref = run_ref_host_dump(obj, 1.0)
@@ -135,9 +135,9 @@ def _resample_like_reference(img):
 def test_textured_scene_equals_reference_loader(tmp_path):
     """map_Kd PPM textures, vt coordinates on every face vertex (kept for textured materials
     only), the textures resampled to 512x512 as the reference's packing does."""
-    from oracle.build import build_ref
+    from oracle.build import build_ref, reference_dir
     from oracle.refdump import run_ref_host_dump
-    build_ref()
+    build_ref(reference_dir())
     spec = scenes.textured_box()
     obj = spec.write_obj(tmp_path / "t.obj")
     ref = run_ref_host_dump(obj, 1.0)
@@ -202,9 +202,9 @@ def test_obj_reader_threads_give_the_sequential_result(tmp_path):
 
 @pytest.mark.reference
 def test_threaded_obj_reader_equals_reference(tmp_path):
-    from oracle.build import build_ref
+    from oracle.build import build_ref, reference_dir
     from oracle.refdump import run_ref_host_dump
-    build_ref()
+    build_ref(reference_dir())
     big = _quirky_obj(tmp_path, "big.obj", 16000)
     ref = run_ref_host_dump(big, 1.5)
     mine = g.Mesh.load_obj(str(big), (0, 0, 0), 1.5).build_bvh().arrays()
@@ -217,20 +217,20 @@ def test_drop_in_gpurt_header_with_reference_host_code(tmp_path):
     the TMesh + TBVH into exactly the arrays the reference builds; without a GPU it reports
     SPPM_ERR_NO_DEVICE through its status instead of crashing."""
     import subprocess
-    from oracle.build import REFERENCE, build_ref
+    from oracle.build import build_ref, reference_dir
     from oracle.refdump import read_dump, run_ref_host_dump
     from glslppm_gb300 import native as N
-    exe = build_ref().get("gpurt_shim")
+    exe = build_ref(reference_dir()).get("gpurt_shim")
     assert exe is not None
     out = tmp_path / "shim.bin"
     frames = 3 if N.device_count() else 2
-    proc = subprocess.run([str(exe), "cornell_metal.obj", "0.01", str(out), str(frames)], cwd=str(REFERENCE),
+    proc = subprocess.run([str(exe), "cornell_metal.obj", "0.01", str(out), str(frames)], cwd=str(reference_dir()),
                           capture_output=True, text=True)
     if N.device_count():
         assert proc.returncode == 0 and "rendered 3 frames" in proc.stdout
     else:
         assert proc.returncode == N.ERR_NO_DEVICE and "no CUDA device" in proc.stdout
-    a, b = read_dump(out), run_ref_host_dump(REFERENCE / "cornell_metal.obj", 0.01)
+    a, b = read_dump(out), run_ref_host_dump(reference_dir() / "cornell_metal.obj", 0.01)
     for k in FIELDS:
         assert np.array_equal(np.asarray(a[k]).view(np.uint8), np.asarray(b[k]).view(np.uint8)), k
 
@@ -240,9 +240,9 @@ def test_drop_in_gpurt_header_passes_textures(tmp_path):
     """The CGPURT shim hands the reference TMesh's map_Kd textures over as 512x512 layers, equal
     to the reference's resampling and to our own loader's."""
     import subprocess
-    from oracle.build import build_ref
+    from oracle.build import build_ref, reference_dir
     from oracle.refdump import read_dump, run_ref_host_dump
-    exe = build_ref().get("gpurt_shim")
+    exe = build_ref(reference_dir()).get("gpurt_shim")
     obj = scenes.textured_box().write_obj(tmp_path / "t.obj")
     out = tmp_path / "shim.bin"
     subprocess.run([str(exe), obj.name, "1.0", str(out), "0"], cwd=str(tmp_path), check=True, capture_output=True)

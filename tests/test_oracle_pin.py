@@ -35,9 +35,9 @@ def compare(o, r, label):
 
 def run(scene, cam, R, checkpoints, textured=False, lens=None):
     from oracle.binding import Oracle
-    from oracle.build import build_ref
+    from oracle.build import build_ref, reference_dir
     from oracle.refdump import RefShaders
-    build_ref()
+    build_ref(reference_dir())
     cfg = g.default_config(R)
     r = RefShaders(scene, cam, R)
     if lens is not None:

@@ -23,24 +23,28 @@ def call(fn, ptr, resolution, op, stream):
     return st, np.array(list(out), dtype=np.float32)
 
 
-def test_no_alloc_reduce_matches_the_allocating_entry_point_twice():
+@pytest.mark.parametrize("op", [0, 1, 2], ids=["min", "max", "sum"])
+def test_no_alloc_reduce_matches_the_allocating_entry_point_twice(op):
     torch = pytest.importorskip("torch")
     from glslppm_gb300 import native as N
     stream = torch.cuda.current_stream().cuda_stream
-    rng = np.random.default_rng(3)
-    calls = [(1024, 2), (256, 0)]  # two calls in a row, different sizes and operations
-    textures = [torch.from_numpy((rng.standard_normal((r * r, 4)) * 50).astype(np.float32)).cuda() for r, _ in calls]
+    rng = np.random.default_rng(3 + op)
+    # two calls in a row for each size: the second finds the first one's contents in the scratch;
+    # resolution 2 runs a single level, 1024 is the largest the scratch holds
+    resolutions = [1024, 1024, 256, 2, 2, 32]
+    textures = [torch.from_numpy((rng.standard_normal((r * r, 4)) * 50).astype(np.float32)).cuda()
+                for r in resolutions]
     expected = []
-    for (r, op), t in zip(calls, textures):
+    for r, t in zip(resolutions, textures):
         st, ref = call(N.lib.sppm_reduce_texture, t.data_ptr(), r, op, stream)
         assert st == N.OK, N.last_error()
         expected.append(ref)
-    # first call on this device performs the one-time set-up (symbol address lookup)
-    st, _ = call(N.lib.sppm_reduce_texture_noalloc, textures[1].data_ptr(), calls[1][0], 1, stream)
+    # the first call on this device performs the one-time set-up (symbol address lookup)
+    st, _ = call(N.lib.sppm_reduce_texture_noalloc, textures[2].data_ptr(), resolutions[2], (op + 1) % 3, stream)
     assert st == N.OK, N.last_error()
     torch.cuda.synchronize()
     free_before = torch.cuda.mem_get_info()[0]
-    for (r, op), t, ref in zip(calls, textures, expected):
+    for r, t, ref in zip(resolutions, textures, expected):
         st, got = call(N.lib.sppm_reduce_texture_noalloc, t.data_ptr(), r, op, stream)
         assert st == N.OK, N.last_error()
         assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (r, op, got, ref)
