@@ -174,11 +174,22 @@ def profile_traffic(kernel: str, workload: str = "cornell1024"):
     return None
 
 
-def make_renderer(device: int, precision: int = 0, eye_pass_interval: int = 10):
+def cornell_mesh():
+    """The Cornell box as the product's host code loads it: the generated scene written as OBJ/MTL,
+    read by the OBJ loader (the reference's loading rules) and given the exact-SAH BVH -- the same
+    arrays, word for word, as the reference's own host code makes of that OBJ
+    (tests/golden/cornell_box_scene.npz, which the CPU reference arm renders)."""
     import glslppm_gb300 as g
     from glslppm_gb300 import scenes
     sc = scenes.cornell_box()
-    mesh = sc.to_mesh()
+    with tempfile.TemporaryDirectory() as td:
+        mesh = g.Mesh.load_obj(str(sc.write_obj(Path(td) / "cornell_box.obj"))).build_bvh()
+    return sc, mesh
+
+
+def make_renderer(device: int, precision: int = 0, eye_pass_interval: int = 10):
+    import glslppm_gb300 as g
+    sc, mesh = cornell_mesh()
     cfg = g.default_config(1024, radius_rule=1, radius_fraction=0.005, precision=precision,
                            eye_pass_interval=eye_pass_interval)
     cam = g.look_at(sc.camera_origin, sc.camera_lookat, 1024, 1024, sc.fov)
@@ -186,6 +197,12 @@ def make_renderer(device: int, precision: int = 0, eye_pass_interval: int = 10):
     r.upload_scene(mesh)
     r.set_camera(cam)
     return r, mesh, cfg, cam
+
+
+def headline_config(precision: str, eye_pass_interval: int, world: int) -> dict:
+    """The `config` of the headline line, identical for the GPU arm and the CPU reference arm."""
+    return dict(WORKLOAD, precision=precision, l2="working set > 129 MB L2 (no flush)",
+                eye_pass_every=eye_pass_interval, parallelism=f"replicas x{world}")
 
 
 def autotune(ctx, args, cycles: int):
@@ -227,16 +244,16 @@ def sum_over_ranks(x: float, world: int) -> float:
 
 
 def cpu_baseline_run(max_seconds: float = 25.0, max_frames: int | None = None, warmup: int = 0):
-    """The CPU oracle on the same workload, all host threads, a bounded number of passes after
-    `warmup` untimed ones."""
-    import glslppm_gb300 as g
-    from glslppm_gb300 import scenes
+    """The CPU oracle (the C restatement of the reference's shaders, OpenMP over all host threads)
+    on the same workload, a bounded number of passes after `warmup` untimed ones.  The scene, its
+    BVH and the camera are those the reference's own host code (mesh.cpp, bvh.cpp, camera.cpp) made
+    of the Cornell box OBJ (tests/golden/cornell_box_scene.npz); the product library is not loaded."""
     from oracle.binding import Oracle
-    sc = scenes.cornell_box()
-    mesh = sc.to_mesh()
-    cfg = g.default_config(1024, radius_rule=1, radius_fraction=0.005)
-    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 1024, 1024, sc.fov)
-    o = Oracle(cfg, mesh.scene(), cam)
+    from oracle.structs import RADIUS_DIAGONAL, camera_from_npz, default_config, scene_from_npz
+    scene, d = scene_from_npz(REPO / "tests" / "golden" / "cornell_box_scene.npz")
+    cfg = default_config(1024, radius_rule=RADIUS_DIAGONAL, radius_fraction=0.005)
+    cam = camera_from_npz(d, 1024, 1024)
+    o = Oracle(cfg, scene, cam)
     if warmup:
         o.run_frames(warmup)
     f0 = o.frame_info()
@@ -265,20 +282,23 @@ def run_reference(args, rank, world):
     budget = float(os.environ.get("SPPM_REFERENCE_SECONDS", "60"))
     res = cpu_baseline_run(max_seconds=budget, max_frames=args.steps, warmup=args.warmup)
     v = res["photons"] / res["seconds"] / 1e6
+    sample = (f"{res['frames']} passes of the 1024x1024 / 2^20-photon workload after {args.warmup} untimed "
+              f"ones, {res['seconds']:.1f} s")
     line = {
         "metric": "SPPM Mphotons/s + Mrays/s at fixed RMSE vs FP64 oracle, plain vs batched",
         "value": round(v, 4), "unit": "Mphotons/s", "impl": "reference", "n_gpus": args.gpus,
         "steps": res["frames"], "requested_steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000.0 * res["seconds"] / res["frames"], 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(WORKLOAD, sample=f"{res['frames']} passes after {args.warmup} untimed ones"),
+        "config": headline_config("fp32", 10, world),
         "mrays_per_s": round(res["segments"] / res["seconds"] / 1e6, 4),
         "cpu_baseline": {"value": round(v, 4), "unit": "Mphotons/s", "cores": res["cores"], "kind": "port",
-                         "sample": f"{res['frames']} passes of the 1024x1024 / 2^20-photon workload after "
-                                   f"{args.warmup} untimed ones"},
+                         "sample": sample},
         "e2e": {"value": round(v, 4), "unit": "Mphotons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's GLSL pipeline needs OpenGL, unavailable on this machine; this arm runs the CPU "
-                "restatement of the reference's shaders (oracle/sppm_oracle.c) on the host cores",
+                "restatement of the reference's shaders (oracle/sppm_oracle.c) on the host cores, on the scene, BVH "
+                "and camera the reference's own host code built (tests/golden/cornell_box_scene.npz); the product "
+                "library is not loaded",
     }
     print(json.dumps(line), flush=True)
 
@@ -386,9 +406,8 @@ def run_gpu(args, rank, world, local):
             "value": round(value, 3), "unit": "Mphotons/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": round(1000.0 * t / K, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(WORKLOAD, precision=args.precision, l2="working set > 129 MB L2 (no flush)",
-                           eye_pass_every=args.eye_pass_interval,
-                           parallelism=f"replicas x{world}", tuning=tuning),
+            "config": headline_config(args.precision, args.eye_pass_interval, world),
+            "tuning": tuning,
             "mrays_per_s": round(mrays, 3),
             "stage_ms_per_launch": {k: round(v[0] / v[1], 4) for k, v in stages.items() if v[1]},
             "stage_bandwidth": stage_bandwidth(stages, npix, P, (fi1.photon_segments - fi0.photon_segments) / K,

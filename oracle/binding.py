@@ -2,7 +2,9 @@
 of bench.py use it).
 
 ``Oracle(config, scene, camera, fp64=False)`` mirrors the native Renderer's state-reading API, so a
-parity test reads the same state kinds from both and compares them.
+parity test reads the same state kinds from both and compares them.  config, scene and camera are
+the sppm.h structs, either the product's (glslppm_gb300.native) or the oracle's own mirror
+(oracle.structs, same layout); this module never loads the product library.
 """
 from __future__ import annotations
 
@@ -96,7 +98,7 @@ class Oracle:
         return out
 
     def frame_info(self):
-        from glslppm_gb300.native import FrameInfo
+        from .structs import FrameInfo
         fi = FrameInfo()
         self.lib.frame_info(self._h, C.addressof(fi))
         return fi

@@ -10,9 +10,14 @@ reference sources are present):
   kat_hash.npz             a seeded 64x64 photon set and its stochastic hashed grid (winner and
                            count per slot, oracle);
   kat_frames_cm32.npz      the oracle's state after 1, 10 and 23 frames of a 32x32 image with 32x32
-                           photon slots on cornell_metal, with the camera used.
+                           photon slots on cornell_metal, with the camera used;
+  cornell_box_scene.npz    the generated 7,948-triangle Cornell box of the 256x256 and 1024x1024
+                           workloads (glslppm_gb300.scenes.cornell_box written as OBJ/MTL) as the
+                           reference's own host code loads it and builds its BVH, with the
+                           TCamera of its default view at 1024x1024: the scene of bench.py's CPU
+                           reference arm, which must not use the product's loader or BVH builder.
 
-usage: python tests/golden/make_golden.py
+usage: python tests/golden/make_golden.py [name ...]   (default: every fixture)
 """
 from __future__ import annotations
 
@@ -49,9 +54,29 @@ def scene_dict(d: dict) -> dict:
     return out
 
 
-def main() -> None:
+def cornell_box_fixture() -> None:
+    import tempfile
+
+    from glslppm_gb300 import scenes
+    sc = scenes.cornell_box()
+    with tempfile.TemporaryDirectory() as td:
+        obj = sc.write_obj(Path(td) / "cornell_box.obj")
+        d = run_ref_host_dump(obj, 1.0, (sc.camera_origin, sc.camera_lookat, 1024, 1024, sc.fov))
+    sd = scene_dict(d)
+    sd["camera_origin"] = np.asarray(sc.camera_origin, np.float32)
+    sd["camera_lookat"] = np.asarray(sc.camera_lookat, np.float32)
+    sd["fov"] = np.float32(sc.fov)
+    save("cornell_box_scene.npz", **sd)
+
+
+def main(names: list[str]) -> None:
     build_oracle()
     build_ref(reference_dir())
+    if names:
+        for n in names:
+            {"cornell_box_scene": cornell_box_fixture}[n]()
+        return
+    cornell_box_fixture()
     import glslppm_gb300 as g
     from oracle.binding import Oracle, gpurnd_sequence, hash_build
     from tests.golden.fixtures import camera_from, scene_arrays_from
@@ -117,4 +142,4 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -117,3 +117,44 @@ def test_invalid_configs_are_rejected(native_lib):
         with pytest.raises(N.SppmError) as e:
             g.Renderer(g.default_config(16, **bad))
         assert e.value.status in (N.ERR_ARG, N.ERR_UNSUPPORTED)
+
+
+def test_oracle_struct_mirror_matches_the_product_structs(native_lib):
+    """oracle/structs.py (used where the product library must not be loaded) has the layout of the
+    product's sppm.h structs, and its default configuration is sppm_config_defaults'."""
+    import ctypes as C
+
+    import glslppm_gb300 as g
+    from oracle import structs as OS
+    N = native_lib
+    for mine, theirs in ((OS.Config, N.Config), (OS.Material, N.Material), (OS.Scene, N.Scene),
+                         (OS.Camera, N.Camera), (OS.FrameInfo, N.FrameInfo)):
+        assert C.sizeof(mine) == C.sizeof(theirs), mine.__name__
+        assert [(f, getattr(mine, f).offset) for f, _ in mine._fields_] == \
+               [(f, getattr(theirs, f).offset) for f, _ in theirs._fields_], mine.__name__
+    for res in (16, 1024):
+        a, b = OS.default_config(res), g.default_config(res)
+        assert bytes(a) == bytes(b)
+
+
+def test_cornell_box_fixture_is_the_product_scene(tmp_path):
+    """The Cornell box of tests/golden/cornell_box_scene.npz (the reference's host code's loader,
+    BVH and camera on the generated OBJ, made by make_golden.py) equals what the product's OBJ
+    loader, BVH builder and camera make of the same OBJ, word for word -- so the CPU reference arm
+    of bench.py renders exactly the GPU arm's scene without loading the product library."""
+    import glslppm_gb300 as g
+    from glslppm_gb300 import scenes
+    from oracle.structs import camera_from_npz, scene_from_npz
+    s, d = scene_from_npz(REPO / "tests" / "golden" / "cornell_box_scene.npz")
+    sc = scenes.cornell_box()
+    mine = g.Mesh.load_obj(str(sc.write_obj(tmp_path / "cornell_box.obj"))).build_bvh().arrays()
+    for k in ("positions", "normals", "material_ids", "light_triangles", "light_cdf", "bbox_min", "bbox_max",
+              "node_bounds", "node_triangle", "order_base", "order_miss"):
+        a = np.ascontiguousarray(getattr(mine, k))
+        b = np.ascontiguousarray(d[k])
+        assert a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8)), k
+    assert np.float32(mine.light_area) == np.float32(d["light_area"])
+    assert np.array_equal(mine.materials["color"], d["mat_color"])
+    assert np.array_equal(mine.materials["brdf"], d["mat_brdf"])
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 1024, 1024, sc.fov)
+    assert bytes(cam) == bytes(camera_from_npz(d, 1024, 1024))

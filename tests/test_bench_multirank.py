@@ -61,3 +61,24 @@ def test_reference_arm_under_torchrun_prints_one_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_arm_does_not_load_the_product_library():
+    """The CPU reference arm renders the reference host code's scene (a committed fixture) with the
+    oracle alone: the product package is never imported and libsppm.so never mapped, and its config
+    is the GPU arm's headline config."""
+    env = dict(os.environ, SPPM_REFERENCE_SECONDS="1")
+    code = (f"import sys; sys.path.insert(0, {str(REPO)!r}); "
+            "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3']; "
+            "import bench; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('PRODUCT' if ('libsppm' in maps or any(m.startswith('glslppm_gb300') for m in sys.modules)) "
+            "else 'CLEAN')")
+    p = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, env=env, cwd=REPO)
+    assert p.returncode == 0, p.stderr[-2000:]
+    out = p.stdout.strip().splitlines()
+    assert out[-1] == "CLEAN"
+    d = json.loads(next(ln for ln in out if ln.startswith("{")))
+    sys.path.insert(0, str(REPO))
+    import bench
+    assert d["config"] == bench.headline_config("fp32", 10, 1)
