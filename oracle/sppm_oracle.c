@@ -142,6 +142,7 @@ static inline void schrage_step(const real in[4], real out[4]) {
     }
 }
 
+#ifndef ORACLE_FP64
 static inline real gpu_rnd(vec4* n) {
     real s[4] = {n->x, n->y, n->z, n->w}, o[4];
     schrage_step(s, o);
@@ -163,6 +164,74 @@ static inline uint32_t hash_cell(vec3 idx, real grid_scale, real hash_scale1, re
     if (h > hash_num - RC(1.0)) h = hash_num - RC(1.0);
     return (uint32_t)h;
 }
+#else
+/* The double-precision oracle draws the single-precision random sequence: GPURnd and the cell
+ * hash (both pseudo-random functions of the reference, not part of the estimator's arithmetic) run
+ * in single precision exactly as in the FP32 build.  An FP64 render therefore consumes the same
+ * random numbers as an FP32 render of the same seed, and the two images differ only through the
+ * precision of the light transport and of the estimator (a flipped comparison changes what follows
+ * on that path), not through independent samples. */
+static float RNDF_Q[4], RNDF_R[4], RNDF_A[4], RNDF_M2[4], RNDF_MINV[4], RNDF_QINV[4];
+static int rndf_ready = 0;
+
+static void rndf_init(void) {
+    if (rndf_ready) return;
+    static const float q[4] = {1225.0f, 1585.0f, 2457.0f, 2098.0f};
+    static const float r[4] = {1112.0f, 367.0f, 92.0f, 265.0f};
+    static const float a[4] = {3423.0f, 2646.0f, 1707.0f, 1999.0f};
+    static const float m[4] = {4194287.0f, 4194277.0f, 4194191.0f, 4194167.0f};
+    for (int i = 0; i < 4; i++) {
+        RNDF_Q[i] = q[i];
+        RNDF_R[i] = r[i];
+        RNDF_A[i] = a[i];
+        RNDF_M2[i] = 0.5f * m[i];
+        RNDF_MINV[i] = 1.0f / m[i];
+        RNDF_QINV[i] = 1.0f / q[i];
+    }
+    rndf_ready = 1;
+}
+
+static inline void schrage_step_f32(const float in[4], float out[4]) {
+    for (int i = 0; i < 4; i++) {
+        const float beta = floorf(in[i] * RNDF_QINV[i]);
+        const float p = RNDF_A[i] * (in[i] - beta * RNDF_Q[i]) - beta * RNDF_R[i];
+        const float sg = -p > 0.0f ? 1.0f : (-p < 0.0f ? -1.0f : 0.0f);
+        out[i] = p + (sg * RNDF_M2[i] + RNDF_M2[i]);
+    }
+}
+
+static inline float rnd_fold_f32(const float o[4]) {
+    return ((o[0] * RNDF_MINV[0] - o[1] * RNDF_MINV[1]) + o[2] * RNDF_MINV[2]) - o[3] * RNDF_MINV[3];
+}
+
+static inline real gpu_rnd(vec4* n) {
+    rndf_init();
+    float s[4] = {(float)n->x, (float)n->y, (float)n->z, (float)n->w}, o[4];
+    schrage_step_f32(s, o);
+    n->x = o[0];
+    n->y = o[1];
+    n->z = o[2];
+    n->w = o[3];
+    const float d = rnd_fold_f32(o);
+    return (real)(d - floorf(d));
+}
+
+static inline uint32_t hash_cell(vec3 idx, real grid_scale, real hash_scale1, real hash_num) {
+    (void)hash_scale1;
+    rndf_init();
+    const float G = (float)grid_scale;
+    const float hs1 = 4194304.0f / G;
+    float s[4] = {(float)idx.x * hs1, (float)idx.y * hs1, (float)idx.z * hs1, (G * 0.5f) * hs1};
+    float o[4];
+    schrage_step_f32(s, o);
+    const float d = rnd_fold_f32(o);
+    const float hn = (float)hash_num;
+    float h = floorf((d - floorf(d)) * hn);
+    if (!(h >= 0.0f)) h = 0.0f;
+    if (h > hn - 1.0f) h = hn - 1.0f;
+    return (uint32_t)h;
+}
+#endif
 
 /* ------------------------------------------------------------------------------------------ */
 /* scene in the reference's packed form                                                        */

@@ -1,0 +1,184 @@
+"""Parity of the CUDA FP32 path with the CPU oracle at the full sizes of the benchmark workloads.
+
+The small cases of test_gpu_parity.py never reach the limits that only bind at scale: the ray
+queue and its 8^3 x 24 bins, the 4096-entry deferred eye list, the persistent refill of the
+traversal, atomic contention on a hash table at load factor 1.  Here, word for word against the
+oracle (the C restatement of glslppm.cpp:214-536 and the shaders, progressive.fs:98-142):
+
+* the 256x256 workload in full: the Cornell box with 2^16 photon slots, 64 passes, radius 0.5% of
+  the scene diagonal, on the default launch shapes and on the shapes the autotuner picks;
+* the 1024x1024 workload for 21 passes (three eye passes): 2^20 photon slots, autotuned shapes;
+* the 64-job batched workload (seeded Cornell variants) advanced 21 passes as one batch with
+  autotuned shapes: the job with the most triangles, a 1024x1024 job and a 2^19-photon job.
+
+Each case also states the radiance image's error against the double-precision oracle run with the
+same seed and the same random sequence (its GPURnd and cell hash are the single-precision ones), so
+the difference is the precision of the light transport alone; it must stay within 1% relative RMSE.
+"""
+import numpy as np
+import pytest
+
+import glslppm_gb300 as g
+from glslppm_gb300 import native as N
+from oracle.binding import Oracle
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["hit_position", "hit_reflectance", "hit_normal", "eye_rng", "hit_triangle", "hit_t", "emission_n",
+         "flux_radius", "photon_position", "photon_flux", "photon_direction", "photon_rng", "photon_hit",
+         "slot_winner", "slot_count"]
+
+
+def bits(a):
+    a = np.ascontiguousarray(a)
+    return a.view(np.uint32) if a.dtype.itemsize == 4 else a.view(np.uint8)
+
+
+def assert_same(what, gpu, cpu):
+    gb, cb = bits(gpu), bits(cpu)
+    assert gb.shape == cb.shape, f"{what}: shape {gb.shape} vs {cb.shape}"
+    bad = np.nonzero((gb.reshape(len(gb), -1) != cb.reshape(len(cb), -1)).any(axis=1))[0]
+    assert bad.size == 0, f"{what}: {bad.size} of {len(gb)} elements differ; first {bad[:5]}"
+
+
+def compare(read_state, read_image, frame_info, o, k, label):
+    for kind in KINDS:
+        assert_same(f"{label}: {kind} after {k} frames", read_state(kind), o.read_state(kind))
+    fg, fo = frame_info(), o.frame_info()
+    assert fg.frames == fo.frames == k
+    assert fg.photons_emitted == fo.photons_emitted and fg.num_photons_f32 == fo.num_photons_f32
+    assert fg.eye_samples == fo.eye_samples
+    assert fg.grid_scale == fo.grid_scale and fg.initial_radius == fo.initial_radius
+    assert list(fg.bbox_min) == list(fo.bbox_min) and list(fg.bbox_max) == list(fo.bbox_max)
+    assert fg.photon_segments == fo.photon_segments and fg.eye_segments == fo.eye_segments
+    img = read_image()
+    assert_same(f"{label}: radiance after {k} frames", img.reshape(-1, 3), o.read_image(0).astype(np.float32).reshape(-1, 3))
+    return img
+
+
+def precision_error(img32, cfg, scene, cam, frames):
+    """Relative RMSE and per-pixel relative error of an FP32 image against the FP64 oracle run with
+    the same seed and random sequence for the same number of frames."""
+    o64 = Oracle(cfg, scene, cam, fp64=True)
+    o64.run_frames(frames)
+    ref = o64.read_image(0)
+    o64.close()
+    a = img32.astype(np.float64)
+    rmse = float(np.sqrt(np.mean((a - ref) ** 2)) / np.sqrt(np.mean(ref ** 2)))
+    rel = np.abs(a - ref) / np.maximum(np.abs(ref), 1e-6)
+    return {"rel_rmse": rmse, "max_rel": float(rel.max()), "p99_rel": float(np.percentile(rel, 99)),
+            "frac_within_1e-3": float(np.mean(rel <= 1e-3))}
+
+
+def tuned_shapes(make, cycles=1):
+    """The autotuner's shapes, chosen on a scratch context/batch of the same workload (the tuner
+    advances the job it runs on, so the compared render starts fresh with the chosen shapes)."""
+    scratch = make()
+    best, _ = scratch.autotune(cycles)
+    scratch.close()
+    return best.as_dict()
+
+
+def test_256_workload_in_full_default_and_tuned_shapes():
+    import bench
+    sc, mesh = bench.cornell_mesh()
+    cfg = g.default_config(256, radius_rule=N.RADIUS_DIAGONAL, radius_fraction=0.005)
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 256, 256, sc.fov)
+    scene = mesh.scene()
+
+    def make():
+        r = g.Renderer(cfg)
+        r.upload_scene(mesh)
+        r.set_camera(cam)
+        return r
+
+    r = make()
+    o = Oracle(cfg, scene, cam)
+    done = 0
+    for k in (1, 10, 11, 64):
+        r.run_passes(k - done)
+        o.run_frames(k - done)
+        done = k
+        r.synchronize()
+        img = compare(r.read_state, r.read_image, r.frame_info, o, k, "default shapes")
+    r.close()
+    shapes = tuned_shapes(make)
+    t = make()
+    t.set_tuning(**shapes)
+    t.run_passes(64)
+    t.synchronize()
+    compare(t.read_state, t.read_image, t.frame_info, o, 64, f"tuned shapes {shapes}")
+    t.close()
+    err = precision_error(img, cfg, scene, cam, 64)
+    print("256x256, 64 passes, FP32 vs FP64 oracle:", err)
+    assert err["rel_rmse"] <= 0.01, err
+
+
+def test_1024_workload_21_passes_tuned_shapes():
+    import bench
+    sc, mesh = bench.cornell_mesh()
+    cfg = g.default_config(1024, radius_rule=N.RADIUS_DIAGONAL, radius_fraction=0.005)
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 1024, 1024, sc.fov)
+    scene = mesh.scene()
+
+    def make():
+        r = g.Renderer(cfg)
+        r.upload_scene(mesh)
+        r.set_camera(cam)
+        return r
+
+    shapes = tuned_shapes(make)
+    r = make()
+    r.set_tuning(**shapes)
+    o = Oracle(cfg, scene, cam)
+    done = 0
+    for k in (1, 11, 21):
+        r.run_passes(k - done)
+        o.run_frames(k - done)
+        done = k
+        r.synchronize()
+        img = compare(r.read_state, r.read_image, r.frame_info, o, k, f"tuned shapes {shapes}")
+    r.close()
+    err = precision_error(img, cfg, scene, cam, 21)
+    print("1024x1024, 21 passes, FP32 vs FP64 oracle:", err)
+    assert err["rel_rmse"] <= 0.01, err
+
+
+def test_batched_workload_jobs_match_the_oracle():
+    import bench
+    jobs = bench.build_jobs(64)
+
+    def make():
+        b = g.Batch(precision=N.PRECISION_FP32, max_jobs=len(jobs))
+        ids = [b.add_job(cfg, m, cam) for (_, m, cfg, cam) in jobs]
+        b._ids = ids
+        return b
+
+    shapes = tuned_shapes(make)
+    b = make()
+    b.set_tuning(**shapes)
+    K = 21
+    b.run_passes(K)
+    b.synchronize()
+    # the job with the most triangles, a 1024x1024 job and a 2^19-photon job (distinct)
+    picks = [max(range(len(jobs)), key=lambda i: jobs[i][0].scene.num_triangles)]
+    for pred in (lambda c: c.width == 1024, lambda c: c.photon_width * c.photon_height == 1 << 19):
+        i = next((i for i, j in enumerate(jobs) if pred(j[2]) and i not in picks), None)
+        if i is not None:
+            picks.append(i)
+    assert len(picks) >= 3
+    for i in picks:
+        s, m, cfg, cam = jobs[i]
+        jid = b._ids[i]
+        o = Oracle(cfg, m.scene(), cam)
+        o.run_frames(K)
+        label = (f"batch job {i} ({s.scene.num_triangles} triangles, {cfg.width}x{cfg.height}, "
+                 f"{cfg.photon_width}x{cfg.photon_height} photons, shapes {shapes})")
+        img = compare(lambda kind: b.read_state(jid, kind), lambda: b.read_image(jid), lambda: b.frame_info(jid), o,
+                      K, label)
+        o.close()
+        if i == picks[0]:
+            err = precision_error(img, cfg, m.scene(), cam, K)
+            print(f"{label}: FP32 vs FP64 oracle:", err)
+            assert err["rel_rmse"] <= 0.01, err
+    b.close()
