@@ -159,7 +159,7 @@ int sppm_read_state(sppm_ctx* c, uint32_t kind, void* dst, size_t bytes) {
     SPPM_CK(cudaSetDevice(c->rt.device));
     SPPM_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->rt.stream));
     const int st = c->rt.synchronize();
-    if (st == SPPM_OK) state_to_host_layout(kind, dst, bytes);
+    if (st == SPPM_OK) state_to_host_layout(kind, dst, bytes, c->job.cfg.flags);
     return st;
 }
 
@@ -333,12 +333,44 @@ void sppm_host_free(void* ptr) {
     if (ptr) cudaFreeHost(ptr);
 }
 
+int sppm_debug_photon_rays(sppm_ctx* c, float* org, float* dir, uint32_t* photon, size_t capacity, size_t* count) {
+    if (!c || !count) return fail(SPPM_ERR_ARG, "null argument");
+    if (c->rt.flags & SPPM_FLAG_FUSED_PHOTON)
+        return fail(SPPM_ERR_STATE, "the fused photon kernel keeps no ray queue");
+    SPPM_CK(cudaSetDevice(c->rt.device));
+    SPPM_CK(cudaStreamSynchronize(c->rt.stream));
+    const RayQueue& q = c->rt.queue;
+    uint32_t n = 0;
+    if (q.counters) SPPM_CK(cudaMemcpy(&n, q.counters, 4, cudaMemcpyDeviceToHost));
+    *count = n;
+    if (!org && !dir && !photon) return SPPM_OK;  // size query
+    if (!org || !dir || !photon) return fail(SPPM_ERR_ARG, "null argument");
+    if (capacity < n) return fail(SPPM_ERR_ARG, "the last pass traced %u photon rays; capacity %zu", n, capacity);
+    std::vector<float4> o(n), d(n);
+    if (n) {
+        SPPM_CK(cudaMemcpy(o.data(), q.org, (size_t)n * sizeof(float4), cudaMemcpyDeviceToHost));
+        SPPM_CK(cudaMemcpy(d.data(), q.dir, (size_t)n * sizeof(float4), cudaMemcpyDeviceToHost));
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        org[3 * i] = o[i].x, org[3 * i + 1] = o[i].y, org[3 * i + 2] = o[i].z;
+        dir[3 * i] = d[i].x, dir[3 * i + 1] = d[i].y, dir[3 * i + 2] = d[i].z;
+        uint32_t g;
+        memcpy(&g, &o[i].w, 4);
+        photon[i] = g;
+    }
+    return SPPM_OK;
+}
+
 int sppm_debug_trace(sppm_ctx* c, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
                      int32_t* tri, float* t) {
     if (!c || !org || !dir || !tri || !t) return fail(SPPM_ERR_ARG, "null argument");
     if (!c->job.have_scene) return fail(SPPM_ERR_STATE, "upload a scene first");
-    if (mode < 0 || mode > 2)
-        return fail(SPPM_ERR_ARG, "mode must be 0 (thread per ray), 1 (warp per ray) or 2 (block per ray)");
+    if (mode < 0 || mode > 3)
+        return fail(SPPM_ERR_ARG,
+                    "mode must be 0 (thread per ray), 1 (warp per ray), 2 (block per ray) or 3 (4-wide quantised)");
+    if (mode == 3 && !c->job.desc.scene.nodes4)
+        return fail(SPPM_ERR_STATE, "mode 3 traces the mixed-precision 4-wide BVH: create the context with "
+                                    "SPPM_PRECISION_MIXED");
     if (n == 0) return SPPM_OK;
     if (n > (1u << 26)) return fail(SPPM_ERR_ARG, "n too large");
     SPPM_CK(cudaSetDevice(c->rt.device));

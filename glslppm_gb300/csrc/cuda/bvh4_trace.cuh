@@ -4,7 +4,9 @@
 // Node4Dev: w[0] = origin xyz, exponent bytes x|y|z|child count; w[1] = the four child links (>= 0
 // node, < 0 ~triangle, INT32_MIN empty); w[2] = lower box bytes x,y,z and upper x; w[3] = upper
 // y,z.  A child box is origin + byte * 2^(exponent-127) per axis, rounded outward when the tree
-// was built, so the slab tests are conservative.
+// was built; the slab distances are widened by a bound on their rounding, and triangles are
+// tested with the exact path's arithmetic (tri_test_exact), so the closest hit -- triangle, t and
+// barycentrics -- is the exact traversal's except where two triangles give the same t.
 #pragma once
 
 #include "device_common.cuh"
@@ -31,24 +33,85 @@ __device__ __forceinline__ float byte_f(uint32_t w, uint32_t sel) {
     return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f;
 }
 
-// slab distances of child K's box: plane = origin + byte * 2^e, so its distance along the ray is
-// byte * (2^e / d) + (origin - o) / d = fmaf(byte, A, B) with the per-node A = 2^e * (1/d) (exact:
-// a power-of-two scale) and B = fmaf(origin, 1/d, -o/d)
+// ---- conservative slab tests over the quantised boxes ------------------------------------------
+// A child plane is P = origin + q * 2^e (q a byte); its distance along the ray is computed as
+//     fma(q, A, B -+ E),  A = 2^e * r (exact scaling of r = fl(1/d)),  B = fma(origin, r, n),
+//     n = fl(-o * r).
+// Against the exact distance (P' - o) / d to the enclosing plane P' = fl(origin + q 2^e) that the
+// builder checked, the roundings of r, n, B, B -+ E, the final fma and P' add at most
+// 5 u S (1 + O(u)), u = 2^-24, with S = (|origin| + |o| + 255 * 2^e) / |d|
+// (each rounding's error is u times a term bounded by S).  E = 16 u S', S' the same sum computed
+// from |r|, |n| and |A| (relative error a few u), exceeds that bound, so the near distance is never
+// above the exact entry and the far distance never below the exact exit: a box the exact
+// arithmetic enters is never culled (Ize, "Robust BVH Ray Traversal", JCGT 2013, applies the same
+// argument to the plain slab test).  The near plane of each axis is chosen by the sign of the
+// direction once per ray, so a child needs no per-axis min/max.
+constexpr float kSlabErr = 9.5367431640625e-07f;  // 16 * 2^-24
+// a box entered later than the closest hit so far by less than this relative margin is still
+// visited: the exact triangle test's own rounding may put the winner's t just below its box entry
+constexpr float kCullMargin = 1.000244140625f;    // 1 + 2^-12
+
+// (|r| and |n| are free operand modifiers; r < 0 selects the upper bound as the near plane)
+struct Ray4 {
+    float ox, oy, oz, dx, dy, dz;
+    float rx, ry, rz, nx, ny, nz;     // r = 1/slab_dir(d), n = -o * r
+};
+
+__device__ __forceinline__ void ray4_setup(Ray4& R, float ox, float oy, float oz, float dx, float dy, float dz) {
+    R.ox = ox, R.oy = oy, R.oz = oz, R.dx = dx, R.dy = dy, R.dz = dz;
+    R.rx = 1.0f / slab_dir(dx), R.ry = 1.0f / slab_dir(dy), R.rz = 1.0f / slab_dir(dz);
+    R.nx = -ox * R.rx, R.ny = -oy * R.ry, R.nz = -oz * R.rz;
+}
+
+// the node's per-axis slab operands for one ray
+struct Slab4 {
+    float Ax, Ay, Az;        // 2^e * r
+    float Nx, Ny, Nz;        // B - E (near planes)
+    float Fx, Fy, Fz;        // B + E (far planes)
+    uint32_t nwx, nwy, nwz;  // words holding the near-plane bytes of the four children
+    uint32_t fwx, fwy, fwz;  // ... and the far-plane bytes
+};
+
+__device__ __forceinline__ float slab_err(float origin, float r, float n, float A) {
+    return kSlabErr * fmaf(255.0f, fabsf(A), fmaf(fabsf(origin), fabsf(r), fabsf(n)));
+}
+
+__device__ __forceinline__ void slab4_setup(Slab4& S, const Ray4& R, const float4& w0, const float4& w2,
+                                            const float4& w3) {
+    const uint32_t eb = __float_as_uint(w0.w);
+    S.Ax = node_scale(eb & 0xFF) * R.rx;
+    S.Ay = node_scale((eb >> 8) & 0xFF) * R.ry;
+    S.Az = node_scale((eb >> 16) & 0xFF) * R.rz;
+    const float Bx = fmaf(w0.x, R.rx, R.nx), By = fmaf(w0.y, R.ry, R.ny), Bz = fmaf(w0.z, R.rz, R.nz);
+    const float Ex = slab_err(w0.x, R.rx, R.nx, S.Ax);
+    const float Ey = slab_err(w0.y, R.ry, R.ny, S.Ay);
+    const float Ez = slab_err(w0.z, R.rz, R.nz, S.Az);
+    S.Nx = Bx - Ex, S.Ny = By - Ey, S.Nz = Bz - Ez;
+    S.Fx = Bx + Ex, S.Fy = By + Ey, S.Fz = Bz + Ez;
+    // lower bytes: x w2.x, y w2.y, z w2.z; upper bytes: x w2.w, y w3.x, z w3.y
+    const uint32_t lx = __float_as_uint(w2.x), ly = __float_as_uint(w2.y), lz = __float_as_uint(w2.z);
+    const uint32_t hx = __float_as_uint(w2.w), hy = __float_as_uint(w3.x), hz = __float_as_uint(w3.y);
+    const bool negx = R.rx < 0.0f, negy = R.ry < 0.0f, negz = R.rz < 0.0f;
+    S.nwx = negx ? hx : lx, S.fwx = negx ? lx : hx;
+    S.nwy = negy ? hy : ly, S.fwy = negy ? ly : hy;
+    S.nwz = negz ? hz : lz, S.fwz = negz ? lz : hz;
+}
+
+// conservative entry distance of child K (clamped at 0) and whether the ray may hit its box before
+// tcull (the closest hit so far times kCullMargin)
 template <int K>
-__device__ __forceinline__ void child_box(const float4& w2, const float4& w3, float Ax, float Ay, float Az, float Bx,
-                                          float By, float Bz, float tbest, float& tn, bool& hit) {
+__device__ __forceinline__ void child_box(const Slab4& S, float tcull, float& tn, bool& hit) {
     constexpr uint32_t sel = 0x7650u | (uint32_t)K;  // byte K of the word into byte 0, 0x4B into byte 3
-    const float ax = fmaf(byte_f(__float_as_uint(w2.x), sel), Ax, Bx);
-    const float ay = fmaf(byte_f(__float_as_uint(w2.y), sel), Ay, By);
-    const float az = fmaf(byte_f(__float_as_uint(w2.z), sel), Az, Bz);
-    const float bx = fmaf(byte_f(__float_as_uint(w2.w), sel), Ax, Bx);
-    const float by = fmaf(byte_f(__float_as_uint(w3.x), sel), Ay, By);
-    const float bz = fmaf(byte_f(__float_as_uint(w3.y), sel), Az, Bz);
-    const float t0 = fmaxf(fmax3(fminf(ax, bx), fminf(ay, by), fminf(az, bz)), 0.0f);
-    // the far bound widened by a few ulps so that rounding never rejects a grazing hit
-    const float t1 = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fmaxf(az, bz)) * 1.00000036f;
+    const float nx = fmaf(byte_f(S.nwx, sel), S.Ax, S.Nx);
+    const float ny = fmaf(byte_f(S.nwy, sel), S.Ay, S.Ny);
+    const float nz = fmaf(byte_f(S.nwz, sel), S.Az, S.Nz);
+    const float fx = fmaf(byte_f(S.fwx, sel), S.Ax, S.Fx);
+    const float fy = fmaf(byte_f(S.fwy, sel), S.Ay, S.Fy);
+    const float fz = fmaf(byte_f(S.fwz, sel), S.Az, S.Fz);
+    const float t0 = fmaxf(fmax3(nx, ny, nz), 0.0f);
+    const float t1 = fmin3(fx, fy, fz);
     tn = t0;
-    hit = t0 <= t1 && t0 <= tbest;
+    hit = t0 <= t1 && t0 <= tcull;
 }
 
 __device__ __forceinline__ void cswap(float& ta, int32_t& ca, float& tb, int32_t& cb) {
@@ -71,8 +134,8 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
     h.t = tmax0;
     h.tri = -1;
     h.bu = h.bv = h.bw = 0.0f;
-    const float rx = 1.0f / slab_dir(dir.x), ry = 1.0f / slab_dir(dir.y), rz = 1.0f / slab_dir(dir.z);
-    const float nx = -org.x * rx, ny = -org.y * ry, nz = -org.z * rz;
+    Ray4 R;
+    ray4_setup(R, org.x, org.y, org.z, dir.x, dir.y, dir.z);
     int32_t stack_node[kStack];
     float stack_t[kStack];
     int sp = 0;
@@ -87,19 +150,18 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
         float4 w0, w1, w2, w3;
         ldg32(np, w0, w1);
         ldg32(np + 2, w2, w3);
-        const uint32_t eb = __float_as_uint(w0.w);
-        const float sx = node_scale(eb & 0xFF), sy = node_scale((eb >> 8) & 0xFF), sz = node_scale((eb >> 16) & 0xFF);
-        const int cnt = (int)(eb >> 24);
+        const int cnt = (int)(__float_as_uint(w0.w) >> 24);
         int32_t ch[4] = {__float_as_int(w1.x), __float_as_int(w1.y), __float_as_int(w1.z), __float_as_int(w1.w)};
-        // slab test of the (up to) four children
+        // conservative slab test of the (up to) four children
         float tnear[4];
         bool hit[4];
-        const float Ax = sx * rx, Ay = sy * ry, Az = sz * rz;
-        const float Bx = fmaf(w0.x, rx, nx), By = fmaf(w0.y, ry, ny), Bz = fmaf(w0.z, rz, nz);
-        child_box<0>(w2, w3, Ax, Ay, Az, Bx, By, Bz, h.t, tnear[0], hit[0]);
-        child_box<1>(w2, w3, Ax, Ay, Az, Bx, By, Bz, h.t, tnear[1], hit[1]);
-        child_box<2>(w2, w3, Ax, Ay, Az, Bx, By, Bz, h.t, tnear[2], hit[2]);
-        child_box<3>(w2, w3, Ax, Ay, Az, Bx, By, Bz, h.t, tnear[3], hit[3]);
+        Slab4 S;
+        slab4_setup(S, R, w0, w2, w3);
+        const float tcull = h.t * kCullMargin;
+        child_box<0>(S, tcull, tnear[0], hit[0]);
+        child_box<1>(S, tcull, tnear[1], hit[1]);
+        child_box<2>(S, tcull, tnear[2], hit[2]);
+        child_box<3>(S, tcull, tnear[3], hit[3]);
         // leaf children: their triangles in child order (a closer hit shrinks the search), one copy
         // of the test in a loop over the leaves
         uint32_t leaves = 0;
@@ -118,21 +180,9 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
             const float4 a = __ldg(&tri_isect[(size_t)tri * 3 + 0]);
             const float4 b = __ldg(&tri_isect[(size_t)tri * 3 + 1]);
             const float4 c = __ldg(&tri_isect[(size_t)tri * 3 + 2]);
-            const f3 e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
-            const float pvx = dir.y * e1.z - dir.z * e1.y, pvy = dir.z * e1.x - dir.x * e1.z,
-                        pvz = dir.x * e1.y - dir.y * e1.x;
-            const float det = e0.x * pvx + e0.y * pvy + e0.z * pvz;
-            if (!PHOTON && cull && !(det > 1e-10f)) continue;
-            const float inv = 1.0f / det;
-            const float tvx = org.x - a.x, tvy = org.y - a.y, tvz = org.z - a.z;
-            const float u = (tvx * pvx + tvy * pvy + tvz * pvz) * inv;
-            if (!(u >= 0.0f && u <= 1.0f)) continue;
-            const float qx = tvy * e0.z - tvz * e0.y, qy = tvz * e0.x - tvx * e0.z, qz = tvx * e0.y - tvy * e0.x;
-            const float v = (dir.x * qx + dir.y * qy + dir.z * qz) * inv;
-            const float t = (e1.x * qx + e1.y * qy + e1.z * qz) * inv;
-            const float w = 1.0f - u - v;
-            if (v >= 0.0f && w >= 0.0f && t >= 0.0f && t < h.t) {
-                h.t = t;
+            float tt, u, v, w;
+            if (tri_test_exact(a, b, c, org, dir, !PHOTON && cull, h.t, tt, u, v, w)) {
+                h.t = tt;
                 h.tri = tri;
                 h.bu = v;
                 h.bv = w;
@@ -142,9 +192,10 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
         // internal children hit before the closest hit so far, sorted near to far: the nearest
         // is next, the others go on the stack farthest first
         const float inf = __int_as_float(0x7f800000);
+        const float tcull2 = h.t * kCullMargin;
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            if (!(hit[k] && tnear[k] <= h.t)) tnear[k] = inf;
+            if (!(hit[k] && tnear[k] <= tcull2)) tnear[k] = inf;
         cswap(tnear[0], ch[0], tnear[1], ch[1]);
         cswap(tnear[2], ch[2], tnear[3], ch[3]);
         cswap(tnear[0], ch[0], tnear[2], ch[2]);
@@ -165,7 +216,7 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
         bool found = false;
         while (sp > 0) {
             sp--;
-            if (stack_t[sp] <= h.t) {
+            if (stack_t[sp] <= h.t * kCullMargin) {
                 cur = stack_node[sp];
                 found = true;
                 break;

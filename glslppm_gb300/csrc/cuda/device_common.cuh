@@ -234,6 +234,26 @@ __device__ __forceinline__ f3 refract(f3 i, f3 n, float eta) {
 __device__ __forceinline__ float signf(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
 __device__ __forceinline__ float fractf(float x) { return xsub(x, floorf(x)); }
 
+// ---- the triangle test of raytrace() (eyeraytrace.fs:200-243, photontrace.fs:196-236) --------
+// Moller-Trumbore on the packed operands (a = v0 | e0.x, b = e0.yz | e1.xy, c.x = e1.z), every
+// operation correctly rounded in the shaders' order, so a triangle's t, u, v and w are the same
+// numbers wherever this is called (plain and mixed traversals alike).  Returns true when the
+// triangle is hit at 0 <= t < tbest; cull: reject det <= 1e-10 (back faces of a first eye bounce).
+__device__ __forceinline__ bool tri_test_exact(const float4& a, const float4& b, const float4& c, f3 org, f3 dir,
+                                               bool cull, float tbest, float& tt, float& u, float& v, float& w) {
+    const f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
+    const f3 pv = cross(dir, e1);
+    const float det = dot(e0, pv);
+    if (cull && !(det > 1e-10f)) return false;
+    const f3 tv = sub(org, v0);
+    const f3 qv = cross(tv, e0);
+    u = xdiv(dot(tv, pv), det);
+    v = xdiv(dot(dir, qv), det);
+    tt = xdiv(dot(e1, qv), det);
+    w = xsub(xsub(1.0f, u), v);
+    return u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt < tbest;
+}
+
 // ---- GPURnd (eyeraytrace.fs:326-347) and the cell hash (hash.fs:21-48) ---------------------
 // lane constants q, r, a, m and the single-precision 1/m, 1/q, m/2 the shaders derive from them
 #define SPPM_RND_LANE(i, q, r, a, m, qinv, minv)                                                \

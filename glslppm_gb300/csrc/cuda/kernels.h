@@ -49,7 +49,7 @@ uint32_t trace_photons_blocks_per_sm();
 void launch_trace_photons4(const LaunchSet& ls, const RayQueue& q, uint32_t persistent_blocks, cudaStream_t s);
 uint32_t trace_photons4_blocks_per_sm();
 void launch_slot_fill(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
-void launch_gather_mixed(const LaunchSet& ls, uint32_t block, cudaStream_t s);
+void launch_gather_mixed(const LaunchSet& ls, uint32_t block, bool any_fp64, cudaStream_t s);
 void launch_resolve_mixed(const LaunchSet& ls, uint32_t display, cudaStream_t s);
 void launch_gather_fp32(const LaunchSet& ls, uint32_t block, cudaStream_t s);
 void launch_resolve_fp32(const LaunchSet& ls, uint32_t display, cudaStream_t s);

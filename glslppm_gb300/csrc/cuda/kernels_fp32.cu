@@ -102,24 +102,14 @@ __device__ __forceinline__ Hit trace_exact(const DevScene& s, f3 org, f3 dir, bo
             const float4 a = __ldg(&s.tri_isect[(size_t)t * 3 + 0]);
             const float4 b = __ldg(&s.tri_isect[(size_t)t * 3 + 1]);
             const float4 c = __ldg(&s.tri_isect[(size_t)t * 3 + 2]);
-            const f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
-            const f3 pv = cross(dir, e1);
-            const float det = dot(e0, pv);
-            if (PHOTON || !cull || det > 1e-10f) {
-                const f3 tv = sub(org, v0);
-                const f3 qv = cross(tv, e0);
-                const float u = xdiv(dot(tv, pv), det);
-                const float v = xdiv(dot(dir, qv), det);
-                const float tt = xdiv(dot(e1, qv), det);
-                const float w = xsub(xsub(1.0f, u), v);
-                if (u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt < h.t) {
-                    h.t = tt;
-                    h.tri = t;
-                    h.mat = __float_as_int(c.y);
-                    h.bu = v;
-                    h.bv = w;
-                    h.bw = u;
-                }
+            float tt, u, v, w;
+            if (tri_test_exact(a, b, c, org, dir, !PHOTON && cull, h.t, tt, u, v, w)) {
+                h.t = tt;
+                h.tri = t;
+                h.mat = __float_as_int(c.y);
+                h.bu = v;
+                h.bv = w;
+                h.bw = u;
             }
         }
         const int32_t next = hit ? i + 1 : __float_as_int(A.w);
@@ -1742,7 +1732,9 @@ __global__ void k_fpmath(int fn, const float* x, const float* y, float* out, uin
 }
 
 // single rays through the exact traversal: mode 0 one thread per ray (trace_exact), mode 1 one
-// warp per ray (coop_trace_exact); photon rays skip emitters, eye rays may cull back faces
+// warp per ray (coop_trace_exact), mode 2 one block per ray (block_trace_exact), mode 3 the mixed
+// path's 4-wide quantised traversal one per thread (trace4); photon rays skip emitters, eye rays
+// may cull back faces
 template <bool PHOTON>
 __global__ void __launch_bounds__(1024) k_debug_trace(DevScene s, const float* org, const float* dir, uint32_t n,
                                                      int cull, int mode, int32_t* tri, float* t, uint32_t* err) {
@@ -1764,6 +1756,15 @@ __global__ void __launch_bounds__(1024) k_debug_trace(DevScene s, const float* o
         if (i >= n) return;
         const Hit h = trace_exact<PHOTON>(s, mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]),
                                           mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]), cull != 0, e);
+        tri[i] = h.tri;
+        t[i] = h.t;
+    } else if (mode == 3) {
+        // the mixed path's 4-wide quantised traversal (the eye pass's trace4)
+        const uint32_t i = grid_tid();
+        if (i >= n) return;
+        const Hit4 h = trace4<PHOTON>(s.nodes4, s.tri_isect, mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]),
+                                      mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]), cull != 0,
+                                      PHOTON ? 1.0e30f : 1.0e20f, e);
         tri[i] = h.tri;
         t[i] = h.t;
     } else {
@@ -1910,7 +1911,8 @@ void launch_debug_trace(const DevScene& sc, const float* org, const float* dir, 
                         int mode, int32_t* tri, float* t, uint32_t* err, cudaStream_t s) {
     if (!n) return;
     const uint32_t threads = mode == 2 ? kBlockWalk : 128;
-    const uint32_t blocks = mode == 0 ? blocks_for(n, 128) : (mode == 1 ? blocks_for(n, 4) : (n < 256 ? n : 256u));
+    const uint32_t blocks =
+        (mode == 0 || mode == 3) ? blocks_for(n, 128) : (mode == 1 ? blocks_for(n, 4) : (n < 256 ? n : 256u));
     if (photon) k_debug_trace<true><<<blocks, threads, 0, s>>>(sc, org, dir, n, cull, mode, tri, t, err);
     else k_debug_trace<false><<<blocks, threads, 0, s>>>(sc, org, dir, n, cull, mode, tri, t, err);
 }

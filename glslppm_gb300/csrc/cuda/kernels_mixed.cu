@@ -2,10 +2,11 @@
 //
 // What changes against the plain FP32 path, and why:
 //  * photon segments are traced through a 4-wide BVH whose child boxes are 8-bit outward-rounded
-//    offsets (64-byte nodes: one node fetch tests four boxes), closest-child-first with a stack,
-//    slab tests and the triangle test in fused multiply-adds with one reciprocal per triangle --
-//    the boxes are conservative and the triangle test is single precision, so the reported
-//    triangle is the true closest one up to ties at equal distance;
+//    offsets (64-byte nodes: one node fetch tests four boxes), closest-child-first with a stack;
+//    the slab distances are fused multiply-adds widened by a bound on their rounding (never
+//    culling a box the exact arithmetic enters) and triangles are tested with the plain path's
+//    arithmetic, so the reported triangle, t and barycentrics are the exact traversal's except
+//    where two triangles give the same t;
 //  * the photon a hash slot keeps is stored once per slot as a 32-byte record -- cell (int16 x3),
 //    position inside the cell (unorm16 x3), flux (FP16 x3, scaled by 1/(light area * pi)),
 //    direction (snorm16 x3) and the slot's photon count -- so the gather reads one sector per cell
@@ -53,7 +54,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
     uint32_t idx = kNeed;
     const Node4Dev* nodes = nullptr;
     const float4* tri_isect = nullptr;
-    float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, rx = 0, ry = 0, rz = 0, nx = 0, ny = 0, nz = 0;
+    Ray4 R;
+    ray4_setup(R, 0.0f, 0.0f, 0.0f, 1.0f, 1.0f, 1.0f);
     float ht = 1.0e30f, hbu = 0, hbv = 0, hbw = 0;
     int32_t htri = -1, cur = 0;
     int sp = 0;
@@ -83,9 +85,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
                     const DevScene& S = ls.jobs[ls.job_ids[job_k]].scene;
                     nodes = S.nodes4;
                     tri_isect = S.tri_isect;
-                    ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
-                    rx = 1.0f / slab_dir(dx), ry = 1.0f / slab_dir(dy), rz = 1.0f / slab_dir(dz);
-                    nx = -ox * rx, ny = -oy * ry, nz = -oz * rz;
+                    ray4_setup(R, o.x, o.y, o.z, d.x, d.y, d.z);
                     ht = 1.0e30f;
                     htri = -1;
                     hbu = hbv = hbw = 0.0f;
@@ -109,17 +109,16 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
             float4 w0, w1, w2, w3;
             ldg32(np, w0, w1);
             ldg32(np + 2, w2, w3);
-            const uint32_t eb = __float_as_uint(w0.w);
-            const float sx = node_scale(eb & 0xFF), sy = node_scale((eb >> 8) & 0xFF), sz = node_scale((eb >> 16) & 0xFF);
-            const int cnt = (int)(eb >> 24);
+            const int cnt = (int)(__float_as_uint(w0.w) >> 24);
             float t[4];
             bool hit[4];
-            const float Ax = sx * rx, Ay = sy * ry, Az = sz * rz;
-            const float Bx = fmaf(w0.x, rx, nx), By = fmaf(w0.y, ry, ny), Bz = fmaf(w0.z, rz, nz);
-            child_box<0>(w2, w3, Ax, Ay, Az, Bx, By, Bz, ht, t[0], hit[0]);
-            child_box<1>(w2, w3, Ax, Ay, Az, Bx, By, Bz, ht, t[1], hit[1]);
-            child_box<2>(w2, w3, Ax, Ay, Az, Bx, By, Bz, ht, t[2], hit[2]);
-            child_box<3>(w2, w3, Ax, Ay, Az, Bx, By, Bz, ht, t[3], hit[3]);
+            Slab4 S;
+            slab4_setup(S, R, w0, w2, w3);
+            const float tcull = ht * kCullMargin;
+            child_box<0>(S, tcull, t[0], hit[0]);
+            child_box<1>(S, tcull, t[1], hit[1]);
+            child_box<2>(S, tcull, t[2], hit[2]);
+            child_box<3>(S, tcull, t[3], hit[3]);
             int32_t c[4] = {__float_as_int(w1.x), __float_as_int(w1.y), __float_as_int(w1.z), __float_as_int(w1.w)};
             // leaf children hit: their triangles, in child order (photons pass through emitters);
             // one copy of the test in a loop over the leaves, so a warp runs it as many times as
@@ -140,17 +139,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
                 const float4 a = __ldg(&tri_isect[(size_t)code * 3 + 0]);
                 const float4 b = __ldg(&tri_isect[(size_t)code * 3 + 1]);
                 const float4 cc = __ldg(&tri_isect[(size_t)code * 3 + 2]);
-                const float e0x = a.w, e0y = b.x, e0z = b.y, e1x = b.z, e1y = b.w, e1z = cc.x;
-                const float pvx = dy * e1z - dz * e1y, pvy = dz * e1x - dx * e1z, pvz = dx * e1y - dy * e1x;
-                const float det = e0x * pvx + e0y * pvy + e0z * pvz;
-                const float inv = 1.0f / det;
-                const float tvx = ox - a.x, tvy = oy - a.y, tvz = oz - a.z;
-                const float u = (tvx * pvx + tvy * pvy + tvz * pvz) * inv;
-                const float qx = tvy * e0z - tvz * e0y, qy = tvz * e0x - tvx * e0z, qz = tvx * e0y - tvy * e0x;
-                const float v = (dx * qx + dy * qy + dz * qz) * inv;
-                const float tt = (e1x * qx + e1y * qy + e1z * qz) * inv;
-                const float w = 1.0f - u - v;
-                if (u >= 0.0f && v >= 0.0f && w >= 0.0f && tt >= 0.0f && tt < ht) {
+                float tt, u, v, w;
+                if (tri_test_exact(a, b, cc, mk(R.ox, R.oy, R.oz), mk(R.dx, R.dy, R.dz), false, ht, tt, u, v, w)) {
                     ht = tt;
                     htri = code;
                     hbu = v;
@@ -159,9 +149,10 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
                 }
             }
             // internal children hit before the current closest hit, sorted near to far
+            const float tcull2 = ht * kCullMargin;
 #pragma unroll
             for (int k = 0; k < 4; k++)
-                if (!(hit[k] && t[k] <= ht)) t[k] = __int_as_float(0x7f800000);
+                if (!(hit[k] && t[k] <= tcull2)) t[k] = __int_as_float(0x7f800000);
             cswap(t[0], c[0], t[1], c[1]);
             cswap(t[2], c[2], t[3], c[3]);
             cswap(t[0], c[0], t[2], c[2]);
@@ -185,7 +176,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
             while (sp > 0) {
                 sp--;
                 const float st_t = sp < kSmemStack ? s_t[sp][tid] : l_t[sp - kSmemStack];
-                if (st_t <= ht) {
+                if (st_t <= ht * kCullMargin) {
                     cur = sp < kSmemStack ? s_node[sp][tid] : l_node[sp - kSmemStack];
                     found = true;
                     break;
@@ -260,7 +251,9 @@ __device__ __forceinline__ float2 df_add(float2 x, float2 y) {
     return df_fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(x.y, y.y)));
 }
 
-// progressive.fs with the slot records, FP32 flux gathering and double-float statistics
+// progressive.fs with the slot records, FP32 flux gathering and double-float statistics (ANY_F64:
+// the variant launched when some job of the launch keeps IEEE double statistics)
+template <bool ANY_F64>
 __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
     const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
     if (gi >= ls.total) return;
@@ -276,11 +269,26 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
         st->photon_segments += st->segments_frame;
     }
     const float2 zero = make_float2(0.0f, 0.0f);
-    float2 N = J.px.stat_n[p];
-    float2 R2 = frame == 0 ? df_two_prod(st->r0, st->r0) : J.px.stat_r2[p];
-    float2 tx = frame == 0 ? zero : J.px.stat_tau[3 * (size_t)p + 0];
-    float2 ty = frame == 0 ? zero : J.px.stat_tau[3 * (size_t)p + 1];
-    float2 tz = frame == 0 ? zero : J.px.stat_tau[3 * (size_t)p + 2];
+    // the statistics' 8-byte words hold double-float pairs, or IEEE doubles for jobs with
+    // SPPM_FLAG_FP64_STATISTICS
+    const bool f64 = ANY_F64 && (J.flags & SPPM_FLAG_FP64_STATISTICS) != 0;
+    float2 N = zero, R2 = zero, tx = zero, ty = zero, tz = zero;
+    double R2d64 = 0.0, T64[3] = {0.0, 0.0, 0.0};
+    if (f64) {
+        R2d64 = frame == 0 ? (double)st->r0 * (double)st->r0 : reinterpret_cast<const double*>(J.px.stat_r2)[p];
+        if (frame != 0) {
+            const double* Td = reinterpret_cast<const double*>(J.px.stat_tau) + 3 * (size_t)p;
+            T64[0] = Td[0], T64[1] = Td[1], T64[2] = Td[2];
+        }
+        R2 = make_float2((float)R2d64, 0.0f);
+        N = make_float2((float)reinterpret_cast<const double*>(J.px.stat_n)[p], 0.0f);
+    } else {
+        N = J.px.stat_n[p];
+        R2 = frame == 0 ? df_two_prod(st->r0, st->r0) : J.px.stat_r2[p];
+        tx = frame == 0 ? zero : J.px.stat_tau[3 * (size_t)p + 0];
+        ty = frame == 0 ? zero : J.px.stat_tau[3 * (size_t)p + 1];
+        tz = frame == 0 ? zero : J.px.stat_tau[3 * (size_t)p + 2];
+    }
     if (J.px.tri[p] >= 0) {
         const float G = st->grid_scale;
         const float hs1 = st->hash_scale1;
@@ -320,17 +328,39 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
             fz += fb_.x * cf;
             M += cf;
         }
+        const float s = J.scene.flux_unscale * 0.318309886f;
+        if (f64) {
+            // IEEE double statistics: the shrink ratio (N + alpha M) / (N + M), N, R^2 and tau in
+            // FP64 arithmetic (the FP32 flux sums enter once, rounded to double exactly)
+            double* Nd = reinterpret_cast<double*>(J.px.stat_n) + p;
+            double* R2d = reinterpret_cast<double*>(J.px.stat_r2) + p;
+            double* Td = reinterpret_cast<double*>(J.px.stat_tau) + 3 * (size_t)p;
+            const double n0 = *Nd, m = (double)M, a = (double)J.alpha;
+            const double ratio = M > 0.0f ? fmin((n0 + a * m) / (n0 + m), 1.0) : 1.0;
+            *R2d = R2d64 * ratio;
+            *Nd = fma(a, m, n0);
+            const double fs = (double)s;
+            Td[0] = (T64[0] + (double)fx * fs * (double)qr4.x) * ratio;
+            Td[1] = (T64[1] + (double)fy * fs * (double)qr4.y) * ratio;
+            Td[2] = (T64[2] + (double)fz * fs * (double)qr4.z) * ratio;
+            return;
+        }
         // shrink ratio (N + alpha M) / (N + M) = 1 - (1 - alpha) M / (N + M), computed in FP32 (its
         // relative error ~1e-7 per pass); the statistics accumulate in double-float
         const float denom = (N.x + N.y) + M;
         const float ggf = M > 0.0f ? fminf(1.0f - (1.0f - J.alpha) * (M / denom), 1.0f) : 1.0f;
         R2 = df_mul_f(R2, ggf);
         N = df_add(N, df_two_prod(J.alpha, M));
-        const float s = J.scene.flux_unscale * 0.318309886f;
         tx = df_add(df_mul_f(tx, ggf), make_float2(fx * s * qr4.x * ggf, 0.0f));
         ty = df_add(df_mul_f(ty, ggf), make_float2(fy * s * qr4.y * ggf, 0.0f));
         tz = df_add(df_mul_f(tz, ggf), make_float2(fz * s * qr4.z * ggf, 0.0f));
         J.px.stat_n[p] = N;
+    }
+    if (f64) {
+        reinterpret_cast<double*>(J.px.stat_r2)[p] = R2d64;
+        double* Td = reinterpret_cast<double*>(J.px.stat_tau) + 3 * (size_t)p;
+        Td[0] = T64[0], Td[1] = T64[1], Td[2] = T64[2];
+        return;
     }
     J.px.stat_r2[p] = R2;
     J.px.stat_tau[3 * (size_t)p + 0] = tx;
@@ -338,20 +368,23 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
     J.px.stat_tau[3 * (size_t)p + 2] = tz;
 }
 
-// re.fs from the double-float statistics (the image is FP32: the pairs' high parts carry it)
+// re.fs from the statistics (the image is FP32: the pairs' high parts, or the doubles, carry it)
 __global__ void k_resolve_mixed(LaunchSet ls, uint32_t display) {
     const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
     if (gi >= ls.total) return;
     const int k = find_job(ls, gi);
     const JobDesc& J = ls.jobs[ls.job_ids[k]];
     const uint32_t p = gi - ls.prefix[k];
+    const bool f64 = (J.flags & SPPM_FLAG_FP64_STATISTICS) != 0;
     const float2 r2 = J.px.stat_r2[p];
-    const float den = (r2.x + r2.y) * 3.14159265f * (float)J.state->num_photons;
+    const float r2f = f64 ? (float)reinterpret_cast<const double*>(J.px.stat_r2)[p] : r2.x + r2.y;
+    const float den = r2f * 3.14159265f * (float)J.state->num_photons;
     const float4 qe = J.px.emi_n[p];
     const float e[3] = {qe.x, qe.y, qe.z};
     for (int c = 0; c < 3; c++) {
         const float2 t = J.px.stat_tau[3 * (size_t)p + c];
-        float v = (t.x + t.y) / den + e[c];
+        const float tf = f64 ? (float)reinterpret_cast<const double*>(J.px.stat_tau)[3 * (size_t)p + c] : t.x + t.y;
+        float v = tf / den + e[c];
         if (display) {
             v = 1.0f - sppm_fexp(-v * 60000.0f);
             v = v < 0.0031308f ? 12.92f * v : 1.055f * sppm_fpow(v, 0.416666666667f) - 0.055f;
@@ -373,9 +406,11 @@ uint32_t trace_photons4_blocks_per_sm() {
 void launch_slot_fill(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
     if (q.capacity) k_slot_fill<<<blocks_for(q.capacity, 256), 256, 0, s>>>(ls, q);
 }
-void launch_gather_mixed(const LaunchSet& ls, uint32_t block, cudaStream_t s) {
+void launch_gather_mixed(const LaunchSet& ls, uint32_t block, bool any_fp64, cudaStream_t s) {
     const uint32_t b = block >= 32 && block <= 256 && block % 32 == 0 ? block : 256;
-    if (ls.total) k_gather_mixed<<<blocks_for(ls.total, b), b, 0, s>>>(ls);
+    if (!ls.total) return;
+    if (any_fp64) k_gather_mixed<true><<<blocks_for(ls.total, b), b, 0, s>>>(ls);
+    else k_gather_mixed<false><<<blocks_for(ls.total, b), b, 0, s>>>(ls);
 }
 void launch_resolve_mixed(const LaunchSet& ls, uint32_t display, cudaStream_t s) {
     if (ls.total) k_resolve_mixed<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls, display);

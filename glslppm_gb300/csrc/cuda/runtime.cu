@@ -33,8 +33,9 @@ int launch_check(const char* what) {
     return SPPM_OK;
 }
 
-void state_to_host_layout(uint32_t kind, void* buf, size_t bytes) {
+void state_to_host_layout(uint32_t kind, void* buf, size_t bytes, uint32_t flags) {
     if (kind < SPPM_STATE_STATS_N || kind > SPPM_STATE_STATS_TAU) return;
+    if (flags & SPPM_FLAG_FP64_STATISTICS) return;  // already IEEE doubles
     char* b = static_cast<char*>(buf);
     for (size_t i = 0; i + 8 <= bytes; i += 8) {
         float pair[2];
@@ -58,6 +59,8 @@ int validate_config(const sppm_config* c) {
     if (c->radius_rule > SPPM_RADIUS_DIAGONAL) return fail(SPPM_ERR_ARG, "unknown radius rule %u", c->radius_rule);
     if (!(c->alpha > 0.0f && c->alpha <= 1.0f)) return fail(SPPM_ERR_ARG, "alpha must be in (0, 1]");
     if (c->eye_pass_interval > 4096) return fail(SPPM_ERR_ARG, "eye_pass_interval must be at most 4096");
+    if ((c->flags & SPPM_FLAG_FP64_STATISTICS) && c->precision != SPPM_PRECISION_MIXED)
+        return fail(SPPM_ERR_ARG, "SPPM_FLAG_FP64_STATISTICS applies to SPPM_PRECISION_MIXED only");
     return SPPM_OK;
 }
 
@@ -696,7 +699,7 @@ int Job::save_checkpoint(void* dst, size_t bytes, cudaStream_t s) const {
     h.PW = PW;
     h.PH = PH;
     h.hash_num = hash_num;
-    h.precision = cfg.precision;
+    h.precision = cfg.precision | (cfg.flags & SPPM_FLAG_FP64_STATISTICS ? 0x100u : 0u);
     h.state_bytes = (uint32_t)sizeof(JobState);
     h.seed_mode = cfg.seed_mode;
     h.seed = cfg.seed;
@@ -725,7 +728,8 @@ int Job::load_checkpoint(const void* src, size_t bytes, cudaStream_t s, uint32_t
     memcpy(&h, p, sizeof(h));
     if (memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != 2 || h.state_bytes != sizeof(JobState))
         return fail(SPPM_ERR_ARG, "not a checkpoint of this build");
-    if (h.W != W || h.H != H || h.PW != PW || h.PH != PH || h.hash_num != hash_num || h.precision != cfg.precision)
+    const uint32_t prec = cfg.precision | (cfg.flags & SPPM_FLAG_FP64_STATISTICS ? 0x100u : 0u);
+    if (h.W != W || h.H != H || h.PW != PW || h.PH != PH || h.hash_num != hash_num || h.precision != prec)
         return fail(SPPM_ERR_ARG, "checkpoint of a %ux%u image with %ux%u photons (%u slots, precision %u) does not "
                     "fit this job", h.W, h.H, h.PW, h.PH, h.hash_num, h.precision);
     if (h.seed_mode != cfg.seed_mode || h.seed != cfg.seed)
@@ -1012,7 +1016,7 @@ int Runner::enqueue_frame(uint32_t phase) {
         timed(SPPM_STAGE_PHOTON_STORE, false);
     }
     timed(SPPM_STAGE_GATHER, true);
-    if (mixed) launch_gather_mixed(pix, tune.gather_block, stream);
+    if (mixed) launch_gather_mixed(pix, tune.gather_block, fp64_stats, stream);
     else launch_gather_fp32(pix, tune.gather_block, stream);
     timed(SPPM_STAGE_GATHER, false);
     return launch_check("SPPM frame");
@@ -1036,6 +1040,7 @@ int Runner::build_graph(uint32_t phase, FrameGraph& g) {
     g.mask = timing_mask;
     g.counting = count_traversal;
     g.textured = textured;
+    g.fp64 = fp64_stats;
     size_t n = 0;
     SPPM_CK(cudaGraphGetNodes(graph, nullptr, &n));
     std::vector<cudaGraphNode_t> nodes(n);
@@ -1064,12 +1069,15 @@ int Runner::run(uint32_t n) {
     // the kernel variants with texture lookups when some job's scene has texture coordinates
     textured = false;
     for (const Job* j : active) textured = textured || j->desc.scene.tri_tex != nullptr;
+    fp64_stats = false;
+    for (const Job* j : active) fp64_stats = fp64_stats || (j->cfg.flags & SPPM_FLAG_FP64_STATISTICS) != 0;
     // the traversal-counting kernels run eagerly (they are a measurement pass)
     const bool use_graphs = !(flags & SPPM_FLAG_EAGER_LAUNCH) && !count_traversal;
     for (uint32_t k = 0; k < n; k++) {
         const uint32_t phase = (uint32_t)(frames % eye_interval);
         FrameGraph& g = graphs[phase_has_eye(phase) ? phase : eye_interval];
-        if (!g.exec || g.mask != timing_mask || g.counting != count_traversal || g.textured != textured) {
+        if (!g.exec || g.mask != timing_mask || g.counting != count_traversal || g.textured != textured ||
+            g.fp64 != fp64_stats) {
             // captured, and launched only in graph mode; eager mode keeps it to count kernels
             if ((st = build_graph(phase, g))) return st;
         }

@@ -59,8 +59,9 @@ struct Arena {
 
 int validate_config(const sppm_config* c);
 // state kinds whose device layout differs from what readers get: the mixed-precision statistics
-// are double-float pairs on the device and doubles for the reader (converted in place)
-void state_to_host_layout(uint32_t kind, void* buf, size_t bytes);
+// are double-float pairs on the device and doubles for the reader (converted in place), unless the
+// job keeps IEEE doubles (SPPM_FLAG_FP64_STATISTICS)
+void state_to_host_layout(uint32_t kind, void* buf, size_t bytes, uint32_t flags);
 int launch_check(const char* what);
 
 // the caller's view of a job's frame counters
@@ -144,6 +145,7 @@ struct FrameGraph {
     uint32_t kernels = 0;   // kernel nodes (launches per replay)
     bool counting = false;  // captured with the traversal-counting kernels
     bool textured = false;  // captured with the kernel variants that look up textures
+    bool fp64 = false;      // captured with the gather variant for IEEE double statistics
     cudaGraphNode_t ev_a[SPPM_STAGE_COUNT] = {}, ev_b[SPPM_STAGE_COUNT] = {};
     void drop();
 };
@@ -186,6 +188,7 @@ struct Runner {
     uint32_t timing_mask = 0;  // bit k: time stage k
     bool count_traversal = false;
     bool textured = false;         // some active job's scene has texture coordinates
+    bool fp64_stats = false;       // some active job keeps IEEE double statistics
     std::vector<StageEvent> pending;
     size_t open_stage[SPPM_STAGE_COUNT] = {0};  // pending entry of each stage's last start
     std::vector<cudaEvent_t> event_pool;

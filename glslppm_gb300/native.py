@@ -34,6 +34,7 @@ FLAG_GL_DEPTH_CLIP = 0x1
 FLAG_FUSED_PHOTON = 0x2
 FLAG_UNBINNED_RAYS = 0x4
 FLAG_EAGER_LAUNCH = 0x8
+FLAG_FP64_STATISTICS = 0x10
 IMAGE_RADIANCE, IMAGE_DISPLAY = 0, 1
 STAGES = ("frame_begin", "eye", "grid", "photon", "gather", "resolve", "photon_trace", "photon_store", "ray_bins")
 
@@ -182,6 +183,7 @@ SIGNATURES = {
     "sppm_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "sppm_debug_fpmath": (C.c_int, [C.c_int, P, P, P, C.c_size_t]),
     "sppm_debug_trace": (C.c_int, [P, P, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P]),
+    "sppm_debug_photon_rays": (C.c_int, [P, P, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "sppm_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
     "sppm_write_image_file": (C.c_int, [C.c_char_p, P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "sppm_host_free": (None, [P]),

@@ -303,7 +303,8 @@ class Renderer:
     def debug_trace(self, org: np.ndarray, dir: np.ndarray, photon: bool = True, cull: bool = False,
                     mode: int = 0) -> tuple[np.ndarray, np.ndarray]:
         """Single rays through the exact traversal of the uploaded scene: (triangle or -1, t).
-        mode 0 traces one ray per thread, mode 1 one ray per warp, mode 2 one ray per block."""
+        mode 0 traces one ray per thread, mode 1 one ray per warp, mode 2 one ray per block; mode 3
+        the mixed path's 4-wide quantised BVH (mixed-precision contexts)."""
         org = np.ascontiguousarray(org, dtype=np.float32).reshape(-1, 3)
         dir = np.ascontiguousarray(dir, dtype=np.float32).reshape(-1, 3)
         n = org.shape[0]
@@ -312,6 +313,18 @@ class Renderer:
         N.check(N.lib.sppm_debug_trace(self._h, org.ctypes.data, dir.ctypes.data, n, int(photon), int(cull), mode,
                                        tri.ctypes.data, t.ctypes.data))
         return tri, t
+
+    def debug_photon_rays(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """The photon rays the last pass traced: (origins [n, 3], directions [n, 3], photon slots [n])."""
+        n = C.c_size_t()
+        N.check(N.lib.sppm_debug_photon_rays(self._h, None, None, None, 0, C.byref(n)))
+        cnt = n.value
+        org = np.empty((cnt, 3), np.float32)
+        dir = np.empty((cnt, 3), np.float32)
+        ph = np.empty(cnt, np.uint32)
+        N.check(N.lib.sppm_debug_photon_rays(self._h, org.ctypes.data, dir.ctypes.data, ph.ctypes.data, cnt,
+                                             C.byref(n)))
+        return org[: n.value], dir[: n.value], ph[: n.value]
 
     def save_checkpoint(self) -> bytes:
         """The progressive state as a flat binary (sppm_save_checkpoint)."""

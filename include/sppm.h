@@ -82,6 +82,10 @@ typedef enum sppm_seed_mode {
                                         frame's CUDA graph (same results) */
 #define SPPM_FLAG_UNBINNED_RAYS 0x4u /* wavefront pass: trace the photon rays in queue order instead
                                         of binned by direction class and origin cell (same results) */
+#define SPPM_FLAG_FP64_STATISTICS 0x10u /* mixed precision only: keep N, R^2 and tau in IEEE double and
+                                           update them in FP64 arithmetic instead of double-float
+                                           pairs (same memory; the GPU's FP64 rate makes the gather
+                                           slower) */
 
 typedef struct sppm_config {
     uint32_t width, height;               /* image (ImageResolution x ImageResolution in the ref)  */
@@ -395,9 +399,16 @@ int sppm_debug_fpmath(int fn, const float* x, const float* y, float* out, size_t
    with back-face culling when cull != 0 otherwise): tri[i] = closest triangle or -1, t[i] = its
    t (the initial bound when nothing is hit).  mode 0 traces one ray per thread, mode 1 one ray
    per warp, mode 2 one ray per block of 1024 threads (the form the photon pass uses for rays
-   with a zero direction component); all give the same result. */
+   with a zero direction component); all give the same result.  Mode 3 traces the mixed
+   path's 4-wide quantised BVH instead (contexts of SPPM_PRECISION_MIXED): its triangle and t equal
+   the exact traversal's except where two triangles give the same t. */
 int sppm_debug_trace(sppm_ctx* ctx, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
                      int32_t* tri, float* t);
+/* The photon rays the last pass traced (the wavefront's ray queue; not with
+   SPPM_FLAG_FUSED_PHOTON): *count rays, origin and direction (3 floats each) and the photon slot
+   each belongs to.  With org, dir and photon all null only *count is set.  For tests that trace
+   the same rays again through sppm_debug_trace. */
+int sppm_debug_photon_rays(sppm_ctx* ctx, float* org, float* dir, uint32_t* photon, size_t capacity, size_t* count);
 /* Page-locked host memory (cudaMallocHost) for the host buffers of sppm_read_image and friends:
    copies to it run at the interconnect's DMA rate instead of being staged through the driver. */
 int sppm_host_alloc(size_t bytes, void** ptr);
