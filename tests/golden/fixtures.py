@@ -42,3 +42,14 @@ def load_cornell_metal():
     """(scene arrays, raw dict) of the reference's cornell_metal.obj as its host code loads it."""
     d = load_npz("cornell_metal_scene.npz")
     return scene_arrays_from(d), d
+
+
+def c1_camera_and_scene():
+    """The 256x256 workload's scene (the Cornell box as the reference's host code loads it) and
+    camera, exactly as tests/golden/make_converged_reference.py rendered its converged reference."""
+    import glslppm_gb300 as g
+    d = load_npz("cornell_box_scene.npz")
+    scene = g.scene_from_arrays(scene_arrays_from(d))
+    cam = camera_from(d, 256, 256)
+    cam.distance = float(load_npz("c1_converged_fp64.npz")["cam_distance"])
+    return scene, cam
