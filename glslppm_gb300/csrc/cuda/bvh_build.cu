@@ -1,27 +1,32 @@
-// GPU construction of the threaded BVH arrays (sppm_mesh_build_bvh_gpu): a linear BVH.
+// GPU construction of the threaded BVH arrays (sppm_mesh_build_bvh_gpu, sppm_mesh_build_bvh_gpu_ex).
 //
 // The host builder (csrc/host/scene_bvh.cpp) reproduces the reference's exact-SAH tree node for
-// node, which costs seconds per million triangles.  This builder makes a different tree in the
+// node, which costs seconds per million triangles.  These builders make a different tree in the
 // same layout, in milliseconds:
 //  1. 30-bit Morton code of each triangle centroid in the scene box; triangles sorted by
 //     (code, index);
-//  2. the radix tree over the sorted codes (Karras, "Maximizing parallelism in the construction
-//     of BVHs, octrees, and k-d trees", HPG 2012): internal node i covers a key range found from
-//     the longest common prefixes of its neighbours, its split is the first key whose prefix with
-//     the range's first key is shorter than the range's common prefix; equal codes are told apart
-//     by their position;
-//  3. boxes and subtree sizes bottom-up (the second child to finish computes its parent);
-//  4. the six threaded orderings of the reference's layout (bvh.cpp:159-168, 287-315): canonical
+//  2a. PLOC (the default): parallel locally-ordered clustering (Meister and Bittner, "Parallel
+//     Locally-Ordered Clustering for Bounding Volume Hierarchy Construction", IEEE TVCG 2018).
+//     The sorted leaves are the first clusters; every round, each cluster finds the neighbour
+//     within kPlocRadius positions of the cluster order whose union box has the smallest surface
+//     area (ties to the lower position, so the closest pair overall is always mutual), mutual
+//     pairs merge into a new node, and the clusters are compacted in order; the rounds end with
+//     one cluster.  The tree approaches a full SAH sweep's quality;
+//  2b. the radix tree over the sorted codes (Karras, "Maximizing parallelism in the construction
+//     of BVHs, octrees, and k-d trees", HPG 2012), then boxes and subtree sizes bottom-up (the
+//     second child to finish computes its parent): faster to build, more nodes per ray;
+//  3. the six threaded orderings of the reference's layout (bvh.cpp:159-168, 287-315): canonical
 //     child order = smaller min.x first, orderings 1..5 keep that order only when the face's
 //     predicate holds, nodes numbered in preorder; each node finds its preorder position by
 //     walking to the root (position = sum over ancestors of 1 + the node count of the sibling
 //     subtree that precedes it; a subtree of k leaves has 2k-1 nodes), and its miss link is the
 //     node that follows its subtree.
-// Triangle sorting uses cub::DeviceRadixSort (the CUDA toolkit's sort).
+// Triangle sorting and cluster compaction use cub (the CUDA toolkit's device primitives).
 #include <cstdint>
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_select.cuh>
 #include <cuda_runtime.h>
 
 #include "../host/scene_internal.h"
@@ -128,6 +133,101 @@ __global__ void k_bounds(const uint32_t* __restrict__ sorted_tri, const GBox* __
     }
 }
 
+// ---- PLOC ------------------------------------------------------------------------------------
+constexpr int kPlocRadius = 16;
+constexpr int kPlocBlock = 256;
+
+__device__ __forceinline__ GBox box_union(const GBox& a, const GBox& b) {
+    GBox u;
+    for (int c = 0; c < 3; c++) {
+        u.mn[c] = fminf(a.mn[c], b.mn[c]);
+        u.mx[c] = fmaxf(a.mx[c], b.mx[c]);
+    }
+    return u;
+}
+
+__device__ __forceinline__ float box_area(const GBox& b) {
+    const float dx = b.mx[0] - b.mn[0], dy = b.mx[1] - b.mn[1], dz = b.mx[2] - b.mn[2];
+    return dx * dy + dy * dz + dz * dx;  // half the surface area: only the order matters
+}
+
+// leaf k (sorted position) = node n-1+k; the first clusters are the leaves in Morton order
+__global__ void k_ploc_leaves(const uint32_t* __restrict__ sorted_tri, const GBox* __restrict__ tri_box, int n,
+                              GBox* __restrict__ box, int32_t* __restrict__ size, int32_t* __restrict__ cluster) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int node = (n - 1) + k;
+    box[node] = tri_box[sorted_tri[k]];
+    size[node] = 1;
+    cluster[k] = node;
+}
+
+// each cluster's nearest neighbour within kPlocRadius positions (smallest union area; ties to the
+// lower position); the window's boxes are staged in shared memory
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_nearest(const int32_t* __restrict__ cluster, int nc,
+                                                           const GBox* __restrict__ box, int32_t* __restrict__ nearest) {
+    __shared__ GBox sb[kPlocBlock + 2 * kPlocRadius];
+    const int b0 = blockIdx.x * kPlocBlock;
+    for (int t = threadIdx.x; t < kPlocBlock + 2 * kPlocRadius; t += kPlocBlock) {
+        const int g = b0 - kPlocRadius + t;
+        if (g >= 0 && g < nc) sb[t] = box[cluster[g]];
+    }
+    __syncthreads();
+    const int i = b0 + (int)threadIdx.x;
+    if (i >= nc) return;
+    const GBox bi = sb[threadIdx.x + kPlocRadius];
+    float best = __int_as_float(0x7f800000);
+    int bj = -1;
+    const int lo = max(0, i - kPlocRadius), hi = min(nc - 1, i + kPlocRadius);
+    for (int j = lo; j <= hi; j++) {
+        if (j == i) continue;
+        float a = box_area(box_union(bi, sb[j - b0 + kPlocRadius]));
+        if (!(a == a)) a = __int_as_float(0x7f800000);  // a box with NaN coordinates: farthest
+        if (bj < 0 || a < best) {  // ascending j: an equal area keeps the lower position
+            best = a;
+            bj = j;
+        }
+    }
+    nearest[i] = bj;
+}
+
+// mutual nearest neighbours merge (the lower position creates the node and takes its place; the
+// higher one leaves); everything else stays.  keep[i] = 1 for the clusters of the next round.
+__global__ void k_ploc_merge(const int32_t* __restrict__ cluster, int nc, const int32_t* __restrict__ nearest,
+                             GBox* __restrict__ box, int32_t* __restrict__ size, int32_t* __restrict__ left,
+                             int32_t* __restrict__ right, int32_t* __restrict__ parent, uint32_t* __restrict__ next_id,
+                             int32_t* __restrict__ merged, uint8_t* __restrict__ keep, int max_internal,
+                             uint32_t* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    const int j = nearest[i];
+    const bool mutual = j >= 0 && nearest[j] == i;
+    if (!mutual) {
+        merged[i] = cluster[i];
+        keep[i] = 1;
+        return;
+    }
+    if (i > j) {
+        keep[i] = 0;
+        return;
+    }
+    const uint32_t id = atomicAdd(next_id, 1u);
+    if ((int)id >= max_internal) {  // cannot happen for a consistent clustering; never write past
+        atomicOr(err, 2u);
+        keep[i] = 0;
+        return;
+    }
+    const int a = cluster[i], b = cluster[j];
+    left[id] = a;
+    right[id] = b;
+    parent[a] = (int32_t)id;
+    parent[b] = (int32_t)id;
+    box[id] = box_union(box[a], box[b]);
+    size[id] = size[a] + size[b];
+    merged[i] = (int32_t)id;
+    keep[i] = 1;
+}
+
 // does ordering `face` put the canonical first child (a) first? (bvh.cpp:287-301)
 __device__ __forceinline__ bool keep_order(int face, const GBox& a, const GBox& b) {
     switch (face) {
@@ -198,8 +298,12 @@ struct DevBuf {
 
 }  // namespace
 
-extern "C" int sppm_mesh_build_bvh_gpu(sppm_mesh* m, int device) {
+namespace {
+
+int build_gpu(sppm_mesh* m, int device, int builder) {
     if (!m) return fail(SPPM_ERR_ARG, "sppm_mesh_build_bvh_gpu: null mesh");
+    if (builder != SPPM_BVH_GPU_PLOC && builder != SPPM_BVH_GPU_LBVH)
+        return fail(SPPM_ERR_ARG, "sppm_mesh_build_bvh_gpu_ex: unknown builder %d", builder);
     const int n = (int)m->num_triangles;
     if (n < 1) return fail(SPPM_ERR_ARG, "sppm_mesh_build_bvh_gpu: mesh has no triangles");
     if (n > (1 << 28)) return fail(SPPM_ERR_ARG, "sppm_mesh_build_bvh_gpu: more than 2^28 triangles");
@@ -222,9 +326,10 @@ extern "C" int sppm_mesh_build_bvh_gpu(sppm_mesh* m, int device) {
     }
     DevBuf<float> d_cen, d_bounds;
     DevBuf<GBox> d_tb, d_box;
-    DevBuf<uint32_t> d_code, d_code2, d_idx, d_idx2, d_arr, d_err;
-    DevBuf<int32_t> d_left, d_right, d_parent, d_size, d_tri, d_base, d_miss;
-    DevBuf<char> d_tmp;
+    DevBuf<uint32_t> d_code, d_code2, d_idx, d_idx2, d_arr, d_err, d_next;
+    DevBuf<int32_t> d_left, d_right, d_parent, d_size, d_tri, d_base, d_miss, d_clu, d_clu2, d_near, d_nsel;
+    DevBuf<uint8_t> d_keep;
+    DevBuf<char> d_tmp, d_tmp2;
     cudaError_t e = cudaSuccess;
     auto A = [&](cudaError_t r) {
         if (e == cudaSuccess) e = r;
@@ -246,6 +351,14 @@ extern "C" int sppm_mesh_build_bvh_gpu(sppm_mesh* m, int device) {
     A(d_tri.alloc(nn));
     A(d_base.alloc((size_t)6 * nn));
     A(d_miss.alloc((size_t)6 * nn));
+    if (builder == SPPM_BVH_GPU_PLOC) {
+        A(d_clu.alloc(n));
+        A(d_clu2.alloc(n));
+        A(d_near.alloc(n));
+        A(d_keep.alloc(n));
+        A(d_nsel.alloc(1));
+        A(d_next.alloc(1));
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         return fail(SPPM_ERR_OOM, "sppm_mesh_build_bvh_gpu: device allocation failed: %s", cudaGetErrorString(e));
@@ -267,11 +380,48 @@ extern "C" int sppm_mesh_build_bvh_gpu(sppm_mesh* m, int device) {
     A(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, d_code.p, d_code2.p, d_idx.p, d_idx2.p, n, 0, 30));
     A(d_tmp.alloc(tmp_bytes));
     A(cub::DeviceRadixSort::SortPairs(d_tmp.p, tmp_bytes, d_code.p, d_code2.p, d_idx.p, d_idx2.p, n, 0, 30));
-    if (e == cudaSuccess && n > 1) k_radix_tree<<<(n - 1 + T - 1) / T, T>>>(d_code2.p, n, d_left.p, d_right.p, d_parent.p);
-    A(cudaGetLastError());
-    if (e == cudaSuccess)
-        k_bounds<<<gb, T>>>(d_idx2.p, d_tb.p, n, d_left.p, d_right.p, d_parent.p, d_box.p, d_size.p, d_arr.p);
-    A(cudaGetLastError());
+    if (builder == SPPM_BVH_GPU_LBVH) {
+        if (e == cudaSuccess && n > 1)
+            k_radix_tree<<<(n - 1 + T - 1) / T, T>>>(d_code2.p, n, d_left.p, d_right.p, d_parent.p);
+        A(cudaGetLastError());
+        if (e == cudaSuccess)
+            k_bounds<<<gb, T>>>(d_idx2.p, d_tb.p, n, d_left.p, d_right.p, d_parent.p, d_box.p, d_size.p, d_arr.p);
+        A(cudaGetLastError());
+    } else {
+        if (e == cudaSuccess) k_ploc_leaves<<<gb, T>>>(d_idx2.p, d_tb.p, n, d_box.p, d_size.p, d_clu.p);
+        A(cudaGetLastError());
+        A(cudaMemset(d_next.p, 0, 4));
+        size_t sel_bytes = 0;
+        A(cub::DeviceSelect::Flagged(nullptr, sel_bytes, d_clu2.p, d_keep.p, d_clu.p, d_nsel.p, n));
+        A(d_tmp2.alloc(sel_bytes));
+        // every round merges at least the closest pair, so n - 1 rounds bound the loop
+        int nc = n;
+        for (int round = 0; nc > 1 && e == cudaSuccess; round++) {
+            if (round >= n) {
+                e = cudaErrorUnknown;
+                return fail(SPPM_ERR_STATE, "sppm_mesh_build_bvh_gpu: clustering made no progress");
+            }
+            const int blocks = (nc + kPlocBlock - 1) / kPlocBlock;
+            k_ploc_nearest<<<blocks, kPlocBlock>>>(d_clu.p, nc, d_box.p, d_near.p);
+            k_ploc_merge<<<(nc + T - 1) / T, T>>>(d_clu.p, nc, d_near.p, d_box.p, d_size.p, d_left.p, d_right.p,
+                                                  d_parent.p, d_next.p, d_clu2.p, d_keep.p, n - 1, d_err.p);
+            A(cudaGetLastError());
+            A(cub::DeviceSelect::Flagged(d_tmp2.p, sel_bytes, d_clu2.p, d_keep.p, d_clu.p, d_nsel.p, nc));
+            int32_t left_count = 0;
+            A(cudaMemcpy(&left_count, d_nsel.p, 4, cudaMemcpyDeviceToHost));
+            if (e == cudaSuccess && (left_count < 1 || left_count >= nc)) {
+                return fail(SPPM_ERR_STATE, "sppm_mesh_build_bvh_gpu: clustering round %d kept %d of %d clusters",
+                            round, left_count, nc);
+            }
+            nc = left_count;
+        }
+        // the last cluster is the root
+        int32_t root = 0;
+        A(cudaMemcpy(&root, d_clu.p, 4, cudaMemcpyDeviceToHost));
+        const int32_t none = -1;
+        if (e == cudaSuccess && (root < 0 || root >= nn)) return fail(SPPM_ERR_STATE, "bad root %d", root);
+        A(cudaMemcpy(d_parent.p + root, &none, 4, cudaMemcpyHostToDevice));
+    }
     if (e == cudaSuccess)
         k_orderings<<<(nn + T - 1) / T, T>>>(n, d_idx2.p, d_left.p, d_right.p, d_parent.p, d_box.p, d_size.p,
                                              d_bounds.p, d_tri.p, d_base.p, d_miss.p, d_err.p);
@@ -280,7 +430,7 @@ extern "C" int sppm_mesh_build_bvh_gpu(sppm_mesh* m, int device) {
     uint32_t err = 0;
     A(cudaMemcpy(&err, d_err.p, 4, cudaMemcpyDeviceToHost));
     if (e != cudaSuccess) return fail(SPPM_ERR_CUDA, "sppm_mesh_build_bvh_gpu: %s", cudaGetErrorString(e));
-    if (err) return fail(SPPM_ERR_STATE, "sppm_mesh_build_bvh_gpu: inconsistent radix tree");
+    if (err) return fail(SPPM_ERR_STATE, "sppm_mesh_build_bvh_gpu: inconsistent tree (%u)", err);
     m->num_nodes = (uint32_t)nn;
     m->node_bounds.resize((size_t)nn * 6);
     m->node_triangle.resize(nn);
@@ -292,4 +442,12 @@ extern "C" int sppm_mesh_build_bvh_gpu(sppm_mesh* m, int device) {
     A(cudaMemcpy(m->order_miss.data(), d_miss.p, (size_t)6 * nn * 4, cudaMemcpyDeviceToHost));
     if (e != cudaSuccess) return fail(SPPM_ERR_CUDA, "sppm_mesh_build_bvh_gpu: %s", cudaGetErrorString(e));
     return SPPM_OK;
+}
+
+}  // namespace
+
+extern "C" int sppm_mesh_build_bvh_gpu(sppm_mesh* m, int device) { return build_gpu(m, device, SPPM_BVH_GPU_PLOC); }
+
+extern "C" int sppm_mesh_build_bvh_gpu_ex(sppm_mesh* m, int device, int builder) {
+    return build_gpu(m, device, builder);
 }

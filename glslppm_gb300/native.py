@@ -36,6 +36,7 @@ FLAG_UNBINNED_RAYS = 0x4
 FLAG_EAGER_LAUNCH = 0x8
 FLAG_FP64_STATISTICS = 0x10
 IMAGE_RADIANCE, IMAGE_DISPLAY = 0, 1
+BVH_GPU_PLOC, BVH_GPU_LBVH = 0, 1
 STAGES = ("frame_begin", "eye", "grid", "photon", "gather", "resolve", "photon_trace", "photon_store", "ray_bins")
 
 STATE = {
@@ -146,6 +147,7 @@ SIGNATURES = {
     "sppm_mesh_from_arrays": (C.c_int, [C.c_uint32, P, P, P, C.c_uint32, P, C.POINTER(P)]),
     "sppm_mesh_build_bvh": (C.c_int, [P]),
     "sppm_mesh_build_bvh_gpu": (C.c_int, [P, C.c_int]),
+    "sppm_mesh_build_bvh_gpu_ex": (C.c_int, [P, C.c_int, C.c_int]),
     "sppm_mesh_get_scene": (C.c_int, [P, C.POINTER(Scene)]),
     "sppm_mesh_destroy": (None, [P]),
     "sppm_create": (C.c_int, [C.POINTER(Config), C.c_int, C.POINTER(P)]),

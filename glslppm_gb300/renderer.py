@@ -92,12 +92,13 @@ class Mesh:
                                             mid.ctypes.data, len(mats), mats.ctypes.data, C.byref(out)))
         return cls(out.value)
 
-    def build_bvh(self, gpu: bool = False, device: int = 0) -> "Mesh":
+    def build_bvh(self, gpu: bool = False, device: int = 0, builder: str = "ploc") -> "Mesh":
         """TBVH::Build on the host (the reference's exact-SAH tree), or with gpu=True the same
-        arrays from a linear BVH built on the GPU (a different tree, milliseconds per million
-        triangles)."""
+        arrays from a tree built on the GPU (a different tree, milliseconds per million triangles):
+        builder "ploc" (locally-ordered clustering, near-SAH quality) or "lbvh" (radix tree)."""
         if gpu:
-            N.check(N.lib.sppm_mesh_build_bvh_gpu(self._h, device))
+            b = {"ploc": N.BVH_GPU_PLOC, "lbvh": N.BVH_GPU_LBVH}[builder]
+            N.check(N.lib.sppm_mesh_build_bvh_gpu_ex(self._h, device, b))
         else:
             N.check(N.lib.sppm_mesh_build_bvh(self._h))
         return self

@@ -171,11 +171,18 @@ int sppm_mesh_from_arrays(uint32_t num_triangles, const float* positions, const 
    orderings.  Stores the node arrays in the mesh. */
 int sppm_mesh_build_bvh(sppm_mesh* mesh);
 /* The same BVH arrays (node boxes and triangles, six threaded orderings with the reference's
-   child-order rules) from a linear BVH built on the GPU: Morton-ordered triangles and a radix
-   tree instead of the exact-SAH splits, so the tree differs from sppm_mesh_build_bvh's (rays
-   find the same closest triangle except at exact ties) and is built in milliseconds for
-   multi-million-triangle meshes.  No counterpart in the reference (bvh.cpp builds on the host). */
+   child-order rules) from a tree built on the GPU in milliseconds for multi-million-triangle
+   meshes: Morton-ordered triangles clustered bottom-up (PLOC: mutual nearest neighbours by
+   union-box area within a window of the cluster order), a tree close to a full SAH sweep's.  It
+   differs from sppm_mesh_build_bvh's exact-SAH tree, so rays find the same closest triangle
+   except at exact ties.  No counterpart in the reference (bvh.cpp builds on the host). */
 int sppm_mesh_build_bvh_gpu(sppm_mesh* mesh, int device);
+/* The GPU build with a chosen builder: SPPM_BVH_GPU_PLOC (the default above) or
+   SPPM_BVH_GPU_LBVH, the linear BVH of a radix tree over the Morton codes (Karras 2012): faster
+   to build, more nodes visited per ray. */
+#define SPPM_BVH_GPU_PLOC 0
+#define SPPM_BVH_GPU_LBVH 1
+int sppm_mesh_build_bvh_gpu_ex(sppm_mesh* mesh, int device, int builder);
 /* Fills *scene with pointers into the mesh (valid until sppm_mesh_destroy). */
 int sppm_mesh_get_scene(const sppm_mesh* mesh, sppm_scene* scene);
 void sppm_mesh_destroy(sppm_mesh* mesh);

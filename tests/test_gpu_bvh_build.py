@@ -1,6 +1,7 @@
-"""The GPU-built linear BVH has the layout of the reference's threaded BVH (six preorder
-orderings, miss links to the node after each subtree, boxes that contain their children) and
-finds the same closest triangles as the host-built exact-SAH tree."""
+"""The GPU-built BVHs (locally-ordered clustering, the default, and the radix-tree linear BVH)
+have the layout of the reference's threaded BVH (six preorder orderings, miss links to the node
+after each subtree, boxes that contain their children) and find the same closest triangles as the
+host-built exact-SAH tree; the clustered tree needs fewer node visits per ray than the radix tree."""
 import numpy as np
 import pytest
 
@@ -41,10 +42,12 @@ def check_layout(a):
             assert np.all(b[q, :3] <= b[c, :3]) and np.all(b[q, 3:] >= b[c, 3:])
 
 
-def test_gpu_bvh_layout_and_closest_hits():
+@pytest.mark.parametrize("builder", ["ploc", "lbvh"])
+def test_gpu_bvh_layout_and_closest_hits(builder):
     sc = scenes.cornell_variant(11, min_tris=3000, max_tris=6000).scene
     host = sc.to_mesh()
-    dev = g.Mesh.from_arrays(sc.positions, sc.material_ids, sc.material_array(), sc.normals).build_bvh(gpu=True)
+    dev = g.Mesh.from_arrays(sc.positions, sc.material_ids, sc.material_array(), sc.normals).build_bvh(
+        gpu=True, builder=builder)
     ad = dev.arrays()
     check_layout(ad)
     ah = host.arrays()
@@ -86,11 +89,12 @@ def test_gpu_bvh_renders_like_the_host_bvh():
     assert rel < 0.02, rel
 
 
-def test_gpu_bvh_single_triangle_and_mixed_path():
+@pytest.mark.parametrize("builder", ["ploc", "lbvh"])
+def test_gpu_bvh_single_triangle_and_mixed_path(builder):
     pos = np.array([[[0, 0, 0], [1, 0, 0], [0, 1, 0]]], dtype=np.float32)
     mats = np.zeros(1, dtype=g.renderer.MATERIAL_DTYPE)
     mats[0]["color"] = (0.5, 0.5, 0.5)
-    m = g.Mesh.from_arrays(pos, np.zeros(1, np.int32), mats).build_bvh(gpu=True)
+    m = g.Mesh.from_arrays(pos, np.zeros(1, np.int32), mats).build_bvh(gpu=True, builder=builder)
     a = m.arrays()
     assert a.node_bounds.shape == (1, 6) and a.node_triangle[0] == 0
     assert np.all(a.order_base == 0) and np.all(a.order_miss == 1)
@@ -102,3 +106,24 @@ def test_gpu_bvh_single_triangle_and_mixed_path():
     r.run_passes(3)
     r.synchronize()
     assert np.isfinite(r.read_image()).all()
+
+
+def test_clustered_tree_needs_fewer_node_visits_than_the_radix_tree():
+    """Locally-ordered clustering against the Morton radix tree on the batched workload's largest
+    job (398k triangles): node visits per photon segment (the traversal counters), with the
+    exact-SAH host tree beside them."""
+    sc = scenes.cornell_variant(17).scene
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, 64, 64, sc.fov)
+    visits = {}
+    for name in ("host", "ploc", "lbvh"):
+        m = g.Mesh.from_arrays(sc.positions, sc.material_ids, sc.material_array(), sc.normals)
+        m = m.build_bvh() if name == "host" else m.build_bvh(gpu=True, builder=name)
+        r = g.Renderer(g.default_config(64, photon_width=256, photon_height=256, radius_rule=N.RADIUS_DIAGONAL,
+                                        radius_fraction=0.005))
+        r.upload_scene(m)
+        r.set_camera(cam)
+        r.run_passes(2)
+        visits[name] = r.traversal_counters(passes=4)["nodes_per_segment"]
+        r.close()
+    print("nodes per photon segment:", visits)
+    assert visits["ploc"] < visits["lbvh"]
