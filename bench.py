@@ -530,10 +530,13 @@ def convergence(dev: int) -> dict | None:
 
 def passes_for_target(target_rmse: float, npix: int, photons_per_pass: int, cap: int = 1 << 20) -> int:
     """Pass count at which a job reaches `target_rmse` relative RMSE against a converged FP64
-    reference, from the power-law fit over photons per pixel of tests/golden/convergence_c1.json."""
+    reference, from the power-law fit over photons per pixel of tests/golden/convergence_c1.json
+    (the 256x256 workload, one photon per pixel per pass).  A job with more photons per pixel per
+    pass still needs as many passes as the calibration workload: the gather radius shrinks once per
+    pass, and with few passes its bias, not the photon noise, sets the error."""
     cal = json.loads((REPO / "tests" / "golden" / "convergence_c1.json").read_text())["fit"]
     ppp = (cal["a"] / target_rmse) ** (1.0 / cal["b"])
-    return int(min(cap, max(1, math.ceil(ppp * npix / photons_per_pass))))
+    return int(min(cap, max(1, math.ceil(ppp), math.ceil(ppp * npix / photons_per_pass))))
 
 
 def build_jobs(n_jobs: int, seed0: int = 0):

@@ -165,13 +165,15 @@ struct RayQueue {
                              // (0: 32 for the exact walk, 8 for the 4-wide one)
 };
 
-// the work of one launch: items [prefix[k], prefix[k+1]) belong to jobs[job_ids[k]]
+// the work of one launch: items [prefix[k], prefix[k+1]) belong to jobs[job_ids[k]]; a launch
+// covers the global items [first, total) (first > 0 for the later waves of the photon pass)
 struct LaunchSet {
     const JobDesc* jobs;
     const uint32_t* job_ids;
     const uint32_t* prefix;
     uint32_t njobs;
     uint32_t total;
+    uint32_t first;
 };
 
 __device__ __forceinline__ int find_job(const LaunchSet& ls, uint32_t g) {

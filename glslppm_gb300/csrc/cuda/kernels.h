@@ -38,6 +38,7 @@ void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, bool texture
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s);
 void launch_photon_fp32(const LaunchSet& ls, bool count_traversal, bool textured, cudaStream_t s);
 void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, bool textured, cudaStream_t s);
+void launch_queue_reset(const RayQueue& q, cudaStream_t s);
 void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool count_traversal,
                                uint32_t persistent_blocks, cudaStream_t s);
 void launch_ray_bins(const RayQueue& q, cudaStream_t s);
@@ -48,7 +49,7 @@ uint32_t trace_photons_blocks_per_sm();
 // mixed-precision path (kernels_mixed.cu)
 void launch_trace_photons4(const LaunchSet& ls, const RayQueue& q, uint32_t persistent_blocks, cudaStream_t s);
 uint32_t trace_photons4_blocks_per_sm();
-void launch_slot_fill(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
+void launch_slot_fill(const LaunchSet& hash_slots, cudaStream_t s);
 void launch_gather_mixed(const LaunchSet& ls, uint32_t block, bool any_fp64, cudaStream_t s);
 void launch_resolve_mixed(const LaunchSet& ls, uint32_t display, cudaStream_t s);
 void launch_gather_fp32(const LaunchSet& ls, uint32_t block, cudaStream_t s);

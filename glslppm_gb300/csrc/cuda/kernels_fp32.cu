@@ -636,6 +636,18 @@ __global__ void k_frame_begin(LaunchSet ls, RayQueue q) {
     }
 }
 
+// the photon ray queue emptied for the next wave of the photon pass (the eye pass's deferred
+// pixel count, counters[3], belongs to the eye branch running beside the waves and is kept)
+__global__ void k_queue_reset(RayQueue q) {
+    const uint32_t g = grid_tid();
+    if (g == 0) {
+        q.counters[0] = 0;
+        q.counters[1] = 0;
+        q.counters[2] = 0;
+    }
+    if (q.bins && g < kRayBins) q.bins[g] = 0u;
+}
+
 // ----------------------------------------------------------------------------------------------
 // k_eye: eyeraytrace.fs main (:396-554) + max/min reduction of the hit positions
 // ----------------------------------------------------------------------------------------------
@@ -1248,7 +1260,7 @@ __global__ void __launch_bounds__(128) k_photon_gen(LaunchSet ls, RayQueue q) {
     __shared__ uint32_t warp_emit[4], warp_valid[4];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     {
-        const uint32_t g0 = grid_tid();
+        const uint32_t g0 = ls.first + grid_tid();
         const bool valid = g0 < ls.total;
         bool emit = false;
         int2 h = make_int2(-1, 0);
@@ -1857,9 +1869,13 @@ void launch_photon_fp32(const LaunchSet& ls, bool count, bool textured, cudaStre
 }
 
 void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, bool textured, cudaStream_t s) {
-    if (!ls.total) return;
-    if (textured) k_photon_gen<true><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q);
-    else k_photon_gen<false><<<blocks_for(ls.total, 128), 128, 0, s>>>(ls, q);
+    if (ls.total <= ls.first) return;
+    const uint32_t n = ls.total - ls.first;
+    if (textured) k_photon_gen<true><<<blocks_for(n, 128), 128, 0, s>>>(ls, q);
+    else k_photon_gen<false><<<blocks_for(n, 128), 128, 0, s>>>(ls, q);
+}
+void launch_queue_reset(const RayQueue& q, cudaStream_t s) {
+    if (q.counters) k_queue_reset<<<blocks_for(kRayBins, 256), 256, 0, s>>>(q);
 }
 void launch_ray_bins(const RayQueue& q, cudaStream_t s) {
     if (!q.key || !q.capacity) return;

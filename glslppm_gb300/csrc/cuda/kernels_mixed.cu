@@ -192,17 +192,16 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
     if (err) atomicOr(&ls.jobs[ls.job_ids[job_k]].state->err, err);
 }
 
-// the winner of each slot writes the slot's 32-byte record (after all photons are hashed)
-__global__ void __launch_bounds__(256) k_slot_fill(LaunchSet ls, RayQueue q) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= q.counters[0]) return;
-    const uint32_t slot = __float_as_uint(q.hit[i].x);  // k_photon_store left the slot here
-    if (slot == 0xFFFFFFFFu) return;
-    const uint32_t g = __float_as_uint(q.org[i].w);
+// each occupied slot's 32-byte record from its winner (after every photon of the pass is hashed,
+// in all waves); one thread per hash slot of every job
+__global__ void __launch_bounds__(256) k_slot_fill(LaunchSet ls) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ls.total) return;
     const int k = find_job(ls, g);
     const JobDesc& J = ls.jobs[ls.job_ids[k]];
-    const uint32_t sidx = g - ls.prefix[k];
-    if (J.winner[slot] != sidx) return;
+    const uint32_t slot = g - ls.prefix[k];
+    const uint32_t sidx = J.winner[slot];
+    if (sidx == kEmptySlot) return;
     const JobState* st = J.state;
     const float4 p = J.ph.pos[sidx], f = J.ph.flux[sidx], dd = J.ph.dir[sidx];
     const float G = st->grid_scale;
@@ -403,8 +402,8 @@ uint32_t trace_photons4_blocks_per_sm() {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_trace_photons4, kTraceBlock, 0) != cudaSuccess) n = 4;
     return n > 0 ? (uint32_t)n : 1u;
 }
-void launch_slot_fill(const LaunchSet& ls, const RayQueue& q, cudaStream_t s) {
-    if (q.capacity) k_slot_fill<<<blocks_for(q.capacity, 256), 256, 0, s>>>(ls, q);
+void launch_slot_fill(const LaunchSet& hash_slots, cudaStream_t s) {
+    if (hash_slots.total) k_slot_fill<<<blocks_for(hash_slots.total, 256), 256, 0, s>>>(hash_slots);
 }
 void launch_gather_mixed(const LaunchSet& ls, uint32_t block, bool any_fp64, cudaStream_t s) {
     const uint32_t b = block >= 32 && block <= 256 && block % 32 == 0 ? block : 256;

@@ -760,7 +760,7 @@ int Job::load_checkpoint(const void* src, size_t bytes, cudaStream_t s, uint32_t
 }
 
 LaunchSet Job::self_set(const JobDesc* table, uint32_t which) const {
-    LaunchSet ls;
+    LaunchSet ls{};
     ls.jobs = table;
     ls.job_ids = d_self;
     ls.prefix = d_self + 1 + 2 * which;
@@ -882,7 +882,7 @@ int Runner::rebuild() {
     uint32_t* d_t = table_mem.take<uint32_t>(std::max<size_t>(t.size(), 1));
     SPPM_CK(cudaMemcpy(d_t, t.data(), t.size() * 4, cudaMemcpyHostToDevice));
     auto mk = [&](size_t ids, size_t prefix, uint32_t nj, uint64_t total) {
-        LaunchSet ls;
+        LaunchSet ls{};
         ls.jobs = d_jobs;
         ls.job_ids = d_t + ids;
         ls.prefix = d_t + prefix;
@@ -997,23 +997,44 @@ int Runner::enqueue_frame(uint32_t phase) {
         launch_photon_fp32(pho, count_traversal, textured, stream);
         timed(SPPM_STAGE_PHOTON, false);
     } else {
-        timed(SPPM_STAGE_PHOTON, true);
-        launch_photon_gen_fp32(pho, q, textured, stream);
-        timed(SPPM_STAGE_PHOTON, false);
-        if (q.key) {
-            timed(SPPM_STAGE_RAY_BINS, true);
-            launch_ray_bins(q, stream);
-            timed(SPPM_STAGE_RAY_BINS, false);
+        // the photon pass in waves of at most tune.photon_wave slots (one wave by default): each
+        // wave generates, bins, traces and stores its photons through the ray queue; the hash
+        // insertion is a commutative count and an atomic minimum, so the grid is the same for
+        // any wave size
+        const uint32_t wave = tune.photon_wave && tune.photon_wave < pho.total ? tune.photon_wave : pho.total;
+        bool joined = false;
+        for (uint32_t first = 0; first < pho.total; first += wave) {
+            LaunchSet w = pho;
+            w.first = first;
+            w.total = pho.total - first > wave ? first + wave : pho.total;
+            RayQueue qw = q;
+            qw.capacity = w.total - first < q.capacity ? w.total - first : q.capacity;
+            if (first) launch_queue_reset(qw, stream);  // k_frame_begin emptied it for the first wave
+            timed(SPPM_STAGE_PHOTON, true);
+            launch_photon_gen_fp32(w, qw, textured, stream);
+            timed(SPPM_STAGE_PHOTON, false);
+            if (qw.key) {
+                timed(SPPM_STAGE_RAY_BINS, true);
+                launch_ray_bins(qw, stream);
+                timed(SPPM_STAGE_RAY_BINS, false);
+            }
+            timed(SPPM_STAGE_PHOTON_TRACE, true);
+            if (mixed) launch_trace_photons4(pho, qw, trace_blocks, stream);
+            else launch_trace_photons_fp32(pho, qw, count_traversal, trace_blocks, stream);
+            timed(SPPM_STAGE_PHOTON_TRACE, false);
+            if (eye && !joined) {
+                SPPM_CK(cudaStreamWaitEvent(stream, join_ev, 0));  // the store needs the eye pass's grid
+                joined = true;
+            }
+            timed(SPPM_STAGE_PHOTON_STORE, true);
+            launch_photon_store_fp32(pho, qw, tune.store_block, stream);
+            timed(SPPM_STAGE_PHOTON_STORE, false);
         }
-        timed(SPPM_STAGE_PHOTON_TRACE, true);
-        if (mixed) launch_trace_photons4(pho, q, trace_blocks, stream);
-        else launch_trace_photons_fp32(pho, q, count_traversal, trace_blocks, stream);
-        timed(SPPM_STAGE_PHOTON_TRACE, false);
-        if (eye) SPPM_CK(cudaStreamWaitEvent(stream, join_ev, 0));
-        timed(SPPM_STAGE_PHOTON_STORE, true);
-        launch_photon_store_fp32(pho, q, tune.store_block, stream);
-        if (mixed) launch_slot_fill(pho, q, stream);
-        timed(SPPM_STAGE_PHOTON_STORE, false);
+        if (mixed) {
+            timed(SPPM_STAGE_PHOTON_STORE, true);
+            launch_slot_fill(hsh, stream);
+            timed(SPPM_STAGE_PHOTON_STORE, false);
+        }
     }
     timed(SPPM_STAGE_GATHER, true);
     if (mixed) launch_gather_mixed(pix, tune.gather_block, fp64_stats, stream);
@@ -1144,6 +1165,7 @@ int Runner::set_tuning(const sppm_tuning* t) {
     if (!block_ok(t->eye_block, 128) || !block_ok(t->store_block, 128) || !block_ok(t->gather_block, 256))
         return fail(SPPM_ERR_ARG, "block sizes are 0 or multiples of 32 up to 128 (eye, store) and 256 (gather)");
     if (t->unbinned_rays > 1) return fail(SPPM_ERR_ARG, "unbinned_rays is 0 or 1");
+    if (t->photon_wave && t->photon_wave < 1024) return fail(SPPM_ERR_ARG, "photon_wave is 0 or at least 1024");
     SPPM_CK(cudaSetDevice(device));
     SPPM_CK(cudaStreamSynchronize(stream));
     tune = *t;
@@ -1227,6 +1249,11 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
         if ((st = knob(&sppm_tuning::gather_block, {256u, 128u, 64u}))) return st;
         if ((st = knob(&sppm_tuning::store_block, {128u, 64u}))) return st;
         if ((st = knob(&sppm_tuning::eye_block, {128u, 64u}))) return st;
+        // wavefront queue depth: the whole pass in one wave, or in 2, 4 or 8 waves
+        std::vector<uint32_t> waves = {0u};
+        for (uint32_t d : {2u, 4u, 8u})
+            if (pho.total / d >= 65536u) waves.push_back((pho.total + d - 1) / d);
+        if ((st = knob(&sppm_tuning::photon_wave, waves))) return st;
         if (!changed) break;
     }
     if ((st = set_tuning(&cur))) return st;

@@ -333,6 +333,10 @@ typedef struct sppm_tuning {
     uint32_t store_block;         /* of the photon store + hash insertion (0 = 128; 32..128)    */
     uint32_t gather_block;        /* of the gather + progressive update (0 = 256; 32..256)      */
     uint32_t unbinned_rays;       /* 1: photon rays traced in queue order instead of binned     */
+    uint32_t photon_wave;         /* wavefront queue depth: photon slots generated, binned,
+                                     traced and stored per wave of the photon pass, so a wave's
+                                     ray queue and photon records stay in L2 from one kernel to
+                                     the next (0 = every slot in one wave; else >= 1024)         */
 } sppm_tuning;
 /* Block sizes are multiples of 32.  The frame graphs are captured again with the new shapes. */
 int sppm_set_tuning(sppm_ctx* ctx, const sppm_tuning* tuning);

@@ -41,6 +41,8 @@ def test_serving_targets_from_the_calibration():
     # a quarter of the photons per pass takes four times the passes
     assert bench.passes_for_target(0.02, 256 * 256, 1 << 14) == pytest.approx(4 * p2, rel=0.01)
     assert bench.passes_for_target(0.10, 256 * 256, 1 << 16) < p2
+    # more photons per pixel per pass than the calibration workload: still its pass count
+    assert bench.passes_for_target(0.02, 128 * 128, 1 << 19) == p2
 
 
 @pytest.mark.gpu

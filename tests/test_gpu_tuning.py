@@ -19,6 +19,8 @@ TUNINGS = [
     dict(trace_refill_steps=64, unbinned_rays=1),
     dict(gather_block=64, store_block=32, eye_block=32),
     dict(trace_blocks_per_sm=2, trace_refill_steps=5, gather_block=96, store_block=64, eye_block=96),
+    dict(photon_wave=1024),  # the photon pass in three waves of at most 1024 slots
+    dict(photon_wave=2048, unbinned_rays=1, trace_refill_steps=4),
 ]
 
 
@@ -79,7 +81,7 @@ def test_defaults_reported_and_bad_shapes_rejected(cornell_c1_mesh):
     assert (t.eye_block, t.store_block, t.gather_block, t.unbinned_rays) == (128, 128, 256, 0)
     for bad in (dict(gather_block=48), dict(eye_block=256), dict(store_block=160),
                 dict(trace_blocks_per_sm=t.trace_blocks_per_sm + 1), dict(unbinned_rays=2),
-                dict(trace_refill_steps=5000)):
+                dict(trace_refill_steps=5000), dict(photon_wave=512)):
         with pytest.raises(N.SppmError) as e:
             r.set_tuning(**bad)
         assert e.value.status == N.ERR_ARG, bad
@@ -193,3 +195,19 @@ def test_tuning_on_textured_deferred_and_environment_paths(tmp_path, cornell_c1_
     cfg = g.default_config(w, height=h, photon_width=64, photon_height=32, radius_rule=N.RADIUS_DIAGONAL,
                            radius_fraction=0.01)
     _pair(cfg, scene, cam, tuning)
+
+
+@pytest.mark.parametrize("precision", [N.PRECISION_FP32, N.PRECISION_MIXED])
+def test_photon_waves_render_the_same_bits(cornell_c1_mesh, precision):
+    """The photon pass in waves (the wavefront queue depth): 256x256 photon slots in 1, 4 and 5
+    waves (the last one short), with eye passes between, give the default context's state."""
+    sc, mesh = cornell_c1_mesh
+    ref = _renderer(sc, mesh, precision, w=64, h=64, pw=256, ph=256)
+    ref.run_passes(12)
+    want = _state(ref, precision)
+    for wave in (16384, 13200):
+        r = _renderer(sc, mesh, precision, w=64, h=64, pw=256, ph=256)
+        r.set_tuning(photon_wave=wave)
+        assert r.get_tuning().photon_wave == wave
+        r.run_passes(12)
+        _same(want, _state(r, precision), f"photon_wave={wave}")
