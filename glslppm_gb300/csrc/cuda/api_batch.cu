@@ -24,9 +24,9 @@ struct sppm_batch {
 
 namespace {
 
-// ray queue bytes per photon slot: org, dir, hit (3 x 16), set-aside list (4), binning key (8)
-// and permutation (4)
-constexpr uint64_t kQueueBytesPerSlot = 3 * 16 + 4 + 8 + 4;
+// ray queue bytes per photon slot: org, dir, hit (3 x 16), set-aside list (4), binning key (8),
+// permutation (4), tail-walk list (4) and state (16)
+constexpr uint64_t kQueueBytesPerSlot = 3 * 16 + 4 + 8 + 4 + 4 + 16;
 
 Job* job_of(const sppm_batch* b, uint32_t id) {
     if (!b || id >= b->slots.size()) return nullptr;

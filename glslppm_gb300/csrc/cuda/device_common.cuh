@@ -153,9 +153,11 @@ struct RayQueue {
     float4* dir;
     float4* hit;          // (triangle or -1 as int bits, barycentrics v, w, u)
     uint32_t* counters;   // [0] rays queued, [1] fetch head of the trace kernel, [2] rays set aside,
-                          // [3] eye pixels deferred
+                          // [3] eye pixels deferred, [4] walks handed to the tail kernel
     uint32_t capacity;
     uint32_t* slow;       // [capacity] queue indices of the rays traced one per warp
+    uint32_t* tail_list;  // [capacity] queue indices of the walks the tail kernel finishes
+    float4* tail_state;   // [capacity] their state: closest t, material, next node, steps
     // binning (all null when the rays are traced in queue order)
     uint2* key;           // [capacity] (bin, rank within the bin)
     uint32_t* bins;       // [kRayBins] counts, then exclusive offsets
@@ -163,6 +165,8 @@ struct RayQueue {
     uint32_t* eye_deferred;  // [kEyeDeferred] launch indices of the deferred eye pixels
     uint32_t refill_steps;   // traversal steps a warp takes between refills of its idle lanes
                              // (0: 32 for the exact walk, 8 for the 4-wide one)
+    uint32_t tail_lanes;     // exact walk: once the queue is drained, a warp with at most this many
+                             // walking lanes finishes them with the warp-cooperative walk (0: never)
 };
 
 // the work of one launch: items [prefix[k], prefix[k+1]) belong to jobs[job_ids[k]]; a launch

@@ -136,23 +136,21 @@ __device__ __forceinline__ bool slab_degenerate(f3 d) {
 // when its box passes with the t of the closest hit so far; a visited leaf replaces the closest
 // hit when its triangle test passes with that t; the walk goes to node + 1 after a hit and to
 // the miss link otherwise.
+// The walk may also be resumed where a scalar walk stopped: at node `start` with the closest hit
+// `h0` after `steps0` steps (coop_trace_exact_from); the result is the scalar walk's all the same.
 template <bool PHOTON, bool COUNT>
-__device__ __noinline__ Hit coop_trace_exact(const DevScene& s, f3 org, f3 dir, bool cull, uint32_t& err,
-                                             TraversalCount* cnt) {
+__device__ __forceinline__ Hit coop_trace_exact_from(const DevScene& s, f3 org, f3 dir, bool cull, uint32_t& err,
+                                                  TraversalCount* cnt, int32_t start, Hit h0, uint32_t steps0) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     const int lane = (int)(threadIdx.x & 31);
-    Hit h;
-    h.t = PHOTON ? 1.0e30f : 1.0e20f;
-    h.tri = -1;
-    h.mat = -1;
-    h.bu = h.bv = h.bw = 0.0f;
+    Hit h = h0;
     const NodeX* nodes = s.nodes + (size_t)cube_face(dir) * s.num_nodes;
     const f3 rcp = mk(xdiv(1.0f, dir.x), xdiv(1.0f, dir.y), xdiv(1.0f, dir.z));
     const f3 t0 = mul(neg(rcp), org);
     const int32_t nn = (int32_t)s.num_nodes;
-    int32_t cur = 0;
-    uint32_t steps = 0;
-    bool done = false;
+    int32_t cur = start;
+    uint32_t steps = steps0;
+    bool done = start < 0 || start >= nn;
     while (!done) {
         const int32_t base = cur;
         const int32_t j = base + lane;
@@ -264,6 +262,17 @@ __device__ __noinline__ Hit coop_trace_exact(const DevScene& s, f3 org, f3 dir, 
         }
     }
     return h;
+}
+
+template <bool PHOTON, bool COUNT>
+__device__ __forceinline__ Hit coop_trace_exact(const DevScene& s, f3 org, f3 dir, bool cull, uint32_t& err,
+                                                TraversalCount* cnt) {
+    Hit h;
+    h.t = PHOTON ? 1.0e30f : 1.0e20f;
+    h.tri = -1;
+    h.mat = -1;
+    h.bu = h.bv = h.bw = 0.0f;
+    return coop_trace_exact_from<PHOTON, COUNT>(s, org, dir, cull, err, cnt, 0, h, 0u);
 }
 
 // Block-wide form of the same walk (1024 threads, one ray, the same result bit for bit): the
@@ -606,6 +615,7 @@ __global__ void k_frame_begin(LaunchSet ls, RayQueue q) {
         q.counters[1] = 0;
         q.counters[2] = 0;
         q.counters[3] = 0;
+        q.counters[4] = 0;
     }
     if (q.bins && g < kRayBins) q.bins[g] = 0u;
     if (g >= ls.total) return;
@@ -644,6 +654,7 @@ __global__ void k_queue_reset(RayQueue q) {
         q.counters[0] = 0;
         q.counters[1] = 0;
         q.counters[2] = 0;
+        q.counters[4] = 0;
     }
     if (q.bins && g < kRayBins) q.bins[g] = 0u;
 }
@@ -1480,6 +1491,24 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
             }
         }
         if (__all_sync(0xFFFFFFFFu, idx == kDone)) break;
+        // the tail: once the queue is drained, a warp left with a few long walks hands them to
+        // k_trace_photons_tail, which finishes each with all 32 lanes of a warp, resumed where the
+        // lane stands (coop_trace_exact_from, the same result bit for bit): a walk's chain of
+        // dependent node loads becomes windows of 32 loads in flight
+        if (q.tail_lanes) {
+            const unsigned act = __ballot_sync(0xFFFFFFFFu, idx < kDone);
+            const unsigned drained = __ballot_sync(0xFFFFFFFFu, idx == kDone);
+            if (drained && act && (uint32_t)__popc(act) <= q.tail_lanes) {
+                if (idx < kDone) {
+                    q.hit[idx] = make_float4(__int_as_float(h.tri), h.bu, h.bv, h.bw);
+                    q.tail_state[idx] = make_float4(h.t, __int_as_float(h.mat), __int_as_float(node),
+                                                    __int_as_float(steps));
+                    q.tail_list[atomicAdd(&q.counters[4], 1u)] = idx;
+                    idx = kDone;
+                }
+                continue;  // every walk of the warp is handed over; the next iteration leaves the loop
+            }
+        }
         if (idx >= kDone) continue;
         bool finished = false;
 #pragma unroll 1
@@ -1536,6 +1565,41 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
     }
     if (COUNT) flush_counts();
     if (err) atomicOr(&ls.jobs[ls.job_ids[job_k]].state->err, err);
+}
+
+// the walks k_trace_photons handed over once its queue was drained: one warp per walk, resumed at
+// the node, closest hit and step count where its lane stopped
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_photons_tail(LaunchSet ls, RayQueue q) {
+    const uint32_t n = q.counters[4];
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    const unsigned lane = threadIdx.x & 31;
+    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += warps) {
+        const uint32_t idx = q.tail_list[w];
+        const float4 o = q.org[idx], d = q.dir[idx], hr = q.hit[idx], ts = q.tail_state[idx];
+        const int job_k = find_job(ls, __float_as_uint(o.w));
+        const JobDesc& J = ls.jobs[ls.job_ids[job_k]];
+        Hit h0;
+        h0.t = ts.x;
+        h0.mat = __float_as_int(ts.y);
+        h0.tri = __float_as_int(hr.x);
+        h0.bu = hr.y;
+        h0.bv = hr.z;
+        h0.bw = hr.w;
+        uint32_t err = 0;
+        TraversalCount ct;
+        const Hit h = coop_trace_exact_from<true, COUNT>(J.scene, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), false, err,
+                                                         &ct, __float_as_int(ts.z), h0, (uint32_t)__float_as_int(ts.w));
+        if (lane == 0) {
+            q.hit[idx] = make_float4(__int_as_float(h.tri), h.bu, h.bv, h.bw);
+            if (err) atomicOr(&J.state->err, err);
+            if (COUNT) {
+                atomicAdd(&J.state->count_nodes, (unsigned long long)ct.nodes);
+                atomicAdd(&J.state->count_tris, (unsigned long long)ct.tris);
+                atomicAdd(&J.state->count_segments, 1ull);
+            }
+        }
+    }
 }
 
 // the rays k_trace_photons set aside (slab_degenerate directions), one block of 1024 threads per
@@ -1888,6 +1952,11 @@ void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool coun
     if (!ls.total) return;
     if (count) k_trace_photons<true><<<persistent_blocks, 128, 0, s>>>(ls, q);
     else k_trace_photons<false><<<persistent_blocks, 128, 0, s>>>(ls, q);
+    if (q.tail_lanes && q.tail_list) {
+        // one warp per handed-over walk: enough warps for every SM
+        if (count) k_trace_photons_tail<true><<<persistent_blocks, 128, 0, s>>>(ls, q);
+        else k_trace_photons_tail<false><<<persistent_blocks, 128, 0, s>>>(ls, q);
+    }
     launch_trace_photons_coop(ls, q, count, s);
 }
 void launch_trace_photons_coop(const LaunchSet& ls, const RayQueue& q, bool count, cudaStream_t s) {

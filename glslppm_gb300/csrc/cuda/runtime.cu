@@ -12,6 +12,10 @@ using sppm::fail;
 
 namespace sppm_rt {
 
+// exact traversal: walking lanes at or below which a warp finishes its walks cooperatively
+// once the ray queue is drained (sppm_tuning.trace_tail_lanes = 0)
+constexpr uint32_t kDefaultTailLanes = 8;
+
 int Arena::reserve(size_t bytes) {
     release();
     size = bytes;
@@ -909,7 +913,7 @@ int Runner::rebuild() {
         const bool binned = !(flags & SPPM_FLAG_UNBINNED_RAYS);
         const size_t c = std::max<uint32_t>(cap, 1);
         size_t bytes = 3 * Arena::align(c * 16) + Arena::align(64) + Arena::align(c * 4) +
-                       Arena::align(kEyeDeferred * 4);
+                       Arena::align(kEyeDeferred * 4) + Arena::align(c * 4) + Arena::align(c * 16);
         if (binned) bytes += Arena::align(c * 8) + Arena::align(c * 4) + Arena::align(kRayBins * 4);
         if ((st = queue_mem.reserve(bytes))) return st;
         Arena& a = queue_mem;
@@ -919,6 +923,8 @@ int Runner::rebuild() {
         queue.hit = a.take<float4>(c);
         queue.counters = a.take<uint32_t>(16);
         queue.slow = a.take<uint32_t>(c);
+        queue.tail_list = a.take<uint32_t>(c);
+        queue.tail_state = a.take<float4>(c);
         queue.eye_deferred = a.take<uint32_t>(kEyeDeferred);
         if (binned) {
             queue.key = a.take<uint2>(c);
@@ -968,6 +974,7 @@ int Runner::enqueue_frame(uint32_t phase) {
     // traced in queue order
     RayQueue q = queue;
     q.refill_steps = tune.trace_refill_steps;
+    q.tail_lanes = tune.trace_tail_lanes == 0 ? kDefaultTailLanes : (tune.trace_tail_lanes > 32 ? 0u : tune.trace_tail_lanes);
     if (tune.unbinned_rays) {
         q.key = nullptr;
         q.perm = nullptr;
@@ -1166,6 +1173,7 @@ int Runner::set_tuning(const sppm_tuning* t) {
         return fail(SPPM_ERR_ARG, "block sizes are 0 or multiples of 32 up to 128 (eye, store) and 256 (gather)");
     if (t->unbinned_rays > 1) return fail(SPPM_ERR_ARG, "unbinned_rays is 0 or 1");
     if (t->photon_wave && t->photon_wave < 1024) return fail(SPPM_ERR_ARG, "photon_wave is 0 or at least 1024");
+    if (t->trace_tail_lanes > 64) return fail(SPPM_ERR_ARG, "trace_tail_lanes is 0..32, or 33..64 for never");
     SPPM_CK(cudaSetDevice(device));
     SPPM_CK(cudaStreamSynchronize(stream));
     tune = *t;
@@ -1181,6 +1189,7 @@ void Runner::get_tuning(sppm_tuning* t) const {
     if (!t->eye_block) t->eye_block = 128;
     if (!t->store_block) t->store_block = 128;
     if (!t->gather_block) t->gather_block = 256;
+    if (!t->trace_tail_lanes) t->trace_tail_lanes = kDefaultTailLanes;
     if (flags & SPPM_FLAG_UNBINNED_RAYS) t->unbinned_rays = 1;  // created without ray bins
 }
 
@@ -1249,6 +1258,8 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
         if ((st = knob(&sppm_tuning::gather_block, {256u, 128u, 64u}))) return st;
         if ((st = knob(&sppm_tuning::store_block, {128u, 64u}))) return st;
         if ((st = knob(&sppm_tuning::eye_block, {128u, 64u}))) return st;
+        if (precision == SPPM_PRECISION_FP32 && (st = knob(&sppm_tuning::trace_tail_lanes, {64u, 2u, 4u, 8u, 16u})))
+            return st;
         // wavefront queue depth: the whole pass in one wave, or in 2, 4 or 8 waves
         std::vector<uint32_t> waves = {0u};
         for (uint32_t d : {2u, 4u, 8u})
