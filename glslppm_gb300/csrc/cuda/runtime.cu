@@ -12,9 +12,6 @@ using sppm::fail;
 
 namespace sppm_rt {
 
-// exact traversal: walking lanes at or below which a warp finishes its walks cooperatively
-// once the ray queue is drained (sppm_tuning.trace_tail_lanes = 0)
-constexpr uint32_t kDefaultTailLanes = 8;
 
 int Arena::reserve(size_t bytes) {
     release();
@@ -974,7 +971,7 @@ int Runner::enqueue_frame(uint32_t phase) {
     // traced in queue order
     RayQueue q = queue;
     q.refill_steps = tune.trace_refill_steps;
-    q.tail_lanes = tune.trace_tail_lanes == 0 ? kDefaultTailLanes : (tune.trace_tail_lanes > 32 ? 0u : tune.trace_tail_lanes);
+    q.tail_lanes = tune.trace_tail_lanes;
     if (tune.unbinned_rays) {
         q.key = nullptr;
         q.perm = nullptr;
@@ -1173,7 +1170,7 @@ int Runner::set_tuning(const sppm_tuning* t) {
         return fail(SPPM_ERR_ARG, "block sizes are 0 or multiples of 32 up to 128 (eye, store) and 256 (gather)");
     if (t->unbinned_rays > 1) return fail(SPPM_ERR_ARG, "unbinned_rays is 0 or 1");
     if (t->photon_wave && t->photon_wave < 1024) return fail(SPPM_ERR_ARG, "photon_wave is 0 or at least 1024");
-    if (t->trace_tail_lanes > 64) return fail(SPPM_ERR_ARG, "trace_tail_lanes is 0..32, or 33..64 for never");
+    if (t->trace_tail_lanes > 32) return fail(SPPM_ERR_ARG, "trace_tail_lanes is 0 (off) .. 32");
     SPPM_CK(cudaSetDevice(device));
     SPPM_CK(cudaStreamSynchronize(stream));
     tune = *t;
@@ -1189,7 +1186,6 @@ void Runner::get_tuning(sppm_tuning* t) const {
     if (!t->eye_block) t->eye_block = 128;
     if (!t->store_block) t->store_block = 128;
     if (!t->gather_block) t->gather_block = 256;
-    if (!t->trace_tail_lanes) t->trace_tail_lanes = kDefaultTailLanes;
     if (flags & SPPM_FLAG_UNBINNED_RAYS) t->unbinned_rays = 1;  // created without ray bins
 }
 
@@ -1258,7 +1254,7 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
         if ((st = knob(&sppm_tuning::gather_block, {256u, 128u, 64u}))) return st;
         if ((st = knob(&sppm_tuning::store_block, {128u, 64u}))) return st;
         if ((st = knob(&sppm_tuning::eye_block, {128u, 64u}))) return st;
-        if (precision == SPPM_PRECISION_FP32 && (st = knob(&sppm_tuning::trace_tail_lanes, {64u, 2u, 4u, 8u, 16u})))
+        if (precision == SPPM_PRECISION_FP32 && (st = knob(&sppm_tuning::trace_tail_lanes, {0u, 2u, 8u})))
             return st;
         // wavefront queue depth: the whole pass in one wave, or in 2, 4 or 8 waves
         std::vector<uint32_t> waves = {0u};

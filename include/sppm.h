@@ -334,9 +334,9 @@ typedef struct sppm_tuning {
     uint32_t gather_block;        /* of the gather + progressive update (0 = 256; 32..256)      */
     uint32_t unbinned_rays;       /* 1: photon rays traced in queue order instead of binned     */
     uint32_t trace_tail_lanes;    /* exact traversal: once the ray queue is drained, a warp with
-                                     at most this many walking lanes finishes those walks with
-                                     all 32 lanes (the warp-cooperative walk; same results)
-                                     (0 = 8; above 32 = never)                                   */
+                                     at most this many walking lanes hands those walks to a tail
+                                     kernel that finishes each with all 32 lanes of a warp (the
+                                     warp-cooperative walk; same results) (0 = off, up to 32)   */
     uint32_t photon_wave;         /* wavefront queue depth: photon slots generated, binned,
                                      traced and stored per wave of the photon pass, so a wave's
                                      ray queue and photon records stay in L2 from one kernel to
