@@ -1032,11 +1032,8 @@ int Runner::enqueue_frame(uint32_t phase) {
             }
             timed(SPPM_STAGE_PHOTON_STORE, true);
             launch_photon_store_fp32(pho, qw, tune.store_block, stream);
-            timed(SPPM_STAGE_PHOTON_STORE, false);
-        }
-        if (mixed) {
-            timed(SPPM_STAGE_PHOTON_STORE, true);
-            launch_slot_fill(hsh, stream);
+            // the mixed path's slot records are filled after the last wave, inside its store timing
+            if (mixed && w.total == pho.total) launch_slot_fill(hsh, stream);
             timed(SPPM_STAGE_PHOTON_STORE, false);
         }
     }
