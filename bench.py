@@ -429,7 +429,8 @@ def measure_cornell(args, world: int, dev: int, precision: str) -> dict:
         r32.close()
     else:
         cnt = traversal_counters(r)
-    kernel = "k_trace_photons4" if prec == N.PRECISION_MIXED else "k_trace_photons"
+    wide = prec == N.PRECISION_MIXED or bool((tuning or {}).get("wide_bvh"))
+    kernel = "k_trace_photons4" if wide else "k_trace_photons"
     roof = roofline_of(cnt, tr_ms / tr_n if tr_n else 0.0, kernel, "cornell1024", peak, peak_kind, LIMITER_L2)
     r.close()
     # the whole configuration (1000 passes) end to end on a fresh context with the tuned shapes
@@ -854,7 +855,8 @@ def run_large(args, world, local, K, W, prec: int, sc, mesh, setup: dict) -> dic
         r32.run_passes(W)
         cnt = traversal_counters(r32)
         r32.close()
-    kname = "k_trace_photons4" if prec == N.PRECISION_MIXED else "k_trace_photons"
+    wide = prec == N.PRECISION_MIXED or bool((tuning or {}).get("wide_bvh"))
+    kname = "k_trace_photons4" if wide else "k_trace_photons"
     roof = roofline_of(cnt, tr_ms / tr_n if tr_n else 0.0, kname, "largemesh", peak, peak_kind, LIMITER_HBM)
     r.close()
     full = None

@@ -5,8 +5,9 @@
 // node, < 0 ~triangle, INT32_MIN empty); w[2] = lower box bytes x,y,z and upper x; w[3] = upper
 // y,z.  A child box is origin + byte * 2^(exponent-127) per axis, rounded outward when the tree
 // was built; the slab distances are widened by a bound on their rounding, and triangles are
-// tested with the exact path's arithmetic (tri_test_exact), so the closest hit -- triangle, t and
-// barycentrics -- is the exact traversal's except where two triangles give the same t.
+// tested with the exact path's arithmetic (tri_hit_exact), so the closest hit -- triangle, t and
+// barycentrics -- is the exact traversal's; where two triangles give the same t, the leaf ranks of
+// the exact walk's ordering (DevScene::tri_rank) pick the one it meets first.
 #pragma once
 
 #include "device_common.cuh"
@@ -127,9 +128,12 @@ __device__ __forceinline__ void cswap(float& ta, int32_t& ca, float& tb, int32_t
 
 // closest hit through the 4-wide BVH; PHOTON rays skip emitters, eye rays of the first bounce
 // cull back faces (eyeraytrace.fs:130)
+// rank: the leaf positions of the ordering the exact walk would take for this ray (tri_rank of
+// its cube face) or null; at an equal t the triangle the exact walk meets first wins, as there
 template <bool PHOTON>
 __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const float4* __restrict__ tri_isect, f3 org,
-                                       f3 dir, bool cull, float tmax0, uint32_t& err) {
+                                       f3 dir, bool cull, float tmax0, uint32_t& err,
+                                       const int32_t* __restrict__ rank = nullptr) {
     Hit4 h;
     h.t = tmax0;
     h.tri = -1;
@@ -181,7 +185,8 @@ __device__ __forceinline__ Hit4 trace4(const Node4Dev* __restrict__ nodes, const
             const float4 b = __ldg(&tri_isect[(size_t)tri * 3 + 1]);
             const float4 c = __ldg(&tri_isect[(size_t)tri * 3 + 2]);
             float tt, u, v, w;
-            if (tri_test_exact(a, b, c, org, dir, !PHOTON && cull, h.t, tt, u, v, w)) {
+            if (tri_hit_exact(a, b, c, org, dir, !PHOTON && cull, tt, u, v, w) &&
+                (tt < h.t || (rank && tt == h.t && h.tri >= 0 && __ldg(&rank[tri]) < __ldg(&rank[h.tri])))) {
                 h.t = tt;
                 h.tri = tri;
                 h.bu = v;

@@ -84,6 +84,9 @@ struct DevScene {
     const uint8_t* tex;
     const int32_t* mat_layer;
     float mat_rcp;             // MaterialNumRcp = 1 / num_mats
+    // [6][num_tris]: each triangle's leaf position in the six threaded orderings -- the order in
+    // which the exact walk meets it, so the 4-wide walk breaks ties at equal t the same way
+    const int32_t* tri_rank;
 };
 
 struct DevPixels {
@@ -245,8 +248,9 @@ __device__ __forceinline__ float fractf(float x) { return xsub(x, floorf(x)); }
 // operation correctly rounded in the shaders' order, so a triangle's t, u, v and w are the same
 // numbers wherever this is called (plain and mixed traversals alike).  Returns true when the
 // triangle is hit at 0 <= t < tbest; cull: reject det <= 1e-10 (back faces of a first eye bounce).
-__device__ __forceinline__ bool tri_test_exact(const float4& a, const float4& b, const float4& c, f3 org, f3 dir,
-                                               bool cull, float tbest, float& tt, float& u, float& v, float& w) {
+// tri_hit_exact: the same test without the comparison against the closest hit so far.
+__device__ __forceinline__ bool tri_hit_exact(const float4& a, const float4& b, const float4& c, f3 org, f3 dir,
+                                              bool cull, float& tt, float& u, float& v, float& w) {
     const f3 v0 = mk(a.x, a.y, a.z), e0 = mk(a.w, b.x, b.y), e1 = mk(b.z, b.w, c.x);
     const f3 pv = cross(dir, e1);
     const float det = dot(e0, pv);
@@ -257,7 +261,20 @@ __device__ __forceinline__ bool tri_test_exact(const float4& a, const float4& b,
     v = xdiv(dot(dir, qv), det);
     tt = xdiv(dot(e1, qv), det);
     w = xsub(xsub(1.0f, u), v);
-    return u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f && tt < tbest;
+    return u >= 0.0f && v >= 0.0f && tt >= 0.0f && w >= 0.0f;
+}
+__device__ __forceinline__ bool tri_test_exact(const float4& a, const float4& b, const float4& c, f3 org, f3 dir,
+                                               bool cull, float tbest, float& tt, float& u, float& v, float& w) {
+    return tri_hit_exact(a, b, c, org, dir, cull, tt, u, v, w) && tt < tbest;
+}
+
+// the ordering a ray walks: the cube face of its direction (major axis, ties x before y before z;
+// the negative face when that component is < 0)
+__device__ __forceinline__ int cube_face(f3 d) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    if (ax >= ay && ax >= az) return d.x < 0.0f ? 1 : 0;
+    if (ay >= az) return d.y < 0.0f ? 3 : 2;
+    return d.z < 0.0f ? 5 : 4;
 }
 
 // ---- GPURnd (eyeraytrace.fs:326-347) and the cell hash (hash.fs:21-48) ---------------------

@@ -37,13 +37,6 @@ struct Hit {
     float bu, bv, bw;  // Barycentric = (v, w, u)
 };
 
-__device__ __forceinline__ int cube_face(f3 d) {
-    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
-    if (ax >= ay && ax >= az) return d.x < 0.0f ? 1 : 0;
-    if (ay >= az) return d.y < 0.0f ? 3 : 2;
-    return d.z < 0.0f ? 5 : 4;
-}
-
 // bin of a queued ray: direction class (cube face x signs of the two minor components) and the
 // Morton index of its origin's cell in a grid over the scene's bounding cube
 __device__ __forceinline__ uint32_t spread_bits4(uint32_t v) {  // bits 0..3 -> 0, 3, 6, 9
@@ -682,7 +675,8 @@ __device__ __forceinline__ void warp_bbox_atomics(JobState* st, f3 p, int job_k)
 
 // eye rays of the mixed path walk the 4-wide quantised BVH (the material comes from the triangle)
 __device__ __forceinline__ Hit trace_eye4(const DevScene& s, f3 org, f3 dir, bool cull, uint32_t& err) {
-    const Hit4 h4 = trace4<false>(s.nodes4, s.tri_isect, org, dir, cull, 1.0e20f, err);
+    const Hit4 h4 = trace4<false>(s.nodes4, s.tri_isect, org, dir, cull, 1.0e20f, err,
+                                  s.tri_rank ? s.tri_rank + (size_t)cube_face(dir) * s.num_tris : nullptr);
     Hit h;
     h.t = h4.t;
     h.tri = h4.tri;
@@ -1838,9 +1832,10 @@ __global__ void __launch_bounds__(1024) k_debug_trace(DevScene s, const float* o
         // the mixed path's 4-wide quantised traversal (the eye pass's trace4)
         const uint32_t i = grid_tid();
         if (i >= n) return;
-        const Hit4 h = trace4<PHOTON>(s.nodes4, s.tri_isect, mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]),
-                                      mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]), cull != 0,
-                                      PHOTON ? 1.0e30f : 1.0e20f, e);
+        const f3 d3 = mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+        const Hit4 h = trace4<PHOTON>(s.nodes4, s.tri_isect, mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]), d3,
+                                      cull != 0, PHOTON ? 1.0e30f : 1.0e20f, e,
+                                      s.tri_rank ? s.tri_rank + (size_t)cube_face(d3) * s.num_tris : nullptr);
         tri[i] = h.tri;
         t[i] = h.t;
     } else {

@@ -5,8 +5,9 @@
 //    offsets (64-byte nodes: one node fetch tests four boxes), closest-child-first with a stack;
 //    the slab distances are fused multiply-adds widened by a bound on their rounding (never
 //    culling a box the exact arithmetic enters) and triangles are tested with the plain path's
-//    arithmetic, so the reported triangle, t and barycentrics are the exact traversal's except
-//    where two triangles give the same t;
+//    arithmetic, so the reported triangle, t and barycentrics are the exact traversal's (at an
+//    equal t the triangle the exact walk meets first, by the leaf ranks of its ordering) -- which
+//    also lets the plain FP32 path trace through this BVH (sppm_tuning.wide_bvh);
 //  * the photon a hash slot keeps is stored once per slot as a 32-byte record -- cell (int16 x3),
 //    position inside the cell (unorm16 x3), flux (FP16 x3, scaled by 1/(light area * pi)),
 //    direction (snorm16 x3) and the slot's photon count -- so the gather reads one sector per cell
@@ -29,6 +30,15 @@ namespace sppm_dev {
 constexpr int kTraceBlock = 128;
 constexpr int kSmemStack = 16;  // top of each thread's stack, in shared memory (16 KB per block)
 constexpr int kLocalStack = kStack - kSmemStack;  // deeper entries, in local memory (rarely touched)
+
+// at an equal t: does the exact walk meet triangle a before triangle b?  (the leaf ranks of the
+// ray's ordering; looked up only at ties, so the walk keeps no pointer to them)
+__device__ __noinline__ bool met_first(const LaunchSet& ls, int job_k, const Ray4& R, int32_t a, int32_t b) {
+    const DevScene& S = ls.jobs[ls.job_ids[job_k]].scene;
+    if (!S.tri_rank) return false;
+    const int32_t* rank = S.tri_rank + (size_t)cube_face(mk(R.dx, R.dy, R.dz)) * S.num_tris;
+    return __ldg(&rank[a]) < __ldg(&rank[b]);
+}
 
 // photon segments through the 4-wide BVH: persistent warps with dynamic ray fetch (a lane whose
 // ray finished takes the next queued ray), one node per lane per step, closest child first, the
@@ -140,7 +150,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
                 const float4 b = __ldg(&tri_isect[(size_t)code * 3 + 1]);
                 const float4 cc = __ldg(&tri_isect[(size_t)code * 3 + 2]);
                 float tt, u, v, w;
-                if (tri_test_exact(a, b, cc, mk(R.ox, R.oy, R.oz), mk(R.dx, R.dy, R.dz), false, ht, tt, u, v, w)) {
+                if (tri_hit_exact(a, b, cc, mk(R.ox, R.oy, R.oz), mk(R.dx, R.dy, R.dz), false, tt, u, v, w) &&
+                    (tt < ht || (tt == ht && htri >= 0 && met_first(ls, job_k, R, code, htri)))) {
                     ht = tt;
                     htri = code;
                     hbu = v;

@@ -126,6 +126,7 @@ struct Packed {
     std::vector<int32_t> light_tri;
     std::vector<float2> tri_tex;     // empty when no texture coordinate is below 1e10
     std::vector<int32_t> mat_layer;  // [num_materials]
+    std::vector<int32_t> rank;       // [6][num_tris] leaf position of each triangle per ordering
 };
 
 int check_scene(const sppm_scene* s) {
@@ -193,6 +194,7 @@ int pack_scene(const sppm_scene* s, Packed& out) {
         out.shade[(size_t)t * 6 + 5] = make_float4(N[7], N[8], 0.0f, 0.0f);
     }
     out.nodes.resize((size_t)6 * nn);
+    out.rank.assign((size_t)6 * nt, 0x7FFFFFFF);
     std::vector<uint8_t> seen(nn);
     for (int o = 0; o < 6; o++) {
         std::fill(seen.begin(), seen.end(), 0);
@@ -213,6 +215,7 @@ int pack_scene(const sppm_scene* s, Packed& out) {
             d.miss = (raw < 0 || (uint32_t)raw >= nn) ? -1 : raw;
             int32_t tri = s->node_triangle[c];
             if (tri >= (int32_t)nt) return fail(SPPM_ERR_ARG, "node %d: triangle %d out of range", c, tri);
+            if (tri >= 0) out.rank[(size_t)o * nt + tri] = (int32_t)i;
             if (tri >= 0 && s->materials[s->material_ids[tri]].brdf == -1) tri |= kEmitterBit;
             d.tri = tri < 0 ? -1 : tri;
         }
@@ -279,9 +282,10 @@ uint64_t Job::scene_bytes(const sppm_scene& s, uint32_t precision) {
                  2 * Arena::align(std::max<uint64_t>(s.num_lights, 1) * 4) + 1024 +
                  Arena::align((uint64_t)s.num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4) +
                  Arena::align(std::max<uint64_t>(s.num_materials, 1) * 4) + (s.texcoords ? Arena::align(nt * 24) : 0);
-    // the 4-wide tree has at most one node per internal binary node
-    if (precision == SPPM_PRECISION_MIXED) b += Arena::align(std::max<uint64_t>(nn, 1) * sizeof(sppm::Node4));
-    else b += Arena::align(sizeof(sppm::Node4));
+    // the 4-wide tree (both precisions: the plain path may trace through it, sppm_tuning.wide_bvh)
+    // has at most one node per internal binary node; the triangles' leaf ranks take 24 bytes each
+    (void)precision;
+    b += Arena::align(std::max<uint64_t>(nn, 1) * sizeof(sppm::Node4)) + Arena::align(6 * nt * 4);
     return b;
 }
 
@@ -521,13 +525,17 @@ int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
     int st = pack_scene(scene, pk);
     if (st) return st;
     std::vector<sppm::Node4> nodes4;
-    if (cfg.precision == SPPM_PRECISION_MIXED) {
+    {  // both precisions: the plain path may trace through the 4-wide tree too (wide_bvh); a tree
+       // the 4-wide walk cannot take is an error for the mixed path only (the plain path then
+       // keeps its binary walk)
         uint32_t depth = 0;
         const int b4 = sppm::build_bvh4(*scene, nodes4, &depth);
-        if (b4) return fail(SPPM_ERR_ARG, "4-wide BVH construction failed (%d): inconsistent BVH arrays", b4);
-        if (depth > sppm::kBvh4MaxDepth)
+        const bool mixed = cfg.precision == SPPM_PRECISION_MIXED;
+        if (b4 && mixed) return fail(SPPM_ERR_ARG, "4-wide BVH construction failed (%d): inconsistent BVH arrays", b4);
+        if (depth > sppm::kBvh4MaxDepth && mixed)
             return fail(SPPM_ERR_UNSUPPORTED, "4-wide BVH depth %u exceeds the traversal stack (%u levels)", depth,
                         sppm::kBvh4MaxDepth);
+        if (b4 || depth > sppm::kBvh4MaxDepth) nodes4.clear();
         for (auto& n : nodes4)  // photon rays pass through lights: mark leaf triangles of emitters
             for (int k = 0; k < n.count; k++)
                 if (n.child[k] < 0 && n.child[k] != sppm::kChildEmpty) {
@@ -541,6 +549,7 @@ int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
                          Arena::align(std::max<size_t>(pk.light_tri.size(), 1) * 4) +
                          Arena::align(std::max<size_t>(nodes4.size(), 1) * sizeof(sppm::Node4)) + 1024 +
                          Arena::align(pk.tri_tex.size() * sizeof(float2)) + Arena::align(pk.mat_layer.size() * 4) +
+                         Arena::align(pk.rank.size() * 4) +
                          Arena::align((size_t)scene->num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4);
     SPPM_CK(cudaStreamSynchronize(s));
     if ((st = scene_mem.reserve(bytes))) return st;
@@ -571,6 +580,9 @@ int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
         if (!tex) return fail(SPPM_ERR_OOM, "scene arena sizing error (textures)");
         SPPM_CK(cudaMemcpyAsync(tex, scene->textures, tb, cudaMemcpyHostToDevice, s));
     }
+    int32_t* rank = nullptr;
+    if ((st = put(scene_mem, pk.rank, &rank, s))) return st;
+    S.tri_rank = rank;
     S.tri_tex = pk.tri_tex.empty() ? nullptr : ttex;
     S.mat_layer = mlayer;
     S.tex = tex;
@@ -827,6 +839,7 @@ int Runner::init(int dev, uint32_t prec, uint32_t fl, uint32_t interval, uint32_
     SPPM_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
     sms = (uint32_t)nsm;
     trace_fit = precision == SPPM_PRECISION_MIXED ? trace_photons4_blocks_per_sm() : trace_photons_blocks_per_sm();
+    trace_fit4 = trace_photons4_blocks_per_sm();
     trace_blocks = sms * trace_fit;
     graphs.resize(eye_interval + 1);
     dirty = true;
@@ -983,18 +996,22 @@ int Runner::enqueue_frame(uint32_t phase) {
     // the eye pass and the grid it sets run beside the photon generation and traversal (which do
     // not read them); the photon store (hash insertion) waits for the grid
     const bool eye = phase_has_eye(phase);
+    const bool mixed = precision == SPPM_PRECISION_MIXED;
+    // the plain path through the 4-wide BVH (the same hits): not for the traversal-counting pass,
+    // which measures the binary walk
+    const bool wide = mixed || (tune.wide_bvh && wide_ok && !count_traversal);
+    const uint32_t wide_blocks = std::min(trace_blocks, sms * trace_fit4);
     if (eye) {
         SPPM_CK(cudaEventRecord(fork_ev, stream));
         SPPM_CK(cudaStreamWaitEvent(side, fork_ev, 0));
         timed(SPPM_STAGE_EYE, true, side);
-        launch_eye(eye_pix[phase], q, precision == SPPM_PRECISION_MIXED, textured, tune.eye_block, side);
+        launch_eye(eye_pix[phase], q, wide, textured, tune.eye_block, side);
         timed(SPPM_STAGE_EYE, false, side);
         timed(SPPM_STAGE_GRID, true, side);
         launch_grid(d_jobs, eye_ids[phase], eye_pix[phase].njobs, side);
         timed(SPPM_STAGE_GRID, false, side);
         SPPM_CK(cudaEventRecord(join_ev, side));
     }
-    const bool mixed = precision == SPPM_PRECISION_MIXED;
     if ((flags & SPPM_FLAG_FUSED_PHOTON) && !mixed) {
         if (eye) SPPM_CK(cudaStreamWaitEvent(stream, join_ev, 0));
         timed(SPPM_STAGE_PHOTON, true);
@@ -1023,7 +1040,7 @@ int Runner::enqueue_frame(uint32_t phase) {
                 timed(SPPM_STAGE_RAY_BINS, false);
             }
             timed(SPPM_STAGE_PHOTON_TRACE, true);
-            if (mixed) launch_trace_photons4(pho, qw, trace_blocks, stream);
+            if (wide) launch_trace_photons4(pho, qw, mixed ? trace_blocks : wide_blocks, stream);
             else launch_trace_photons_fp32(pho, qw, count_traversal, trace_blocks, stream);
             timed(SPPM_STAGE_PHOTON_TRACE, false);
             if (eye && !joined) {
@@ -1063,6 +1080,7 @@ int Runner::build_graph(uint32_t phase, FrameGraph& g) {
     g.counting = count_traversal;
     g.textured = textured;
     g.fp64 = fp64_stats;
+    g.wide = tune.wide_bvh && wide_ok;
     size_t n = 0;
     SPPM_CK(cudaGraphGetNodes(graph, nullptr, &n));
     std::vector<cudaGraphNode_t> nodes(n);
@@ -1093,13 +1111,15 @@ int Runner::run(uint32_t n) {
     for (const Job* j : active) textured = textured || j->desc.scene.tri_tex != nullptr;
     fp64_stats = false;
     for (const Job* j : active) fp64_stats = fp64_stats || (j->cfg.flags & SPPM_FLAG_FP64_STATISTICS) != 0;
+    wide_ok = true;
+    for (const Job* j : active) wide_ok = wide_ok && j->desc.scene.nodes4 != nullptr;
     // the traversal-counting kernels run eagerly (they are a measurement pass)
     const bool use_graphs = !(flags & SPPM_FLAG_EAGER_LAUNCH) && !count_traversal;
     for (uint32_t k = 0; k < n; k++) {
         const uint32_t phase = (uint32_t)(frames % eye_interval);
         FrameGraph& g = graphs[phase_has_eye(phase) ? phase : eye_interval];
         if (!g.exec || g.mask != timing_mask || g.counting != count_traversal || g.textured != textured ||
-            g.fp64 != fp64_stats) {
+            g.fp64 != fp64_stats || g.wide != (tune.wide_bvh && wide_ok)) {
             // captured, and launched only in graph mode; eager mode keeps it to count kernels
             if ((st = build_graph(phase, g))) return st;
         }
@@ -1168,6 +1188,7 @@ int Runner::set_tuning(const sppm_tuning* t) {
     if (t->unbinned_rays > 1) return fail(SPPM_ERR_ARG, "unbinned_rays is 0 or 1");
     if (t->photon_wave && t->photon_wave < 1024) return fail(SPPM_ERR_ARG, "photon_wave is 0 or at least 1024");
     if (t->trace_tail_lanes > 32) return fail(SPPM_ERR_ARG, "trace_tail_lanes is 0 (off) .. 32");
+    if (t->wide_bvh > 1) return fail(SPPM_ERR_ARG, "wide_bvh is 0 or 1");
     SPPM_CK(cudaSetDevice(device));
     SPPM_CK(cudaStreamSynchronize(stream));
     tune = *t;
@@ -1227,19 +1248,25 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
     std::vector<uint32_t> blocks;
     for (uint32_t b : {trace_fit, (3 * trace_fit + 3) / 4, (trace_fit + 1) / 2})
         if (b >= 1 && std::find(blocks.begin(), blocks.end(), b) == blocks.end()) blocks.push_back(b);
-    // ray order and refill interval interact: searched together as a grid first
-    for (uint32_t ub : {0u, 1u}) {
-        if (ub && !queue.key) continue;
-        for (uint32_t rs : {4u, 8u, 16u, 32u, 64u}) {
-            if (ub == cur.unbinned_rays && rs == cur.trace_refill_steps) continue;
-            sppm_tuning t = cur;
-            t.unbinned_rays = ub;
-            t.trace_refill_steps = rs;
-            float ms = 0.0f;
-            if ((st = measure(t, &ms))) return st;
-            if (ms < 0.99f * cur_ms) {
-                cur = t;
-                cur_ms = ms;
+    // the walk (plain path: binary or 4-wide), ray order and refill interval interact: searched
+    // together as a grid first
+    const uint32_t cur_wide = cur.wide_bvh;
+    for (uint32_t wd : {0u, 1u}) {
+        if (wd != cur_wide && (precision != SPPM_PRECISION_FP32 || !wide_ok)) continue;
+        for (uint32_t ub : {0u, 1u}) {
+            if (ub && !queue.key) continue;
+            for (uint32_t rs : {4u, 8u, 16u, 32u, 64u}) {
+                if (wd == cur.wide_bvh && ub == cur.unbinned_rays && rs == cur.trace_refill_steps) continue;
+                sppm_tuning t = cur;
+                t.wide_bvh = wd;
+                t.unbinned_rays = ub;
+                t.trace_refill_steps = rs;
+                float ms = 0.0f;
+                if ((st = measure(t, &ms))) return st;
+                if (ms < 0.99f * cur_ms) {
+                    cur = t;
+                    cur_ms = ms;
+                }
             }
         }
     }

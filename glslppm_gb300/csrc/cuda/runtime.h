@@ -146,6 +146,7 @@ struct FrameGraph {
     bool counting = false;  // captured with the traversal-counting kernels
     bool textured = false;  // captured with the kernel variants that look up textures
     bool fp64 = false;      // captured with the gather variant for IEEE double statistics
+    bool wide = false;      // captured with the plain path tracing through the 4-wide BVH
     cudaGraphNode_t ev_a[SPPM_STAGE_COUNT] = {}, ev_b[SPPM_STAGE_COUNT] = {};
     void drop();
 };
@@ -189,6 +190,8 @@ struct Runner {
     bool count_traversal = false;
     bool textured = false;         // some active job's scene has texture coordinates
     bool fp64_stats = false;       // some active job keeps IEEE double statistics
+    bool wide_ok = false;          // every active job has the 4-wide BVH (the plain path may use it)
+    uint32_t trace_fit4 = 0;       // 4-wide traversal blocks of 128 threads that fit on one SM
     std::vector<StageEvent> pending;
     size_t open_stage[SPPM_STAGE_COUNT] = {0};  // pending entry of each stage's last start
     std::vector<cudaEvent_t> event_pool;

@@ -110,7 +110,7 @@ class BatchInfo(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("trace_refill_steps", C.c_uint32), ("eye_block", C.c_uint32),
                 ("store_block", C.c_uint32), ("gather_block", C.c_uint32), ("unbinned_rays", C.c_uint32),
-                ("trace_tail_lanes", C.c_uint32), ("photon_wave", C.c_uint32)]
+                ("trace_tail_lanes", C.c_uint32), ("wide_bvh", C.c_uint32), ("photon_wave", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {name: int(getattr(self, name)) for name, _ in self._fields_}

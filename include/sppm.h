@@ -337,6 +337,12 @@ typedef struct sppm_tuning {
                                      at most this many walking lanes hands those walks to a tail
                                      kernel that finishes each with all 32 lanes of a warp (the
                                      warp-cooperative walk; same results) (0 = off, up to 32)   */
+    uint32_t wide_bvh;            /* plain FP32 path: 1 traces eye and photon rays through the
+                                     4-wide quantised BVH (conservative slab tests, the exact
+                                     triangle test, ties at equal t broken by the exact walk's
+                                     order) instead of the binary threaded walk: the same hits,
+                                     fewer node fetches on large scenes.  Ignored by the mixed
+                                     path, which always uses it.                                 */
     uint32_t photon_wave;         /* wavefront queue depth: photon slots generated, binned,
                                      traced and stored per wave of the photon pass, so a wave's
                                      ray queue and photon records stay in L2 from one kernel to

@@ -53,9 +53,10 @@ MIXED_CASES = {
 @pytest.mark.parametrize("case", list(MIXED_CASES))
 def test_mixed_hit_ids_are_exact_or_ties(case):
     """Every photon segment of three passes and every primary eye ray: the 4-wide quantised
-    traversal must report the exact traversal's triangle, or a different triangle at the same t
-    (bit for bit).  A ray that is neither fails the test.  The photon pass's own kernel
-    (k_trace_photons4) must agree with the single-ray 4-wide walk on every one of its rays."""
+    traversal must report the exact traversal's triangle and t -- at an equal t the triangle the
+    exact walk meets first (the leaf ranks of its ordering).  A ray with another triangle fails the
+    test, whether or not its t is the same.  The photon pass's own kernel (k_trace_photons4) must
+    agree with the single-ray 4-wide walk on every one of its rays."""
     make, w, h, pw, ph = MIXED_CASES[case]
     sc, mesh = make()
     cam = g.look_at(sc.camera_origin, sc.camera_lookat, w, h, sc.fov)
@@ -78,6 +79,7 @@ def test_mixed_hit_ids_are_exact_or_ties(case):
         assert bad.size == 0, (f"{case} frame {frame}: {bad.size} of {len(org)} photon segments hit another "
                                f"triangle at another t; first: exact {tri_e[bad[:3]]} {t_e[bad[:3]]}, "
                                f"4-wide {tri_m[bad[:3]]} {t_m[bad[:3]]}")
+        assert n == 0, f"{case} frame {frame}: {ties} ties broken unlike the exact walk"
         # the same triangle gives the same t (the triangle test is the exact path's)
         same = tri_e == tri_m
         assert np.array_equal(t_e[same].view(np.uint32), t_m[same].view(np.uint32))
@@ -87,6 +89,7 @@ def test_mixed_hit_ids_are_exact_or_ties(case):
     n, ties, bad = classify(tri_e, t_e, tri_m, t_m)
     report["eye"] = (len(org), n, ties)
     assert bad.size == 0, f"{case}: {bad.size} eye rays hit another triangle at another t"
+    assert n == 0, f"{case}: {ties} eye-ray ties broken unlike the exact walk"
     print(case, "rays, mismatches, ties:", report)
 
 

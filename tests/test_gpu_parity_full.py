@@ -144,6 +144,41 @@ def test_1024_workload_21_passes_tuned_shapes():
     assert err["rel_rmse"] <= 0.01, err
 
 
+@pytest.mark.parametrize("scene", ["cornell-1024", "variant-398k"])
+def test_plain_path_through_the_4wide_bvh_matches_the_oracle(scene):
+    """sppm_tuning.wide_bvh: the plain FP32 path traced through the 4-wide quantised BVH
+    (conservative slab tests, the exact triangle test, ties at equal t broken in the exact walk's
+    order) gives the oracle's state word for word -- the 1024x1024 workload for 21 passes, and the
+    batched workload's largest job (398k triangles) alone for 11 passes."""
+    import bench
+    from glslppm_gb300 import scenes
+    if scene == "cornell-1024":
+        sc, mesh = bench.cornell_mesh()
+        w = h = pw = 1024
+        ph, checkpoints = 1024, (1, 11, 21)
+    else:
+        sc = scenes.cornell_variant(17).scene
+        mesh = sc.to_mesh()
+        w, h, pw, ph, checkpoints = 512, 512, 1024, 512, (1, 11)
+    cfg = g.default_config(w, height=h, photon_width=pw, photon_height=ph, radius_rule=N.RADIUS_DIAGONAL,
+                           radius_fraction=0.005)
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, w, h, sc.fov)
+    r = g.Renderer(cfg)
+    r.upload_scene(mesh)
+    r.set_camera(cam)
+    r.set_tuning(wide_bvh=1, trace_refill_steps=8, unbinned_rays=1)
+    assert r.get_tuning().wide_bvh == 1
+    o = Oracle(cfg, mesh.scene(), cam)
+    done = 0
+    for k in checkpoints:
+        r.run_passes(k - done)
+        o.run_frames(k - done)
+        done = k
+        r.synchronize()
+        compare(r.read_state, r.read_image, r.frame_info, o, k, f"{scene} through the 4-wide BVH")
+    r.close()
+
+
 def test_batched_workload_jobs_match_the_oracle():
     import bench
     jobs = bench.build_jobs(64)

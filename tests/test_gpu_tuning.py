@@ -22,6 +22,8 @@ TUNINGS = [
     dict(trace_tail_lanes=8),   # a drained warp with at most 8 walking lanes hands them over
     dict(trace_tail_lanes=32, trace_refill_steps=4),  # every drained warp hands its walks over
     dict(trace_tail_lanes=1),
+    dict(wide_bvh=1),  # the plain path through the 4-wide BVH (exact-order ties)
+    dict(wide_bvh=1, trace_refill_steps=4, unbinned_rays=1, photon_wave=1024),
     dict(photon_wave=1024),  # the photon pass in three waves of at most 1024 slots
     dict(photon_wave=2048, unbinned_rays=1, trace_refill_steps=4),
 ]
@@ -84,7 +86,8 @@ def test_defaults_reported_and_bad_shapes_rejected(cornell_c1_mesh):
     assert (t.eye_block, t.store_block, t.gather_block, t.unbinned_rays) == (128, 128, 256, 0)
     for bad in (dict(gather_block=48), dict(eye_block=256), dict(store_block=160),
                 dict(trace_blocks_per_sm=t.trace_blocks_per_sm + 1), dict(unbinned_rays=2),
-                dict(trace_refill_steps=5000), dict(photon_wave=512), dict(trace_tail_lanes=33)):
+                dict(trace_refill_steps=5000), dict(photon_wave=512), dict(trace_tail_lanes=33),
+                dict(wide_bvh=2)):
         with pytest.raises(N.SppmError) as e:
             r.set_tuning(**bad)
         assert e.value.status == N.ERR_ARG, bad
