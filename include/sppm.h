@@ -50,9 +50,10 @@ typedef enum sppm_precision {
        the shaders write it, transcendentals from sppm_fpmath.h.  Bit-identical to the CPU
        restatement of the shaders. */
     SPPM_PRECISION_FP32 = 0,
-    /* Mixed: FMA-contracted traversal over outward-rounded quantised child boxes, photon flux
-       and direction stored in FP16, flux gathered in FP32, per-pixel N, R^2 and tau as double-float
-       pairs (read as doubles). */
+    /* Mixed: 4-wide traversal over outward-rounded quantised child boxes (FMA slab tests widened
+       by their rounding bound, the exact triangle test, ties at equal t in the exact walk's order:
+       the same hits as the plain walk), photon flux and direction stored in FP16, flux gathered in
+       FP32, per-pixel N, R^2 and tau as double-float pairs (read as doubles). */
     SPPM_PRECISION_MIXED = 1
 } sppm_precision;
 
