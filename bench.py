@@ -356,10 +356,21 @@ def roofline_of(cnt, trace_ms_per_launch: float, kernel: str, workload: str, pea
     return out
 
 
-LIMITER_L2 = ("dependent node loads and divergence: the BVH (3 MB) is L2-resident, so DRAM carries only the ray "
-              "queue (dram_frac); issue-active 62%, 12.6 of 32 lanes active (profiles/k_trace_photons_cornell1024.md)")
-LIMITER_HBM = ("BVH and triangles (2.2 GB) exceed L2: node fetches reach DRAM; dependent-load latency at the measured "
-               "dram_frac (profiles/k_trace_photons_largemesh.md)")
+LIMITER_L2 = {
+    "k_trace_photons": ("dependent node loads and divergence: the BVH (3 MB) is L2-resident, so DRAM carries only the "
+                        "ray queue (dram_frac); issue-active 62%, 12.6 of 32 lanes active "
+                        "(profiles/k_trace_photons_cornell1024.md)"),
+    "k_trace_photons4": ("instruction issue: the BVH (3 MB) is L2-resident, so DRAM carries only the ray queue "
+                         "(dram_frac); issue-active 80%, 13.5 of 32 lanes active "
+                         "(profiles/k_trace_photons4_cornell1024.md)"),
+}
+LIMITER_HBM = {
+    "k_trace_photons": ("BVH and triangles (2.2 GB) exceed L2: node fetches reach DRAM; dependent-load latency at the "
+                        "measured dram_frac, issue-active 28% (profiles/k_trace_photons_largemesh.md)"),
+    "k_trace_photons4": ("BVH and triangles (2.2 GB) exceed L2, but the 4-wide walk fetches a quarter as many nodes: "
+                         "instruction issue, issue-active 72% at the measured dram_frac "
+                         "(profiles/k_trace_photons_largemesh.md)"),
+}
 
 
 def measure_cornell(args, world: int, dev: int, precision: str) -> dict:
@@ -431,7 +442,7 @@ def measure_cornell(args, world: int, dev: int, precision: str) -> dict:
         cnt = traversal_counters(r)
     wide = prec == N.PRECISION_MIXED or bool((tuning or {}).get("wide_bvh"))
     kernel = "k_trace_photons4" if wide else "k_trace_photons"
-    roof = roofline_of(cnt, tr_ms / tr_n if tr_n else 0.0, kernel, "cornell1024", peak, peak_kind, LIMITER_L2)
+    roof = roofline_of(cnt, tr_ms / tr_n if tr_n else 0.0, kernel, "cornell1024", peak, peak_kind, LIMITER_L2[kernel])
     r.close()
     # the whole configuration (1000 passes) end to end on a fresh context with the tuned shapes
     rf = make_renderer(dev, precision=prec, eye_pass_interval=args.eye_pass_interval)[0]
@@ -522,8 +533,10 @@ def convergence(dev: int) -> dict | None:
                        device=dev)
         r.upload_scene(mesh)
         r.set_camera(cam)
-        r.run_passes(64)
+        # the whole 256x256 configuration (64 passes) end to end: one sppm_run_passes, one read
+        full = full_config_run(r, 64)
         out[f"{name}_rel_rmse_after_64_passes"] = round(rel_rmse(r.read_image(), ref), 5)
+        out[f"{name}_full_config_256"] = {k: full[k] for k in ("passes", "seconds", "mphotons_per_s")}
         r.close()
     out["calibration_rel_rmse_by_passes"] = cal["rel_rmse_by_passes"]
     return out
@@ -857,7 +870,7 @@ def run_large(args, world, local, K, W, prec: int, sc, mesh, setup: dict) -> dic
         r32.close()
     wide = prec == N.PRECISION_MIXED or bool((tuning or {}).get("wide_bvh"))
     kname = "k_trace_photons4" if wide else "k_trace_photons"
-    roof = roofline_of(cnt, tr_ms / tr_n if tr_n else 0.0, kname, "largemesh", peak, peak_kind, LIMITER_HBM)
+    roof = roofline_of(cnt, tr_ms / tr_n if tr_n else 0.0, kname, "largemesh", peak, peak_kind, LIMITER_HBM[kname])
     r.close()
     full = None
     if not args.no_full_config:
