@@ -361,6 +361,29 @@ int sppm_debug_photon_rays(sppm_ctx* c, float* org, float* dir, uint32_t* photon
     return SPPM_OK;
 }
 
+int sppm_debug_photon_grid(sppm_ctx* c, uint32_t* offsets, size_t offsets_capacity, uint32_t* records,
+                           size_t records_capacity, uint32_t* num_records) {
+    if (!c || !num_records) return fail(SPPM_ERR_ARG, "null argument");
+    if (!(c->job.cfg.flags & SPPM_FLAG_PHOTON_GRID))
+        return fail(SPPM_ERR_STATE, "the context was created without SPPM_FLAG_PHOTON_GRID");
+    SPPM_CK(cudaSetDevice(c->rt.device));
+    SPPM_CK(cudaStreamSynchronize(c->rt.stream));
+    const PhotonGrid& g = c->rt.grid;
+    if (!g.ofs || c->rt.frames == 0) return fail(SPPM_ERR_STATE, "no pass has run yet");
+    const uint32_t hn = c->job.hash_num;
+    uint32_t n = 0;
+    SPPM_CK(cudaMemcpy(&n, g.ofs + hn, 4, cudaMemcpyDeviceToHost));
+    *num_records = n;
+    if (!offsets && !records) return SPPM_OK;  // size query
+    if (!offsets || !records) return fail(SPPM_ERR_ARG, "null argument");
+    if (offsets_capacity < (size_t)hn + 1 || records_capacity < (size_t)n * 4)
+        return fail(SPPM_ERR_ARG, "the grid holds %u slots and %u records: capacities %zu and %zu words", hn, n,
+                    offsets_capacity, records_capacity);
+    SPPM_CK(cudaMemcpy(offsets, g.ofs, ((size_t)hn + 1) * 4, cudaMemcpyDeviceToHost));
+    if (n) SPPM_CK(cudaMemcpy(records, g.rec, (size_t)n * 16, cudaMemcpyDeviceToHost));
+    return SPPM_OK;
+}
+
 int sppm_debug_trace(sppm_ctx* c, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
                      int32_t* tri, float* t) {
     if (!c || !org || !dir || !tri || !t) return fail(SPPM_ERR_ARG, "null argument");

@@ -102,8 +102,10 @@ int sppm_batch_job_bytes(const sppm_batch* b, const sppm_config* cfg, const sppm
     if (!b || !cfg || !scene || !bytes) return fail(SPPM_ERR_ARG, "null argument");
     int st = validate_config(cfg);
     if (st) return st;
-    *bytes = Job::state_bytes(*cfg) + Job::scene_bytes(*scene, cfg->precision) +
-             kQueueBytesPerSlot * (uint64_t)cfg->photon_width * cfg->photon_height;
+    const uint64_t P = (uint64_t)cfg->photon_width * cfg->photon_height;
+    *bytes = Job::state_bytes(*cfg) + Job::scene_bytes(*scene, cfg->precision) + kQueueBytesPerSlot * P;
+    // the launch's counting-sort grid: a 16-byte record per photon slot, an offset per hash slot
+    if (cfg->flags & SPPM_FLAG_PHOTON_GRID) *bytes += 16 * P + 4 * (uint64_t)(cfg->hash_slots ? cfg->hash_slots : P);
     return SPPM_OK;
 }
 

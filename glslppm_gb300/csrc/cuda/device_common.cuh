@@ -10,6 +10,8 @@
 //   pixels  float4 SoA: position, reflectance, normal, rng, (emission, N), (tau, R); int tri; float t
 //   photons float4 SoA: position(+nrm.x), flux(+nrm.y), direction(+nrm.z), rng; int2 (tri, depth)
 //   hash    uint32 winner[slots], uint32 count[slots]
+//   grid    (SPPM_FLAG_PHOTON_GRID) uint2 key[photons]; per launch uint32 ofs[slots + 1] and
+//           16-byte records[photons] in hash-slot order (photon_grid.cuh)
 // float4 SoA keeps every per-item access a single coalesced 16-byte load or store.
 #pragma once
 
@@ -130,6 +132,8 @@ struct JobDesc {
     uint32_t* winner;
     uint32_t* count;
     SlotRec* slots;  // mixed path
+    uint2* grid_key;  // [P] counting-sort grid (SPPM_FLAG_PHOTON_GRID): each stored photon's
+                      // (hash slot, rank among the slot's photons) of the current pass
     JobState* state;
     float* image;  // W*H*3 resolve target
     float cam_pos[3], cam_u[3], cam_v[3], cam_w[3];
@@ -170,6 +174,19 @@ struct RayQueue {
                              // (0: 32 for the exact walk, 8 for the 4-wide one)
     uint32_t tail_lanes;     // exact walk: once the queue is drained, a warp with at most this many
                              // walking lanes finishes them with the warp-cooperative walk (0: never)
+};
+
+// counting-sort photon grid of the jobs of a launch with SPPM_FLAG_PHOTON_GRID, rebuilt every
+// pass: the records of job k's hash slot s are rec[ofs[b + s]] .. rec[ofs[b + s + 1] - 1], b = the
+// job's first hash slot in the launch (the hash-slot launch set's prefix[k]); photon_grid.cuh has
+// the record format and the cells
+struct PhotonGrid {
+    uint32_t* ofs;        // [hash slots of the launch + 1] exclusive prefix sums of the slot counts
+    uint4* rec;           // [photon slots of the launch] 16-byte photon records in slot order
+    uint32_t* tile_sums;  // [tiles of 2048 hash slots] their sums, then exclusive prefix sums
+    uint32_t tiles;
+    uint32_t rec_capacity;
+    uint32_t shift;       // grid cells: the reference's split 2^shift times along each axis
 };
 
 // the work of one launch: items [prefix[k], prefix[k+1]) belong to jobs[job_ids[k]]; a launch

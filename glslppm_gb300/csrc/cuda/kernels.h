@@ -43,15 +43,26 @@ void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool coun
                                uint32_t persistent_blocks, cudaStream_t s);
 void launch_ray_bins(const RayQueue& q, cudaStream_t s);
 void launch_trace_photons_coop(const LaunchSet& ls, const RayQueue& q, bool count_traversal, cudaStream_t s);
-void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, uint32_t block, cudaStream_t s);
+// grid_shift: the counting-sort grid's cell split (log2) for jobs with SPPM_FLAG_PHOTON_GRID
+void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, uint32_t block, uint32_t grid_shift,
+                              cudaStream_t s);
 uint32_t trace_photons_blocks_per_sm();
 
 // mixed-precision path (kernels_mixed.cu)
 void launch_trace_photons4(const LaunchSet& ls, const RayQueue& q, uint32_t persistent_blocks, cudaStream_t s);
 uint32_t trace_photons4_blocks_per_sm();
 void launch_slot_fill(const LaunchSet& hash_slots, cudaStream_t s);
-void launch_gather_mixed(const LaunchSet& ls, uint32_t block, bool any_fp64, cudaStream_t s);
+// grid: the launch's counting-sort photon grid when some job has SPPM_FLAG_PHOTON_GRID (else null),
+// and then ls covers the pixels in 8x4 tiles (a warp per tile); slot_prefix: the hash-slot launch
+// set's prefix sums
+void launch_gather_mixed(const LaunchSet& ls, uint32_t block, bool any_fp64, const uint32_t* slot_prefix,
+                         const PhotonGrid* grid, cudaStream_t s);
 void launch_resolve_mixed(const LaunchSet& ls, uint32_t display, cudaStream_t s);
+
+// counting-sort photon grid (kernels_grid.cu): scan tiles for a launch's hash slots, and the
+// scan of the slots' counts + the scatter of the records, after the photon pass's last store
+uint32_t grid_tiles(uint32_t hash_slots);
+void launch_grid_sort(const LaunchSet& hash_slots, const LaunchSet& photons, const PhotonGrid& grid, cudaStream_t s);
 void launch_gather_fp32(const LaunchSet& ls, uint32_t block, cudaStream_t s);
 void launch_resolve_fp32(const LaunchSet& ls, uint32_t display, cudaStream_t s);
 void launch_hash_build(const float4* pos, const float4* flux, uint32_t pw, uint32_t ph, uint32_t hash_num,

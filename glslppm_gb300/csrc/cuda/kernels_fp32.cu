@@ -24,6 +24,7 @@
 #include "bvh4_trace.cuh"
 #include "device_common.cuh"
 #include "kernels.h"
+#include "photon_grid.cuh"
 
 namespace sppm_dev {
 
@@ -1150,8 +1151,10 @@ __device__ __forceinline__ void photon_terminate(const JobDesc& J, uint32_t sidx
 }
 
 // store the traced photon (photontrace.fs :692-709); returns the hash slot or 0xFFFFFFFF
+// (jobs with SPPM_FLAG_PHOTON_GRID: the slot of the counting-sort grid's cell, split grid_shift
+// times, or 0xFFFFFFFF for a photon outside the grid)
 __device__ __forceinline__ uint32_t photon_store(const JobDesc& J, const JobState* st, uint32_t sidx, const Hit& h,
-                                                 f3 rdir, f3 flux, float depth) {
+                                                 f3 rdir, f3 flux, float depth, uint32_t grid_shift = 0) {
     const DevScene& S = J.scene;
     f3 ppos = mk(0, 0, 0), pnrm = mk(0, 0, 0), pg = mk(0, 0, 0);
     int brdf = 0;
@@ -1170,6 +1173,7 @@ __device__ __forceinline__ uint32_t photon_store(const JobDesc& J, const JobStat
     J.ph.dir[sidx] = f4(rdir, pnrm.z);
     J.ph.hit[sidx] = make_int2(h.tri, (int)depth);
     if (flux.x < 0.0f) return 0xFFFFFFFFu;
+    if (J.flags & SPPM_FLAG_PHOTON_GRID) return grid_photon_slot(J, st, grid_shift, ppos.x, ppos.y, ppos.z);
     // hash.fs main (:51-68): cell = floor((p - BBoxMin) * GridScale), slot = hash(cell)
     const f3 cell = mk(floorf(xmul(xsub(ppos.x, st->bbmin[0]), st->grid_scale)),
                        floorf(xmul(xsub(ppos.y, st->bbmin[1]), st->grid_scale)),
@@ -1187,6 +1191,17 @@ __device__ __forceinline__ void hash_insert(const JobDesc& J, int k, uint32_t si
     const unsigned peers = __match_any_sync(active, key);
     if (store) {
         const uint32_t n = __popc(peers);
+        if (J.flags & SPPM_FLAG_PHOTON_GRID) {
+            // counting-sort grid: the count, and each photon's rank among its slot's photons (the
+            // order of the ranks within a slot is arbitrary: the gather's sums do not depend on it)
+            const int leader = __ffs(peers) - 1;
+            uint32_t base = 0;
+            if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(&J.count[slot], n);
+            base = __shfl_sync(peers, base, leader);
+            const uint32_t below = peers & ((1u << (threadIdx.x & 31)) - 1u);
+            J.grid_key[sidx] = make_uint2(slot, base + __popc(below));
+            return;
+        }
         const uint32_t wmin = __reduce_min_sync(peers, clipped ? 0xFFFFFFFFu : sidx);
         if ((threadIdx.x & 31) == (__ffs(peers) - 1)) {
             atomicAdd(&J.count[slot], n);
@@ -1625,7 +1640,7 @@ __global__ void __launch_bounds__(kBlockWalk) k_trace_photons_coop(LaunchSet ls,
 }
 
 // store: shade the hit of each queued ray, write the photon record, insert it into the grid
-__global__ void __launch_bounds__(128) k_photon_store(LaunchSet ls, RayQueue q) {
+__global__ void __launch_bounds__(128) k_photon_store(LaunchSet ls, RayQueue q, uint32_t grid_shift) {
     const uint32_t qi = grid_tid();
     if (qi >= q.counters[0]) return;
     const float4 o = q.org[qi], d = q.dir[qi], hr = q.hit[qi];
@@ -1642,7 +1657,7 @@ __global__ void __launch_bounds__(128) k_photon_store(LaunchSet ls, RayQueue q) 
     h.mat = h.tri >= 0 ? __float_as_int(__ldg(&J.scene.tri_isect[(size_t)h.tri * 3 + 2]).y) : -1;
     const float4 f = J.ph.flux[sidx];
     const int depth = J.ph.hit[sidx].y;
-    const uint32_t slot = photon_store(J, st, sidx, h, mk(d.x, d.y, d.z), mk(f.x, f.y, f.z), (float)depth);
+    const uint32_t slot = photon_store(J, st, sidx, h, mk(d.x, d.y, d.z), mk(f.x, f.y, f.z), (float)depth, grid_shift);
     q.hit[qi].x = __uint_as_float(slot);  // for the slot records of the mixed path
     hash_insert(J, k, sidx, slot, __activemask());
 }
@@ -1960,9 +1975,10 @@ void launch_trace_photons_coop(const LaunchSet& ls, const RayQueue& q, bool coun
     else k_trace_photons_coop<false><<<64, kBlockWalk, 0, s>>>(ls, q);
 }
 
-void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, uint32_t block, cudaStream_t s) {
+void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, uint32_t block, uint32_t grid_shift,
+                              cudaStream_t s) {
     const uint32_t b = block_or(block, 128);
-    if (ls.total) k_photon_store<<<blocks_for(q.capacity, b), b, 0, s>>>(ls, q);
+    if (ls.total) k_photon_store<<<blocks_for(q.capacity, b), b, 0, s>>>(ls, q, grid_shift);
 }
 
 uint32_t trace_photons_blocks_per_sm() {

@@ -24,6 +24,7 @@
 #include "bvh4_trace.cuh"
 #include "device_common.cuh"
 #include "kernels.h"
+#include "photon_grid.cuh"
 
 namespace sppm_dev {
 
@@ -261,16 +262,284 @@ __device__ __forceinline__ float2 df_add(float2 x, float2 y) {
     return df_fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(x.y, y.y)));
 }
 
-// progressive.fs with the slot records, FP32 flux gathering and double-float statistics (ANY_F64:
-// the variant launched when some job of the launch keeps IEEE double statistics)
-template <bool ANY_F64>
-__global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
+// AccumulatePhotons (progressive.fs:65-95) over EVERY photon within the radius, read from the
+// counting-sort grid: the hit point visits the grid cells its sphere touches (with a margin of a
+// fixed-point unit and 1e-4 of the radius beyond the rounding of the distance test), and counts
+// the photons of each cell (the record's cell equals the visited one: a slot also holds the
+// photons of other cells that hash to it) inside the radius and facing it.  Each counts once; the
+// flux sums are exact (FP16 values as integers in units of 2^-24), so they depend neither on the
+// order of the records within a slot nor on the cells' size.
+__device__ __forceinline__ void grid_accumulate(const PhotonGrid& grid, uint32_t slot_base, uint32_t hash_num,
+                                                const JobState* st, float gx, float gy, float gz, float R2f,
+                                                float4 qn4, float& fx, float& fy, float& fz, float& M) {
+    const int F = grid_frac_bits(st), Fc = grid_cell_bits(F, grid.shift);
+    const float sF = grid_frac_scale(F);
+    const float G = st->grid_scale;
+    // the hit point in grid fixed point (exact products) and the radius in the same units; a
+    // record's coordinate q stands for q + 0.5, and (q + 0.5) - u = q - (u - 0.5), both exact
+    const float ux = __fmul_rn(gx, sF), uy = __fmul_rn(gy, sF), uz = __fmul_rn(gz, sF);
+    const float vx = __fsub_rn(ux, 0.5f), vy = __fsub_rn(uy, 0.5f), vz = __fsub_rn(uz, 0.5f);
+    const float rq2 = __fmul_rn(__fmul_rn(__fmul_rn(R2f, G), G), __fmul_rn(sF, sF));
+    const float rq = sqrtf(rq2) * 1.0001f + 1.0f;
+    auto lo = [&](float u) -> uint32_t {
+        const float v = u - rq;
+        return v > 0.0f ? (uint32_t)v >> Fc : 0u;
+    };
+    auto hi = [&](float u) -> uint32_t {
+        const float v = u + rq;
+        return (v < 2097150.0f ? (uint32_t)v : 2097150u) >> Fc;
+    };
+    const uint32_t x0 = lo(ux), y0 = lo(uy), z0 = lo(uz);
+    const uint32_t nx = hi(ux) - x0 + 1u, ny = hi(uy) - y0 + 1u, nz = hi(uz) - z0 + 1u;
+    // a radius up to the initial one spans at most 2 * 8 / 2 + 2 cells an axis; a hit point
+    // outside the grid or a radius that is not finite gathers nothing
+    const bool sane = ux >= 0.0f && uy >= 0.0f && uz >= 0.0f && rq < 4.0e6f && nx <= 64 && ny <= 64 && nz <= 64;
+    const uint32_t ncell = sane ? nx * ny * nz : 0u;
+    unsigned long long sr = 0, sg = 0, sb = 0;
+    uint32_t m = 0;
+    // the cells in x-fastest order; the next cell's record range is loaded while the current
+    // cell's records are tested
+    uint32_t cx = x0, cy = y0, cz = z0;
+    uint32_t slot = grid_cell_slot(cx, cy, cz, hash_num);
+    uint32_t beg = __ldg(&grid.ofs[slot_base + slot]), end = __ldg(&grid.ofs[slot_base + slot + 1]);
+    for (uint32_t n = 0; n < ncell; n++) {
+        uint32_t nxc = cx + 1u, nyc = cy, nzc = cz;
+        if (nxc == x0 + nx) {
+            nxc = x0;
+            if (++nyc == y0 + ny) {
+                nyc = y0;
+                ++nzc;
+            }
+        }
+        uint32_t nbeg = 0, nend = 0;
+        if (n + 1 < ncell) {
+            const uint32_t ns = grid_cell_slot(nxc, nyc, nzc, hash_num);
+            nbeg = __ldg(&grid.ofs[slot_base + ns]);
+            nend = __ldg(&grid.ofs[slot_base + ns + 1]);
+        }
+        for (uint32_t i = beg; i < end; i++) {
+            const uint4 r = __ldg(&grid.rec[i]);
+            const unsigned long long q = ((unsigned long long)r.y << 32) | r.x;
+            const uint32_t qx = (uint32_t)q & kGridCoordNone, qy = (uint32_t)(q >> 21) & kGridCoordNone,
+                           qz = (uint32_t)(q >> 42);
+            if ((qx >> Fc) != cx || (qy >> Fc) != cy || (qz >> Fc) != cz) continue;
+            const float dx = __fsub_rn((float)qx, vx), dy = __fsub_rn((float)qy, vy), dz = __fsub_rn((float)qz, vz);
+            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            if (!(d2 < rq2)) continue;
+            if (!(grid_oct8_dot(r.w >> 16, qn4.x, qn4.y, qn4.z) < 0.0f)) continue;
+            sr += grid_half_fixed(r.z & 0xFFFFu);
+            sg += grid_half_fixed(r.z >> 16);
+            sb += grid_half_fixed(r.w & 0xFFFFu);
+            m++;
+        }
+        cx = nxc, cy = nyc, cz = nzc;
+        beg = nbeg, end = nend;
+    }
+    fx = __fmul_rn(__ull2float_rn(sr), 5.9604644775390625e-8f);  // * 2^-24 (exact)
+    fy = __fmul_rn(__ull2float_rn(sg), 5.9604644775390625e-8f);
+    fz = __fmul_rn(__ull2float_rn(sb), 5.9604644775390625e-8f);
+    M = (float)m;
+}
+
+// The grid gather of a warp's 32 pixels (an 8x4 tile).  Neighbouring hit points visit mostly the
+// same cells, so when every lane with a hit point belongs to the same job and the union of the
+// lanes' cell boxes holds at most kCoopMaxCells cells (and at most four times the largest lane's
+// box), the warp walks that union together: a lane per cell looks up the cells' record ranges in
+// one round, a warp scan concatenates them, and the concatenated records are loaded and decoded in
+// batches of 32 (a lane per record, the test that the record lies in its cell included) into
+// shared memory, where every lane tests every record of the batch against its own hit point.  A
+// lane accepts exactly the photons inside its radius (the union holds all of them, and each photon
+// sits in one cell), so its sums equal its own walk's; otherwise every lane walks its own cells
+// (grid_accumulate).  All 32 lanes call it.
+constexpr uint32_t kCoopMaxCells = 64;
+
+struct GridWarpSmem {
+    uint32_t cell_off[kCoopMaxCells + 1];  // the cells' first index in the concatenation
+    uint32_t cell_beg[kCoopMaxCells];      // their first record
+    float4 rec[32];                        // the batch: the position (cells' fixed point) + flux r|g
+    uint32_t w[32];                        // flux b | direction
+};
+
+__device__ __forceinline__ void grid_gather_warp(const LaunchSet& ls, const uint32_t* slot_prefix,
+                                                 const PhotonGrid& grid, bool live, uint32_t k_in, uint32_t p,
+                                                 GridWarpSmem& sm, float& fx, float& fy, float& fz, float& M) {
+    const unsigned full = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    bool has = false;
+    uint32_t k = 0;
+    float gx = 0.0f, gy = 0.0f, gz = 0.0f, R2f = 0.0f, vx = 0.0f, vy = 0.0f, vz = 0.0f, rq2 = 0.0f;
+    float4 qn4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint32_t x0 = 0xFFFFFFFFu, y0 = 0xFFFFFFFFu, z0 = 0xFFFFFFFFu, x1 = 0, y1 = 0, z1 = 0, own = 0;
+    int Fc = 0;
+    const JobState* st = nullptr;
+    if (live) {
+        k = k_in;
+        const JobDesc& J = ls.jobs[ls.job_ids[k]];
+        if ((J.flags & SPPM_FLAG_PHOTON_GRID) && J.px.tri[p] >= 0) {
+            st = J.state;
+            const bool f64 = (J.flags & SPPM_FLAG_FP64_STATISTICS) != 0;
+            if (st->frame == 0) {
+                R2f = f64 ? (float)((double)st->r0 * (double)st->r0) : __fmul_rn(st->r0, st->r0);
+            } else if (f64) {
+                R2f = (float)reinterpret_cast<const double*>(J.px.stat_r2)[p];
+            } else {
+                const float2 r2 = J.px.stat_r2[p];
+                R2f = r2.x + r2.y;
+            }
+            const float G = st->grid_scale;
+            const float4 qp4 = J.px.pos[p];
+            qn4 = J.px.nrm[p];
+            gx = __fmul_rn(fabsf(__fsub_rn(qp4.x, st->bbmin[0])), G);
+            gy = __fmul_rn(fabsf(__fsub_rn(qp4.y, st->bbmin[1])), G);
+            gz = __fmul_rn(fabsf(__fsub_rn(qp4.z, st->bbmin[2])), G);
+            const int F = grid_frac_bits(st);
+            Fc = grid_cell_bits(F, grid.shift);
+            const float sF = grid_frac_scale(F);
+            const float ux = __fmul_rn(gx, sF), uy = __fmul_rn(gy, sF), uz = __fmul_rn(gz, sF);
+            vx = __fsub_rn(ux, 0.5f), vy = __fsub_rn(uy, 0.5f), vz = __fsub_rn(uz, 0.5f);
+            rq2 = __fmul_rn(__fmul_rn(__fmul_rn(R2f, G), G), __fmul_rn(sF, sF));
+            const float rq = sqrtf(rq2) * 1.0001f + 1.0f;
+            if (ux >= 0.0f && uy >= 0.0f && uz >= 0.0f && rq < 4.0e6f) {
+                has = true;
+                auto lo = [&](float u) -> uint32_t {
+                    const float v = u - rq;
+                    return v > 0.0f ? (uint32_t)v >> Fc : 0u;
+                };
+                auto hi = [&](float u) -> uint32_t {
+                    const float v = u + rq;
+                    return (v < 2097150.0f ? (uint32_t)v : 2097150u) >> Fc;
+                };
+                x0 = lo(ux), y0 = lo(uy), z0 = lo(uz), x1 = hi(ux), y1 = hi(uy), z1 = hi(uz);
+                own = (x1 - x0 + 1u) * (y1 - y0 + 1u) * (z1 - z0 + 1u);
+            }
+        }
+    }
+    fx = fy = fz = M = 0.0f;
+    const unsigned hasmask = __ballot_sync(full, has);
+    if (!hasmask) return;
+    const uint32_t kmin = __reduce_min_sync(full, has ? k : 0xFFFFFFFFu);
+    const uint32_t kmax = __reduce_max_sync(full, has ? k : 0u);
+    const uint32_t X0 = __reduce_min_sync(full, x0), Y0 = __reduce_min_sync(full, y0), Z0 = __reduce_min_sync(full, z0);
+    const uint32_t X1 = __reduce_max_sync(full, x1), Y1 = __reduce_max_sync(full, y1), Z1 = __reduce_max_sync(full, z1);
+    const uint32_t own_max = __reduce_max_sync(full, own);
+    const uint32_t UX = X1 - X0 + 1u, UY = Y1 - Y0 + 1u, UZ = Z1 - Z0 + 1u;
+    const unsigned long long ucells = (unsigned long long)UX * UY * UZ;
+    if (kmin != kmax || ucells > 4ull * own_max || ucells > kCoopMaxCells) {
+        if (has) {
+            const JobDesc& J = ls.jobs[ls.job_ids[k]];
+            grid_accumulate(grid, __ldg(&slot_prefix[k]), J.hash_num, st, gx, gy, gz, R2f, qn4, fx, fy, fz, M);
+        }
+        return;
+    }
+    // the warp's job (uniform)
+    const JobDesc& J = ls.jobs[ls.job_ids[kmin]];
+    const uint32_t slot_base = __ldg(&slot_prefix[kmin]), hash_num = J.hash_num, nc = (uint32_t)ucells;
+    const int Fw = __shfl_sync(full, Fc, __ffs(hasmask) - 1);
+    // a lane per cell (two rounds for up to 64 cells): the record ranges, concatenated by a scan
+    uint32_t run = 0;
+    for (uint32_t c0 = 0; c0 < nc; c0 += 32u) {
+        const uint32_t c = c0 + lane;
+        uint32_t b = 0, n = 0;
+        if (c < nc) {
+            const uint32_t cx = X0 + c % UX, t = c / UX, cy = Y0 + t % UY, cz = Z0 + t / UY;
+            const uint32_t slot = grid_cell_slot(cx, cy, cz, hash_num);
+            b = __ldg(&grid.ofs[slot_base + slot]);
+            n = __ldg(&grid.ofs[slot_base + slot + 1]) - b;
+        }
+        uint32_t incl = n;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(full, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        if (c < nc) {
+            sm.cell_off[c] = run + incl - n;
+            sm.cell_beg[c] = b;
+        }
+        run += __shfl_sync(full, incl, 31);
+    }
+    if (lane == 0) sm.cell_off[nc] = run;
+    __syncwarp();
+    unsigned long long sr = 0, sg = 0, sb = 0;
+    uint32_t m = 0;
+    for (uint32_t base = 0; base < run; base += 32u) {
+        const uint32_t g = base + lane;
+        float4 ent = make_float4(__int_as_float(0x7FC00000), 0.0f, 0.0f, 0.0f);  // NaN: never inside
+        uint32_t w = 0;
+        if (g < run) {
+            // the cell of concatenation index g: the last cell starting at or before g
+            uint32_t lo = 0, hi = nc - 1u;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1u) >> 1;
+                if (sm.cell_off[mid] <= g) lo = mid;
+                else hi = mid - 1u;
+            }
+            const uint32_t cx = X0 + lo % UX, t = lo / UX, cy = Y0 + t % UY, cz = Z0 + t / UY;
+            const uint4 r = __ldg(&grid.rec[sm.cell_beg[lo] + (g - sm.cell_off[lo])]);
+            const unsigned long long q = ((unsigned long long)r.y << 32) | r.x;
+            const uint32_t qx = (uint32_t)q & kGridCoordNone, qy = (uint32_t)(q >> 21) & kGridCoordNone,
+                           qz = (uint32_t)(q >> 42);
+            if ((qx >> Fw) == cx && (qy >> Fw) == cy && (qz >> Fw) == cz)
+                ent = make_float4((float)qx, (float)qy, (float)qz, __uint_as_float(r.z));
+            w = r.w;
+        }
+        sm.rec[lane] = ent;
+        sm.w[lane] = w;
+        __syncwarp();
+        const uint32_t n = run - base < 32u ? run - base : 32u;
+        if (has) {
+            for (uint32_t j = 0; j < n; j++) {
+                const float4 c = sm.rec[j];
+                const float dx = __fsub_rn(c.x, vx), dy = __fsub_rn(c.y, vy), dz = __fsub_rn(c.z, vz);
+                const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                if (!(d2 < rq2)) continue;
+                const uint32_t ww = sm.w[j];
+                if (!(grid_oct8_dot(ww >> 16, qn4.x, qn4.y, qn4.z) < 0.0f)) continue;
+                const uint32_t rz = __float_as_uint(c.w);
+                sr += grid_half_fixed(rz & 0xFFFFu);
+                sg += grid_half_fixed(rz >> 16);
+                sb += grid_half_fixed(ww & 0xFFFFu);
+                m++;
+            }
+        }
+        __syncwarp();
+    }
+    fx = __fmul_rn(__ull2float_rn(sr), 5.9604644775390625e-8f);  // * 2^-24 (exact)
+    fy = __fmul_rn(__ull2float_rn(sg), 5.9604644775390625e-8f);
+    fz = __fmul_rn(__ull2float_rn(sb), 5.9604644775390625e-8f);
+    M = (float)m;
+}
+
+// progressive.fs with the slot records (or, for jobs with SPPM_FLAG_PHOTON_GRID, every photon of
+// the counting-sort grid), FP32 flux gathering and double-float statistics (ANY_F64: the variant
+// launched when some job of the launch keeps IEEE double statistics; ANY_GRID: when some job uses
+// the grid; slot_prefix: the hash-slot launch set's prefix sums)
+template <bool ANY_F64, bool ANY_GRID>
+__global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls, const uint32_t* slot_prefix, PhotonGrid grid) {
     const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gi >= ls.total) return;
-    const int k = find_job(ls, gi);
+    bool live = gi < ls.total;
+    int k = 0;
+    uint32_t p = 0;
+    if (live) {
+        k = find_job(ls, gi);
+        p = gi - ls.prefix[k];
+        if (ANY_GRID) {
+            // the launch covers each job in 8x4-pixel tiles, a warp per tile (neighbouring hit points)
+            const JobDesc& Jt = ls.jobs[ls.job_ids[k]];
+            const uint32_t tw = (Jt.W + 7u) >> 3, tile = p >> 5, lane = p & 31u;
+            const uint32_t px = (tile % tw) * 8u + (lane & 7u), py = (tile / tw) * 4u + (lane >> 3);
+            live = px < Jt.W && py < Jt.H;
+            p = py * Jt.W + px;
+        }
+    }
+    float gfx = 0.0f, gfy = 0.0f, gfz = 0.0f, gM = 0.0f;
+    if (ANY_GRID) {
+        __shared__ GridWarpSmem s_grid[256 / 32];
+        grid_gather_warp(ls, slot_prefix, grid, live, (uint32_t)k, p, s_grid[threadIdx.x >> 5], gfx, gfy, gfz, gM);
+    }
+    if (!live) return;
     const JobDesc& J = ls.jobs[ls.job_ids[k]];
     JobState* st = J.state;
-    const uint32_t p = gi - ls.prefix[k];
     const uint32_t frame = st->frame;
     if (p == 0) {
         const uint32_t e = st->emitted_frame;
@@ -304,12 +573,16 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
         const float hs1 = st->hash_scale1;
         const float hn = (float)J.hash_num;
         const float4 qp4 = J.px.pos[p], qn4 = J.px.nrm[p], qr4 = J.px.refl[p];
-        const float gx = fabsf(qp4.x - st->bbmin[0]) * G, gy = fabsf(qp4.y - st->bbmin[1]) * G,
-                    gz = fabsf(qp4.z - st->bbmin[2]) * G;
+        const float gx = __fmul_rn(fabsf(__fsub_rn(qp4.x, st->bbmin[0])), G),
+                    gy = __fmul_rn(fabsf(__fsub_rn(qp4.y, st->bbmin[1])), G),
+                    gz = __fmul_rn(fabsf(__fsub_rn(qp4.z, st->bbmin[2])), G);
         const float ix = floorf(gx - 0.5f), iy = floorf(gy - 0.5f), iz = floorf(gz - 0.5f);
         const float R2f = R2.x + R2.y;  // the in-radius test in FP32
         const float invG = 1.0f / G;
         float fx = 0.0f, fy = 0.0f, fz = 0.0f, M = 0.0f;
+        if (ANY_GRID && (J.flags & SPPM_FLAG_PHOTON_GRID)) {
+            fx = gfx, fy = gfy, fz = gfz, M = gM;
+        } else {
         uint32_t slots[8];
         hash_cells8(mk(ix, iy, iz), G, hs1, hn, slots);
 #pragma unroll
@@ -337,6 +610,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(LaunchSet ls) {
             fy += frg.y * cf;
             fz += fb_.x * cf;
             M += cf;
+        }
         }
         const float s = J.scene.flux_unscale * 0.318309886f;
         if (f64) {
@@ -416,11 +690,19 @@ uint32_t trace_photons4_blocks_per_sm() {
 void launch_slot_fill(const LaunchSet& hash_slots, cudaStream_t s) {
     if (hash_slots.total) k_slot_fill<<<blocks_for(hash_slots.total, 256), 256, 0, s>>>(hash_slots);
 }
-void launch_gather_mixed(const LaunchSet& ls, uint32_t block, bool any_fp64, cudaStream_t s) {
+void launch_gather_mixed(const LaunchSet& ls, uint32_t block, bool any_fp64, const uint32_t* slot_prefix,
+                         const PhotonGrid* grid, cudaStream_t s) {
     const uint32_t b = block >= 32 && block <= 256 && block % 32 == 0 ? block : 256;
     if (!ls.total) return;
-    if (any_fp64) k_gather_mixed<true><<<blocks_for(ls.total, b), b, 0, s>>>(ls);
-    else k_gather_mixed<false><<<blocks_for(ls.total, b), b, 0, s>>>(ls);
+    const PhotonGrid g = grid ? *grid : PhotonGrid{};
+    const uint32_t n = blocks_for(ls.total, b);
+    if (grid) {
+        if (any_fp64) k_gather_mixed<true, true><<<n, b, 0, s>>>(ls, slot_prefix, g);
+        else k_gather_mixed<false, true><<<n, b, 0, s>>>(ls, slot_prefix, g);
+    } else {
+        if (any_fp64) k_gather_mixed<true, false><<<n, b, 0, s>>>(ls, slot_prefix, g);
+        else k_gather_mixed<false, false><<<n, b, 0, s>>>(ls, slot_prefix, g);
+    }
 }
 void launch_resolve_mixed(const LaunchSet& ls, uint32_t display, cudaStream_t s) {
     if (ls.total) k_resolve_mixed<<<blocks_for(ls.total, 256), 256, 0, s>>>(ls, display);

@@ -62,6 +62,8 @@ int validate_config(const sppm_config* c) {
     if (c->eye_pass_interval > 4096) return fail(SPPM_ERR_ARG, "eye_pass_interval must be at most 4096");
     if ((c->flags & SPPM_FLAG_FP64_STATISTICS) && c->precision != SPPM_PRECISION_MIXED)
         return fail(SPPM_ERR_ARG, "SPPM_FLAG_FP64_STATISTICS applies to SPPM_PRECISION_MIXED only");
+    if ((c->flags & SPPM_FLAG_PHOTON_GRID) && c->precision != SPPM_PRECISION_MIXED)
+        return fail(SPPM_ERR_ARG, "SPPM_FLAG_PHOTON_GRID applies to SPPM_PRECISION_MIXED only");
     return SPPM_OK;
 }
 
@@ -272,6 +274,7 @@ uint64_t Job::state_bytes(const sppm_config& cfg) {
     b += 2 * Arena::align(hn * 4);
     if (cfg.precision == SPPM_PRECISION_MIXED)
         b += Arena::align(hn * sizeof(SlotRec)) + 2 * Arena::align(np * 8) + Arena::align(np * 24);
+    if (cfg.flags & SPPM_FLAG_PHOTON_GRID) b += Arena::align(P * 8);
     return b;
 }
 
@@ -331,6 +334,10 @@ int Job::init(const sppm_config& c, JobDesc* dd, uint32_t sl, cudaStream_t s) {
         J.px.stat_r2 = a.take<float2>(np);
         J.px.stat_tau = a.take<float2>(np * 3);
         if (!J.px.stat_tau) return fail(SPPM_ERR_OOM, "state arena sizing error (mixed)");
+    }
+    if (c.flags & SPPM_FLAG_PHOTON_GRID) {
+        J.grid_key = a.take<uint2>(P);
+        if (!J.grid_key) return fail(SPPM_ERR_OOM, "state arena sizing error (photon grid)");
     }
     if (!J.count) return fail(SPPM_ERR_OOM, "state arena sizing error");
     J.state = d_state;
@@ -860,20 +867,24 @@ int Runner::rebuild() {
     // launch tables: ids[n], prefix pixels/photons/hash [n+1] each, then per phase the ids and
     // pixel prefix of the jobs that start an eye pass at that phase
     std::vector<uint32_t> t;
-    t.reserve(4 * (size_t)n + 3 + (size_t)L * (2 * n + 1));
-    uint64_t tot[3] = {0, 0, 0};
+    t.reserve(5 * (size_t)n + 4 + (size_t)L * (2 * n + 1));
+    uint64_t tot[4] = {0, 0, 0, 0};
     for (Job* j : active) t.push_back(j->slot);
     const size_t pre = t.size();
-    for (int w = 0; w < 3; w++) {
+    // pixels, photon slots, hash slots, and the threads of the pixels in 8x4 tiles (a warp per tile)
+    for (int w = 0; w < 4; w++) {
         uint64_t acc = 0;
         for (Job* j : active) {
             t.push_back((uint32_t)acc);
-            acc += w == 0 ? j->npix : (w == 1 ? j->P : j->hash_num);
+            acc += w == 0 ? j->npix
+                 : w == 1 ? j->P
+                 : w == 2 ? j->hash_num
+                          : 32ull * ((j->W + 7) / 8) * ((j->H + 3) / 4);
         }
         t.push_back((uint32_t)acc);
         tot[w] = acc;
     }
-    if (tot[0] > 0xFFFFFFFFull || tot[1] > (1ull << 31) || tot[2] > 0xFFFFFFFFull)
+    if (tot[0] > 0xFFFFFFFFull || tot[1] > (1ull << 31) || tot[2] > 0xFFFFFFFFull || tot[3] > 0xFFFFFFFFull)
         return fail(SPPM_ERR_OOM, "jobs exceed 2^32 pixels or hash slots or 2^31 photon slots in one launch");
     std::vector<size_t> eye_off(L), eye_cnt(L);
     for (uint32_t p = 0; p < L; p++) {
@@ -907,6 +918,7 @@ int Runner::rebuild() {
     pix = mk(0, pre, n, tot[0]);
     pho = mk(0, pre + (n + 1), n, tot[1]);
     hsh = mk(0, pre + 2 * (n + 1), n, tot[2]);
+    pix_tiles = mk(0, pre + 3 * (n + 1), n, tot[3]);
     eye_pix.assign(L, LaunchSet{});
     eye_ids.assign(L, nullptr);
     for (uint32_t p = 0; p < L; p++) {
@@ -944,6 +956,34 @@ int Runner::rebuild() {
         queue.capacity = (uint32_t)c;
         SPPM_CK(cudaMemset(queue.counters, 0, 64));
     }
+    // the counting-sort photon grid, when some job uses it: offsets per hash slot (+1), a record
+    // per photon slot and the scan's tile sums, for the whole launch
+    any_grid = false;
+    for (const Job* j : active) any_grid = any_grid || (j->cfg.flags & SPPM_FLAG_PHOTON_GRID) != 0;
+    if (any_grid) {
+        const uint32_t tiles = grid_tiles((uint32_t)tot[2]);
+        const uint64_t need_slots = tot[2] + 1, need_photons = std::max<uint64_t>(tot[1], 1);
+        if (need_slots > grid_slots_cap || need_photons > grid_photons_cap || tiles > grid_tiles_cap) {
+            const size_t bytes = Arena::align(need_slots * 4) + Arena::align(need_photons * 16) +
+                                 Arena::align(std::max<uint32_t>(tiles, 1) * 4);
+            grid = PhotonGrid{};
+            grid_slots_cap = grid_photons_cap = 0;
+            grid_tiles_cap = 0;
+            if ((st = grid_mem.reserve(bytes))) return st;
+            grid.ofs = grid_mem.take<uint32_t>(need_slots);
+            grid.rec = grid_mem.take<uint4>(need_photons);
+            grid.tile_sums = grid_mem.take<uint32_t>(std::max<uint32_t>(tiles, 1));
+            grid_slots_cap = need_slots;
+            grid_photons_cap = need_photons;
+            grid_tiles_cap = tiles;
+        }
+        grid.tiles = tiles;
+        grid.rec_capacity = (uint32_t)grid_photons_cap;
+    }
+    any_slot_records = false;
+    for (const Job* j : active)
+        any_slot_records = any_slot_records || (j->cfg.precision == SPPM_PRECISION_MIXED &&
+                                                !(j->cfg.flags & SPPM_FLAG_PHOTON_GRID));
     dirty = false;
     return SPPM_OK;
 }
@@ -1048,14 +1088,23 @@ int Runner::enqueue_frame(uint32_t phase) {
                 joined = true;
             }
             timed(SPPM_STAGE_PHOTON_STORE, true);
-            launch_photon_store_fp32(pho, qw, tune.store_block, stream);
+            launch_photon_store_fp32(pho, qw, tune.store_block, grid_shift(), stream);
             // the mixed path's slot records are filled after the last wave, inside its store timing
-            if (mixed && w.total == pho.total) launch_slot_fill(hsh, stream);
+            if (mixed && any_slot_records && w.total == pho.total) launch_slot_fill(hsh, stream);
             timed(SPPM_STAGE_PHOTON_STORE, false);
         }
     }
+    if (any_grid) {
+        // the counting-sort grid of the pass: every wave's photons are counted and ranked
+        grid.shift = grid_shift();
+        timed(SPPM_STAGE_PHOTON_SORT, true);
+        launch_grid_sort(hsh, pho, grid, stream);
+        timed(SPPM_STAGE_PHOTON_SORT, false);
+    }
     timed(SPPM_STAGE_GATHER, true);
-    if (mixed) launch_gather_mixed(pix, tune.gather_block, fp64_stats, stream);
+    if (mixed)
+        launch_gather_mixed(any_grid ? pix_tiles : pix, tune.gather_block, fp64_stats, hsh.prefix,
+                            any_grid ? &grid : nullptr, stream);
     else launch_gather_fp32(pix, tune.gather_block, stream);
     timed(SPPM_STAGE_GATHER, false);
     return launch_check("SPPM frame");
@@ -1189,6 +1238,8 @@ int Runner::set_tuning(const sppm_tuning* t) {
     if (t->photon_wave && t->photon_wave < 1024) return fail(SPPM_ERR_ARG, "photon_wave is 0 or at least 1024");
     if (t->trace_tail_lanes > 32) return fail(SPPM_ERR_ARG, "trace_tail_lanes is 0 (off) .. 32");
     if (t->wide_bvh > 1) return fail(SPPM_ERR_ARG, "wide_bvh is 0 or 1");
+    if (t->grid_cell_split > 8 || (t->grid_cell_split & (t->grid_cell_split - 1)))
+        return fail(SPPM_ERR_ARG, "grid_cell_split is 0 (default), 1, 2, 4 or 8");
     SPPM_CK(cudaSetDevice(device));
     SPPM_CK(cudaStreamSynchronize(stream));
     tune = *t;
@@ -1204,6 +1255,7 @@ void Runner::get_tuning(sppm_tuning* t) const {
     if (!t->eye_block) t->eye_block = 128;
     if (!t->store_block) t->store_block = 128;
     if (!t->gather_block) t->gather_block = 256;
+    if (!t->grid_cell_split) t->grid_cell_split = kDefaultGridCellSplit;
     if (flags & SPPM_FLAG_UNBINNED_RAYS) t->unbinned_rays = 1;  // created without ray bins
 }
 
@@ -1285,6 +1337,7 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
         for (uint32_t d : {2u, 4u, 8u})
             if (pho.total / d >= 65536u) waves.push_back((pho.total + d - 1) / d);
         if ((st = knob(&sppm_tuning::photon_wave, waves))) return st;
+        if (any_grid && (st = knob(&sppm_tuning::grid_cell_split, {1u, 2u, 4u}))) return st;
         if (!changed) break;
     }
     if ((st = set_tuning(&cur))) return st;

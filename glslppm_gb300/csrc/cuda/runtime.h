@@ -152,6 +152,8 @@ struct FrameGraph {
 };
 
 // queues the frames of a set of jobs on one stream
+constexpr uint32_t kDefaultGridCellSplit = 2;
+
 struct Runner {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -175,8 +177,20 @@ struct Runner {
     JobDesc* d_jobs = nullptr;
     Arena table_mem, queue_mem;    // rebuilt when the set of jobs changes
     RayQueue queue{};
+    Arena grid_mem;                // counting-sort photon grid (jobs with SPPM_FLAG_PHOTON_GRID)
+    PhotonGrid grid{};
+    uint64_t grid_slots_cap = 0, grid_photons_cap = 0;
+    uint32_t grid_tiles_cap = 0;
+    bool any_grid = false;         // some active job uses the counting-sort photon grid
+    // log2 of the grid cells per reference cell along an axis (sppm_tuning.grid_cell_split)
+    uint32_t grid_shift() const {
+        const uint32_t s = tune.grid_cell_split ? tune.grid_cell_split : kDefaultGridCellSplit;
+        return s >= 8 ? 3u : s >= 4 ? 2u : s >= 2 ? 1u : 0u;
+    }
+    bool any_slot_records = false; // some active mixed job gathers from the slot records
     std::vector<Job*> active;      // launch order
     LaunchSet pix{}, pho{}, hsh{};
+    LaunchSet pix_tiles{};         // the pixels in 8x4 tiles, a warp per tile (the grid gather)
     std::vector<LaunchSet> eye_pix;          // per phase (frame mod eye_interval)
     std::vector<const uint32_t*> eye_ids;    // per phase: the job ids of eye_pix
     uint64_t frames = 0;                     // frames queued

@@ -35,9 +35,11 @@ FLAG_FUSED_PHOTON = 0x2
 FLAG_UNBINNED_RAYS = 0x4
 FLAG_EAGER_LAUNCH = 0x8
 FLAG_FP64_STATISTICS = 0x10
+FLAG_PHOTON_GRID = 0x20
 IMAGE_RADIANCE, IMAGE_DISPLAY = 0, 1
 BVH_GPU_PLOC, BVH_GPU_LBVH = 0, 1
-STAGES = ("frame_begin", "eye", "grid", "photon", "gather", "resolve", "photon_trace", "photon_store", "ray_bins")
+STAGES = ("frame_begin", "eye", "grid", "photon", "gather", "resolve", "photon_trace", "photon_store", "ray_bins",
+          "photon_sort")
 
 STATE = {
     "hit_position": 0, "hit_reflectance": 1, "hit_normal": 2, "eye_rng": 3, "hit_triangle": 4,
@@ -110,7 +112,8 @@ class BatchInfo(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("trace_blocks_per_sm", C.c_uint32), ("trace_refill_steps", C.c_uint32), ("eye_block", C.c_uint32),
                 ("store_block", C.c_uint32), ("gather_block", C.c_uint32), ("unbinned_rays", C.c_uint32),
-                ("trace_tail_lanes", C.c_uint32), ("wide_bvh", C.c_uint32), ("photon_wave", C.c_uint32)]
+                ("trace_tail_lanes", C.c_uint32), ("wide_bvh", C.c_uint32), ("photon_wave", C.c_uint32),
+                ("grid_cell_split", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
@@ -187,6 +190,7 @@ SIGNATURES = {
     "sppm_debug_fpmath": (C.c_int, [C.c_int, P, P, P, C.c_size_t]),
     "sppm_debug_trace": (C.c_int, [P, P, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P]),
     "sppm_debug_photon_rays": (C.c_int, [P, P, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "sppm_debug_photon_grid": (C.c_int, [P, P, C.c_size_t, P, C.c_size_t, C.POINTER(C.c_uint32)]),
     "sppm_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
     "sppm_write_image_file": (C.c_int, [C.c_char_p, P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "sppm_host_free": (None, [P]),

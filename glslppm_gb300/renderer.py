@@ -327,6 +327,18 @@ class Renderer:
                                              C.byref(n)))
         return org[: n.value], dir[: n.value], ph[: n.value]
 
+    def debug_photon_grid(self) -> tuple[np.ndarray, np.ndarray]:
+        """The counting-sort photon grid of the last pass (SPPM_FLAG_PHOTON_GRID): (offsets
+        [hash_slots + 1], records [n, 4] uint32 in slot order; within a slot in no fixed order)."""
+        n = C.c_uint32()
+        N.check(N.lib.sppm_debug_photon_grid(self._h, None, 0, None, 0, C.byref(n)))
+        hn = self.config.hash_slots or self.config.photon_width * self.config.photon_height
+        ofs = np.empty(hn + 1, np.uint32)
+        rec = np.empty((max(n.value, 1), 4), np.uint32)
+        N.check(N.lib.sppm_debug_photon_grid(self._h, ofs.ctypes.data, ofs.size, rec.ctypes.data, rec.size,
+                                             C.byref(n)))
+        return ofs, rec[: n.value]
+
     def save_checkpoint(self) -> bytes:
         """The progressive state as a flat binary (sppm_save_checkpoint)."""
         n = int(N.lib.sppm_checkpoint_bytes(self._h))

@@ -87,6 +87,17 @@ typedef enum sppm_seed_mode {
                                            update them in FP64 arithmetic instead of double-float
                                            pairs (same memory; the GPU's FP64 rate makes the gather
                                            slower) */
+#define SPPM_FLAG_PHOTON_GRID 0x20u /* mixed precision only: the counting-sort photon grid.  After each
+                                       photon pass every stored photon is sorted by hash slot (the
+                                       slots' photon counts, an exclusive scan, a scatter of 16-byte
+                                       records: position in 21-bit grid fixed point, FP16 flux, 8-bit
+                                       octahedral direction), and the gather sums EVERY photon of the
+                                       2x2x2 cells within the radius instead of the slot's winner times
+                                       the slot's count.  The cells, the hash and the radius update are
+                                       the reference's; the per-pass estimate has the same expectation
+                                       and a far smaller variance (the image differs from the plain
+                                       path's, converging to the same limit).  Flux sums are exact
+                                       (integer), so results do not depend on the order of the sort. */
 
 typedef struct sppm_config {
     uint32_t width, height;               /* image (ImageResolution x ImageResolution in the ref)  */
@@ -311,7 +322,8 @@ typedef enum sppm_stage {
     SPPM_STAGE_PHOTON_TRACE = 6, /* photon segment traversal (wavefront pass)              */
     SPPM_STAGE_PHOTON_STORE = 7, /* photon store + hash.fs/scatter/correction (wavefront)  */
     SPPM_STAGE_RAY_BINS = 8,     /* counting sort of the photon rays into bins (wavefront)  */
-    SPPM_STAGE_COUNT = 9
+    SPPM_STAGE_PHOTON_SORT = 9,  /* counting-sort photon grid (SPPM_FLAG_PHOTON_GRID)        */
+    SPPM_STAGE_COUNT = 10
 } sppm_stage;
 int sppm_enable_stage_timing(sppm_ctx* ctx, int enable);
 /* Times only the stages whose bit (1 << stage) is set; 0 turns timing off. */
@@ -348,6 +360,11 @@ typedef struct sppm_tuning {
                                      traced and stored per wave of the photon pass, so a wave's
                                      ray queue and photon records stay in L2 from one kernel to
                                      the next (0 = every slot in one wave; else >= 1024)         */
+    uint32_t grid_cell_split;     /* counting-sort photon grid (SPPM_FLAG_PHOTON_GRID): grid cells
+                                     per reference cell along each axis -- 1, 2, 4 or 8 (0 = 2);
+                                     a hit point visits the cells its radius touches, so finer
+                                     cells mean fewer photons visited and more cells looked up
+                                     (same results)                                              */
 } sppm_tuning;
 /* Block sizes are multiples of 32.  The frame graphs are captured again with the new shapes. */
 int sppm_set_tuning(sppm_ctx* ctx, const sppm_tuning* tuning);
@@ -422,8 +439,9 @@ int sppm_debug_fpmath(int fn, const float* x, const float* y, float* out, size_t
    t (the initial bound when nothing is hit).  mode 0 traces one ray per thread, mode 1 one ray
    per warp, mode 2 one ray per block of 1024 threads (the form the photon pass uses for rays
    with a zero direction component); all give the same result.  Mode 3 traces the mixed
-   path's 4-wide quantised BVH instead (contexts of SPPM_PRECISION_MIXED): its triangle and t equal
-   the exact traversal's except where two triangles give the same t. */
+   path's 4-wide quantised BVH instead (contexts of SPPM_PRECISION_MIXED, or any context whose scene
+   has the 4-wide tree): its triangle and t equal the exact traversal's, ties at equal t included
+   (broken by each triangle's leaf position in the ray's ordering). */
 int sppm_debug_trace(sppm_ctx* ctx, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
                      int32_t* tri, float* t);
 /* The photon rays the last pass traced (the wavefront's ray queue; not with
@@ -431,6 +449,17 @@ int sppm_debug_trace(sppm_ctx* ctx, const float* org, const float* dir, size_t n
    each belongs to.  With org, dir and photon all null only *count is set.  For tests that trace
    the same rays again through sppm_debug_trace. */
 int sppm_debug_photon_rays(sppm_ctx* ctx, float* org, float* dir, uint32_t* photon, size_t capacity, size_t* count);
+/* The counting-sort photon grid of the last pass (contexts with SPPM_FLAG_PHOTON_GRID): offsets
+   [hash_slots + 1] (the records of slot s are offsets[s] .. offsets[s+1]-1) and records [4 words
+   per stored photon] in slot order; *num_records = offsets[hash_slots].  Word 0-1: the position as
+   three 21-bit unsigned fixed-point grid coordinates (x | y << 21 | z << 42 of a 64-bit word, low
+   word first; coordinate = floor((p - bbox_min) * grid_scale * 2^F) with F = 21 - bits(cells + 1),
+   cells = the grid's largest cell count along an axis; all ones: outside the grid); word 2: flux
+   r | g << 16 (FP16, scaled by 1 / (light area * 3.141592)); word 3: flux b | direction << 16
+   (octahedral, two signed 8-bit components).  Within a slot the order of the records is not
+   fixed.  With offsets and records null only *num_records is set. */
+int sppm_debug_photon_grid(sppm_ctx* ctx, uint32_t* offsets, size_t offsets_capacity, uint32_t* records,
+                           size_t records_capacity, uint32_t* num_records);
 /* Page-locked host memory (cudaMallocHost) for the host buffers of sppm_read_image and friends:
    copies to it run at the interconnect's DMA rate instead of being staged through the driver. */
 int sppm_host_alloc(size_t bytes, void** ptr);

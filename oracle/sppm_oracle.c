@@ -273,6 +273,8 @@ typedef struct oracle_ctx {
     uint8_t* p_emitted;
     /* hash table */
     uint32_t *winner, *count;
+    /* counting-sort photon grid (SPPM_FLAG_PHOTON_GRID): photon ids by hash slot, ascending */
+    uint32_t *g_ofs, *g_ids, *g_cur;
     /* frame state */
     uint32_t frame, eye_samples;
     uint32_t xs[4];
@@ -868,6 +870,185 @@ static void gather_pixel(oracle_ctx* c, size_t p) {
 }
 
 /* ------------------------------------------------------------------------------------------ */
+/* counting-sort photon grid (SPPM_FLAG_PHOTON_GRID) -- not part of the reference: the CUDA      */
+/* mixed path's estimator, which keeps every stored photon sorted by the reference's hash slot  */
+/* (hash.fs:51-68) and sums all photons of the 2x2x2 cells inside the radius (progressive.fs's   */
+/* AccumulatePhotons :65-95 over every photon instead of a slot's winner times its count).      */
+/* The single-precision build restates the CUDA records bit for bit (21-bit grid fixed point,   */
+/* FP16 flux scaled by 1/(light area * 3.141592), 8-bit octahedral direction; the CUDA side is  */
+/* glslppm_gb300/csrc/cuda/photon_grid.cuh), so it counts the same photons per pixel and forms  */
+/* the same flux sums; the double-precision build gathers the unquantised photons.              */
+/* ------------------------------------------------------------------------------------------ */
+static uint32_t grid_photon_slot(const oracle_ctx* c, uint32_t id) {
+    const real hs1 = RC(4194304.0) / c->grid_scale;
+    const vec3 pp = xyz(c->p_pos[id]);
+    const vec3 cell = v3(R_FLOOR((pp.x - c->bbmin[0]) * c->grid_scale), R_FLOOR((pp.y - c->bbmin[1]) * c->grid_scale),
+                         R_FLOOR((pp.z - c->bbmin[2]) * c->grid_scale));
+    return hash_cell(cell, c->grid_scale, hs1, (real)c->hash_num);
+}
+
+/* the stored photons (flux >= 0) by slot, ids ascending within a slot */
+static void grid_build(oracle_ctx* c) {
+    memset(c->g_ofs, 0, sizeof(uint32_t) * ((size_t)c->hash_num + 1));
+    for (uint32_t id = 0; id < c->P; id++)
+        if (c->p_flux[id].x >= RC(0.0)) c->g_ofs[grid_photon_slot(c, id) + 1]++;
+    for (uint32_t k = 0; k < c->hash_num; k++) c->g_ofs[k + 1] += c->g_ofs[k];
+    memcpy(c->g_cur, c->g_ofs, sizeof(uint32_t) * c->hash_num);
+    for (uint32_t id = 0; id < c->P; id++)
+        if (c->p_flux[id].x >= RC(0.0)) c->g_ids[c->g_cur[grid_photon_slot(c, id)]++] = id;
+}
+
+#ifndef ORACLE_FP64
+static int grid_frac_bits(const oracle_ctx* c) {
+    uint32_t cells = 0;
+    for (int k = 0; k < 3; k++) {
+        const float e = (c->bbmax[k] - c->bbmin[k]) * c->grid_scale;
+        const uint32_t n = e > 0.0f ? (e < 2097152.0f ? (uint32_t)ceilf(e) : 2097152u) : 0u;
+        if (n > cells) cells = n;
+    }
+    int b = 0;
+    for (uint32_t v = cells + 1u; v; v >>= 1) b++;
+    return b < 21 ? 21 - b : 0;
+}
+static uint32_t grid_coord(float p, float bbmin, float G, float sF) {
+    const float v = ((p - bbmin) * G) * sF;
+    return v >= 0.0f && v < 2097151.0f ? (uint32_t)v : 0x1FFFFFu;
+}
+/* IEEE round-to-nearest-even conversion of a non-negative float of at most 65504 to FP16 bits */
+static uint32_t half_rn(float f) {
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    const uint32_t e = (x >> 23) & 0xFFu, m = x & 0x7FFFFFu;
+    if (e == 0) return 0u;
+    const int he = (int)e - 112; /* FP16 biased exponent */
+    if (he <= 0) {               /* FP16 subnormal: the value in units of 2^-24 is (m | 2^23) / 2^(126 - e) */
+        const uint32_t s = 126u - e, mf = m | 0x800000u;
+        if (s > 24u) return 0u;
+        const uint32_t q = mf >> s, rem = mf & ((1u << s) - 1u), half = 1u << (s - 1u);
+        return q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u);
+    }
+    uint32_t h = ((uint32_t)he << 10) | (m >> 13);
+    const uint32_t rem = m & 0x1FFFu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+    return h;
+}
+static uint32_t grid_oct8(float x, float y, float z) {
+    const float s = (fabsf(x) + fabsf(y)) + fabsf(z);
+    if (!(s > 0.0f)) return 0u;
+    float ox = x / s, oy = y / s;
+    if (z < 0.0f) {
+        const float tx = (1.0f - fabsf(oy)) * copysignf(1.0f, ox);
+        const float ty = (1.0f - fabsf(ox)) * copysignf(1.0f, oy);
+        ox = tx;
+        oy = ty;
+    }
+    const int a = (int)lrintf(ox * 127.0f), b = (int)lrintf(oy * 127.0f);
+    return ((uint32_t)a & 0xFFu) | (((uint32_t)b & 0xFFu) << 8);
+}
+static float grid_oct8_dot(uint32_t code, float nx, float ny, float nz) {
+    float x = (float)(int)(int8_t)(code & 0xFFu), y = (float)(int)(int8_t)((code >> 8) & 0xFFu);
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float z = 127.0f - ax - ay;
+    if (z < 0.0f) {
+        const float tx = (127.0f - ay) * copysignf(1.0f, x);
+        y = (127.0f - ax) * copysignf(1.0f, y);
+        x = tx;
+    }
+    return (nx * x + ny * y) + nz * z;
+}
+static uint64_t half_fixed(uint32_t h) {
+    const uint32_t e = (h >> 10) & 31u, m = h & 1023u;
+    return e ? (uint64_t)(m | 1024u) << (e - 1u) : (uint64_t)m;
+}
+#endif
+
+static void grid_gather_pixel(oracle_ctx* c, size_t p) {
+    const real G = c->grid_scale;
+    const real hs1 = RC(4194304.0) / G;
+    const real hn = (real)c->hash_num;
+    const real alpha = (real)c->cfg.alpha;
+    const vec3 qp = xyz(c->q_pos[p]), qn = xyz(c->q_nrm[p]);
+    vec4 qfr = c->q_flux_r[p];
+    vec4 qe = c->q_emi_n[p];
+    const vec3 qr = xyz(c->q_refl[p]);
+    real N = qe.w;
+    real R = qfr.w;
+    vec3 tau = xyz(qfr);
+    if (c->q_tri[p] >= 0) {
+        const real gx = R_FABS(qp.x - c->bbmin[0]) * G, gy = R_FABS(qp.y - c->bbmin[1]) * G,
+                   gz = R_FABS(qp.z - c->bbmin[2]) * G;
+        vec3 flux = v3(0, 0, 0);
+        real M = RC(0.0);
+        /* the reference cells the sphere of radius R touches (every photon inside R is in one) */
+#ifndef ORACLE_FP64
+        const int F = grid_frac_bits(c);
+        const float sF = ldexpf(1.0f, F);
+        const float ux = gx * sF, uy = gy * sF, uz = gz * sF;
+        const float rq2 = ((R * R * G) * G) * (sF * sF);
+        const float rq = sqrtf(rq2) * 1.0001f + 1.0f;
+        const float fu = c->sc.light_area != 0.0f ? c->sc.light_area * 3.141592f : 1.0f, fs = 1.0f / fu;
+        uint64_t sr = 0, sg = 0, sb = 0;
+        uint32_t m = 0;
+#define GRID_LO(u) ((u) - rq > 0.0f ? (int)((uint32_t)((u) - rq) >> F) : 0)
+#define GRID_HI(u) ((int)(((u) + rq < 2097150.0f ? (uint32_t)((u) + rq) : 2097150u) >> F))
+        const int x0 = GRID_LO(ux), x1 = GRID_HI(ux), y0 = GRID_LO(uy), y1 = GRID_HI(uy), z0 = GRID_LO(uz),
+                  z1 = GRID_HI(uz);
+#undef GRID_LO
+#undef GRID_HI
+#else
+        const real rg = R * G * (1.0 + 1e-9);
+        const int x0 = (int)floor(gx - rg), x1 = (int)floor(gx + rg), y0 = (int)floor(gy - rg), y1 = (int)floor(gy + rg),
+                  z0 = (int)floor(gz - rg), z1 = (int)floor(gz + rg);
+#endif
+        for (int iz = z0; iz <= z1; iz++) {
+            for (int iy = y0; iy <= y1; iy++) {
+                for (int ix = x0; ix <= x1; ix++) {
+                    const vec3 cell = v3((real)ix, (real)iy, (real)iz);
+                    const uint32_t slot = hash_cell(cell, G, hs1, hn);
+                    for (uint32_t k = c->g_ofs[slot]; k < c->g_ofs[slot + 1]; k++) {
+                        const uint32_t id = c->g_ids[k];
+                        const vec4 pf = c->p_flux[id], pp = c->p_pos[id], pd = c->p_dir[id];
+#ifndef ORACLE_FP64
+                        const uint32_t qx = grid_coord(pp.x, c->bbmin[0], G, sF), qy = grid_coord(pp.y, c->bbmin[1], G, sF),
+                                       qz = grid_coord(pp.z, c->bbmin[2], G, sF);
+                        if ((qx >> F) != (uint32_t)cell.x || (qy >> F) != (uint32_t)cell.y || (qz >> F) != (uint32_t)cell.z)
+                            continue;
+                        const float dx = ((float)qx + 0.5f) - ux, dy = ((float)qy + 0.5f) - uy, dz = ((float)qz + 0.5f) - uz;
+                        if (!((dx * dx + dy * dy) + dz * dz < rq2)) continue;
+                        if (!(grid_oct8_dot(grid_oct8(pd.x, pd.y, pd.z), qn.x, qn.y, qn.z) < 0.0f)) continue;
+                        sr += half_fixed(half_rn(fminf(pf.x * fs, 65504.0f)));
+                        sg += half_fixed(half_rn(fminf(pf.y * fs, 65504.0f)));
+                        sb += half_fixed(half_rn(fminf(pf.z * fs, 65504.0f)));
+                        m++;
+#else
+                        const vec3 pc = v3(R_FLOOR((pp.x - c->bbmin[0]) * G), R_FLOOR((pp.y - c->bbmin[1]) * G),
+                                           R_FLOOR((pp.z - c->bbmin[2]) * G));
+                        if (pc.x != cell.x || pc.y != cell.y || pc.z != cell.z) continue;
+                        if (!(length3(sub3(xyz(pp), qp)) < R && dot3(qn, neg3(xyz(pd))) > RC(0.0))) continue;
+                        flux = add3(flux, xyz(pf));
+                        M += RC(1.0);
+#endif
+                    }
+                }
+            }
+        }
+#ifndef ORACLE_FP64
+        flux = v3(((float)sr * 5.9604644775390625e-8f) * fu, ((float)sg * 5.9604644775390625e-8f) * fu,
+                  ((float)sb * 5.9604644775390625e-8f) * fu);
+        M = (float)m;
+#endif
+        flux = mul3(flux, scl3(qr, RC(0.31830995240629591621063460818591)));
+        const real g = R_FMIN((N + alpha * M) / (N + M), RC(1.0));
+        R = R * R_SQRT(g);
+        N = N + M * alpha;
+        tau = scl3(add3(tau, flux), g);
+    }
+    c->q_flux_r[p] = v4(tau, R);
+    qe.w = N;
+    c->q_emi_n[p] = qe;
+}
+
+/* ------------------------------------------------------------------------------------------ */
 /* frame schedule (m_display, glslppm.cpp:214-536)                                             */
 /* ------------------------------------------------------------------------------------------ */
 static float xorshift_frand(uint32_t* s) {
@@ -1019,9 +1200,15 @@ static void run_frame(oracle_ctx* c) {
     c->photon_segments += segments;
     c->num_photons += emitted;
     c->num_photons_f32 += (float)(int)emitted;
-    hash_build(c);
+    if (c->cfg.flags & SPPM_FLAG_PHOTON_GRID) {
+        grid_build(c);
+#pragma omp parallel for schedule(dynamic, 256)
+        for (long long p = 0; p < (long long)npix; p++) grid_gather_pixel(c, (size_t)p);
+    } else {
+        hash_build(c);
 #pragma omp parallel for schedule(static)
-    for (long long p = 0; p < (long long)npix; p++) gather_pixel(c, (size_t)p);
+        for (long long p = 0; p < (long long)npix; p++) gather_pixel(c, (size_t)p);
+    }
     c->frame++;
 }
 
@@ -1146,6 +1333,11 @@ EXPORT oracle_ctx* ORACLE_API(create)(const sppm_config* cfg, const sppm_scene* 
     c->p_emitted = (uint8_t*)malloc(c->P);
     c->winner = (uint32_t*)malloc(sizeof(uint32_t) * c->hash_num);
     c->count = (uint32_t*)malloc(sizeof(uint32_t) * c->hash_num);
+    if (cfg->flags & SPPM_FLAG_PHOTON_GRID) {
+        c->g_ofs = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)c->hash_num + 1));
+        c->g_ids = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)c->P);
+        c->g_cur = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)c->hash_num);
+    }
     reset_state(c);
     if (cfg->radius_rule == SPPM_RADIUS_DIAGONAL) {
         const float dx = scene->bbox_max[0] - scene->bbox_min[0];
@@ -1411,5 +1603,8 @@ EXPORT void ORACLE_API(destroy)(oracle_ctx* c) {
     free(c->p_emitted);
     free(c->winner);
     free(c->count);
+    free(c->g_ofs);
+    free(c->g_ids);
+    free(c->g_cur);
     free(c);
 }

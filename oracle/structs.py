@@ -17,6 +17,7 @@ import numpy as np
 RADIUS_FOOTPRINT, RADIUS_DIAGONAL = 0, 1
 SEED_XORSHIFT, SEED_HASH = 0, 1
 FLAG_GL_DEPTH_CLIP = 0x1
+FLAG_PHOTON_GRID = 0x20
 
 
 class Config(C.Structure):

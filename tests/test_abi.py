@@ -113,7 +113,8 @@ def test_create_without_a_device_fails_cleanly(native_lib):
 def test_invalid_configs_are_rejected(native_lib):
     import glslppm_gb300 as g
     N = native_lib
-    for bad in (dict(width=0), dict(alpha=0.0), dict(max_path_length=0), dict(precision=9), dict(seed_mode=5)):
+    for bad in (dict(width=0), dict(alpha=0.0), dict(max_path_length=0), dict(precision=9), dict(seed_mode=5),
+                dict(flags=N.FLAG_PHOTON_GRID), dict(flags=N.FLAG_FP64_STATISTICS)):
         with pytest.raises(N.SppmError) as e:
             g.Renderer(g.default_config(16, **bad))
         assert e.value.status in (N.ERR_ARG, N.ERR_UNSUPPORTED)
