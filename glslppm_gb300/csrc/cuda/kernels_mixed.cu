@@ -351,7 +351,7 @@ __device__ __forceinline__ void grid_accumulate(const PhotonGrid& grid, uint32_t
 // lane accepts exactly the photons inside its radius (the union holds all of them, and each photon
 // sits in one cell), so its sums equal its own walk's; otherwise every lane walks its own cells
 // (grid_accumulate).  All 32 lanes call it.
-constexpr uint32_t kCoopMaxCells = 64;
+constexpr uint32_t kCoopMaxCells = 128;
 
 struct GridWarpSmem {
     uint32_t cell_off[kCoopMaxCells + 1];  // the cells' first index in the concatenation
@@ -370,6 +370,8 @@ __device__ __forceinline__ void grid_gather_warp(const LaunchSet& ls, const uint
     float gx = 0.0f, gy = 0.0f, gz = 0.0f, R2f = 0.0f, vx = 0.0f, vy = 0.0f, vz = 0.0f, rq2 = 0.0f;
     float4 qn4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     uint32_t x0 = 0xFFFFFFFFu, y0 = 0xFFFFFFFFu, z0 = 0xFFFFFFFFu, x1 = 0, y1 = 0, z1 = 0, own = 0;
+    // the lane's sphere's box in fixed-point units (empty without a hit point)
+    int bx0 = 0x7FFFFFFF, by0 = 0x7FFFFFFF, bz0 = 0x7FFFFFFF, bx1 = -1, by1 = -1, bz1 = -1;
     int Fc = 0;
     const JobState* st = nullptr;
     if (live) {
@@ -401,6 +403,8 @@ __device__ __forceinline__ void grid_gather_warp(const LaunchSet& ls, const uint
             const float rq = sqrtf(rq2) * 1.0001f + 1.0f;
             if (ux >= 0.0f && uy >= 0.0f && uz >= 0.0f && rq < 4.0e6f) {
                 has = true;
+                bx0 = (int)floorf(vx - rq), by0 = (int)floorf(vy - rq), bz0 = (int)floorf(vz - rq);
+                bx1 = (int)ceilf(vx + rq), by1 = (int)ceilf(vy + rq), bz1 = (int)ceilf(vz + rq);
                 auto lo = [&](float u) -> uint32_t {
                     const float v = u - rq;
                     return v > 0.0f ? (uint32_t)v >> Fc : 0u;
@@ -435,7 +439,7 @@ __device__ __forceinline__ void grid_gather_warp(const LaunchSet& ls, const uint
     const JobDesc& J = ls.jobs[ls.job_ids[kmin]];
     const uint32_t slot_base = __ldg(&slot_prefix[kmin]), hash_num = J.hash_num, nc = (uint32_t)ucells;
     const int Fw = __shfl_sync(full, Fc, __ffs(hasmask) - 1);
-    // a lane per cell (two rounds for up to 64 cells): the record ranges, concatenated by a scan
+    // a lane per cell (rounds of 32 cells): the record ranges, concatenated by a scan
     uint32_t run = 0;
     for (uint32_t c0 = 0; c0 < nc; c0 += 32u) {
         const uint32_t c = c0 + lane;
@@ -460,12 +464,16 @@ __device__ __forceinline__ void grid_gather_warp(const LaunchSet& ls, const uint
     }
     if (lane == 0) sm.cell_off[nc] = run;
     __syncwarp();
+    // the box of the lanes' spheres: a record outside it is inside no lane's radius
+    const int BX0 = __reduce_min_sync(full, bx0), BY0 = __reduce_min_sync(full, by0), BZ0 = __reduce_min_sync(full, bz0);
+    const int BX1 = __reduce_max_sync(full, bx1), BY1 = __reduce_max_sync(full, by1), BZ1 = __reduce_max_sync(full, bz1);
     unsigned long long sr = 0, sg = 0, sb = 0;
     uint32_t m = 0;
     for (uint32_t base = 0; base < run; base += 32u) {
         const uint32_t g = base + lane;
-        float4 ent = make_float4(__int_as_float(0x7FC00000), 0.0f, 0.0f, 0.0f);  // NaN: never inside
+        float4 ent = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         uint32_t w = 0;
+        bool keep = false;
         if (g < run) {
             // the cell of concatenation index g: the last cell starting at or before g
             uint32_t lo = 0, hi = nc - 1u;
@@ -479,15 +487,22 @@ __device__ __forceinline__ void grid_gather_warp(const LaunchSet& ls, const uint
             const unsigned long long q = ((unsigned long long)r.y << 32) | r.x;
             const uint32_t qx = (uint32_t)q & kGridCoordNone, qy = (uint32_t)(q >> 21) & kGridCoordNone,
                            qz = (uint32_t)(q >> 42);
-            if ((qx >> Fw) == cx && (qy >> Fw) == cy && (qz >> Fw) == cz)
-                ent = make_float4((float)qx, (float)qy, (float)qz, __uint_as_float(r.z));
+            keep = (qx >> Fw) == cx && (qy >> Fw) == cy && (qz >> Fw) == cz && (int)qx >= BX0 && (int)qx <= BX1 &&
+                   (int)qy >= BY0 && (int)qy <= BY1 && (int)qz >= BZ0 && (int)qz <= BZ1;
+            ent = make_float4((float)qx, (float)qy, (float)qz, __uint_as_float(r.z));
             w = r.w;
         }
-        sm.rec[lane] = ent;
-        sm.w[lane] = w;
+        // the batch's records that may lie inside some lane's radius, packed to the front
+        const unsigned kept = __ballot_sync(full, keep);
+        if (keep) {
+            const uint32_t at = __popc(kept & ((1u << lane) - 1u));
+            sm.rec[at] = ent;
+            sm.w[at] = w;
+        }
         __syncwarp();
-        const uint32_t n = run - base < 32u ? run - base : 32u;
+        const uint32_t n = __popc(kept);
         if (has) {
+#pragma unroll 2
             for (uint32_t j = 0; j < n; j++) {
                 const float4 c = sm.rec[j];
                 const float dx = __fsub_rn(c.x, vx), dy = __fsub_rn(c.y, vy), dz = __fsub_rn(c.z, vz);
