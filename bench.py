@@ -217,11 +217,12 @@ def cornell_mesh():
     return sc, mesh
 
 
-def make_renderer(device: int, precision: int = 0, eye_pass_interval: int = 10):
+def make_renderer(device: int, precision: int = 0, eye_pass_interval: int = 10, flags: int = 0, seed: int = 0):
     import glslppm_gb300 as g
     sc, mesh = cornell_mesh()
     cfg = g.default_config(1024, radius_rule=1, radius_fraction=0.005, precision=precision,
-                           eye_pass_interval=eye_pass_interval)
+                           eye_pass_interval=eye_pass_interval, seed=seed)
+    cfg.flags |= flags
     cam = g.look_at(sc.camera_origin, sc.camera_lookat, 1024, 1024, sc.fov)
     r = g.Renderer(cfg, device=device)
     r.upload_scene(mesh)
@@ -373,14 +374,14 @@ LIMITER_HBM = {
 }
 
 
-def measure_cornell(args, world: int, dev: int, precision: str) -> dict:
-    """The headline workload at one precision: autotuned launch shapes, W warm-up passes, K
-    device-timed passes, a stage breakdown, the streamed end-to-end steps, the traversal roofline and
-    the whole configuration end to end."""
+def measure_cornell(args, world: int, dev: int, precision: str, flags: int = 0) -> dict:
+    """The headline workload at one precision (flags: e.g. the mixed path's counting-sort photon
+    grid): autotuned launch shapes, W warm-up passes, K device-timed passes, a stage breakdown, the
+    streamed end-to-end steps, the traversal roofline and the whole configuration end to end."""
     import glslppm_gb300 as g
     from glslppm_gb300 import native as N
     prec = N.PRECISION_MIXED if precision == "mixed" else N.PRECISION_FP32
-    r, mesh, cfg, cam = make_renderer(dev, precision=prec, eye_pass_interval=args.eye_pass_interval)
+    r, mesh, cfg, cam = make_renderer(dev, precision=prec, eye_pass_interval=args.eye_pass_interval, flags=flags)
     K, W = args.steps, args.warmup
     P = cfg.photon_width * cfg.photon_height
     npix = cfg.width * cfg.height
@@ -445,7 +446,7 @@ def measure_cornell(args, world: int, dev: int, precision: str) -> dict:
     roof = roofline_of(cnt, tr_ms / tr_n if tr_n else 0.0, kernel, "cornell1024", peak, peak_kind, LIMITER_L2[kernel])
     r.close()
     # the whole configuration (1000 passes) end to end on a fresh context with the tuned shapes
-    rf = make_renderer(dev, precision=prec, eye_pass_interval=args.eye_pass_interval)[0]
+    rf = make_renderer(dev, precision=prec, eye_pass_interval=args.eye_pass_interval, flags=flags)[0]
     if tuning:
         rf.set_tuning(**tuning)
     full = full_config_run(rf, WORKLOAD["passes_in_config"]) if not args.no_full_config else None
@@ -476,14 +477,17 @@ def error_stats(img, ref) -> dict:
             "frac_pixels_within_1e-3": round(float(np.mean(rel <= 1e-3)), 4)}
 
 
-def gpu_images(dev: int, cfg_fp32, scene_mesh, cam, passes: int, tuning: dict | None = None) -> dict:
-    """The radiance images of fresh FP32 and mixed contexts after `passes` passes."""
+def gpu_images(dev: int, cfg_fp32, scene_mesh, cam, passes: int, tuning: dict | None = None,
+               paths=(("fp32", 0, 0), ("mixed", 1, 0))) -> dict:
+    """The radiance images of fresh contexts after `passes` passes: paths = (name, precision, extra
+    flags), by default FP32 and mixed."""
     import glslppm_gb300 as g
     from glslppm_gb300 import native as N
     out = {}
-    for name, prec in (("fp32", N.PRECISION_FP32), ("mixed", N.PRECISION_MIXED)):
+    for name, prec, flags in paths:
         cfg = N.Config.from_buffer_copy(cfg_fp32)
         cfg.precision = prec
+        cfg.flags |= flags
         r = g.Renderer(cfg, device=dev)
         r.upload_scene(scene_mesh)
         r.set_camera(cam)
@@ -527,10 +531,13 @@ def convergence(dev: int) -> dict | None:
     cal = json.loads(calp.read_text())
     from tests.golden.fixtures import c1_camera_and_scene
     mesh, cam = c1_camera_and_scene()
-    out = {"reference": {k: cal["reference"][k] for k in ("passes", "seeds", "photons", "estimated_rel_error")}}
-    for name, prec in (("fp32", N.PRECISION_FP32), ("mixed", N.PRECISION_MIXED)):
-        r = g.Renderer(g.default_config(256, radius_rule=N.RADIUS_DIAGONAL, radius_fraction=0.005, precision=prec),
-                       device=dev)
+    out = {"reference": {k: cal["reference"][k] for k in ("passes", "seeds", "photons", "photon_slots_per_pass",
+                                                          "eye_pass_interval", "estimator", "estimated_rel_error")}}
+    for name, prec, flags in (("fp32", N.PRECISION_FP32, 0), ("mixed", N.PRECISION_MIXED, 0),
+                              ("grid", N.PRECISION_MIXED, N.FLAG_PHOTON_GRID)):
+        cfg = g.default_config(256, radius_rule=N.RADIUS_DIAGONAL, radius_fraction=0.005, precision=prec)
+        cfg.flags |= flags
+        r = g.Renderer(cfg, device=dev)
         r.upload_scene(mesh)
         r.set_camera(cam)
         # the whole 256x256 configuration (64 passes) end to end: one sppm_run_passes, one read
@@ -539,16 +546,51 @@ def convergence(dev: int) -> dict | None:
         out[f"{name}_full_config_256"] = {k: full[k] for k in ("passes", "seconds", "mphotons_per_s")}
         r.close()
     out["calibration_rel_rmse_by_passes"] = cal["rel_rmse_by_passes"]
+    out["grid_calibration_rel_rmse_by_passes"] = cal["grid_rel_rmse_by_passes"]
+    # passes to reach 5% and 2% relative RMSE at the workload's own rate (one photon per pixel per
+    # pass), from each estimator's fit
+    out["passes_for_target"] = {f"{t:.0%}": {"winner": passes_for_target(t, 256 * 256, 1 << 16),
+                                             "grid": passes_for_target(t, 256 * 256, 1 << 16, fit="grid_fit")}
+                                for t in (0.05, 0.02)}
     return out
 
 
-def passes_for_target(target_rmse: float, npix: int, photons_per_pass: int, cap: int = 1 << 20) -> int:
+def noise_by_passes(dev: int, tuning: dict | None, checkpoints=(100, 1000)) -> dict:
+    """Seed-to-seed image noise of the headline workload (1024x1024, 2^20 photons) on the mixed
+    path with the reference's one-winner-per-slot estimator and with the counting-sort grid: the
+    relative RMSE between renders of seeds 1 and 2 after each checkpoint, divided by sqrt(2) (the
+    noise of one render), and the device time per pass of each."""
+    from glslppm_gb300 import native as N
+    out = {}
+    for name, flags in (("winner", 0), ("grid", N.FLAG_PHOTON_GRID)):
+        rs = [make_renderer(dev, precision=N.PRECISION_MIXED, flags=flags, seed=s)[0] for s in (1, 2)]
+        for r in rs:
+            if tuning:
+                r.set_tuning(**tuning)
+        done, noise = 0, {}
+        for k in checkpoints:
+            for r in rs:
+                r.run_passes(k - done)
+            done = k
+            a, b = (r.read_image().astype(np.float64) for r in rs)
+            noise[str(k)] = round(float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(((a + b) / 2) ** 2))) /
+                                  math.sqrt(2.0), 5)
+        ms = rs[0].time_passes(20) / 20
+        for r in rs:
+            r.close()
+        out[name] = {"noise_by_passes": noise, "ms_per_pass": round(ms, 4)}
+    return out
+
+
+def passes_for_target(target_rmse: float, npix: int, photons_per_pass: int, cap: int = 1 << 20,
+                      fit: str = "fit") -> int:
     """Pass count at which a job reaches `target_rmse` relative RMSE against a converged FP64
     reference, from the power-law fit over photons per pixel of tests/golden/convergence_c1.json
-    (the 256x256 workload, one photon per pixel per pass).  A job with more photons per pixel per
-    pass still needs as many passes as the calibration workload: the gather radius shrinks once per
-    pass, and with few passes its bias, not the photon noise, sets the error."""
-    cal = json.loads((REPO / "tests" / "golden" / "convergence_c1.json").read_text())["fit"]
+    (the 256x256 workload, one photon per pixel per pass; fit "fit" for the reference's estimator,
+    "grid_fit" for the counting-sort grid's).  A job with more photons per pixel per pass still
+    needs as many passes as the calibration workload: the gather radius shrinks once per pass, and
+    with few passes its bias, not the photon noise, sets the error."""
+    cal = json.loads((REPO / "tests" / "golden" / "convergence_c1.json").read_text())[fit]
     ppp = (cal["a"] / target_rmse) ** (1.0 / cal["b"])
     return int(min(cap, max(1, math.ceil(ppp), math.ceil(ppp * npix / photons_per_pass))))
 
@@ -936,11 +978,25 @@ def run_gpu(args, rank, world, local):
     }
     if args.precision == "fp32" and not args.no_mixed:
         out["mixed"] = measure_cornell(args, world, local, "mixed")
+        if not args.no_grid:
+            gr = measure_cornell(args, world, local, "mixed", flags=N.FLAG_PHOTON_GRID)
+            out["grid"] = {k: gr[k] for k in ("value", "ms_per_step", "mrays_per_s", "tuning", "stage_ms_per_launch",
+                                              "gpu_launches", "e2e", "clocks", "full_config")}
+            out["grid"]["note"] = ("mixed path with the counting-sort photon grid (SPPM_FLAG_PHOTON_GRID): every photon "
+                                   "within the radius instead of one winner per hash slot times its count")
+            if rank == 0 and world == 1:
+                out["grid"]["noise"] = noise_by_passes(local, out["mixed"].get("tuning"))
     if not args.no_quality:
         r, mesh, cfg, cam = make_renderer(local, precision=N.PRECISION_FP32, eye_pass_interval=args.eye_pass_interval)
         r.close()
         quality_jobs.append(("cornell-1024", cfg, mesh.scene(), cam, QUALITY_PASSES,
                              gpu_images(local, cfg, mesh, cam, QUALITY_PASSES)))
+        if "grid" in out:
+            gcfg = N.Config.from_buffer_copy(cfg)
+            gcfg.flags |= N.FLAG_PHOTON_GRID
+            quality_jobs.append(("cornell-1024-grid", gcfg, mesh.scene(), cam, QUALITY_PASSES,
+                                 gpu_images(local, gcfg, mesh, cam, QUALITY_PASSES,
+                                            paths=(("grid", N.PRECISION_MIXED, 0),))))
         out["_keep_mesh"] = mesh
     batch_tuning = None
     if not args.no_batched:
@@ -974,6 +1030,9 @@ def run_gpu(args, rank, world, local):
                 out["rmse_vs_fp64"] = dict(q["cornell-1024"]["fp32"], passes=QUALITY_PASSES, note=note)
                 if "mixed" in out:
                     out["mixed"]["rmse_vs_fp64"] = dict(q["cornell-1024"]["mixed"], passes=QUALITY_PASSES)
+            if "cornell-1024-grid" in q and "grid" in out:
+                out["grid"]["rmse_vs_fp64"] = dict(q["cornell-1024-grid"]["grid"], passes=QUALITY_PASSES,
+                                                   note="against the FP64 oracle's grid estimator, same seed and sequence")
             if "batched_largest_job" in q and "batched" in out:
                 out["batched"]["rmse_vs_fp64"] = q["batched_largest_job"]
             if "large" in q and "large" in out:
@@ -1096,6 +1155,7 @@ def main():
                     help="skip the image-error figures against the FP64 oracle (and the convergence figure)")
     ap.add_argument("--no-full-config", action="store_true", help="skip the whole-configuration end-to-end runs")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision figures beside the FP32 ones")
+    ap.add_argument("--no-grid", action="store_true", help="skip the counting-sort photon grid's figures")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default launch shapes instead of autotuning them before the warm-up")
     ap.add_argument("--tuning", default=None,
