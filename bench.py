@@ -966,7 +966,9 @@ def run_gpu(args, rank, world, local):
     if world > 1 or rank != 0:
         args.no_quality = True  # replicas: the image-error legs run once, on a single GPU
     quality_jobs: list = []
-    head = measure_cornell(args, world, local, args.precision)
+    if args.photon_grid and args.precision != "mixed":
+        raise SystemExit("--photon-grid applies to --precision mixed")
+    head = measure_cornell(args, world, local, args.precision, flags=N.FLAG_PHOTON_GRID if args.photon_grid else 0)
     out = {
         "metric": METRIC, "value": head["value"], "unit": "Mphotons/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
@@ -976,6 +978,8 @@ def run_gpu(args, rank, world, local):
                                 "e2e", "roofline", "clocks", "full_config")},
         "cpu_baseline": None,
     }
+    if args.photon_grid:
+        out["config"]["estimator"] = "counting-sort photon grid (every photon within the radius)"
     if args.precision == "fp32" and not args.no_mixed:
         out["mixed"] = measure_cornell(args, world, local, "mixed")
         if not args.no_grid:
@@ -1156,6 +1160,8 @@ def main():
     ap.add_argument("--no-full-config", action="store_true", help="skip the whole-configuration end-to-end runs")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision figures beside the FP32 ones")
     ap.add_argument("--no-grid", action="store_true", help="skip the counting-sort photon grid's figures")
+    ap.add_argument("--photon-grid", action="store_true",
+                    help="headline workload on the mixed path with the counting-sort photon grid (--precision mixed)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default launch shapes instead of autotuning them before the warm-up")
     ap.add_argument("--tuning", default=None,
