@@ -45,6 +45,14 @@ class Batch:
         self._sizes[job.value] = (config.width, config.height)
         return int(job.value)
 
+    def add_job_prepared(self, config: N.Config, prepared: "PreparedScene", camera: N.Camera) -> int:
+        """add_job with a scene whose host-side upload work was done ahead of time."""
+        job = C.c_uint32()
+        N.check(N.lib.sppm_batch_add_job_prepared(self._h, C.byref(config), prepared._h, C.byref(camera),
+                                                  C.byref(job)))
+        self._sizes[job.value] = (config.width, config.height)
+        return int(job.value)
+
     def remove_job(self, job: int) -> None:
         N.check(N.lib.sppm_batch_remove_job(self._h, job))
         self._sizes.pop(job, None)
@@ -254,6 +262,27 @@ class Server:
         if getattr(self, "_h", None) is not None and self._h.value:
             N.lib.sppm_server_destroy(self._h)
             self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PreparedScene:
+    """sppm_scene_prepare: a scene's host-side upload work (traversal layout, 4-wide tree, leaf
+    ranks) done on the calling thread; it owns its arrays and may be added to many jobs."""
+
+    def __init__(self, scene):
+        h = C.c_void_p()
+        N.check(N.lib.sppm_scene_prepare(C.byref(_scene(scene)), C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if self._h:
+            N.lib.sppm_scene_prepared_destroy(self._h)
+            self._h = None
 
     def __del__(self):
         try:

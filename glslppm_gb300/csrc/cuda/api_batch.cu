@@ -15,6 +15,10 @@ using namespace sppm_dev;
 using namespace sppm_rt;
 using sppm::fail;
 
+struct sppm_prepared_scene {
+    PreparedScene p;
+};
+
 struct sppm_batch {
     Runner rt;
     sppm_batch_config cfg{};
@@ -45,6 +49,58 @@ uint64_t queued_slots(const sppm_batch* b) {
     for (const auto& j : b->slots)
         if (j) p += j->P;
     return p;
+}
+
+}  // namespace
+
+namespace {
+
+// the bytes a job holds besides its scene arena: state, its share of the ray queue and, with the
+// photon grid, of the launch's grid (a 16-byte record per photon slot, an offset per hash slot)
+uint64_t job_bytes_beside_scene(const sppm_config& cfg) {
+    const uint64_t P = (uint64_t)cfg.photon_width * cfg.photon_height;
+    uint64_t b = Job::state_bytes(cfg) + kQueueBytesPerSlot * P;
+    if (cfg.flags & SPPM_FLAG_PHOTON_GRID) b += 16 * P + 4 * (uint64_t)(cfg.hash_slots ? cfg.hash_slots : P);
+    return b;
+}
+
+int check_job(const sppm_batch* b, const sppm_config* cfg) {
+    int st = validate_config(cfg);
+    if (st) return st;
+    if (cfg->precision != b->cfg.precision)
+        return fail(SPPM_ERR_ARG, "job precision %u differs from the batch's %u", cfg->precision, b->cfg.precision);
+    const uint32_t interval = cfg->eye_pass_interval ? cfg->eye_pass_interval : 1u;
+    if (interval != b->cfg.eye_pass_interval)
+        return fail(SPPM_ERR_ARG, "job eye_pass_interval %u differs from the batch's %u", interval,
+                    b->cfg.eye_pass_interval);
+    return SPPM_OK;
+}
+
+// admits a job of `need` device bytes; upload(job) sends its scene
+template <class Upload>
+int add_job(sppm_batch* b, const sppm_config* cfg, const sppm_camera* cam, uint64_t need, Upload upload,
+            uint32_t* job) {
+    uint32_t id = 0;
+    while (id < b->slots.size() && b->slots[id]) id++;
+    if (id == b->slots.size()) return fail(SPPM_ERR_STATE, "every one of the %u job slots is taken", (uint32_t)id);
+    const uint64_t used = used_bytes(b);
+    if (used + need > b->budget)
+        return fail(SPPM_ERR_OOM, "admission: job needs %llu bytes, %llu of the %llu-byte budget are in use",
+                    (unsigned long long)need, (unsigned long long)used, (unsigned long long)b->budget);
+    SPPM_CK(cudaSetDevice(b->rt.device));
+    SPPM_CK(cudaStreamSynchronize(b->rt.stream));
+    std::unique_ptr<Job> j(new (std::nothrow) Job());
+    if (!j) return fail(SPPM_ERR_OOM, "host allocation failed");
+    int st;
+    if ((st = j->init(*cfg, b->rt.d_jobs + id, id, b->rt.stream))) return st;
+    if ((st = upload(*j))) return st;
+    if ((st = j->set_camera(cam, b->rt.stream))) return st;
+    j->start_frame = (int64_t)b->rt.frames;
+    b->rt.active.push_back(j.get());
+    b->slots[id] = std::move(j);
+    b->rt.dirty = true;
+    *job = id;
+    return SPPM_OK;
 }
 
 }  // namespace
@@ -102,46 +158,54 @@ int sppm_batch_job_bytes(const sppm_batch* b, const sppm_config* cfg, const sppm
     if (!b || !cfg || !scene || !bytes) return fail(SPPM_ERR_ARG, "null argument");
     int st = validate_config(cfg);
     if (st) return st;
-    const uint64_t P = (uint64_t)cfg->photon_width * cfg->photon_height;
-    *bytes = Job::state_bytes(*cfg) + Job::scene_bytes(*scene, cfg->precision) + kQueueBytesPerSlot * P;
-    // the launch's counting-sort grid: a 16-byte record per photon slot, an offset per hash slot
-    if (cfg->flags & SPPM_FLAG_PHOTON_GRID) *bytes += 16 * P + 4 * (uint64_t)(cfg->hash_slots ? cfg->hash_slots : P);
+    *bytes = job_bytes_beside_scene(*cfg) + Job::scene_bytes(*scene, cfg->precision);
+    return SPPM_OK;
+}
+
+int sppm_batch_job_bytes_prepared(const sppm_batch* b, const sppm_config* cfg, const sppm_prepared_scene* scene,
+                                  uint64_t* bytes) {
+    if (!b || !cfg || !scene || !bytes) return fail(SPPM_ERR_ARG, "null argument");
+    int st = validate_config(cfg);
+    if (st) return st;
+    *bytes = job_bytes_beside_scene(*cfg) + scene->p.device_bytes;
     return SPPM_OK;
 }
 
 int sppm_batch_add_job(sppm_batch* b, const sppm_config* cfg, const sppm_scene* scene, const sppm_camera* cam,
                        uint32_t* job) {
     if (!b || !cfg || !scene || !cam || !job) return fail(SPPM_ERR_ARG, "null argument");
-    int st = validate_config(cfg);
+    int st = check_job(b, cfg);
     if (st) return st;
-    if (cfg->precision != b->cfg.precision)
-        return fail(SPPM_ERR_ARG, "job precision %u differs from the batch's %u", cfg->precision, b->cfg.precision);
-    const uint32_t interval = cfg->eye_pass_interval ? cfg->eye_pass_interval : 1u;
-    if (interval != b->cfg.eye_pass_interval)
-        return fail(SPPM_ERR_ARG, "job eye_pass_interval %u differs from the batch's %u", interval,
-                    b->cfg.eye_pass_interval);
-    uint32_t id = 0;
-    while (id < b->slots.size() && b->slots[id]) id++;
-    if (id == b->slots.size()) return fail(SPPM_ERR_STATE, "every one of the %u job slots is taken", (uint32_t)id);
     uint64_t need = 0;
     if ((st = sppm_batch_job_bytes(b, cfg, scene, &need))) return st;
-    const uint64_t used = used_bytes(b);
-    if (used + need > b->budget)
-        return fail(SPPM_ERR_OOM, "admission: job needs %llu bytes, %llu of the %llu-byte budget are in use",
-                    (unsigned long long)need, (unsigned long long)used, (unsigned long long)b->budget);
-    SPPM_CK(cudaSetDevice(b->rt.device));
-    SPPM_CK(cudaStreamSynchronize(b->rt.stream));
-    std::unique_ptr<Job> j(new (std::nothrow) Job());
-    if (!j) return fail(SPPM_ERR_OOM, "host allocation failed");
-    if ((st = j->init(*cfg, b->rt.d_jobs + id, id, b->rt.stream))) return st;
-    if ((st = j->upload_scene(scene, b->rt.stream))) return st;
-    if ((st = j->set_camera(cam, b->rt.stream))) return st;
-    j->start_frame = (int64_t)b->rt.frames;
-    b->rt.active.push_back(j.get());
-    b->slots[id] = std::move(j);
-    b->rt.dirty = true;
-    *job = id;
+    return add_job(b, cfg, cam, need, [&](Job& j) { return j.upload_scene(scene, b->rt.stream); }, job);
+}
+
+int sppm_scene_prepare(const sppm_scene* scene, sppm_prepared_scene** out) {
+    if (!scene || !out) return fail(SPPM_ERR_ARG, "null argument");
+    *out = nullptr;
+    std::unique_ptr<sppm_prepared_scene> p(new (std::nothrow) sppm_prepared_scene());
+    if (!p) return fail(SPPM_ERR_OOM, "host allocation failed");
+    try {
+        const int st = prepare_scene(scene, p->p);
+        if (st) return st;
+    } catch (const std::bad_alloc&) {
+        return fail(SPPM_ERR_OOM, "host allocation failed (scene preparation)");
+    }
+    *out = p.release();
     return SPPM_OK;
+}
+
+void sppm_scene_prepared_destroy(sppm_prepared_scene* scene) { delete scene; }
+
+int sppm_batch_add_job_prepared(sppm_batch* b, const sppm_config* cfg, const sppm_prepared_scene* scene,
+                                const sppm_camera* cam, uint32_t* job) {
+    if (!b || !cfg || !scene || !cam || !job) return fail(SPPM_ERR_ARG, "null argument");
+    int st = check_job(b, cfg);
+    if (st) return st;
+    uint64_t need = 0;
+    if ((st = sppm_batch_job_bytes_prepared(b, cfg, scene, &need))) return st;
+    return add_job(b, cfg, cam, need, [&](Job& j) { return j.upload_prepared(scene->p, b->rt.stream); }, job);
 }
 
 int sppm_batch_remove_job(sppm_batch* b, uint32_t id) {

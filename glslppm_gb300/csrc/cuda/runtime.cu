@@ -120,16 +120,6 @@ void seed_streams(const sppm_config& cfg, uint32_t npix, uint32_t P, std::vector
 }
 
 // ---- scene packing (CGPURT::CreateTextures, gpurt.cpp:47-552, in the traversal layout) --------
-struct Packed {
-    std::vector<NodeX> nodes;
-    std::vector<float4> isect, shade;
-    std::vector<DevMaterial> mats;
-    std::vector<float> light_cdf;
-    std::vector<int32_t> light_tri;
-    std::vector<float2> tri_tex;     // empty when no texture coordinate is below 1e10
-    std::vector<int32_t> mat_layer;  // [num_materials]
-    std::vector<int32_t> rank;       // [6][num_tris] leaf position of each triangle per ordering
-};
 
 int check_scene(const sppm_scene* s) {
     if (!s) return fail(SPPM_ERR_ARG, "null scene");
@@ -527,40 +517,60 @@ int Job::reset(cudaStream_t s) {
     return SPPM_OK;
 }
 
-int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
-    Packed pk;
-    int st = pack_scene(scene, pk);
+int prepare_scene(const sppm_scene* scene, PreparedScene& p) {
+    int st = pack_scene(scene, p.pk);
     if (st) return st;
-    std::vector<sppm::Node4> nodes4;
-    {  // both precisions: the plain path may trace through the 4-wide tree too (wide_bvh); a tree
-       // the 4-wide walk cannot take is an error for the mixed path only (the plain path then
-       // keeps its binary walk)
-        uint32_t depth = 0;
-        const int b4 = sppm::build_bvh4(*scene, nodes4, &depth);
-        const bool mixed = cfg.precision == SPPM_PRECISION_MIXED;
-        if (b4 && mixed) return fail(SPPM_ERR_ARG, "4-wide BVH construction failed (%d): inconsistent BVH arrays", b4);
-        if (depth > sppm::kBvh4MaxDepth && mixed)
-            return fail(SPPM_ERR_UNSUPPORTED, "4-wide BVH depth %u exceeds the traversal stack (%u levels)", depth,
-                        sppm::kBvh4MaxDepth);
-        if (b4 || depth > sppm::kBvh4MaxDepth) nodes4.clear();
-        for (auto& n : nodes4)  // photon rays pass through lights: mark leaf triangles of emitters
-            for (int k = 0; k < n.count; k++)
-                if (n.child[k] < 0 && n.child[k] != sppm::kChildEmpty) {
-                    const int32_t tri = ~n.child[k];
-                    if (scene->materials[scene->material_ids[tri]].brdf == -1) n.child[k] = ~(tri | kEmitterBit);
-                }
-    }
-    const size_t bytes = Arena::align(pk.nodes.size() * sizeof(NodeX)) + Arena::align(pk.isect.size() * 16) +
-                         Arena::align(pk.shade.size() * 16) + Arena::align(pk.mats.size() * sizeof(DevMaterial)) +
-                         Arena::align(std::max<size_t>(pk.light_cdf.size(), 1) * 4) +
-                         Arena::align(std::max<size_t>(pk.light_tri.size(), 1) * 4) +
-                         Arena::align(std::max<size_t>(nodes4.size(), 1) * sizeof(sppm::Node4)) + 1024 +
-                         Arena::align(pk.tri_tex.size() * sizeof(float2)) + Arena::align(pk.mat_layer.size() * 4) +
-                         Arena::align(pk.rank.size() * 4) +
-                         Arena::align((size_t)scene->num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4);
+    // both precisions: the plain path may trace through the 4-wide tree too (wide_bvh); a tree the
+    // 4-wide walk cannot take is an error for the mixed path only (upload_prepared), the plain path
+    // then keeps its binary walk
+    p.bvh4_status = sppm::build_bvh4(*scene, p.nodes4, &p.bvh4_depth);
+    if (p.bvh4_status || p.bvh4_depth > sppm::kBvh4MaxDepth) p.nodes4.clear();
+    for (auto& n : p.nodes4)  // photon rays pass through lights: mark leaf triangles of emitters
+        for (int k = 0; k < n.count; k++)
+            if (n.child[k] < 0 && n.child[k] != sppm::kChildEmpty) {
+                const int32_t tri = ~n.child[k];
+                if (scene->materials[scene->material_ids[tri]].brdf == -1) n.child[k] = ~(tri | kEmitterBit);
+            }
+    if (scene->num_textures)
+        p.textures.assign(scene->textures,
+                          scene->textures + (size_t)scene->num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4);
+    p.shape = *scene;
+    p.shape.positions = p.shape.normals = p.shape.texcoords = p.shape.light_cdf = p.shape.node_bounds = nullptr;
+    p.shape.material_ids = p.shape.light_triangles = p.shape.node_triangle = nullptr;
+    p.shape.order_base = p.shape.order_miss = p.shape.material_texture = nullptr;
+    p.shape.materials = nullptr;
+    p.shape.textures = nullptr;
+    p.fingerprint = scene_fingerprint(*scene);
+    const Packed& pk = p.pk;
+    p.device_bytes = Arena::align(pk.nodes.size() * sizeof(NodeX)) + Arena::align(pk.isect.size() * 16) +
+                     Arena::align(pk.shade.size() * 16) + Arena::align(pk.mats.size() * sizeof(DevMaterial)) +
+                     Arena::align(std::max<size_t>(pk.light_cdf.size(), 1) * 4) +
+                     Arena::align(std::max<size_t>(pk.light_tri.size(), 1) * 4) +
+                     Arena::align(std::max<size_t>(p.nodes4.size(), 1) * sizeof(sppm::Node4)) + 1024 +
+                     Arena::align(pk.tri_tex.size() * sizeof(float2)) + Arena::align(pk.mat_layer.size() * 4) +
+                     Arena::align(pk.rank.size() * 4) + Arena::align(p.textures.size());
+    return SPPM_OK;
+}
+
+int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
+    PreparedScene p;
+    const int st = prepare_scene(scene, p);
+    return st ? st : upload_prepared(p, s);
+}
+
+int Job::upload_prepared(const PreparedScene& p, cudaStream_t s) {
+    const bool mixed = cfg.precision == SPPM_PRECISION_MIXED;
+    if (p.bvh4_status && mixed)
+        return fail(SPPM_ERR_ARG, "4-wide BVH construction failed (%d): inconsistent BVH arrays", p.bvh4_status);
+    if (p.bvh4_depth > sppm::kBvh4MaxDepth && mixed)
+        return fail(SPPM_ERR_UNSUPPORTED, "4-wide BVH depth %u exceeds the traversal stack (%u levels)", p.bvh4_depth,
+                    sppm::kBvh4MaxDepth);
+    const Packed& pk = p.pk;
+    const sppm_scene* scene = &p.shape;
+    int st;
     SPPM_CK(cudaStreamSynchronize(s));
-    if ((st = scene_mem.reserve(bytes))) return st;
-    scene_bytes_used = bytes;
+    if ((st = scene_mem.reserve(p.device_bytes))) return st;
+    scene_bytes_used = p.device_bytes;
     DevScene& S = desc.scene;
     NodeX* nodes;
     float4 *isect, *shade;
@@ -574,18 +584,17 @@ int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
     if ((st = put(scene_mem, pk.light_cdf, &lcdf, s))) return st;
     if ((st = put(scene_mem, pk.light_tri, &ltri, s))) return st;
     sppm::Node4* n4 = nullptr;
-    if ((st = put(scene_mem, nodes4, &n4, s))) return st;
-    S.nodes4 = nodes4.empty() ? nullptr : reinterpret_cast<const Node4Dev*>(n4);
+    if ((st = put(scene_mem, p.nodes4, &n4, s))) return st;
+    S.nodes4 = p.nodes4.empty() ? nullptr : reinterpret_cast<const Node4Dev*>(n4);
     float2* ttex = nullptr;
     int32_t* mlayer = nullptr;
     if ((st = put(scene_mem, pk.tri_tex, &ttex, s))) return st;
     if ((st = put(scene_mem, pk.mat_layer, &mlayer, s))) return st;
     uint8_t* tex = nullptr;
-    if (scene->num_textures) {
-        const size_t tb = (size_t)scene->num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4;
-        tex = scene_mem.take<uint8_t>(tb);
+    if (!p.textures.empty()) {
+        tex = scene_mem.take<uint8_t>(p.textures.size());
         if (!tex) return fail(SPPM_ERR_OOM, "scene arena sizing error (textures)");
-        SPPM_CK(cudaMemcpyAsync(tex, scene->textures, tb, cudaMemcpyHostToDevice, s));
+        SPPM_CK(cudaMemcpyAsync(tex, p.textures.data(), p.textures.size(), cudaMemcpyHostToDevice, s));
     }
     int32_t* rank = nullptr;
     if ((st = put(scene_mem, pk.rank, &rank, s))) return st;
@@ -620,7 +629,7 @@ int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
                        ? cfg.radius_fraction * sppm::sqrt_f32(dx * dx + dy * dy + dz * dz)
                        : 0.0f;
     desc.fixed_radius = fixed_radius;
-    scene_fp = scene_fingerprint(*scene);
+    scene_fp = p.fingerprint;
     have_scene = true;
     if ((st = write_desc(s))) return st;
     return reset(s);

@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 
+#include "../host/scene_bvh4.h"
 #include "../host/scene_internal.h"
 #include "device_common.cuh"
 #include "sppm.h"
@@ -67,6 +68,35 @@ int launch_check(const char* what);
 // the caller's view of a job's frame counters
 void fill_frame_info(const JobState& st, sppm_frame_info* fi);
 
+// a scene in the device layout, on the host (CGPURT::CreateTextures, gpurt.cpp:47-552, in the
+// traversal layout)
+struct Packed {
+    std::vector<NodeX> nodes;
+    std::vector<float4> isect, shade;
+    std::vector<DevMaterial> mats;
+    std::vector<float> light_cdf;
+    std::vector<int32_t> light_tri;
+    std::vector<float2> tri_tex;     // empty when no texture coordinate is below 1e10
+    std::vector<int32_t> mat_layer;  // [num_materials]
+    std::vector<int32_t> rank;       // [6][num_tris] leaf position of each triangle per ordering
+};
+
+// the host-side work of a scene upload -- the traversal layout of the six orderings, the 4-wide
+// tree with its emitter marks, the leaf ranks, a copy of the textures, the checkpoint fingerprint
+// -- done ahead of time on any thread (sppm_scene_prepare); Job::upload_prepared then allocates
+// and copies only
+struct PreparedScene {
+    Packed pk;
+    std::vector<sppm::Node4> nodes4;  // empty when the tree failed or is deeper than the walk's stack
+    int bvh4_status = 0;              // build_bvh4's result
+    uint32_t bvh4_depth = 0;
+    std::vector<uint8_t> textures;
+    sppm_scene shape{};               // the source's counts, light area and bounds (no arrays)
+    uint64_t fingerprint = 0;
+    uint64_t device_bytes = 0;        // of the scene arena
+};
+int prepare_scene(const sppm_scene* scene, PreparedScene& out);
+
 // one render job (scene + camera + progressive state)
 struct Job {
     sppm_config cfg{};
@@ -115,6 +145,7 @@ struct Job {
 
     int init(const sppm_config& cfg, JobDesc* d_desc, uint32_t slot, cudaStream_t s);
     int upload_scene(const sppm_scene* scene, cudaStream_t s);
+    int upload_prepared(const PreparedScene& p, cudaStream_t s);
     int set_camera(const sppm_camera* cam, cudaStream_t s);
     int set_camera_desc(const sppm_camera* cam);  // host descriptor only; uploaded by the caller
     int reset(cudaStream_t s);

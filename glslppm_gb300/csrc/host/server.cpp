@@ -14,6 +14,7 @@
 
 #include "scene_internal.h"
 #include "sppm_server.h"
+#include "sppm_texture.h"
 
 using sppm::fail;
 
@@ -22,8 +23,9 @@ namespace {
 // a request's own copy of the scene arrays (the caller may free theirs once submit returns)
 struct SceneCopy {
     std::vector<float> positions, normals, texcoords, light_cdf, node_bounds;
-    std::vector<int32_t> material_ids, light_triangles, node_triangle, order_base, order_miss;
+    std::vector<int32_t> material_ids, light_triangles, node_triangle, order_base, order_miss, material_texture;
     std::vector<sppm_material> materials;
+    std::vector<uint8_t> textures;
     sppm_scene s{};
 
     template <class T>
@@ -43,6 +45,10 @@ struct SceneCopy {
         grab(node_triangle, in.node_triangle, nn);
         grab(order_base, in.order_base, nn * 6);
         grab(order_miss, in.order_miss, nn * 6);
+        if (in.num_textures) {
+            grab(material_texture, in.material_texture, in.num_materials);
+            grab(textures, in.textures, (size_t)in.num_textures * SPPM_TEXTURE_RES * SPPM_TEXTURE_RES * 4);
+        }
         s = in;
         auto ptr = [](auto& v) { return v.empty() ? nullptr : v.data(); };
         s.positions = ptr(positions);
@@ -56,6 +62,8 @@ struct SceneCopy {
         s.node_triangle = ptr(node_triangle);
         s.order_base = ptr(order_base);
         s.order_miss = ptr(order_miss);
+        s.material_texture = ptr(material_texture);
+        s.textures = ptr(textures);
     }
 };
 
@@ -63,11 +71,14 @@ struct Request {
     uint64_t ticket = 0;
     sppm_config cfg{};
     sppm_camera cam{};
-    SceneCopy scene;
+    SceneCopy scene;                     // until prepared
+    sppm_prepared_scene* prep = nullptr;  // the scene's host-side upload work, done by a worker
+    bool preparing = false;
     uint64_t bytes = 0;
     uint32_t job = 0;
     sppm_request_info info{};
     std::vector<float> image;
+    ~Request() { sppm_scene_prepared_destroy(prep); }
 };
 
 double now_since(std::chrono::steady_clock::time_point t0) {
@@ -90,22 +101,64 @@ struct sppm_server {
     bool stop = false;
     sppm_server_stats stats{};
     std::thread thread;
+    // preparation workers: the host-side work of each queued request's scene upload (the
+    // traversal layout, the 4-wide tree) runs on these threads while the GPU renders, so that
+    // admission only allocates and copies
+    std::vector<std::thread> workers;
+    std::condition_variable cv_prep;
 
     void loop();
+    void prepare_loop();
     void admit(std::unique_lock<std::mutex>& lk);
     void retire();
 };
 
+void sppm_server::prepare_loop() {
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+        Request* r = nullptr;
+        cv_prep.wait(lk, [&] {
+            if (stop) return true;
+            for (Request* q : pending)
+                if (!q->prep && !q->preparing) {
+                    r = q;
+                    return true;
+                }
+            return false;
+        });
+        if (stop) return;
+        r->preparing = true;
+        lk.unlock();
+        sppm_prepared_scene* p = nullptr;
+        const int st = sppm_scene_prepare(&r->scene.s, &p);
+        if (!st) r->scene = SceneCopy{};  // only this worker touches the copy while preparing
+        lk.lock();
+        r->preparing = false;
+        if (st) {
+            pending.erase(std::find(pending.begin(), pending.end(), r));
+            r->info.state = SPPM_REQUEST_FAILED;
+            r->info.status = st;
+            r->info.t_done = now_since(t0);
+            stats.failed++;
+            cv_done.notify_all();
+        } else {
+            r->prep = p;
+            cv_work.notify_all();
+        }
+    }
+}
+
 void sppm_server::admit(std::unique_lock<std::mutex>& lk) {
     while (!pending.empty() && !stop) {
         Request* r = pending.front();
+        if (!r->prep) return;  // its scene is still being prepared (requests are admitted in order)
         sppm_batch_info bi;
         sppm_batch_get_info(batch, &bi);
         if (bi.num_jobs >= bi.max_jobs || bi.bytes_used + r->bytes > budget) return;  // wait for room
         pending.pop_front();
         lk.unlock();
         uint32_t job = 0;
-        const int st = sppm_batch_add_job(batch, &r->cfg, &r->scene.s, &r->cam, &job);
+        const int st = sppm_batch_add_job_prepared(batch, &r->cfg, r->prep, &r->cam, &job);
         lk.lock();
         if (st == SPPM_ERR_OOM && !running.empty()) {  // the device had less room than the estimate
             pending.push_front(r);
@@ -124,7 +177,8 @@ void sppm_server::admit(std::unique_lock<std::mutex>& lk) {
         r->job = job;
         r->info.state = SPPM_REQUEST_RUNNING;
         r->info.t_admit = now_since(t0);
-        r->scene = SceneCopy{};  // uploaded: the host copy is no longer needed
+        sppm_scene_prepared_destroy(r->prep);  // uploaded: the host copy is no longer needed
+        r->prep = nullptr;
         running.push_back(r);
         stats.admitted++;
     }
@@ -169,7 +223,7 @@ void sppm_server::loop() {
         admit(lk);
         if (stop) break;
         if (running.empty()) {
-            cv_work.wait(lk, [&] { return stop || !pending.empty(); });
+            cv_work.wait(lk, [&] { return stop || (!pending.empty() && pending.front()->prep); });
             continue;
         }
         // passes until the next job reaches its target (at most passes_per_step)
@@ -237,10 +291,20 @@ int sppm_server_create(const sppm_server_config* cfg, int device, sppm_server** 
     s->stats.memory_budget = bi.memory_budget;
     s->t0 = std::chrono::steady_clock::now();
     try {
+        const unsigned hw = std::thread::hardware_concurrency();
+        const unsigned nw = std::max(1u, std::min(4u, hw / 4));
+        for (unsigned k = 0; k < nw; k++) s->workers.emplace_back([p = s.get()] { p->prepare_loop(); });
         s->thread = std::thread([p = s.get()] { p->loop(); });
     } catch (...) {
+        {
+            std::lock_guard<std::mutex> g(s->mu);
+            s->stop = true;
+        }
+        s->cv_prep.notify_all();
+        for (auto& w : s->workers)
+            if (w.joinable()) w.join();
         sppm_batch_destroy(s->batch);
-        return fail(SPPM_ERR_OOM, "could not start the server thread");
+        return fail(SPPM_ERR_OOM, "could not start the server threads");
     }
     *out = s.release();
     return SPPM_OK;
@@ -253,7 +317,10 @@ void sppm_server_destroy(sppm_server* s) {
         s->stop = true;
     }
     s->cv_work.notify_all();
+    s->cv_prep.notify_all();
     if (s->thread.joinable()) s->thread.join();
+    for (auto& w : s->workers)
+        if (w.joinable()) w.join();
     sppm_batch_destroy(s->batch);
     delete s;
 }
@@ -293,7 +360,7 @@ int sppm_server_submit(sppm_server* s, const sppm_config* cfg, const sppm_scene*
         s->requests[r->ticket] = std::move(r);
         s->stats.submitted++;
     }
-    s->cv_work.notify_all();
+    s->cv_prep.notify_one();
     return SPPM_OK;
 }
 

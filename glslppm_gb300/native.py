@@ -200,6 +200,10 @@ SIGNATURES = {
     "sppm_batch_create": (C.c_int, [C.POINTER(BatchConfig), C.c_int, C.POINTER(P)]),
     "sppm_batch_destroy": (None, [P]),
     "sppm_batch_job_bytes": (C.c_int, [P, C.POINTER(Config), C.POINTER(Scene), C.POINTER(C.c_uint64)]),
+    "sppm_scene_prepare": (C.c_int, [C.POINTER(Scene), C.POINTER(P)]),
+    "sppm_scene_prepared_destroy": (None, [P]),
+    "sppm_batch_job_bytes_prepared": (C.c_int, [P, C.POINTER(Config), P, C.POINTER(C.c_uint64)]),
+    "sppm_batch_add_job_prepared": (C.c_int, [P, C.POINTER(Config), P, C.POINTER(Camera), C.POINTER(C.c_uint32)]),
     "sppm_batch_add_job": (C.c_int, [P, C.POINTER(Config), C.POINTER(Scene), C.POINTER(Camera),
                                      C.POINTER(C.c_uint32)]),
     "sppm_batch_remove_job": (C.c_int, [P, C.c_uint32]),

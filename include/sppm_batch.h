@@ -54,6 +54,22 @@ int sppm_batch_job_bytes(const sppm_batch* b, const sppm_config* cfg, const sppm
    pass is the batch's next pass. */
 int sppm_batch_add_job(sppm_batch* b, const sppm_config* cfg, const sppm_scene* scene, const sppm_camera* cam,
                        uint32_t* job);
+
+/* Scenes prepared ahead of time.  Adding a job does host work before its copies to the device:
+   the traversal layout of the six node orderings, the 4-wide tree with its leaf ranks, a
+   fingerprint of every array (the reference's CGPURT::CreateTextures, gpurt.cpp:47-552, does the
+   same packing in the frame loop's thread).  sppm_scene_prepare does that work on the calling
+   thread -- any thread, e.g. while the batch renders -- and sppm_batch_add_job_prepared then only
+   allocates and copies: the same job as sppm_batch_add_job.  A prepared scene owns its arrays
+   (the source may be freed once it returns) and may be added to any number of jobs. */
+typedef struct sppm_prepared_scene sppm_prepared_scene;
+int sppm_scene_prepare(const sppm_scene* scene, sppm_prepared_scene** out);
+void sppm_scene_prepared_destroy(sppm_prepared_scene* scene);
+/* sppm_batch_job_bytes for a prepared scene (its scene arena exactly). */
+int sppm_batch_job_bytes_prepared(const sppm_batch* b, const sppm_config* cfg, const sppm_prepared_scene* scene,
+                                  uint64_t* bytes);
+int sppm_batch_add_job_prepared(sppm_batch* b, const sppm_config* cfg, const sppm_prepared_scene* scene,
+                                const sppm_camera* cam, uint32_t* job);
 int sppm_batch_remove_job(sppm_batch* b, uint32_t job);
 int sppm_batch_reset_job(sppm_batch* b, uint32_t job);
 int sppm_batch_set_camera(sppm_batch* b, uint32_t job, const sppm_camera* cam);

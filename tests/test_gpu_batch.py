@@ -226,3 +226,25 @@ def test_cameras_set_in_one_call_equal_one_by_one():
     for ja, jc in zip(ia, ic):
         assert_same(a.read_image(ja), c.read_image(jc), f"job {ja} image")
         assert_same(a.read_state(ja, "hit_position"), c.read_state(jc, "hit_position"), f"job {ja} hits")
+
+
+def test_prepared_scene_jobs_equal_plain_jobs():
+    """A scene prepared ahead of time (sppm_scene_prepare) and added to two jobs gives, word for
+    word, the state of the same job added from the scene itself; the source arrays may be gone."""
+    sc = scenes.cornell_variant(3, min_tris=800, max_tris=3000).scene
+    w, h, pw, ph = 24, 16, 32, 16
+    mesh = sc.to_mesh()
+    prep = g.PreparedScene(mesh)
+    del mesh
+    b = g.Batch(precision=N.PRECISION_MIXED, max_jobs=4)
+    cfg = config_for(w, h, pw, ph, N.PRECISION_MIXED)
+    cam = camera_for(sc, w, h)
+    ids = [b.add_job_prepared(cfg, prep, cam), b.add_job_prepared(cfg, prep, cam), b.add_job(cfg, sc.to_mesh(), cam)]
+    prep.close()
+    b.run_passes(13)
+    b.synchronize()
+    for k in KINDS + ["stats_n", "stats_r2", "stats_tau"]:
+        ref = b.read_state(ids[2], k)
+        for j in ids[:2]:
+            assert_same(b.read_state(j, k), ref, f"job {j} {k}")
+    b.close()
