@@ -8,7 +8,7 @@ from .native import NativeLibraryMissing, SppmError, device_count  # noqa: F401
 from .renderer import (Mesh, Renderer, default_config, look_at, pinned_empty, scene_from_arrays,  # noqa: F401
                        tune_hash_slots, write_image)
 from . import native, scenes  # noqa: F401
-from .batch import Batch, PreparedScene, Server  # noqa: F401
+from .batch import Batch, PreparedScene, PreparedState, Server  # noqa: F401
 
-__all__ = ["Batch", "PreparedScene", "Server", "Mesh", "Renderer", "default_config", "look_at", "pinned_empty", "scene_from_arrays", "tune_hash_slots", "write_image", "SppmError",
+__all__ = ["Batch", "PreparedScene", "PreparedState", "Server", "Mesh", "Renderer", "default_config", "look_at", "pinned_empty", "scene_from_arrays", "tune_hash_slots", "write_image", "SppmError",
            "NativeLibraryMissing", "device_count", "native", "scenes"]

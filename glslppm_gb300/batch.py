@@ -45,10 +45,12 @@ class Batch:
         self._sizes[job.value] = (config.width, config.height)
         return int(job.value)
 
-    def add_job_prepared(self, config: N.Config, prepared: "PreparedScene", camera: N.Camera) -> int:
-        """add_job with a scene whose host-side upload work was done ahead of time."""
+    def add_job_prepared(self, config: N.Config, prepared: "PreparedScene", camera: N.Camera,
+                         state: "PreparedState | None" = None) -> int:
+        """add_job with a scene (and optionally the random-state tables) prepared ahead of time."""
         job = C.c_uint32()
-        N.check(N.lib.sppm_batch_add_job_prepared(self._h, C.byref(config), prepared._h, C.byref(camera),
+        N.check(N.lib.sppm_batch_add_job_prepared(self._h, C.byref(config), prepared._h,
+                                                  state._h if state is not None else None, C.byref(camera),
                                                   C.byref(job)))
         self._sizes[job.value] = (config.width, config.height)
         return int(job.value)
@@ -282,6 +284,26 @@ class PreparedScene:
     def close(self) -> None:
         if self._h:
             N.lib.sppm_scene_prepared_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PreparedState:
+    """sppm_state_prepare: a configuration's seeded random-state tables, made on the calling thread."""
+
+    def __init__(self, config: N.Config):
+        h = C.c_void_p()
+        N.check(N.lib.sppm_state_prepare(C.byref(config), C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if self._h:
+            N.lib.sppm_state_prepared_destroy(self._h)
             self._h = None
 
     def __del__(self):

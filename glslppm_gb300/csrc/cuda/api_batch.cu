@@ -19,6 +19,10 @@ struct sppm_prepared_scene {
     PreparedScene p;
 };
 
+struct sppm_prepared_state {
+    PreparedState p;
+};
+
 struct sppm_batch {
     Runner rt;
     sppm_batch_config cfg{};
@@ -198,14 +202,35 @@ int sppm_scene_prepare(const sppm_scene* scene, sppm_prepared_scene** out) {
 
 void sppm_scene_prepared_destroy(sppm_prepared_scene* scene) { delete scene; }
 
+int sppm_state_prepare(const sppm_config* cfg, sppm_prepared_state** out) {
+    if (!cfg || !out) return fail(SPPM_ERR_ARG, "null argument");
+    *out = nullptr;
+    int st = validate_config(cfg);
+    if (st) return st;
+    std::unique_ptr<sppm_prepared_state> p(new (std::nothrow) sppm_prepared_state());
+    if (!p) return fail(SPPM_ERR_OOM, "host allocation failed");
+    try {
+        prepare_state(*cfg, p->p);
+    } catch (const std::bad_alloc&) {
+        return fail(SPPM_ERR_OOM, "host allocation failed (random-state tables)");
+    }
+    *out = p.release();
+    return SPPM_OK;
+}
+
+void sppm_state_prepared_destroy(sppm_prepared_state* state) { delete state; }
+
 int sppm_batch_add_job_prepared(sppm_batch* b, const sppm_config* cfg, const sppm_prepared_scene* scene,
-                                const sppm_camera* cam, uint32_t* job) {
+                                const sppm_prepared_state* state, const sppm_camera* cam, uint32_t* job) {
     if (!b || !cfg || !scene || !cam || !job) return fail(SPPM_ERR_ARG, "null argument");
     int st = check_job(b, cfg);
     if (st) return st;
+    if (state && !state->p.matches(*cfg)) return fail(SPPM_ERR_ARG, "the prepared state is of another configuration");
     uint64_t need = 0;
     if ((st = sppm_batch_job_bytes_prepared(b, cfg, scene, &need))) return st;
-    return add_job(b, cfg, cam, need, [&](Job& j) { return j.upload_prepared(scene->p, b->rt.stream); }, job);
+    return add_job(
+        b, cfg, cam, need,
+        [&](Job& j) { return j.upload_prepared(scene->p, b->rt.stream, state ? &state->p : nullptr); }, job);
 }
 
 int sppm_batch_remove_job(sppm_batch* b, uint32_t id) {

@@ -481,11 +481,28 @@ int Job::set_camera_desc(const sppm_camera* cam) {
     return SPPM_OK;
 }
 
-int Job::reset(cudaStream_t s) {
-    std::vector<float> eye, ph;
+void prepare_state(const sppm_config& cfg, PreparedState& out) {
+    out.npix = cfg.width * cfg.height;
+    out.P = cfg.photon_width * cfg.photon_height;
+    out.seed = cfg.seed;
+    out.seed_mode = cfg.seed_mode;
+    seed_streams(cfg, out.npix, out.P, out.eye, out.ph, out.xs);
+}
+
+bool PreparedState::matches(const sppm_config& cfg) const {
+    return npix == cfg.width * cfg.height && P == cfg.photon_width * cfg.photon_height && seed == cfg.seed &&
+           seed_mode == cfg.seed_mode;
+}
+
+int Job::reset(cudaStream_t s, const PreparedState* ps) {
+    std::vector<float> eye_own, ph_own;
     JobState st;
     memset(&st, 0, sizeof(st));
-    seed_streams(cfg, npix, P, eye, ph, st.xs);
+    if (ps && !ps->matches(cfg)) return fail(SPPM_ERR_ARG, "the prepared state is of another configuration");
+    if (ps) memcpy(st.xs, ps->xs, sizeof(st.xs));
+    else seed_streams(cfg, npix, P, eye_own, ph_own, st.xs);
+    const std::vector<float>& eye = ps ? ps->eye : eye_own;
+    const std::vector<float>& ph = ps ? ps->ph : ph_own;
     const DevPixels& px = desc.px;
     const DevPhotons& pp = desc.ph;
     SPPM_CK(cudaMemcpyAsync(px.rng, eye.data(), eye.size() * 4, cudaMemcpyHostToDevice, s));
@@ -558,7 +575,7 @@ int Job::upload_scene(const sppm_scene* scene, cudaStream_t s) {
     return st ? st : upload_prepared(p, s);
 }
 
-int Job::upload_prepared(const PreparedScene& p, cudaStream_t s) {
+int Job::upload_prepared(const PreparedScene& p, cudaStream_t s, const PreparedState* ps) {
     const bool mixed = cfg.precision == SPPM_PRECISION_MIXED;
     if (p.bvh4_status && mixed)
         return fail(SPPM_ERR_ARG, "4-wide BVH construction failed (%d): inconsistent BVH arrays", p.bvh4_status);
@@ -632,7 +649,7 @@ int Job::upload_prepared(const PreparedScene& p, cudaStream_t s) {
     scene_fp = p.fingerprint;
     have_scene = true;
     if ((st = write_desc(s))) return st;
-    return reset(s);
+    return reset(s, ps);
 }
 
 int Job::set_camera(const sppm_camera* cam, cudaStream_t s) {

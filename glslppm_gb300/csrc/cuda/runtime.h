@@ -97,6 +97,16 @@ struct PreparedScene {
 };
 int prepare_scene(const sppm_scene* scene, PreparedScene& out);
 
+// a job's seeded random-state tables (RandomizeTextures, glslppm.cpp:77-140: a host-side fill),
+// made ahead of time on any thread (sppm_state_prepare); Job::reset then copies them
+struct PreparedState {
+    std::vector<float> eye, ph;
+    uint32_t xs[4] = {0, 0, 0, 0};
+    uint32_t npix = 0, P = 0, seed = 0, seed_mode = 0;
+    bool matches(const sppm_config& cfg) const;
+};
+void prepare_state(const sppm_config& cfg, PreparedState& out);
+
 // one render job (scene + camera + progressive state)
 struct Job {
     sppm_config cfg{};
@@ -145,10 +155,10 @@ struct Job {
 
     int init(const sppm_config& cfg, JobDesc* d_desc, uint32_t slot, cudaStream_t s);
     int upload_scene(const sppm_scene* scene, cudaStream_t s);
-    int upload_prepared(const PreparedScene& p, cudaStream_t s);
+    int upload_prepared(const PreparedScene& p, cudaStream_t s, const PreparedState* ps = nullptr);
     int set_camera(const sppm_camera* cam, cudaStream_t s);
     int set_camera_desc(const sppm_camera* cam);  // host descriptor only; uploaded by the caller
-    int reset(cudaStream_t s);
+    int reset(cudaStream_t s, const PreparedState* ps = nullptr);  // ps: tables seeded ahead of time
     int write_desc(cudaStream_t s);
     int stage_desc(const JobDesc** src);  // write_desc in two halves, for uploads of many jobs
     int staged(cudaStream_t s);           // in one launch (launch_copy_descs)

@@ -73,12 +73,16 @@ struct Request {
     sppm_camera cam{};
     SceneCopy scene;                     // until prepared
     sppm_prepared_scene* prep = nullptr;  // the scene's host-side upload work, done by a worker
+    sppm_prepared_state* seeds = nullptr;  // and the job's seeded random-state tables
     bool preparing = false;
     uint64_t bytes = 0;
     uint32_t job = 0;
     sppm_request_info info{};
     std::vector<float> image;
-    ~Request() { sppm_scene_prepared_destroy(prep); }
+    ~Request() {
+        sppm_scene_prepared_destroy(prep);
+        sppm_state_prepared_destroy(seeds);
+    }
 };
 
 double now_since(std::chrono::steady_clock::time_point t0) {
@@ -130,11 +134,14 @@ void sppm_server::prepare_loop() {
         r->preparing = true;
         lk.unlock();
         sppm_prepared_scene* p = nullptr;
-        const int st = sppm_scene_prepare(&r->scene.s, &p);
+        sppm_prepared_state* q = nullptr;
+        int st = sppm_scene_prepare(&r->scene.s, &p);
+        if (!st) st = sppm_state_prepare(&r->cfg, &q);
         if (!st) r->scene = SceneCopy{};  // only this worker touches the copy while preparing
         lk.lock();
         r->preparing = false;
         if (st) {
+            sppm_scene_prepared_destroy(p);
             pending.erase(std::find(pending.begin(), pending.end(), r));
             r->info.state = SPPM_REQUEST_FAILED;
             r->info.status = st;
@@ -143,6 +150,7 @@ void sppm_server::prepare_loop() {
             cv_done.notify_all();
         } else {
             r->prep = p;
+            r->seeds = q;
             cv_work.notify_all();
         }
     }
@@ -158,7 +166,7 @@ void sppm_server::admit(std::unique_lock<std::mutex>& lk) {
         pending.pop_front();
         lk.unlock();
         uint32_t job = 0;
-        const int st = sppm_batch_add_job_prepared(batch, &r->cfg, r->prep, &r->cam, &job);
+        const int st = sppm_batch_add_job_prepared(batch, &r->cfg, r->prep, r->seeds, &r->cam, &job);
         lk.lock();
         if (st == SPPM_ERR_OOM && !running.empty()) {  // the device had less room than the estimate
             pending.push_front(r);
@@ -177,8 +185,10 @@ void sppm_server::admit(std::unique_lock<std::mutex>& lk) {
         r->job = job;
         r->info.state = SPPM_REQUEST_RUNNING;
         r->info.t_admit = now_since(t0);
-        sppm_scene_prepared_destroy(r->prep);  // uploaded: the host copy is no longer needed
+        sppm_scene_prepared_destroy(r->prep);  // uploaded: the host copies are no longer needed
+        sppm_state_prepared_destroy(r->seeds);
         r->prep = nullptr;
+        r->seeds = nullptr;
         running.push_back(r);
         stats.admitted++;
     }

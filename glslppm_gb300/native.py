@@ -203,7 +203,9 @@ SIGNATURES = {
     "sppm_scene_prepare": (C.c_int, [C.POINTER(Scene), C.POINTER(P)]),
     "sppm_scene_prepared_destroy": (None, [P]),
     "sppm_batch_job_bytes_prepared": (C.c_int, [P, C.POINTER(Config), P, C.POINTER(C.c_uint64)]),
-    "sppm_batch_add_job_prepared": (C.c_int, [P, C.POINTER(Config), P, C.POINTER(Camera), C.POINTER(C.c_uint32)]),
+    "sppm_batch_add_job_prepared": (C.c_int, [P, C.POINTER(Config), P, P, C.POINTER(Camera), C.POINTER(C.c_uint32)]),
+    "sppm_state_prepare": (C.c_int, [C.POINTER(Config), C.POINTER(P)]),
+    "sppm_state_prepared_destroy": (None, [P]),
     "sppm_batch_add_job": (C.c_int, [P, C.POINTER(Config), C.POINTER(Scene), C.POINTER(Camera),
                                      C.POINTER(C.c_uint32)]),
     "sppm_batch_remove_job": (C.c_int, [P, C.c_uint32]),

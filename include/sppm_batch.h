@@ -68,8 +68,16 @@ void sppm_scene_prepared_destroy(sppm_prepared_scene* scene);
 /* sppm_batch_job_bytes for a prepared scene (its scene arena exactly). */
 int sppm_batch_job_bytes_prepared(const sppm_batch* b, const sppm_config* cfg, const sppm_prepared_scene* scene,
                                   uint64_t* bytes);
+/* A job's seeded random-state tables (the host-side fill of RandomizeTextures, glslppm.cpp:77-140,
+   for this configuration's image, photon buffer, seed and seed mode), made ahead of time on the
+   calling thread. */
+typedef struct sppm_prepared_state sppm_prepared_state;
+int sppm_state_prepare(const sppm_config* cfg, sppm_prepared_state** out);
+void sppm_state_prepared_destroy(sppm_prepared_state* state);
+/* sppm_batch_add_job with a prepared scene and, when state is not NULL, prepared tables (of the
+   same configuration: SPPM_ERR_ARG otherwise); the job is the same. */
 int sppm_batch_add_job_prepared(sppm_batch* b, const sppm_config* cfg, const sppm_prepared_scene* scene,
-                                const sppm_camera* cam, uint32_t* job);
+                                const sppm_prepared_state* state, const sppm_camera* cam, uint32_t* job);
 int sppm_batch_remove_job(sppm_batch* b, uint32_t job);
 int sppm_batch_reset_job(sppm_batch* b, uint32_t job);
 int sppm_batch_set_camera(sppm_batch* b, uint32_t job, const sppm_camera* cam);

@@ -229,8 +229,10 @@ def test_cameras_set_in_one_call_equal_one_by_one():
 
 
 def test_prepared_scene_jobs_equal_plain_jobs():
-    """A scene prepared ahead of time (sppm_scene_prepare) and added to two jobs gives, word for
-    word, the state of the same job added from the scene itself; the source arrays may be gone."""
+    """A scene prepared ahead of time (sppm_scene_prepare) and added to two jobs, one of them with
+    random-state tables prepared ahead too (sppm_state_prepare), gives, word for word, the state of
+    the same job added from the scene itself; the source arrays may be gone; tables of another
+    configuration are refused."""
     sc = scenes.cornell_variant(3, min_tris=800, max_tris=3000).scene
     w, h, pw, ph = 24, 16, 32, 16
     mesh = sc.to_mesh()
@@ -239,8 +241,15 @@ def test_prepared_scene_jobs_equal_plain_jobs():
     b = g.Batch(precision=N.PRECISION_MIXED, max_jobs=4)
     cfg = config_for(w, h, pw, ph, N.PRECISION_MIXED)
     cam = camera_for(sc, w, h)
-    ids = [b.add_job_prepared(cfg, prep, cam), b.add_job_prepared(cfg, prep, cam), b.add_job(cfg, sc.to_mesh(), cam)]
+    seeds = g.PreparedState(cfg)
+    ids = [b.add_job_prepared(cfg, prep, cam), b.add_job_prepared(cfg, prep, cam, seeds),
+           b.add_job(cfg, sc.to_mesh(), cam)]
     prep.close()
+    seeds.close()
+    other = N.Config.from_buffer_copy(cfg)
+    other.seed = 99
+    with pytest.raises(N.SppmError):
+        b.add_job_prepared(cfg, g.PreparedScene(sc.to_mesh()), cam, g.PreparedState(other))
     b.run_passes(13)
     b.synchronize()
     for k in KINDS + ["stats_n", "stats_r2", "stats_tau"]:
