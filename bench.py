@@ -763,7 +763,8 @@ def run_serving(args, device: int, tuning: dict | None = None) -> dict:
     rows = []
     for lam in rates:
         # launch shapes: those the batched workload's autotuner chose (same scene distribution)
-        srv = g.Server(precision=prec, max_jobs=256, memory_budget=180 << 30, passes_per_step=1, device=device,
+        srv = g.Server(precision=prec, max_jobs=256, memory_budget=180 << 30, passes_per_step=args.serve_passes_per_step,
+                       device=device,
                        tuning=tuning)
         n = int(min(args.serve_requests, max(8, math.ceil(lam * args.serve_window))))
         gaps = rng.exponential(1.0 / lam, n)
@@ -819,6 +820,7 @@ def run_serving(args, device: int, tuning: dict | None = None) -> dict:
                      "mean_target_passes": round(float(np.mean([r[3] for r in reqs])), 1),
                      "sampled_achieved_rmse": sampled})
     return {"config": dict(SERVING, precision=args.precision, rates=args.serve_rates,
+                           passes_per_step=args.serve_passes_per_step,
                            target_rel_rmse=args.serve_target_rmse,
                            requests_per_rate=f"min({args.serve_requests}, rate x {args.serve_window} s)",
                            target_passes="from the target RMSE through tests/golden/convergence_c1.json's fit, "
@@ -1185,6 +1187,9 @@ def main():
                     help="each request's target relative RMSE against a converged FP64 reference")
     ap.add_argument("--serve-sample", type=int, default=2, help="requests per rate whose achieved RMSE is measured")
     ap.add_argument("--serve-pool", type=int, default=32)
+    ap.add_argument("--serve-passes-per-step", type=int, default=1,
+                    help="passes the server runs between admissions (a job finishing within a step stops at its "
+                         "own pass count)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

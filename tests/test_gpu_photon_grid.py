@@ -221,3 +221,46 @@ def test_grid_with_photon_waves_and_shapes_is_unchanged(cornell_c1_mesh):
         r.synchronize()
         for k, v in want.items():
             assert np.array_equal(r.read_state(k).view(np.uint8), v.view(np.uint8)), (tune, k)
+
+
+def test_grid_and_slot_jobs_in_one_batch_equal_single_contexts():
+    """A batch of mixed-precision jobs with and without the grid (one launch per stage: the
+    gather runs over 8x4 pixel tiles for every job, the slot records are filled for the jobs
+    without the grid only): every job's state and image equal its single context's word for
+    word."""
+    specs = [(scenes.cornell_variant(4, min_tris=800, max_tris=3000).scene, 32, 24, 32, 16, N.FLAG_PHOTON_GRID),
+             (scenes.cornell_box(), 40, 24, 48, 20, 0),
+             (scenes.cornell_variant(5, min_tris=800, max_tris=3000).scene, 24, 40, 16, 16, N.FLAG_PHOTON_GRID)]
+
+    def cfg_for(w, h, pw, ph, flags):
+        return g.default_config(w, height=h, photon_width=pw, photon_height=ph, radius_rule=N.RADIUS_DIAGONAL,
+                                radius_fraction=0.01, precision=N.PRECISION_MIXED, flags=N.FLAG_GL_DEPTH_CLIP | flags)
+
+    b = g.Batch(precision=N.PRECISION_MIXED, max_jobs=8)
+    meshes = [s[0].to_mesh() for s in specs]
+    cams = [g.look_at(sc.camera_origin, sc.camera_lookat, w, h, sc.fov) for (sc, w, h, _, _, _) in specs]
+    ids = [b.add_job(cfg_for(w, h, pw, ph, f), m, cam) for (sc, w, h, pw, ph, f), m, cam in zip(specs, meshes, cams)]
+    passes = 21
+    b.run_passes(passes)
+    b.synchronize()
+    for jid, (sc, w, h, pw, ph, f), m, cam in zip(ids, specs, meshes, cams):
+        r = render(cfg_for(w, h, pw, ph, f), m, cam, passes)
+        for k in ("stats_n", "stats_r2", "stats_tau", "hit_position"):
+            assert np.array_equal(np.ascontiguousarray(b.read_state(jid, k)).view(np.uint8),
+                                  np.ascontiguousarray(r.read_state(k)).view(np.uint8)), f"job {jid} {k}"
+        assert np.array_equal(b.read_image(jid).view(np.uint8), r.read_image().view(np.uint8)), f"job {jid} image"
+    b.close()
+
+
+def test_grid_with_fp64_statistics_holds_like_double_float(cornell_c1_mesh):
+    """The grid with IEEE double statistics (SPPM_FLAG_FP64_STATISTICS, the FP64 gather variant)
+    and with double-float pairs gather the same photons; over 200 passes at 64x64 their images
+    agree to 1e-5 relative RMSE."""
+    sc, mesh = cornell_c1_mesh
+    res = 64
+    cam = g.look_at(sc.camera_origin, sc.camera_lookat, res, res, sc.fov)
+    a = render(grid_config(res, 64), mesh, cam, 200).read_image().astype(np.float64)
+    b = render(grid_config(res, 64, flags=N.FLAG_FP64_STATISTICS), mesh, cam, 200).read_image().astype(np.float64)
+    e = float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))
+    print(f"200 passes: grid with double-float vs FP64 statistics {e:.2e}")
+    assert np.isfinite(a).all() and e < 1e-5, e
