@@ -105,7 +105,25 @@ def full_config_run(r, passes: int) -> dict:
     return {"passes": passes, "seconds": round(dt, 4), "mphotons_per_s": round(ph / dt / 1e6, 3),
             "mrays_per_s": round(((f1.photon_segments + f1.eye_segments) - (f0.photon_segments + f0.eye_segments))
                                  / dt / 1e6, 3),
-            "note": "one sppm_run_passes call and one sppm_read_image, host wall clock"}
+            "note": "one sppm_run_passes call and one sppm_read_image, host wall clock", "_image": img}
+
+
+def converged_cornell1024(dev: int, passes: int) -> tuple[np.ndarray, float]:
+    """A converged image of the headline workload's scene and camera, rendered on the GPU: the
+    mixed path with the counting-sort grid (whose images are within 2e-4 of the FP64 oracle's grid
+    estimator on the same random sequence) with an eye pass every pass, `passes` passes of 2^20
+    photons from each of two seeds no other run uses, averaged.  SPPM converges to the same
+    pixel-filtered radiance for any estimator and eye-pass interval.  Returns the image and its
+    estimated relative error (half the two runs' relative difference)."""
+    from glslppm_gb300 import native as N
+    imgs = []
+    for seed in (7, 11):
+        r = make_renderer(dev, precision=N.PRECISION_MIXED, eye_pass_interval=1, flags=N.FLAG_PHOTON_GRID,
+                          seed=seed)[0]
+        r.run_passes(passes)
+        imgs.append(r.read_image().astype(np.float64))
+        r.close()
+    return 0.5 * (imgs[0] + imgs[1]), rel_rmse(imgs[0], imgs[1]) / 2.0
 
 
 def measured_peaks():
@@ -451,6 +469,7 @@ def measure_cornell(args, world: int, dev: int, precision: str, flags: int = 0) 
         rf.set_tuning(**tuning)
     full = full_config_run(rf, WORKLOAD["passes_in_config"]) if not args.no_full_config else None
     rf.close()
+    full_image = full.pop("_image") if full else None
     return {
         "value": round(value, 3), "ms_per_step": round(1000.0 * t / K, 4), "mrays_per_s": round(mrays, 3),
         "tuning": tuning,
@@ -459,7 +478,7 @@ def measure_cornell(args, world: int, dev: int, precision: str, flags: int = 0) 
         "gpu_launches": int(launches),
         "e2e": {"value": round(e2e, 3), "unit": "Mphotons/s", "h2d_bytes_per_step": int(N.lib.sppm_camera_upload_bytes()),
                 "d2h_bytes_per_step": int(npix * 3 * 4), "steps": E},
-        "roofline": roof, "clocks": clocks.summary(), "full_config": full,
+        "roofline": roof, "clocks": clocks.summary(), "full_config": full, "_full_image": full_image,
     }
 
 
@@ -542,6 +561,7 @@ def convergence(dev: int) -> dict | None:
         r.set_camera(cam)
         # the whole 256x256 configuration (64 passes) end to end: one sppm_run_passes, one read
         full = full_config_run(r, 64)
+        full.pop("_image")
         out[f"{name}_rel_rmse_after_64_passes"] = round(rel_rmse(r.read_image(), ref), 5)
         out[f"{name}_full_config_256"] = {k: full[k] for k in ("passes", "seconds", "mphotons_per_s")}
         r.close()
@@ -924,6 +944,7 @@ def run_large(args, world, local, K, W, prec: int, sc, mesh, setup: dict) -> dic
         if tuning:
             rf.set_tuning(**tuning)
         full = full_config_run(rf, LARGE["passes_in_config"])
+        full.pop("_image")
         rf.close()
     return {
         "metric": METRIC, "value": round(value, 3), "unit": "Mphotons/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -980,12 +1001,15 @@ def run_gpu(args, rank, world, local):
                                 "e2e", "roofline", "clocks", "full_config")},
         "cpu_baseline": None,
     }
+    full_images = {args.precision: head["_full_image"]}
     if args.photon_grid:
         out["config"]["estimator"] = "counting-sort photon grid (every photon within the radius)"
     if args.precision == "fp32" and not args.no_mixed:
         out["mixed"] = measure_cornell(args, world, local, "mixed")
+        full_images["mixed"] = out["mixed"].pop("_full_image")
         if not args.no_grid:
             gr = measure_cornell(args, world, local, "mixed", flags=N.FLAG_PHOTON_GRID)
+            full_images["grid"] = gr.pop("_full_image")
             out["grid"] = {k: gr[k] for k in ("value", "ms_per_step", "mrays_per_s", "tuning", "stage_ms_per_launch",
                                               "gpu_launches", "e2e", "clocks", "full_config")}
             out["grid"]["note"] = ("mixed path with the counting-sort photon grid (SPPM_FLAG_PHOTON_GRID): every photon "
@@ -1019,6 +1043,16 @@ def run_gpu(args, rank, world, local):
         out["serving"] = run_serving(args, local, batch_tuning)
     if rank == 0 and world == 1 and not args.no_quality:
         out["convergence"] = convergence(local)
+        if not args.no_full_config and all(v is not None for v in full_images.values()):
+            # the whole 1024x1024 configuration's error: each path's image after its 1000 passes
+            # against a converged image of the same scene and camera
+            ref, ref_err = converged_cornell1024(local, args.converged_passes)
+            out["full_config_rel_rmse"] = {
+                **{k: round(rel_rmse(v, ref), 5) for k, v in full_images.items()},
+                "passes": WORKLOAD["passes_in_config"],
+                "reference": {"passes_per_seed": args.converged_passes, "seeds": [7, 11], "eye_pass_every": 1,
+                              "path": "mixed + counting-sort grid (within 2e-4 of the FP64 oracle's grid estimator)",
+                              "estimated_rel_error": round(ref_err, 5)}}
     # the CPU leg (rank 0, one GPU): the oracle timed as the CPU baseline, and as the checker, the
     # double-precision references of the image-error figures
     if rank == 0 and world == 1:
@@ -1162,6 +1196,8 @@ def main():
     ap.add_argument("--no-full-config", action="store_true", help="skip the whole-configuration end-to-end runs")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision figures beside the FP32 ones")
     ap.add_argument("--no-grid", action="store_true", help="skip the counting-sort photon grid's figures")
+    ap.add_argument("--converged-passes", type=int, default=8192,
+                    help="passes per seed of the converged 1024x1024 image the whole configuration is measured against")
     ap.add_argument("--photon-grid", action="store_true",
                     help="headline workload on the mixed path with the counting-sort photon grid (--precision mixed)")
     ap.add_argument("--no-autotune", action="store_true",
