@@ -148,6 +148,7 @@ void sppm_server::prepare_loop() {
             r->info.t_done = now_since(t0);
             stats.failed++;
             cv_done.notify_all();
+            cv_work.notify_all();  // the next request may now be at the front of the queue
         } else {
             r->prep = p;
             r->seeds = q;

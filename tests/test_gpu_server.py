@@ -115,3 +115,23 @@ def test_server_launch_shapes_keep_results():
     with pytest.raises(N.SppmError) as e:
         g.Server(max_jobs=2, tuning=dict(gather_block=40))
     assert e.value.status == N.ERR_ARG
+
+
+def test_a_scene_that_fails_preparation_fails_its_request_only():
+    """The server's preparation workers check each scene: a request whose BVH arrays are
+    inconsistent fails with SPPM_ERR_ARG, and the requests queued behind it are admitted and
+    finish as usual."""
+    (cfg, mesh, cam, passes), (cfg2, mesh2, cam2, passes2) = requests()[:2]
+    bad = N.Scene.from_buffer_copy(mesh.scene())
+    bad.num_nodes = bad.num_nodes - 2  # no longer 2 * triangles - 1
+    srv = g.Server(max_jobs=2)
+    t_bad = srv.submit(cfg, bad, cam, passes)
+    t_ok = srv.submit(cfg2, mesh2, cam2, passes2)
+    i_bad, i_ok = srv.wait(t_bad, timeout=60), srv.wait(t_ok, timeout=120)
+    assert i_bad.state == N.REQUEST_FAILED and i_bad.status == N.ERR_ARG
+    assert i_ok.state == N.REQUEST_DONE and i_ok.passes_done == passes2
+    ref = alone(cfg2, mesh2, cam2, passes2)
+    assert np.array_equal(srv.fetch_image(t_ok).view(np.uint32), ref.view(np.uint32))
+    st = srv.stats()
+    assert st.failed == 1 and st.completed == 1
+    srv.close()
