@@ -1100,8 +1100,10 @@ def run_batched_line(args, rank, world, local):
     value = sum_over_ranks(res["_photons"], world) / t / 1e6
     peak, peak_kind = measured_peaks()
     tr_ms, tr_n = res["_trace"]
-    roof = roofline_of(res["_counters"], tr_ms / tr_n if tr_n else 0.0, "k_trace_photons", "batched64", peak,
-                       peak_kind, "dependent-load latency over 64 jobs' BVHs (5.8M triangles)")
+    wide = prec == N.PRECISION_MIXED or bool((res["tuning"] or {}).get("wide_bvh"))
+    roof = roofline_of(res["_counters"], tr_ms / tr_n if tr_n else 0.0,
+                       "k_trace_photons4" if wide else "k_trace_photons", "batched64", peak, peak_kind,
+                       "dependent-load latency over 64 jobs' BVHs (5.8M triangles)")
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "Mphotons/s", "n_gpus": world, "steps": args.steps,
