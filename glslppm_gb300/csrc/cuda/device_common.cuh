@@ -28,6 +28,8 @@ constexpr int32_t kEmitterBit = 1 << 30;  // leaf triangle belongs to a light (s
 constexpr int32_t kTriMask = kEmitterBit - 1;
 constexpr uint32_t kEmptySlot = 0xFFFFFFFFu;
 
+constexpr uint32_t kCellTable = 4096;  // cells per axis of the plain path's cell-bound table
+
 constexpr uint32_t kErrWatchdogTraverse = 1u;
 constexpr uint32_t kErrWatchdogLight = 2u;
 
@@ -123,6 +125,7 @@ struct JobState {
     unsigned long long num_photons, photon_segments, eye_segments;
     unsigned long long count_nodes, count_tris, count_segments;  // traversal counters (when enabled)
     unsigned long long coop_segments;  // photon segments traced one per warp
+    uint32_t cell_table_n;    // valid entries per axis of JobDesc::cell_bounds (0: none yet)
 };
 
 struct JobDesc {
@@ -132,6 +135,10 @@ struct JobDesc {
     uint32_t* winner;
     uint32_t* count;
     SlotRec* slots;  // mixed path
+    // plain path: c / GridScale + BBMin for the integer cell coordinates c of each axis
+    // ([3][kCellTable]), the bounds of progressive.fs's in-cell test (:79-81), rebuilt after every
+    // eye pass's grid (the same correctly rounded operations as the test's own)
+    float* cell_bounds;
     uint2* grid_key;  // [P] counting-sort grid (SPPM_FLAG_PHOTON_GRID): each stored photon's
                       // (hash slot, rank among the slot's photons) of the current pass
     JobState* state;

@@ -36,6 +36,8 @@ void launch_frame_begin(const LaunchSet& ls, const RayQueue& q, cudaStream_t s);
 // block: threads per block (a multiple of 32 up to the kernel's launch bound; 0 = the bound)
 void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, bool textured, uint32_t block, cudaStream_t s);
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s);
+// the plain path's table of in-cell bounds for the grid launch_grid has just set
+void launch_cell_bounds(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s);
 void launch_photon_fp32(const LaunchSet& ls, bool count_traversal, bool textured, cudaStream_t s);
 void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, bool textured, cudaStream_t s);
 void launch_queue_reset(const RayQueue& q, cudaStream_t s);

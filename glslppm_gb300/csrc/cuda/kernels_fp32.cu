@@ -935,6 +935,28 @@ __global__ void k_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t nj
     if (st->frame == 0) st->r0 = r0;
 }
 
+// k_cell_bounds: the in-cell test's bounds (progressive.fs:79-81: cell / GridScale + BBMin, with the
+// test's own correctly rounded division and addition) for every integer cell coordinate of the
+// grid k_grid has just set, a block per job of the eye phase
+__global__ void __launch_bounds__(256) k_cell_bounds(const JobDesc* jobs, const uint32_t* job_ids) {
+    const JobDesc& J = jobs[job_ids[blockIdx.x]];
+    if (!J.cell_bounds) return;
+    JobState* st = J.state;
+    const float G = st->grid_scale;
+    uint32_t n = 0;
+    for (int a = 0; a < 3; a++) {
+        const float e = xmul(xsub(st->bbmax[a], st->bbmin[a]), G);  // cells along the axis
+        const uint32_t na = e >= 0.0f && e < (float)kCellTable ? (uint32_t)e + 3u : kCellTable;
+        n = max(n, na);
+    }
+    n = min(n, kCellTable);
+    for (uint32_t i = threadIdx.x; i < 3 * n; i += blockDim.x) {
+        const uint32_t a = i / n, c = i - a * n;
+        J.cell_bounds[a * kCellTable + c] = xadd(xdiv((float)c, G), st->bbmin[a]);
+    }
+    if (threadIdx.x == 0) st->cell_table_n = n;
+}
+
 // ----------------------------------------------------------------------------------------------
 // k_photon: photontrace.fs main (:464-720), sum.fs, hash.fs + scatter.vs + correction.vs
 // ----------------------------------------------------------------------------------------------
@@ -1704,14 +1726,29 @@ __global__ void __launch_bounds__(256, 4) k_gather(LaunchSet ls) {
 #pragma unroll
         for (int c = 0; c < 8; c++) win[c] = __ldg(&J.winner[slot[c]]);
         uint32_t inside = 0;
+        // the cells' bounds from the table k_cell_bounds made for this grid (the same values as
+        // the division below), when the 2x2x2 block lies inside it
+        const float tn = (float)st->cell_table_n;
+        const bool table = J.cell_bounds && ii.x >= 0.0f && ii.y >= 0.0f && ii.z >= 0.0f && ii.x + 2.0f < tn &&
+                           ii.y + 2.0f < tn && ii.z + 2.0f < tn;
+        const uint32_t tx = table ? (uint32_t)ii.x : 0u, ty = table ? (uint32_t)ii.y : 0u,
+                       tz = table ? (uint32_t)ii.z : 0u;
 #pragma unroll
         for (int c = 0; c < 8; c++) {
             if (win[c] == kEmptySlot) continue;  // the cleared texel: photon 0 weighted by count 0
             const f3 cell = mk(xadd(ii.x, (float)(c & 1)), xadd(ii.y, (float)((c >> 1) & 1)), xadd(ii.z, (float)(c >> 2)));
             const float4 pp = __ldg(&J.ph.pos[win[c]]);
-            const f3 rmin = mk(xadd(xdiv(cell.x, G), bbmin.x), xadd(xdiv(cell.y, G), bbmin.y), xadd(xdiv(cell.z, G), bbmin.z));
-            const f3 rmax = mk(xadd(xdiv(xadd(cell.x, 1.0f), G), bbmin.x), xadd(xdiv(xadd(cell.y, 1.0f), G), bbmin.y),
-                               xadd(xdiv(xadd(cell.z, 1.0f), G), bbmin.z));
+            f3 rmin, rmax;
+            if (table) {
+                const float* T = J.cell_bounds;
+                const uint32_t cx = tx + (c & 1), cy = ty + ((c >> 1) & 1), cz = tz + (c >> 2);
+                rmin = mk(__ldg(&T[cx]), __ldg(&T[kCellTable + cy]), __ldg(&T[2 * kCellTable + cz]));
+                rmax = mk(__ldg(&T[cx + 1]), __ldg(&T[kCellTable + cy + 1]), __ldg(&T[2 * kCellTable + cz + 1]));
+            } else {
+                rmin = mk(xadd(xdiv(cell.x, G), bbmin.x), xadd(xdiv(cell.y, G), bbmin.y), xadd(xdiv(cell.z, G), bbmin.z));
+                rmax = mk(xadd(xdiv(xadd(cell.x, 1.0f), G), bbmin.x), xadd(xdiv(xadd(cell.y, 1.0f), G), bbmin.y),
+                          xadd(xdiv(xadd(cell.z, 1.0f), G), bbmin.z));
+            }
             if (pp.x > rmin.x && pp.y > rmin.y && pp.z > rmin.z && pp.x < rmax.x && pp.y < rmax.y && pp.z < rmax.z &&
                 length(sub(xyz(pp), qp)) < R)
                 inside |= 1u << c;
@@ -1932,6 +1969,9 @@ void launch_eye(const LaunchSet& ls, const RayQueue& q, bool mixed, bool texture
 }
 void launch_grid(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s) {
     if (njobs) k_grid<<<blocks_for(njobs, 64), 64, 0, s>>>(jobs, job_ids, njobs);
+}
+void launch_cell_bounds(const JobDesc* jobs, const uint32_t* job_ids, uint32_t njobs, cudaStream_t s) {
+    if (njobs) k_cell_bounds<<<njobs, 256, 0, s>>>(jobs, job_ids);
 }
 void launch_photon_fp32(const LaunchSet& ls, bool count, bool textured, cudaStream_t s) {
     if (!ls.total) return;

@@ -265,6 +265,7 @@ uint64_t Job::state_bytes(const sppm_config& cfg) {
     if (cfg.precision == SPPM_PRECISION_MIXED)
         b += Arena::align(hn * sizeof(SlotRec)) + 2 * Arena::align(np * 8) + Arena::align(np * 24);
     if (cfg.flags & SPPM_FLAG_PHOTON_GRID) b += Arena::align(P * 8);
+    if (cfg.precision == SPPM_PRECISION_FP32) b += Arena::align(3 * kCellTable * 4);
     return b;
 }
 
@@ -328,6 +329,10 @@ int Job::init(const sppm_config& c, JobDesc* dd, uint32_t sl, cudaStream_t s) {
     if (c.flags & SPPM_FLAG_PHOTON_GRID) {
         J.grid_key = a.take<uint2>(P);
         if (!J.grid_key) return fail(SPPM_ERR_OOM, "state arena sizing error (photon grid)");
+    }
+    if (c.precision == SPPM_PRECISION_FP32) {
+        J.cell_bounds = a.take<float>(3 * kCellTable);
+        if (!J.cell_bounds) return fail(SPPM_ERR_OOM, "state arena sizing error (cell bounds)");
     }
     if (!J.count) return fail(SPPM_ERR_OOM, "state arena sizing error");
     J.state = d_state;
@@ -791,6 +796,7 @@ int Job::load_checkpoint(const void* src, size_t bytes, cudaStream_t s, uint32_t
     JobState st;
     memcpy(&st, p, sizeof(st));
     p += sizeof(JobState);
+    st.cell_table_n = 0;  // the cell-bound table is not in the checkpoint: the next eye pass builds it
     SPPM_CK(cudaStreamSynchronize(s));
     SPPM_CK(cudaMemcpyAsync(d_state, &st, sizeof(st), cudaMemcpyHostToDevice, s));
     for (uint32_t k = 0; k < kCheckpointKinds; k++) {
@@ -1075,6 +1081,7 @@ int Runner::enqueue_frame(uint32_t phase) {
         timed(SPPM_STAGE_EYE, false, side);
         timed(SPPM_STAGE_GRID, true, side);
         launch_grid(d_jobs, eye_ids[phase], eye_pix[phase].njobs, side);
+        if (!mixed) launch_cell_bounds(d_jobs, eye_ids[phase], eye_pix[phase].njobs, side);
         timed(SPPM_STAGE_GRID, false, side);
         SPPM_CK(cudaEventRecord(join_ev, side));
     }
