@@ -354,8 +354,10 @@ __device__ __forceinline__ void grid_accumulate(const PhotonGrid& grid, uint32_t
 constexpr uint32_t kCoopMaxCells = 128;
 
 struct GridWarpSmem {
-    uint32_t cell_off[kCoopMaxCells + 1];  // the cells' first index in the concatenation
-    uint32_t cell_beg[kCoopMaxCells];      // their first record
+    // the union's cells that hold records, in walk order
+    uint32_t cell_off[kCoopMaxCells + 1];  // first index in the concatenation of their records
+    uint32_t cell_beg[kCoopMaxCells];      // first record
+    uint32_t cell_x[kCoopMaxCells], cell_y[kCoopMaxCells], cell_z[kCoopMaxCells];  // coordinates
     float4 rec[32];                        // the batch: the position (cells' fixed point) + flux r|g
     uint32_t w[32];                        // flux b | direction
 };
@@ -439,13 +441,16 @@ __device__ __forceinline__ void grid_gather_warp(const LaunchSet& ls, const uint
     const JobDesc& J = ls.jobs[ls.job_ids[kmin]];
     const uint32_t slot_base = __ldg(&slot_prefix[kmin]), hash_num = J.hash_num, nc = (uint32_t)ucells;
     const int Fw = __shfl_sync(full, Fc, __ffs(hasmask) - 1);
-    // a lane per cell (rounds of 32 cells): the record ranges, concatenated by a scan
-    uint32_t run = 0;
+    // a lane per cell (rounds of 32 cells): the record ranges, concatenated by a scan; the cells
+    // without records are left out
+    uint32_t run = 0, ne = 0;
+    const unsigned below = (1u << lane) - 1u;
     for (uint32_t c0 = 0; c0 < nc; c0 += 32u) {
         const uint32_t c = c0 + lane;
-        uint32_t b = 0, n = 0;
+        uint32_t b = 0, n = 0, cx = 0, cy = 0, cz = 0;
         if (c < nc) {
-            const uint32_t cx = X0 + c % UX, t = c / UX, cy = Y0 + t % UY, cz = Z0 + t / UY;
+            const uint32_t t = c / UX;
+            cx = X0 + (c - t * UX), cy = Y0 + t % UY, cz = Z0 + t / UY;
             const uint32_t slot = grid_cell_slot(cx, cy, cz, hash_num);
             b = __ldg(&grid.ofs[slot_base + slot]);
             n = __ldg(&grid.ofs[slot_base + slot + 1]) - b;
@@ -456,13 +461,17 @@ __device__ __forceinline__ void grid_gather_warp(const LaunchSet& ls, const uint
             const uint32_t y = __shfl_up_sync(full, incl, d);
             if (lane >= (uint32_t)d) incl += y;
         }
-        if (c < nc) {
-            sm.cell_off[c] = run + incl - n;
-            sm.cell_beg[c] = b;
+        const unsigned held = __ballot_sync(full, n > 0);
+        if (n > 0) {
+            const uint32_t at = ne + __popc(held & below);
+            sm.cell_off[at] = run + incl - n;
+            sm.cell_beg[at] = b;
+            sm.cell_x[at] = cx, sm.cell_y[at] = cy, sm.cell_z[at] = cz;
         }
         run += __shfl_sync(full, incl, 31);
+        ne += __popc(held);
     }
-    if (lane == 0) sm.cell_off[nc] = run;
+    if (lane == 0) sm.cell_off[ne] = run;
     __syncwarp();
     // the box of the lanes' spheres: a record outside it is inside no lane's radius
     const int BX0 = __reduce_min_sync(full, bx0), BY0 = __reduce_min_sync(full, by0), BZ0 = __reduce_min_sync(full, bz0);
@@ -476,13 +485,13 @@ __device__ __forceinline__ void grid_gather_warp(const LaunchSet& ls, const uint
         bool keep = false;
         if (g < run) {
             // the cell of concatenation index g: the last cell starting at or before g
-            uint32_t lo = 0, hi = nc - 1u;
+            uint32_t lo = 0, hi = ne - 1u;
             while (lo < hi) {
                 const uint32_t mid = (lo + hi + 1u) >> 1;
                 if (sm.cell_off[mid] <= g) lo = mid;
                 else hi = mid - 1u;
             }
-            const uint32_t cx = X0 + lo % UX, t = lo / UX, cy = Y0 + t % UY, cz = Z0 + t / UY;
+            const uint32_t cx = sm.cell_x[lo], cy = sm.cell_y[lo], cz = sm.cell_z[lo];
             const uint4 r = __ldg(&grid.rec[sm.cell_beg[lo] + (g - sm.cell_off[lo])]);
             const unsigned long long q = ((unsigned long long)r.y << 32) | r.x;
             const uint32_t qx = (uint32_t)q & kGridCoordNone, qy = (uint32_t)(q >> 21) & kGridCoordNone,
