@@ -848,6 +848,7 @@ Runner::~Runner() {
         cudaStreamDestroy(copy);
     }
     if (resolved_ev) cudaEventDestroy(resolved_ev);
+    if (resolve_done) cudaEventDestroy(resolve_done);
     for (auto& t : tickets) cudaEventDestroy(t.ev);
     for (auto e : ticket_pool) cudaEventDestroy(e);
     if (info_host) cudaFreeHost(info_host);
@@ -871,6 +872,8 @@ int Runner::init(int dev, uint32_t prec, uint32_t fl, uint32_t interval, uint32_
     SPPM_CK(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
     SPPM_CK(cudaStreamCreateWithFlags(&copy, cudaStreamNonBlocking));
     SPPM_CK(cudaEventCreateWithFlags(&resolved_ev, cudaEventDisableTiming));
+    SPPM_CK(cudaEventCreateWithFlags(&resolve_done, cudaEventDisableTiming));
+    SPPM_CK(cudaEventRecord(resolve_done, copy));  // a recorded event from the start
     int st = desc_mem.reserve(Arena::align(sizeof(JobDesc) * std::max<uint32_t>(max_jobs, 1)));
     if (st) return st;
     d_jobs = desc_mem.take<JobDesc>(std::max<uint32_t>(max_jobs, 1));
@@ -1050,6 +1053,12 @@ void Runner::timed(int stage, bool start, cudaStream_t s) {
     }
 }
 
+void Runner::wait_resolve(cudaStream_t s) {
+    // in a capture, an external event-wait node: each replay waits for the event's last record
+    // before the replay's launch
+    cudaStreamWaitEvent(s, resolve_done, capturing ? cudaEventWaitExternal : 0);
+}
+
 // the launches of one frame (m_display, glslppm.cpp:214-536) for every active job
 int Runner::enqueue_frame(uint32_t phase) {
     // the queue as the launches see it: the tuned refill interval, and no bins when the rays are
@@ -1076,6 +1085,7 @@ int Runner::enqueue_frame(uint32_t phase) {
     if (eye) {
         SPPM_CK(cudaEventRecord(fork_ev, stream));
         SPPM_CK(cudaStreamWaitEvent(side, fork_ev, 0));
+        wait_resolve(side);  // the eye pass rewrites the emission a pending resolve reads
         timed(SPPM_STAGE_EYE, true, side);
         launch_eye(eye_pix[phase], q, wide, textured, tune.eye_block, side);
         timed(SPPM_STAGE_EYE, false, side);
@@ -1134,6 +1144,7 @@ int Runner::enqueue_frame(uint32_t phase) {
         launch_grid_sort(hsh, pho, grid, stream);
         timed(SPPM_STAGE_PHOTON_SORT, false);
     }
+    wait_resolve(stream);  // the gather rewrites the statistics a pending resolve reads
     timed(SPPM_STAGE_GATHER, true);
     if (mixed)
         launch_gather_mixed(any_grid ? pix_tiles : pix, tune.gather_block, fp64_stats, hsh.prefix,
@@ -1400,13 +1411,15 @@ int Runner::read_stage_times(float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_
     return SPPM_OK;
 }
 
-int Runner::resolve(Job& j, uint32_t kind) {
+int Runner::resolve(Job& j, uint32_t kind, cudaStream_t s) {
     SPPM_CK(cudaSetDevice(device));
-    if (j.copy_pending) SPPM_CK(cudaStreamWaitEvent(stream, j.copy_ev, 0));
-    timed(SPPM_STAGE_RESOLVE, true);
-    if (precision == SPPM_PRECISION_MIXED) launch_resolve_mixed(j.self_set(d_jobs, 0), kind, stream);
-    else launch_resolve_fp32(j.self_set(d_jobs, 0), kind, stream);
-    timed(SPPM_STAGE_RESOLVE, false);
+    if (!s) s = stream;
+    // the image buffer may still be in a copy to host memory (on `copy`, which is in order)
+    if (j.copy_pending && s != copy) SPPM_CK(cudaStreamWaitEvent(s, j.copy_ev, 0));
+    timed(SPPM_STAGE_RESOLVE, true, s);
+    if (precision == SPPM_PRECISION_MIXED) launch_resolve_mixed(j.self_set(d_jobs, 0), kind, s);
+    else launch_resolve_fp32(j.self_set(d_jobs, 0), kind, s);
+    timed(SPPM_STAGE_RESOLVE, false, s);
     return launch_check("resolve");
 }
 
@@ -1414,8 +1427,14 @@ int Runner::resolve(Job& j, uint32_t kind) {
 constexpr size_t kMaxTickets = 16;
 
 int Runner::read_image_async(Job& j, uint32_t kind, float* rgb, size_t bytes, uint64_t* ticket) {
-    int st = resolve(j, kind);
+    // the resolve and the copy run on `copy`, after the frames queued so far and beside the next
+    // ones, whose eye pass and gather wait for the resolve (resolve_done)
+    SPPM_CK(cudaSetDevice(device));
+    SPPM_CK(cudaEventRecord(resolved_ev, stream));
+    SPPM_CK(cudaStreamWaitEvent(copy, resolved_ev, 0));
+    int st = resolve(j, kind, copy);
     if (st) return st;
+    SPPM_CK(cudaEventRecord(resolve_done, copy));
     if (!j.copy_ev) SPPM_CK(cudaEventCreateWithFlags(&j.copy_ev, cudaEventDisableTiming));
     if (tickets.size() >= kMaxTickets) {
         SPPM_CK(cudaEventSynchronize(tickets.front().ev));
@@ -1429,8 +1448,6 @@ int Runner::read_image_async(Job& j, uint32_t kind, float* rgb, size_t bytes, ui
     } else {
         SPPM_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     }
-    SPPM_CK(cudaEventRecord(resolved_ev, stream));
-    SPPM_CK(cudaStreamWaitEvent(copy, resolved_ev, 0));
     SPPM_CK(cudaMemcpyAsync(rgb, j.d_image, bytes, cudaMemcpyDeviceToHost, copy));
     SPPM_CK(cudaEventRecord(j.copy_ev, copy));
     j.copy_pending = true;

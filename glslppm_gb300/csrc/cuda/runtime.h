@@ -204,6 +204,10 @@ struct Runner {
     // ticket (numbered from 1) whose event marks its end
     cudaStream_t copy = nullptr;
     cudaEvent_t resolved_ev = nullptr;
+    // recorded on `copy` after each resolve that runs there (an asynchronous image read): the next
+    // frame's eye pass and gather, which overwrite what the resolve reads, wait for it (in a frame
+    // graph as external event-wait nodes)
+    cudaEvent_t resolve_done = nullptr;
     struct Ticket {
         uint64_t id;
         cudaEvent_t ev;
@@ -275,7 +279,7 @@ struct Runner {
     // `cycles` eye-pass cycles after one untimed cycle) and keeps the fastest
     int autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass);
     int read_stage_times(float ms[SPPM_STAGE_COUNT], uint32_t launches[SPPM_STAGE_COUNT]);
-    int resolve(Job& j, uint32_t kind);
+    int resolve(Job& j, uint32_t kind, cudaStream_t s = nullptr);  // on `stream` by default
     // resolve + copy of the image into host memory without waiting; *ticket names the copy
     int read_image_async(Job& j, uint32_t kind, float* rgb, size_t bytes, uint64_t* ticket);
     // waits for the copy of `ticket` (block) or reports whether it has ended (*done)
@@ -286,6 +290,7 @@ struct Runner {
     void timed(int stage, bool start, cudaStream_t s = nullptr);
 
   private:
+    void wait_resolve(cudaStream_t s);  // the last asynchronous resolve, before its inputs change
     int enqueue_frame(uint32_t phase);
     int build_graph(uint32_t phase, FrameGraph& g);
     bool phase_has_eye(uint32_t phase) const;

@@ -94,3 +94,35 @@ def test_batch_streamed_images(cornell_c1_mesh):
     c.run_passes(3)
     for j, buf in zip(ids2, bufs):
         assert np.array_equal(buf.view(np.uint32), c.read_image(j).view(np.uint32))
+
+
+def test_streamed_images_of_a_large_image_with_few_photons(cornell_c1_mesh):
+    """A 2048x2048 image with 16x16 photon slots: the resolve of each streamed image (on the copy
+    stream, beside the next pass) takes longer than the next pass's photon kernels, so the next
+    pass's gather must wait for it -- every streamed display and radiance image still equals the
+    synchronous read after the same passes."""
+    sc, mesh = cornell_c1_mesh
+    w = h = 2048
+
+    def renderer():
+        cfg = g.default_config(w, height=h, photon_width=16, photon_height=16, radius_rule=N.RADIUS_DIAGONAL,
+                               radius_fraction=0.01)
+        r = g.Renderer(cfg)
+        r.upload_scene(mesh.scene())
+        r.set_camera(g.look_at(sc.camera_origin, sc.camera_lookat, w, h, sc.fov))
+        return r
+
+    a, b = renderer(), renderer()
+    steps = 6
+    bufs = [g.pinned_empty((h, w, 3), np.float32) for _ in range(steps)]
+    tickets, expect = [], []
+    for i in range(steps):
+        a.run_passes(1)
+        kind = N.IMAGE_DISPLAY if i % 2 == 0 else N.IMAGE_RADIANCE
+        tickets.append(a.read_image_async(bufs[i], kind))
+        b.run_passes(1)
+        expect.append(b.read_image(kind).copy())
+    for t in tickets:
+        a.image_wait(t)
+    for i in range(steps):
+        assert np.array_equal(bufs[i].view(np.uint32), expect[i].view(np.uint32)), f"step {i}"
