@@ -159,7 +159,7 @@ int sppm_read_state(sppm_ctx* c, uint32_t kind, void* dst, size_t bytes) {
     SPPM_CK(cudaSetDevice(c->rt.device));
     SPPM_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->rt.stream));
     const int st = c->rt.synchronize();
-    if (st == SPPM_OK) state_to_host_layout(kind, dst, bytes, c->job.cfg.flags);
+    if (st == SPPM_OK) state_to_host_layout(kind, dst, bytes, c->job.cfg.flags, c->job.P);
     return st;
 }
 

@@ -371,7 +371,7 @@ int sppm_batch_read_state(sppm_batch* b, uint32_t id, uint32_t kind, void* dst, 
     SPPM_CK(cudaSetDevice(b->rt.device));
     SPPM_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, b->rt.stream));
     const int st = b->rt.synchronize();
-    if (st == SPPM_OK) state_to_host_layout(kind, dst, bytes, j->cfg.flags);
+    if (st == SPPM_OK) state_to_host_layout(kind, dst, bytes, j->cfg.flags, j->P);
     return st;
 }
 

@@ -1207,7 +1207,9 @@ __device__ __forceinline__ uint32_t photon_store(const JobDesc& J, const JobStat
 __device__ __forceinline__ void hash_insert(const JobDesc& J, int k, uint32_t sidx, uint32_t slot, unsigned active) {
     const bool store = slot != 0xFFFFFFFFu;
     // photon index order = depth order; photons of the last row with i >= w/2 have z >= 1 and are
-    // clipped by the scatter draw (counted by the correction draw all the same)
+    // clipped by the scatter draw (counted by the correction draw all the same).  A clipped photon
+    // offers P (the photon count) to the minimum: a slot that only clipped photons reach keeps P,
+    // which the gather reads as the cleared texel -- photon 0 -- weighted by the slot's count.
     const bool clipped = (J.flags & SPPM_FLAG_GL_DEPTH_CLIP) && sidx >= (J.PH - 1) * J.PW + (J.PW + 1) / 2;
     const unsigned long long key = store ? ((unsigned long long)k << 32) | slot : ~0ull;
     const unsigned peers = __match_any_sync(active, key);
@@ -1224,7 +1226,7 @@ __device__ __forceinline__ void hash_insert(const JobDesc& J, int k, uint32_t si
             J.grid_key[sidx] = make_uint2(slot, base + __popc(below));
             return;
         }
-        const uint32_t wmin = __reduce_min_sync(peers, clipped ? 0xFFFFFFFFu : sidx);
+        const uint32_t wmin = __reduce_min_sync(peers, clipped ? J.PW * J.PH : sidx);
         if ((threadIdx.x & 31) == (__ffs(peers) - 1)) {
             atomicAdd(&J.count[slot], n);
             if (wmin != 0xFFFFFFFFu) atomicMin(&J.winner[slot], wmin);
@@ -1723,8 +1725,12 @@ __global__ void __launch_bounds__(256, 4) k_gather(LaunchSet ls) {
         // is progressive.fs's)
         uint32_t slot[8], win[8];
         hash_cells8(ii, G, hs1, hn, slot);
+        const uint32_t clipped_only = J.PW * J.PH;  // every photon of the slot clipped: photon 0
 #pragma unroll
-        for (int c = 0; c < 8; c++) win[c] = __ldg(&J.winner[slot[c]]);
+        for (int c = 0; c < 8; c++) {
+            win[c] = __ldg(&J.winner[slot[c]]);
+            if (win[c] == clipped_only) win[c] = 0u;
+        }
         uint32_t inside = 0;
         // the cells' bounds from the table k_cell_bounds made for this grid (the same values as
         // the division below), when the 2x2x2 block lies inside it

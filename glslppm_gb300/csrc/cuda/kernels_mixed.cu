@@ -212,8 +212,9 @@ __global__ void __launch_bounds__(256) k_slot_fill(LaunchSet ls) {
     const int k = find_job(ls, g);
     const JobDesc& J = ls.jobs[ls.job_ids[k]];
     const uint32_t slot = g - ls.prefix[k];
-    const uint32_t sidx = J.winner[slot];
+    uint32_t sidx = J.winner[slot];
     if (sidx == kEmptySlot) return;
+    if (sidx == J.PW * J.PH) sidx = 0;  // every photon of the slot clipped: the cleared texel's photon 0
     const JobState* st = J.state;
     const float4 p = J.ph.pos[sidx], f = J.ph.flux[sidx], dd = J.ph.dir[sidx];
     const float G = st->grid_scale;

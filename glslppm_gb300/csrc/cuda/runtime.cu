@@ -34,7 +34,15 @@ int launch_check(const char* what) {
     return SPPM_OK;
 }
 
-void state_to_host_layout(uint32_t kind, void* buf, size_t bytes, uint32_t flags) {
+void state_to_host_layout(uint32_t kind, void* buf, size_t bytes, uint32_t flags, uint32_t photon_slots) {
+    if (kind == SPPM_STATE_SLOT_WINNER) {
+        // a slot whose photons were all clipped by the scatter's depth test holds P on the
+        // device (the gather reads it as the cleared texel, photon 0); the texture holds no winner
+        uint32_t* w = static_cast<uint32_t*>(buf);
+        for (size_t i = 0; i < bytes / 4; i++)
+            if (w[i] == photon_slots) w[i] = kEmptySlot;
+        return;
+    }
     if (kind < SPPM_STATE_STATS_N || kind > SPPM_STATE_STATS_TAU) return;
     if (flags & SPPM_FLAG_FP64_STATISTICS) return;  // already IEEE doubles
     char* b = static_cast<char*>(buf);

@@ -61,8 +61,9 @@ struct Arena {
 int validate_config(const sppm_config* c);
 // state kinds whose device layout differs from what readers get: the mixed-precision statistics
 // are double-float pairs on the device and doubles for the reader (converted in place), unless the
-// job keeps IEEE doubles (SPPM_FLAG_FP64_STATISTICS)
-void state_to_host_layout(uint32_t kind, void* buf, size_t bytes, uint32_t flags);
+// job keeps IEEE doubles (SPPM_FLAG_FP64_STATISTICS); a slot winner equal to the photon count P
+// (every photon of the slot clipped) reads back as no winner
+void state_to_host_layout(uint32_t kind, void* buf, size_t bytes, uint32_t flags, uint32_t photon_slots);
 int launch_check(const char* what);
 
 // the caller's view of a job's frame counters
