@@ -1352,11 +1352,11 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
     std::vector<uint32_t> blocks;
     for (uint32_t b : {trace_fit, (3 * trace_fit + 3) / 4, (trace_fit + 1) / 2})
         if (b >= 1 && std::find(blocks.begin(), blocks.end(), b) == blocks.end()) blocks.push_back(b);
-    // the walk (plain path: binary or 4-wide), ray order and refill interval interact: searched
-    // together as a grid first
+    // ray order and refill interval interact: searched together as a grid first.  The plain
+    // path's walk stays as set (wide_bvh is the caller's choice, never the tuner's: the 4-wide walk
+    // can find a triangle the reference's rounded box test skips, see sppm_tuning.wide_bvh)
     const uint32_t cur_wide = cur.wide_bvh;
-    for (uint32_t wd : {0u, 1u}) {
-        if (wd != cur_wide && (precision != SPPM_PRECISION_FP32 || !wide_ok)) continue;
+    for (uint32_t wd : {cur_wide}) {
         for (uint32_t ub : {0u, 1u}) {
             if (ub && !queue.key) continue;
             for (uint32_t rs : {4u, 8u, 16u, 32u, 64u}) {

@@ -52,8 +52,9 @@ typedef enum sppm_precision {
     SPPM_PRECISION_FP32 = 0,
     /* Mixed: 4-wide traversal over outward-rounded quantised child boxes (FMA slab tests widened
        by their rounding bound, the exact triangle test, ties at equal t in the exact walk's order:
-       the same hits as the plain walk), photon flux and direction stored in FP16, flux gathered in
-       FP32, per-pixel N, R^2 and tau as double-float pairs (read as doubles). */
+       the plain walk's hits, or a closer triangle where the plain walk's rounded box test skips
+       one), photon flux and direction stored in FP16, flux gathered in FP32, per-pixel N, R^2 and
+       tau as double-float pairs (read as doubles). */
     SPPM_PRECISION_MIXED = 1
 } sppm_precision;
 
@@ -353,9 +354,15 @@ typedef struct sppm_tuning {
     uint32_t wide_bvh;            /* plain FP32 path: 1 traces eye and photon rays through the
                                      4-wide quantised BVH (conservative slab tests, the exact
                                      triangle test, ties at equal t broken by the exact walk's
-                                     order) instead of the binary threaded walk: the same hits,
-                                     fewer node fetches on large scenes.  Ignored by the mixed
-                                     path, which always uses it.                                 */
+                                     order) instead of the binary threaded walk: fewer node
+                                     fetches on large scenes, and the same hits except where the
+                                     reference's own FP32 box test skips a box whose triangle is
+                                     an ulp or two closer than the hit found so far
+                                     (near-coincident triangles): the 4-wide walk then returns
+                                     the closer triangle, so the state is no longer the
+                                     reference's bit for bit (3 of 2M eye rays on a 4.1M-triangle
+                                     mesh; none on the Cornell scenes).  The autotuner never sets
+                                     it.  Ignored by the mixed path, which always uses it.       */
     uint32_t photon_wave;         /* wavefront queue depth: photon slots generated, binned,
                                      traced and stored per wave of the photon pass, so a wave's
                                      ray queue and photon records stay in L2 from one kernel to
@@ -441,7 +448,9 @@ int sppm_debug_fpmath(int fn, const float* x, const float* y, float* out, size_t
    with a zero direction component); all give the same result.  Mode 3 traces the mixed
    path's 4-wide quantised BVH instead (contexts of SPPM_PRECISION_MIXED, or any context whose scene
    has the 4-wide tree): its triangle and t equal the exact traversal's, ties at equal t included
-   (broken by each triangle's leaf position in the ray's ordering). */
+   (broken by each triangle's leaf position in the ray's ordering), except where the exact
+   traversal's rounded box test skips a box whose triangle is closer: mode 3 returns that closer
+   triangle. */
 int sppm_debug_trace(sppm_ctx* ctx, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
                      int32_t* tri, float* t);
 /* The photon rays the last pass traced (the wavefront's ray queue; not with

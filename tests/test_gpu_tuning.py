@@ -22,7 +22,7 @@ TUNINGS = [
     dict(trace_tail_lanes=8),   # a drained warp with at most 8 walking lanes hands them over
     dict(trace_tail_lanes=32, trace_refill_steps=4),  # every drained warp hands its walks over
     dict(trace_tail_lanes=1),
-    dict(wide_bvh=1),  # the plain path through the 4-wide BVH (exact-order ties)
+    dict(wide_bvh=1),  # the plain path through the 4-wide BVH (same hits on these scenes, ties in exact order)
     dict(wide_bvh=1, trace_refill_steps=4, unbinned_rays=1, photon_wave=1024),
     dict(photon_wave=1024),  # the photon pass in three waves of at most 1024 slots
     dict(photon_wave=2048, unbinned_rays=1, trace_refill_steps=4),
