@@ -384,6 +384,21 @@ int sppm_debug_photon_grid(sppm_ctx* c, uint32_t* offsets, size_t offsets_capaci
     return SPPM_OK;
 }
 
+int sppm_debug_ray_bins(sppm_ctx* c, uint32_t* rank, uint64_t* cost, size_t capacity, uint32_t* num_bins) {
+    if (!c || !num_bins) return fail(SPPM_ERR_ARG, "null argument");
+    SPPM_CK(cudaSetDevice(c->rt.device));
+    SPPM_CK(cudaStreamSynchronize(c->rt.stream));
+    const RayQueue& q = c->rt.queue;
+    if (!q.bin_rank || !q.bin_cost) return fail(SPPM_ERR_STATE, "no ray bins: created unbinned, or no pass has run");
+    *num_bins = kRayBins;
+    if (!rank && !cost) return SPPM_OK;  // size query
+    if (!rank || !cost) return fail(SPPM_ERR_ARG, "null argument");
+    if (capacity < kRayBins) return fail(SPPM_ERR_ARG, "capacity %zu < %u bins", capacity, kRayBins);
+    SPPM_CK(cudaMemcpy(rank, q.bin_rank, (size_t)kRayBins * 4, cudaMemcpyDeviceToHost));
+    SPPM_CK(cudaMemcpy(cost, q.bin_cost, (size_t)kRayBins * 8, cudaMemcpyDeviceToHost));
+    return SPPM_OK;
+}
+
 int sppm_debug_trace(sppm_ctx* c, const float* org, const float* dir, size_t n, int photon, int cull, int mode,
                      int32_t* tri, float* t) {
     if (!c || !org || !dir || !tri || !t) return fail(SPPM_ERR_ARG, "null argument");

@@ -175,6 +175,11 @@ struct RayQueue {
     // binning (all null when the rays are traced in queue order)
     uint2* key;           // [capacity] (bin, rank within the bin)
     uint32_t* bins;       // [kRayBins] counts, then exclusive offsets
+    // the order the bins are traced in: bin_rank[ray_bin] = the bin's position (the key's first
+    // word and the index into bins); bin_cost[position] = (node steps << 32) + rays, summed by the
+    // traversal since the last reorder, which puts the bins of the longest mean walks first
+    uint32_t* bin_rank;             // [kRayBins]
+    unsigned long long* bin_cost;   // [kRayBins]
     uint32_t* perm;       // [capacity] queue index of the i-th ray in bin order
     uint32_t* eye_deferred;  // [kEyeDeferred] launch indices of the deferred eye pixels
     uint32_t refill_steps;   // traversal steps a warp takes between refills of its idle lanes
@@ -182,6 +187,19 @@ struct RayQueue {
     uint32_t tail_lanes;     // exact walk: once the queue is drained, a warp with at most this many
                              // walking lanes finishes them with the warp-cooperative walk (0: never)
 };
+
+// a finished walk's node steps into its bin's cost: the lanes that finished together add per bin
+// with one pair of atomics (the rays of a warp mostly share a bin, and so do the warps working at
+// the same time, so per-ray atomics would queue on a few addresses)
+__device__ __forceinline__ void bin_cost_add(const RayQueue& q, uint32_t bin, uint32_t steps) {
+    const unsigned same = __match_any_sync(__activemask(), bin);
+    const uint32_t sum = __reduce_add_sync(same, steps);
+    if ((int)(threadIdx.x & 31) == __ffs(same) - 1) {
+        uint32_t* c = reinterpret_cast<uint32_t*>(q.bin_cost + bin);  // (steps << 32) + rays
+        atomicAdd(c, (uint32_t)__popc(same));
+        atomicAdd(c + 1, sum);
+    }
+}
 
 // counting-sort photon grid of the jobs of a launch with SPPM_FLAG_PHOTON_GRID, rebuilt every
 // pass: the records of job k's hash slot s are rec[ofs[b + s]] .. rec[ofs[b + s + 1] - 1], b = the

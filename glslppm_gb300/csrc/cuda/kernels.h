@@ -44,6 +44,8 @@ void launch_queue_reset(const RayQueue& q, cudaStream_t s);
 void launch_trace_photons_fp32(const LaunchSet& ls, const RayQueue& q, bool count_traversal,
                                uint32_t persistent_blocks, cudaStream_t s);
 void launch_ray_bins(const RayQueue& q, cudaStream_t s);
+// the bins' traversal order from the walks traced since the last call (longest mean first)
+void launch_ray_bins_order(const RayQueue& q, cudaStream_t s);
 void launch_trace_photons_coop(const LaunchSet& ls, const RayQueue& q, bool count_traversal, cudaStream_t s);
 // grid_shift: the counting-sort grid's cell split (log2) for jobs with SPPM_FLAG_PHOTON_GRID
 void launch_photon_store_fp32(const LaunchSet& ls, const RayQueue& q, uint32_t block, uint32_t grid_shift,

@@ -1378,7 +1378,7 @@ __global__ void __launch_bounds__(128) k_photon_gen(LaunchSet ls, RayQueue q) {
         q.dir[qi] = make_float4(R.dir.x, R.dir.y, R.dir.z, 0.0f);
         if (q.key) {
             // lanes with the same bin take consecutive ranks from one atomic
-            const uint32_t bin = ray_bin(J.scene, R.org, R.dir);
+            const uint32_t bin = q.bin_rank[ray_bin(J.scene, R.org, R.dir)];
             const unsigned same = __match_any_sync(live, bin);
             const int lead = __ffs(same) - 1;
             uint32_t rb = 0;
@@ -1435,6 +1435,81 @@ __global__ void __launch_bounds__(1024) k_ray_bins_scan(uint32_t* bins) {
     }
 }
 
+// the bins' traversal order, from the mean walk of their rays since the last reorder: the longest
+// first, so that the persistent traversal starts its longest walks early and its drain (lanes
+// idle while the last walks finish) is short -- a longest-processing-time-first schedule.  One
+// block: the means quantised to 256 keys (0: no ray since the last reorder, placed last); a
+// stable counting sort by descending key, rounds of 1024 bins in bin order, each lane's place
+// among equal keys from the warp histograms of the round.  Any order gives the same results (the
+// rays are independent); this one is deterministic.
+__global__ void __launch_bounds__(1024) k_ray_bins_order(RayQueue q) {
+    constexpr uint32_t kKeys = 256, kRounds = kRayBins / 1024;
+    static_assert(kRayBins % 1024 == 0, "bins must split into rounds of 1024");
+    __shared__ uint32_t base[kKeys], cursor[kKeys];
+    __shared__ uint32_t hist[32][kKeys];  // [warp][key]: counts of the round, then offsets
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t < kKeys) {
+        base[t] = 0;
+        cursor[t] = 0;
+    }
+    __syncthreads();
+    uint32_t key[kRounds];
+#pragma unroll
+    for (uint32_t r = 0; r < kRounds; r++) {
+        const unsigned long long c = q.bin_cost[q.bin_rank[r * 1024 + t]];
+        const uint32_t n = (uint32_t)c, mean = n ? (uint32_t)(c >> 32) / n : 0u;
+        const uint32_t k = n ? 1u + min(254u, mean < 128u ? mean : 128u + (mean - 128u) / 8u) : 0u;
+        key[r] = kKeys - 1u - k;  // descending mean
+        atomicAdd(&base[key[r]], 1u);
+    }
+    __syncthreads();
+    if (warp == 0) {  // exclusive scan of the key totals, 8 keys per lane
+        uint32_t v[kKeys / 32], s = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < kKeys / 32; i++) {
+            v[i] = base[lane * (kKeys / 32) + i];
+            s += v[i];
+        }
+        uint32_t incl = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if ((int)lane >= o) incl += y;
+        }
+        uint32_t run = incl - s;
+#pragma unroll
+        for (uint32_t i = 0; i < kKeys / 32; i++) {
+            base[lane * (kKeys / 32) + i] = run;
+            run += v[i];
+        }
+    }
+    for (uint32_t i = t; i < kRayBins; i += 1024) q.bin_cost[i] = 0ull;  // every cost was read above
+    uint32_t rank[kRounds];
+#pragma unroll
+    for (uint32_t r = 0; r < kRounds; r++) {
+        for (uint32_t i = t; i < 32 * kKeys; i += 1024) (&hist[0][0])[i] = 0u;
+        __syncthreads();
+        const uint32_t k = key[r];
+        const unsigned same = __match_any_sync(0xFFFFFFFFu, k);
+        if ((int)lane == __ffs(same) - 1) hist[warp][k] = __popc(same);
+        __syncthreads();
+        if (t < kKeys) {  // offsets of each warp's lanes among the key's bins so far
+            uint32_t run = cursor[t];
+            for (uint32_t w = 0; w < 32; w++) {
+                const uint32_t c = hist[w][t];
+                hist[w][t] = run;
+                run += c;
+            }
+            cursor[t] = run;
+        }
+        __syncthreads();
+        rank[r] = base[k] + hist[warp][k] + __popc(same & ((1u << lane) - 1u));
+        __syncthreads();
+    }
+#pragma unroll
+    for (uint32_t r = 0; r < kRounds; r++) q.bin_rank[r * 1024 + t] = rank[r];
+}
+
 // perm[offset of the bin + rank] = queue index
 __global__ void __launch_bounds__(256) k_ray_bins_scatter(RayQueue q) {
     const uint32_t qi = grid_tid();
@@ -1446,7 +1521,7 @@ __global__ void __launch_bounds__(256) k_ray_bins_scatter(RayQueue q) {
 // trace: persistent warps; a lane whose ray finished fetches the next one from the queue, so
 // lanes stay busy while their neighbours walk longer paths (dynamic fetch)
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q) {
+__global__ void __launch_bounds__(128, 9) k_trace_photons(LaunchSet ls, RayQueue q) {
     const uint32_t total = q.counters[0];
     const int refill = q.refill_steps ? (int)q.refill_steps : 32;
     const unsigned lane = threadIdx.x & 31;
@@ -1592,6 +1667,7 @@ __global__ void __launch_bounds__(128) k_trace_photons(LaunchSet ls, RayQueue q)
         }
         if (finished) {
             q.hit[idx] = make_float4(__int_as_float(h.tri), h.bu, h.bv, h.bw);
+            if (q.perm) bin_cost_add(q, q.key[idx].x, (uint32_t)steps);
             if (COUNT) tc_segs++;
             idx = kNeed;
         }
@@ -1996,6 +2072,9 @@ void launch_photon_gen_fp32(const LaunchSet& ls, const RayQueue& q, bool texture
 }
 void launch_queue_reset(const RayQueue& q, cudaStream_t s) {
     if (q.counters) k_queue_reset<<<blocks_for(kRayBins, 256), 256, 0, s>>>(q);
+}
+void launch_ray_bins_order(const RayQueue& q, cudaStream_t s) {
+    if (q.key && q.bin_rank && q.bin_cost) k_ray_bins_order<<<1, 1024, 0, s>>>(q);
 }
 void launch_ray_bins(const RayQueue& q, cudaStream_t s) {
     if (!q.key || !q.capacity) return;

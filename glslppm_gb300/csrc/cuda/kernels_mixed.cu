@@ -198,6 +198,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_photons4(LaunchSet ls, Ra
         }
         if (finished) {
             q.hit[idx] = make_float4(__int_as_float(htri), hbu, hbv, hbw);
+            if (q.perm) bin_cost_add(q, q.key[idx].x, visits);
             idx = kNeed;
         }
     }

@@ -979,7 +979,8 @@ int Runner::rebuild() {
         const size_t c = std::max<uint32_t>(cap, 1);
         size_t bytes = 3 * Arena::align(c * 16) + Arena::align(64) + Arena::align(c * 4) +
                        Arena::align(kEyeDeferred * 4) + Arena::align(c * 4) + Arena::align(c * 16);
-        if (binned) bytes += Arena::align(c * 8) + Arena::align(c * 4) + Arena::align(kRayBins * 4);
+        if (binned) bytes += Arena::align(c * 8) + Arena::align(c * 4) + 2 * Arena::align(kRayBins * 4) +
+                             Arena::align(kRayBins * 8);
         if ((st = queue_mem.reserve(bytes))) return st;
         Arena& a = queue_mem;
         queue = RayQueue{};
@@ -995,6 +996,13 @@ int Runner::rebuild() {
             queue.key = a.take<uint2>(c);
             queue.perm = a.take<uint32_t>(c);
             queue.bins = a.take<uint32_t>(kRayBins);
+            // bins traced in their own order until the first reorder
+            queue.bin_rank = a.take<uint32_t>(kRayBins);
+            queue.bin_cost = a.take<unsigned long long>(kRayBins);
+            std::vector<uint32_t> ident(kRayBins);
+            for (uint32_t i = 0; i < kRayBins; i++) ident[i] = i;
+            SPPM_CK(cudaMemcpy(queue.bin_rank, ident.data(), kRayBins * 4, cudaMemcpyHostToDevice));
+            SPPM_CK(cudaMemset(queue.bin_cost, 0, kRayBins * 8));
         }
         queue.capacity = (uint32_t)c;
         SPPM_CK(cudaMemset(queue.counters, 0, 64));
@@ -1078,6 +1086,8 @@ int Runner::enqueue_frame(uint32_t phase) {
         q.key = nullptr;
         q.perm = nullptr;
         q.bins = nullptr;
+        q.bin_rank = nullptr;
+        q.bin_cost = nullptr;
     }
     timed(SPPM_STAGE_FRAME_BEGIN, true);
     launch_frame_begin(hsh, q, stream);
@@ -1122,6 +1132,8 @@ int Runner::enqueue_frame(uint32_t phase) {
             RayQueue qw = q;
             qw.capacity = w.total - first < q.capacity ? w.total - first : q.capacity;
             if (first) launch_queue_reset(qw, stream);  // k_frame_begin emptied it for the first wave
+            // once per eye-pass cycle the bins are reordered by the mean walk of their rays
+            else if (eye && qw.key) launch_ray_bins_order(qw, stream);
             timed(SPPM_STAGE_PHOTON, true);
             launch_photon_gen_fp32(w, qw, textured, stream);
             timed(SPPM_STAGE_PHOTON, false);

@@ -191,6 +191,7 @@ SIGNATURES = {
     "sppm_debug_trace": (C.c_int, [P, P, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P]),
     "sppm_debug_photon_rays": (C.c_int, [P, P, P, P, C.c_size_t, C.POINTER(C.c_size_t)]),
     "sppm_debug_photon_grid": (C.c_int, [P, P, C.c_size_t, P, C.c_size_t, C.POINTER(C.c_uint32)]),
+    "sppm_debug_ray_bins": (C.c_int, [P, P, P, C.c_size_t, C.POINTER(C.c_uint32)]),
     "sppm_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(P)]),
     "sppm_write_image_file": (C.c_int, [C.c_char_p, P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "sppm_host_free": (None, [P]),

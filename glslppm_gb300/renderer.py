@@ -327,6 +327,16 @@ class Renderer:
                                              C.byref(n)))
         return org[: n.value], dir[: n.value], ph[: n.value]
 
+    def debug_ray_bins(self) -> tuple[np.ndarray, np.ndarray]:
+        """The photon traversal's bin order (binned contexts): (rank [bins] = each bin's position,
+        cost [bins] uint64 per position = (node steps << 32) + rays since the last reorder)."""
+        n = C.c_uint32()
+        N.check(N.lib.sppm_debug_ray_bins(self._h, None, None, 0, C.byref(n)))
+        rank = np.empty(n.value, np.uint32)
+        cost = np.empty(n.value, np.uint64)
+        N.check(N.lib.sppm_debug_ray_bins(self._h, rank.ctypes.data, cost.ctypes.data, n.value, C.byref(n)))
+        return rank, cost
+
     def debug_photon_grid(self) -> tuple[np.ndarray, np.ndarray]:
         """The counting-sort photon grid of the last pass (SPPM_FLAG_PHOTON_GRID): (offsets
         [hash_slots + 1], records [n, 4] uint32 in slot order; within a slot in no fixed order)."""

@@ -469,6 +469,17 @@ int sppm_debug_photon_rays(sppm_ctx* ctx, float* org, float* dir, uint32_t* phot
    fixed.  With offsets and records null only *num_records is set. */
 int sppm_debug_photon_grid(sppm_ctx* ctx, uint32_t* offsets, size_t offsets_capacity, uint32_t* records,
                            size_t records_capacity, uint32_t* num_records);
+/* The order the photon traversal takes the ray bins in (contexts with binned rays).  A ray's bin
+   is its direction class (cube face of the direction x the signs of its two minor components,
+   24) x its origin cell (8^3 cells of the scene's bounding sphere, Morton-ordered): bin =
+   class * 512 + cell.  rank[bin] = the bin's position in the traversal order; cost[position] =
+   (node steps << 32) + rays of the walks traced since the last reorder.  At the start of every
+   frame with an eye pass the bins are reordered: by descending mean steps per ray (the mean m
+   quantised to 1 + min(254, m < 128 ? m : 128 + (m - 128) / 8), bins without rays last), equal
+   keys in bin order, and the costs restart from zero; the first frames use bin order.  The order
+   never changes a result.  capacity = entries of each array (at least *num_bins; with rank and
+   cost null only *num_bins is set). */
+int sppm_debug_ray_bins(sppm_ctx* ctx, uint32_t* rank, uint64_t* cost, size_t capacity, uint32_t* num_bins);
 /* Page-locked host memory (cudaMallocHost) for the host buffers of sppm_read_image and friends:
    copies to it run at the interconnect's DMA rate instead of being staged through the driver. */
 int sppm_host_alloc(size_t bytes, void** ptr);
