@@ -377,8 +377,8 @@ def roofline_of(cnt, trace_ms_per_launch: float, kernel: str, workload: str, pea
 
 LIMITER_L2 = {
     "k_trace_photons": ("dependent node loads and divergence: the BVH (3 MB) is L2-resident, so DRAM carries only the "
-                        "ray queue (dram_frac); issue-active 62%, 12.6 of 32 lanes active "
-                        "(profiles/k_trace_photons_cornell1024.md)"),
+                        "ray queue (dram_frac); issue-active 68%, 13.8 of 32 lanes active, bins longest mean walk "
+                        "first (profiles/k_trace_photons_cornell1024.md)"),
     "k_trace_photons4": ("instruction issue: the BVH (3 MB) is L2-resident, so DRAM carries only the ray queue "
                          "(dram_frac); issue-active 80%, 13.5 of 32 lanes active "
                          "(profiles/k_trace_photons4_cornell1024.md)"),
