@@ -167,7 +167,8 @@ struct RayQueue {
     float4* dir;
     float4* hit;          // (triangle or -1 as int bits, barycentrics v, w, u)
     uint32_t* counters;   // [0] rays queued, [1] fetch head of the trace kernel, [2] rays set aside,
-                          // [3] eye pixels deferred, [4] walks handed to the tail kernel
+                          // [3] eye pixels deferred, [4] walks handed to the tail kernel,
+                          // [7] frames since the ray bins were last reordered
     uint32_t capacity;
     uint32_t* slow;       // [capacity] queue indices of the rays traced one per warp
     uint32_t* tail_list;  // [capacity] queue indices of the walks the tail kernel finishes

@@ -610,6 +610,7 @@ __global__ void k_frame_begin(LaunchSet ls, RayQueue q) {
         q.counters[2] = 0;
         q.counters[3] = 0;
         q.counters[4] = 0;
+        q.counters[7] += 1u;  // frames since the bins were last reordered
     }
     if (q.bins && g < kRayBins) q.bins[g] = 0u;
     if (g >= ls.total) return;
@@ -1435,7 +1436,8 @@ __global__ void __launch_bounds__(1024) k_ray_bins_scan(uint32_t* bins) {
     }
 }
 
-// the bins' traversal order, from the mean walk of their rays since the last reorder: the longest
+// the bins' traversal order, from the mean walk of their rays since the last reorder (at most once
+// per 8 frames; the frame kernel counts them): the longest
 // first, so that the persistent traversal starts its longest walks early and its drain (lanes
 // idle while the last walks finish) is short -- a longest-processing-time-first schedule.  One
 // block: the means quantised to 256 keys (0: no ray since the last reorder, placed last); a
@@ -1448,11 +1450,14 @@ __global__ void __launch_bounds__(1024) k_ray_bins_order(RayQueue q) {
     __shared__ uint32_t base[kKeys], cursor[kKeys];
     __shared__ uint32_t hist[32][kKeys];  // [warp][key]: counts of the round, then offsets
     const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // at most once per 8 frames (with an eye pass every frame the sort would cost a few percent)
+    if (q.counters[7] < 8u) return;
     if (t < kKeys) {
         base[t] = 0;
         cursor[t] = 0;
     }
     __syncthreads();
+    if (t == 0) q.counters[7] = 0;
     uint32_t key[kRounds];
 #pragma unroll
     for (uint32_t r = 0; r < kRounds; r++) {

@@ -473,8 +473,8 @@ int sppm_debug_photon_grid(sppm_ctx* ctx, uint32_t* offsets, size_t offsets_capa
    is its direction class (cube face of the direction x the signs of its two minor components,
    24) x its origin cell (8^3 cells of the scene's bounding sphere, Morton-ordered): bin =
    class * 512 + cell.  rank[bin] = the bin's position in the traversal order; cost[position] =
-   (node steps << 32) + rays of the walks traced since the last reorder.  At the start of every
-   frame with an eye pass the bins are reordered: by descending mean steps per ray (the mean m
+   (node steps << 32) + rays of the walks traced since the last reorder.  At the start of a frame
+   with an eye pass that begins 8 or more frames after the last reorder the bins are reordered: by descending mean steps per ray (the mean m
    quantised to 1 + min(254, m < 128 ? m : 128 + (m - 128) / 8), bins without rays last), equal
    keys in bin order, and the costs restart from zero; the first frames use bin order.  The order
    never changes a result.  capacity = entries of each array (at least *num_bins; with rank and

@@ -1,7 +1,8 @@
 """The photon traversal takes its ray bins in order of the mean walk their rays took since the
-last reorder (longest first), reordered at every frame with an eye pass: the order is a
-permutation of the bins, follows the costs the traversal summed exactly as sppm_debug_ray_bins
-states, counts every walk of the exact traversal, and changes no result."""
+last reorder (longest first), reordered at a frame with an eye pass 8 or more frames after the
+last reorder: the order is a permutation of the bins, follows the costs the traversal summed
+exactly as sppm_debug_ray_bins states, counts every walk of the exact traversal, and changes no
+result."""
 import numpy as np
 import pytest
 
@@ -63,6 +64,35 @@ def test_bins_reordered_by_mean_walk(cornell_c1_mesh, precision):
     assert rays > 0 and k.max() > 1
     f21 = r.frame_info()
     assert int((cost20 & 0xFFFFFFFF).sum()) <= f21.photon_segments - f20.photon_segments  # restarted
+    r.close()
+
+
+def expected_order(cost_by_bin: np.ndarray) -> np.ndarray:
+    k = expected_rank(cost_by_bin)
+    order = np.lexsort((np.arange(k.size), -k))
+    want = np.empty(k.size, np.int64)
+    want[order] = np.arange(k.size)
+    return want
+
+
+def test_reorder_cadence_with_an_eye_pass_every_frame(cornell_c1_mesh):
+    """With an eye pass every frame the bins are reordered at frames 7, 15, ... (8 frames apart)."""
+    sc, mesh = cornell_c1_mesh
+    r = renderer(sc, mesh, eye_pass_interval=1)
+    r.set_tuning(unbinned_rays=0)
+    r.run_passes(7)  # frames 0..6: no reorder yet
+    rank, cost = r.debug_ray_bins()
+    assert np.array_equal(rank, np.arange(rank.size))
+    r.run_passes(1)  # frame 7: reorder by the walks of frames 0..6
+    rank7, _ = r.debug_ray_bins()
+    assert np.array_equal(rank7, expected_order(cost[rank]))
+    assert not np.array_equal(rank7, np.arange(rank.size))
+    r.run_passes(7)  # frames 8..14: the order stands
+    rank14, cost14 = r.debug_ray_bins()
+    assert np.array_equal(rank14, rank7)
+    r.run_passes(1)  # frame 15
+    rank15, _ = r.debug_ray_bins()
+    assert np.array_equal(rank15, expected_order(cost14[rank14]))
     r.close()
 
 
