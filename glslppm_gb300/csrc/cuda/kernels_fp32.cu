@@ -1437,9 +1437,9 @@ __global__ void __launch_bounds__(1024) k_ray_bins_scan(uint32_t* bins) {
 }
 
 // the bins' traversal order, from the mean walk of their rays since the last reorder (at most once
-// per 8 frames; the frame kernel counts them): the longest
-// first, so that the persistent traversal starts its longest walks early and its drain (lanes
-// idle while the last walks finish) is short -- a longest-processing-time-first schedule.  One
+// per 8 frames; the frame kernel counts them): the longest first, so that the persistent traversal
+// starts its longest walks early and its drain (lanes idle while the last walks finish) is short
+// -- a longest-processing-time-first schedule.  One
 // block: the means quantised to 256 keys (0: no ray since the last reorder, placed last); a
 // stable counting sort by descending key, rounds of 1024 bins in bin order, each lane's place
 // among equal keys from the warp histograms of the round.  Any order gives the same results (the
