@@ -389,7 +389,8 @@ LIMITER_L2 = {
 }
 LIMITER_HBM = {
     "k_trace_photons": ("BVH and triangles (2.2 GB) exceed L2: node fetches reach DRAM; dependent-load latency at the "
-                        "measured dram_frac, issue-active 28% (profiles/k_trace_photons_largemesh.md)"),
+                        "measured dram_frac, issue-active 42%, bins longest mean walk first "
+                        "(profiles/k_trace_photons_largemesh.md)"),
     "k_trace_photons4": ("BVH and triangles (2.2 GB) exceed L2, but the 4-wide walk fetches a quarter as many nodes: "
                          "instruction issue, issue-active 72% at the measured dram_frac "
                          "(profiles/k_trace_photons_largemesh.md)"),
