@@ -1367,22 +1367,18 @@ int Runner::autotune(uint32_t cycles, sppm_tuning* best, float* ms_per_pass) {
     // ray order and refill interval interact: searched together as a grid first.  The plain
     // path's walk stays as set (wide_bvh is the caller's choice, never the tuner's: the 4-wide walk
     // can find a triangle the reference's rounded box test skips, see sppm_tuning.wide_bvh)
-    const uint32_t cur_wide = cur.wide_bvh;
-    for (uint32_t wd : {cur_wide}) {
-        for (uint32_t ub : {0u, 1u}) {
-            if (ub && !queue.key) continue;
-            for (uint32_t rs : {4u, 8u, 16u, 32u, 64u}) {
-                if (wd == cur.wide_bvh && ub == cur.unbinned_rays && rs == cur.trace_refill_steps) continue;
-                sppm_tuning t = cur;
-                t.wide_bvh = wd;
-                t.unbinned_rays = ub;
-                t.trace_refill_steps = rs;
-                float ms = 0.0f;
-                if ((st = measure(t, &ms))) return st;
-                if (ms < 0.99f * cur_ms) {
-                    cur = t;
-                    cur_ms = ms;
-                }
+    for (uint32_t ub : {0u, 1u}) {
+        if (ub && !queue.key) continue;
+        for (uint32_t rs : {4u, 8u, 16u, 32u, 64u}) {
+            if (ub == cur.unbinned_rays && rs == cur.trace_refill_steps) continue;
+            sppm_tuning t = cur;
+            t.unbinned_rays = ub;
+            t.trace_refill_steps = rs;
+            float ms = 0.0f;
+            if ((st = measure(t, &ms))) return st;
+            if (ms < 0.99f * cur_ms) {
+                cur = t;
+                cur_ms = ms;
             }
         }
     }
